@@ -1,0 +1,299 @@
+"""Host API over the C ABI: a device context plus mirrors of the reference's
+point API for this path (include/helioselene_point.h:113-174):
+
+    HeliosPoint.multi_scalar_mul(scalars, points)       (api_point.cpp:98-116)
+    HeliosPoint.pedersen_commit(r, H, values, gens)     (api_point.cpp:118-144)
+    HeliosPoint.map_to_curve(u)                         (api_point.cpp:146-151)
+    point.to_bytes()                                    (api_point.cpp:66-71)
+    helios_batch_to_affine(points)                      (helios/include/helios_batch_affine.h:55)
+
+and the Selene twins.  Points are held in the reference's own layout
+(helios_jacobian: three radix-2^51 five-limb integers, 120 bytes).  Every
+computation runs on the GPU through libhelioselene_gb300.so.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import threading
+from typing import Iterable, List, Sequence
+
+import numpy as np
+
+from . import _lib as L
+
+
+def _u8(a) -> np.ndarray:
+    if isinstance(a, (bytes, bytearray, memoryview)):
+        return np.frombuffer(bytes(a), dtype=np.uint8)
+    arr = np.ascontiguousarray(a)
+    if arr.dtype != np.uint8:
+        arr = arr.view(np.uint8)
+    return arr.reshape(-1)
+
+
+def _ptr(a: np.ndarray):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+class Context:
+    """One device, one CUDA stream, one grow-only workspace (hs_context)."""
+
+    def __init__(self, device: int = 0):
+        self._lib = L.load()
+        h = ctypes.c_void_p()
+        rc = self._lib.hs_context_create(ctypes.byref(h), int(device))
+        if rc != L.HS_OK:
+            raise L.HsError(rc, "hs_context_create: " + (self._lib.hs_last_error(None) or b"").decode())
+        self._h = h
+        self.device = device
+
+    # -- lifetime --
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.hs_context_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- plumbing --
+    @property
+    def handle(self):
+        return self._h
+
+    def _check(self, rc: int, what: str) -> None:
+        if rc != L.HS_OK:
+            msg = (self._lib.hs_last_error(self._h) or b"").decode()
+            raise L.HsError(rc, f"{what}: {self._lib.hs_strerror(rc).decode()} {msg}")
+
+    @property
+    def launches(self) -> int:
+        return int(self._lib.hs_context_launches(self._h))
+
+    @property
+    def stream(self) -> int:
+        return int(self._lib.hs_context_stream(self._h) or 0)
+
+    def set_window(self, curve: int, n_min: int, n_max: int, window: int) -> None:
+        self._check(self._lib.hs_context_set_window(self._h, curve, n_min, n_max, window), "set_window")
+
+    # -- instrumentation --
+    def profile(self, on: bool = True) -> None:
+        self._check(self._lib.hs_profile_enable(self._h, int(on)), "hs_profile_enable")
+
+    def profile_read(self, reset: bool = True) -> dict:
+        ms, launches, entries = ctypes.c_double(), ctypes.c_uint64(), ctypes.c_uint64()
+        self._check(self._lib.hs_profile_read(self._h, ctypes.byref(ms), ctypes.byref(launches),
+                                              ctypes.byref(entries), int(reset)), "hs_profile_read")
+        return {"accumulate_ms": ms.value, "accumulate_launches": launches.value, "entries": entries.value}
+
+    def measure_imad_peak(self) -> float:
+        v = ctypes.c_double()
+        self._check(self._lib.hs_measure_imad_peak(self._h, ctypes.byref(v)), "hs_measure_imad_peak")
+        return v.value
+
+    # -- MSM --
+    def msm(self, curve: int, scalars, points, point_fmt: int = L.FMT_AFFINE,
+            out_fmt: int = L.FMT_COMPRESSED) -> bytes:
+        s, p = _u8(scalars), _u8(points)
+        n = s.size // 32
+        if s.size != 32 * n or p.size != L.FMT_BYTES[point_fmt] * n:
+            raise ValueError("scalars / points sizes do not match")
+        out = np.zeros(L.FMT_BYTES[out_fmt], np.uint8)
+        self._check(self._lib.hs_msm(self._h, curve, _ptr(s), _ptr(p), point_fmt, n, _ptr(out), out_fmt), "hs_msm")
+        return out.tobytes()
+
+    def msm_device(self, curve: int, d_scalars: int, d_points: int, n: int, d_out: int,
+                   out_fmt: int = L.FMT_JACOBIAN51) -> None:
+        self._check(self._lib.hs_msm_device(self._h, curve, ctypes.c_void_p(d_scalars), ctypes.c_void_p(d_points),
+                                            n, ctypes.c_void_p(d_out), out_fmt), "hs_msm_device")
+
+    def pedersen(self, curve: int, blinding, H, values, generators, point_fmt: int = L.FMT_AFFINE,
+                 out_fmt: int = L.FMT_COMPRESSED) -> bytes:
+        b, h, v, g = _u8(blinding), _u8(H), _u8(values), _u8(generators)
+        n = v.size // 32
+        out = np.zeros(L.FMT_BYTES[out_fmt], np.uint8)
+        self._check(self._lib.hs_pedersen(self._h, curve, _ptr(b), _ptr(h), _ptr(v), _ptr(g), point_fmt, n,
+                                          _ptr(out), out_fmt), "hs_pedersen")
+        return out.tobytes()
+
+    def msm_batch(self, items: Sequence[tuple], point_fmt: int = L.FMT_AFFINE,
+                  out_fmt: int = L.FMT_COMPRESSED) -> List[bytes]:
+        """items: (curve, scalars, points) triples; returns one output per MSM."""
+        keep, descs = [], (L.hs_msm_desc * max(1, len(items)))()
+        outs = []
+        for i, (curve, sc, pts) in enumerate(items):
+            s, p = _u8(sc), _u8(pts)
+            o = np.zeros(L.FMT_BYTES[out_fmt], np.uint8)
+            keep += [s, p]
+            outs.append(o)
+            descs[i].curve, descs[i].n = curve, s.size // 32
+            descs[i].scalars, descs[i].points, descs[i].out = s.ctypes.data, p.ctypes.data, o.ctypes.data
+        self._check(self._lib.hs_msm_batch(self._h, descs, len(items), point_fmt, out_fmt), "hs_msm_batch")
+        return [o.tobytes() for o in outs]
+
+    # -- conversions --
+    def batch_to_affine(self, curve: int, jac51, out_fmt: int = L.FMT_AFFINE) -> np.ndarray:
+        j = _u8(jac51)
+        n = j.size // 120
+        out = np.zeros(n * L.FMT_BYTES[out_fmt], np.uint8)
+        self._check(self._lib.hs_batch_to_affine(self._h, curve, _ptr(j), n, _ptr(out), out_fmt),
+                    "hs_batch_to_affine")
+        return out
+
+    def compress(self, curve: int, points, in_fmt: int) -> np.ndarray:
+        p = _u8(points)
+        n = p.size // L.FMT_BYTES[in_fmt]
+        out = np.zeros(32 * n, np.uint8)
+        self._check(self._lib.hs_compress(self._h, curve, _ptr(p), in_fmt, n, _ptr(out)), "hs_compress")
+        return out
+
+    def map_to_curve(self, curve: int, u, out_fmt: int = L.FMT_AFFINE) -> np.ndarray:
+        uu = _u8(u)
+        n = uu.size // 32
+        out = np.zeros(n * L.FMT_BYTES[out_fmt], np.uint8)
+        self._check(self._lib.hs_map_to_curve(self._h, curve, _ptr(uu), n, _ptr(out), out_fmt), "hs_map_to_curve")
+        return out
+
+    def map_to_curve_device(self, curve: int, d_u: int, n: int, d_out: int) -> None:
+        self._check(self._lib.hs_map_to_curve_device(self._h, curve, ctypes.c_void_p(d_u), n,
+                                                     ctypes.c_void_p(d_out)), "hs_map_to_curve_device")
+
+
+_default = None
+_default_lock = threading.Lock()
+
+
+def default_context() -> Context:
+    global _default
+    with _default_lock:
+        if _default is None:
+            _default = Context(0)
+        return _default
+
+
+# ---------------------------------------------------------------------------
+# radix-2^51 packing (pure integer repacking, the reference's fp_fe layout)
+# ---------------------------------------------------------------------------
+M51 = (1 << 51) - 1
+
+
+def int_to_fe51(v: int) -> List[int]:
+    return [(v >> (51 * i)) & M51 for i in range(5)]
+
+
+def fe51_to_int(limbs: Iterable[int]) -> int:
+    return sum(int(l) << (51 * i) for i, l in enumerate(limbs))
+
+
+def jac51_from_ints(X: int, Y: int, Z: int) -> bytes:
+    return np.array(int_to_fe51(X) + int_to_fe51(Y) + int_to_fe51(Z), dtype=np.uint64).tobytes()
+
+
+def affine64_to_jac51(aff: np.ndarray) -> np.ndarray:
+    """Canonical affine x||y (64 bytes each, zeros = identity) -> helios_jacobian records (Z = 1)."""
+    a = _u8(aff).reshape(-1, 64)
+    out = np.zeros((a.shape[0], 15), np.uint64)
+    for i in range(a.shape[0]):
+        x = int.from_bytes(a[i, :32].tobytes(), "little")
+        y = int.from_bytes(a[i, 32:].tobytes(), "little")
+        if x == 0 and y == 0:
+            out[i] = int_to_fe51(1) + int_to_fe51(1) + int_to_fe51(0)
+        else:
+            out[i] = int_to_fe51(x) + int_to_fe51(y) + int_to_fe51(1)
+    return out.reshape(-1).view(np.uint8)
+
+
+# ---------------------------------------------------------------------------
+# mirrors of HeliosPoint / SelenePoint for the MSM path
+# ---------------------------------------------------------------------------
+class _PointBase:
+    CURVE = L.HELIOS
+
+    def __init__(self, jac51: bytes):
+        if len(jac51) != 120:
+            raise ValueError("a point is one 120-byte helios_jacobian / selene_jacobian record")
+        self.jac51 = bytes(jac51)
+
+    @classmethod
+    def identity(cls):
+        return cls(jac51_from_ints(1, 1, 0))
+
+    @classmethod
+    def from_affine_bytes(cls, aff64) -> "_PointBase":
+        return cls(affine64_to_jac51(np.asarray(_u8(aff64))).tobytes())
+
+    def is_identity(self) -> bool:
+        z = np.frombuffer(self.jac51, dtype=np.uint64)[10:15]
+        return self.to_bytes() == bytes(32) if z.any() else True
+
+    def to_bytes(self, ctx: Context = None) -> bytes:
+        ctx = ctx or default_context()
+        return ctx.compress(self.CURVE, self.jac51, L.FMT_JACOBIAN51).tobytes()
+
+    def __eq__(self, other) -> bool:
+        return type(self) is type(other) and self.to_bytes() == other.to_bytes()
+
+    def __hash__(self):
+        return hash(self.to_bytes())
+
+    @classmethod
+    def multi_scalar_mul(cls, scalars: Sequence[bytes], points: Sequence["_PointBase"], ctx: Context = None):
+        """Sum scalars[i] * points[i]; n == 0 gives the identity (api_point.cpp:100-101)."""
+        ctx = ctx or default_context()
+        if len(scalars) == 0 or len(points) == 0:
+            return cls.identity()
+        s = b"".join(bytes(x) for x in scalars)
+        p = b"".join(pt.jac51 for pt in points)
+        return cls(ctx.msm(cls.CURVE, s, p, L.FMT_JACOBIAN51, L.FMT_JACOBIAN51))
+
+    @classmethod
+    def pedersen_commit(cls, blinding: bytes, H: "_PointBase", values: Sequence[bytes],
+                        generators: Sequence["_PointBase"], ctx: Context = None):
+        """blinding*H + sum values[i]*generators[i] (api_point.cpp:118-144; n == 0 -> identity)."""
+        ctx = ctx or default_context()
+        if len(values) == 0 or len(generators) == 0:
+            return cls.identity()
+        v = b"".join(bytes(x) for x in values)
+        g = b"".join(pt.jac51 for pt in generators)
+        return cls(ctx.pedersen(cls.CURVE, bytes(blinding), H.jac51, v, g, L.FMT_JACOBIAN51, L.FMT_JACOBIAN51))
+
+    @classmethod
+    def map_to_curve(cls, u: bytes, ctx: Context = None):
+        ctx = ctx or default_context()
+        return cls(ctx.map_to_curve(cls.CURVE, bytes(u), L.FMT_JACOBIAN51).tobytes())
+
+
+class HeliosPoint(_PointBase):
+    CURVE = L.HELIOS
+
+
+class SelenePoint(_PointBase):
+    CURVE = L.SELENE
+
+
+def _batch_to_affine(curve: int, points: Sequence[_PointBase], ctx: Context = None) -> List[bytes]:
+    ctx = ctx or default_context()
+    if not points:
+        return []
+    out = ctx.batch_to_affine(curve, b"".join(p.jac51 for p in points), L.FMT_AFFINE)
+    return [out[64 * i:64 * i + 64].tobytes() for i in range(len(points))]
+
+
+def helios_batch_to_affine(points: Sequence[HeliosPoint], ctx: Context = None) -> List[bytes]:
+    """Affine (x||y canonical bytes) of each point, identity -> zeros (helios_batch_affine.h:55-98)."""
+    return _batch_to_affine(L.HELIOS, points, ctx)
+
+
+def selene_batch_to_affine(points: Sequence[SelenePoint], ctx: Context = None) -> List[bytes]:
+    return _batch_to_affine(L.SELENE, points, ctx)

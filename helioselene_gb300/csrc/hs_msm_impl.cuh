@@ -1,0 +1,689 @@
+// hs_msm_impl.cuh -- curve-templated device kernels of the MSM path.
+//
+// Pipeline of one MSM (n points, c-bit signed windows, W = ceil(257/c) windows,
+// B = 2^(c-1) buckets per window), following the reference Pippenger
+// (helios/src/x64/helios_msm_vartime.cpp:265-388) but laid out for the GPU:
+//   1. recode + counting sort (hs_runtime.cu): every (point, window) with a
+//      nonzero digit becomes one entry "point index | sign" placed
+//      contiguously per bucket;
+//   2. k_accumulate: buckets are cut into segments of at most L entries, one
+//      thread sums one segment of affine bases into an XYZZ point;
+//   3. k_merge_light / k_merge_heavy: buckets with several segments are folded
+//      (sequentially when few, by a block-wide tree when many);
+//   4. k_reduce0 / k_reduce_level: per window S = sum_j (j+1) B_j by running
+//      sums over groups of buckets, recursively over the group results;
+//   5. k_combine: Horner over the windows, S = 2^c S + S_k (the reference's
+//      per-window doublings, :285-289), result as canonical Jacobian.
+#pragma once
+
+#include "hs_curve.cuh"
+#include "hs_internal.h"
+
+namespace hs {
+
+// ---------------------------------------------------------------------------
+// memory helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void load_affine(const uint4 *__restrict__ pts, uint32_t idx, Fe &x, Fe &y)
+{
+    const uint4 *p = pts + 4 * (size_t)idx;
+    uint4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2), d = __ldg(p + 3);
+    x.w[0] = a.x; x.w[1] = a.y; x.w[2] = a.z; x.w[3] = a.w;
+    x.w[4] = b.x; x.w[5] = b.y; x.w[6] = b.z; x.w[7] = b.w;
+    y.w[0] = c.x; y.w[1] = c.y; y.w[2] = c.z; y.w[3] = c.w;
+    y.w[4] = d.x; y.w[5] = d.y; y.w[6] = d.z; y.w[7] = d.w;
+}
+
+__device__ __forceinline__ void store_fe(uint4 *o, const Fe &f)
+{
+    o[0] = make_uint4(f.w[0], f.w[1], f.w[2], f.w[3]);
+    o[1] = make_uint4(f.w[4], f.w[5], f.w[6], f.w[7]);
+}
+
+__device__ __forceinline__ Fe load_fe(const uint4 *o)
+{
+    Fe f;
+    uint4 a = o[0], b = o[1];
+    f.w[0] = a.x; f.w[1] = a.y; f.w[2] = a.z; f.w[3] = a.w;
+    f.w[4] = b.x; f.w[5] = b.y; f.w[6] = b.z; f.w[7] = b.w;
+    return f;
+}
+
+__device__ __forceinline__ void store_xyzz(uint4 *o, const Xyzz &p)
+{
+    store_fe(o, p.X);
+    store_fe(o + 2, p.Y);
+    store_fe(o + 4, p.ZZ);
+    store_fe(o + 6, p.ZZZ);
+}
+
+__device__ __forceinline__ Xyzz load_xyzz(const uint4 *o)
+{
+    Xyzz p;
+    p.X = load_fe(o);
+    p.Y = load_fe(o + 2);
+    p.ZZ = load_fe(o + 4);
+    p.ZZZ = load_fe(o + 6);
+    return p;
+}
+
+// ---------------------------------------------------------------------------
+// 2. bucket accumulation: one thread per segment of <= L entries
+// ---------------------------------------------------------------------------
+template <class C>
+__global__ void __launch_bounds__(128) k_accumulate(const uint2 *__restrict__ segs, const uint32_t *__restrict__ seg_total,
+                                                   const uint32_t *__restrict__ sorted, const uint4 *__restrict__ pts,
+                                                   uint4 *__restrict__ seg_sum)
+{
+    using G = Group<C>;
+    using F = typename C::F;
+    const uint32_t S = *seg_total;
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < S; s += gridDim.x * blockDim.x) {
+        const uint2 d = segs[s];
+        Xyzz acc = G::inf();
+        for (uint32_t i = 0; i < d.y; i++) {
+            const uint32_t e = __ldg(sorted + d.x + i);
+            Fe x, y;
+            load_affine(pts, e & 0x7fffffffu, x, y);
+            if (F::is_exact_zero(x) && F::is_exact_zero(y))
+                continue;  // identity base (the reference's Z == 0 input) contributes nothing
+            if (e >> 31)
+                y = F::neg(y);
+            G::add_affine(acc, x, y);
+        }
+        store_xyzz(seg_sum + 8 * (size_t)s, acc);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 3. folding buckets that were cut into several segments
+// ---------------------------------------------------------------------------
+template <class C>
+__global__ void k_merge_light(const uint32_t *__restrict__ seg_off, uint32_t NB, uint4 *__restrict__ seg_sum,
+                              uint32_t *__restrict__ heavy, uint32_t *__restrict__ heavy_n, uint32_t heavy_min)
+{
+    using G = Group<C>;
+    const uint32_t kb = blockIdx.x * blockDim.x + threadIdx.x;
+    if (kb >= NB)
+        return;
+    const uint32_t s0 = seg_off[kb], ns = seg_off[kb + 1] - s0;
+    if (ns < 2)
+        return;
+    if (ns > heavy_min) {
+        heavy[atomicAdd(heavy_n, 1u)] = kb;
+        return;
+    }
+    Xyzz acc = load_xyzz(seg_sum + 8 * (size_t)s0);
+    for (uint32_t j = 1; j < ns; j++)
+        acc = G::add(acc, load_xyzz(seg_sum + 8 * (size_t)(s0 + j)));
+    store_xyzz(seg_sum + 8 * (size_t)s0, acc);
+}
+
+constexpr int HEAVY_THREADS = 128;
+
+template <class C>
+__global__ void __launch_bounds__(HEAVY_THREADS) k_merge_heavy(const uint32_t *__restrict__ seg_off,
+                                                              const uint32_t *__restrict__ heavy,
+                                                              const uint32_t *__restrict__ heavy_n,
+                                                              uint4 *__restrict__ seg_sum)
+{
+    using G = Group<C>;
+    __shared__ uint4 sh[HEAVY_THREADS * 8];
+    const uint32_t cnt = *heavy_n;
+    for (uint32_t h = blockIdx.x; h < cnt; h += gridDim.x) {
+        const uint32_t kb = heavy[h];
+        const uint32_t s0 = seg_off[kb], ns = seg_off[kb + 1] - s0;
+        Xyzz acc = G::inf();
+        for (uint32_t j = threadIdx.x; j < ns; j += HEAVY_THREADS)
+            acc = G::add(acc, load_xyzz(seg_sum + 8 * (size_t)(s0 + j)));
+        store_xyzz(sh + 8 * threadIdx.x, acc);
+        __syncthreads();
+        for (uint32_t stride = HEAVY_THREADS / 2; stride > 0; stride >>= 1) {
+            if (threadIdx.x < stride) {
+                Xyzz a = load_xyzz(sh + 8 * threadIdx.x);
+                Xyzz b = load_xyzz(sh + 8 * (threadIdx.x + stride));
+                store_xyzz(sh + 8 * threadIdx.x, G::add(a, b));
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0)
+            store_xyzz(seg_sum + 8 * (size_t)s0, load_xyzz(sh));
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 4. bucket reduction: S_k = sum_j (j+1) * B_{k,j}
+// ---------------------------------------------------------------------------
+// Level 0: thread (k, t) owns buckets [t*m, (t+1)*m) of window k and returns
+//   A = sum_j (j - t*m + 1) B_j   and   R = sum_j B_j
+// (running sum from the top, as the reference does over the whole window,
+// helios_msm_vartime.cpp:334-361), so that S_k = sum_t (A_t + t*m*R_t).
+template <class C>
+__global__ void k_reduce0(const uint32_t *__restrict__ seg_off, const uint4 *__restrict__ seg_sum, uint32_t W,
+                          uint32_t B, uint32_t m, uint4 *__restrict__ outA, uint4 *__restrict__ outR)
+{
+    using G = Group<C>;
+    const uint32_t T = B / m;
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= W * T)
+        return;
+    const uint32_t k = tid / T, t = tid % T;
+    Xyzz run = G::inf(), acc = G::inf();
+    for (int j = (int)((t + 1) * m) - 1; j >= (int)(t * m); j--) {
+        const uint32_t kb = k * B + (uint32_t)j;
+        const uint32_t s0 = seg_off[kb];
+        if (seg_off[kb + 1] != s0)
+            run = G::add(run, load_xyzz(seg_sum + 8 * (size_t)s0));
+        acc = G::add(acc, run);
+    }
+    store_xyzz(outA + 8 * (size_t)tid, acc);
+    store_xyzz(outR + 8 * (size_t)tid, run);
+}
+
+// Level l: the window sum is S = sum_t (A_t + t*M*R_t) over T pairs.  Group
+// t = u*m + r:  A'_u = sum_r A + M * sum_r r*R,  R'_u = sum_r R,  M' = m*M.
+template <class C>
+__global__ void k_reduce_level(const uint4 *__restrict__ inA, const uint4 *__restrict__ inR, uint32_t W, uint32_t T,
+                               uint32_t m, uint32_t log2M, uint4 *__restrict__ outA, uint4 *__restrict__ outR)
+{
+    using G = Group<C>;
+    const uint32_t U = T / m;
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= W * U)
+        return;
+    const uint32_t k = tid / U, u = tid % U;
+    const size_t base = (size_t)k * T + (size_t)u * m;
+    Xyzz run = G::inf(), acc = G::inf(), asum = G::inf();
+    for (int r = (int)m - 1; r >= 1; r--) {
+        run = G::add(run, load_xyzz(inR + 8 * (base + r)));
+        acc = G::add(acc, run);
+        asum = G::add(asum, load_xyzz(inA + 8 * (base + r)));
+    }
+    run = G::add(run, load_xyzz(inR + 8 * base));
+    asum = G::add(asum, load_xyzz(inA + 8 * base));
+    for (uint32_t i = 0; i < log2M; i++)
+        acc = G::dbl(acc);
+    store_xyzz(outA + 8 * (size_t)tid, G::add(asum, acc));
+    store_xyzz(outR + 8 * (size_t)tid, run);
+}
+
+// ---------------------------------------------------------------------------
+// 5. window combination (Horner) -> canonical Jacobian
+// ---------------------------------------------------------------------------
+template <class C>
+__device__ void store_jacobian_canon(uint32_t *out, const Xyzz &p)
+{
+    using G = Group<C>;
+    using F = typename C::F;
+    Fe X, Y, Z;
+    G::to_jacobian(X, Y, Z, p);
+    X = F::canon(X);
+    Y = F::canon(Y);
+    Z = F::canon(Z);
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        out[i] = X.w[i];
+        out[8 + i] = Y.w[i];
+        out[16 + i] = Z.w[i];
+    }
+}
+
+template <class C>
+__global__ void k_combine(const uint4 *__restrict__ S, uint32_t W, uint32_t c, uint32_t *__restrict__ out)
+{
+    using G = Group<C>;
+    if (blockIdx.x != 0 || threadIdx.x != 0)
+        return;
+    Xyzz total = load_xyzz(S + 8 * (size_t)(W - 1));
+    for (int k = (int)W - 2; k >= 0; k--) {
+        for (uint32_t d = 0; d < c; d++)
+            total = G::dbl(total);
+        total = G::add(total, load_xyzz(S + 8 * (size_t)k));
+    }
+    store_jacobian_canon<C>(out, total);
+}
+
+template <class C>
+cudaError_t msm_tail(Context &ctx, const MsmPlan &p, const MsmBuffers &b)
+{
+    cudaStream_t st = ctx.stream;
+    // 2. accumulate: persistent grid over the device-side segment count
+    {
+        const int threads = 128;
+        const int blocks = ctx.sm_count * 8;
+        cudaEvent_t ev0 = nullptr;
+        prof_begin(ctx, &ev0);
+        k_accumulate<C><<<blocks, threads, 0, st>>>(b.segs, b.seg_off + p.NB, b.sorted, b.points, b.seg_sum);
+        HS_LAUNCH_CHECK(ctx);
+        prof_end(ctx, ev0, (uint64_t)p.n * p.W);
+    }
+    // 3. merge multi-segment buckets
+    {
+        cudaError_t e = cudaMemsetAsync(b.heavy_n, 0, sizeof(uint32_t), st);
+        if (e != cudaSuccess)
+            return e;
+        const int threads = 256;
+        k_merge_light<C><<<(p.NB + threads - 1) / threads, threads, 0, st>>>(b.seg_off, p.NB, b.seg_sum, b.heavy,
+                                                                           b.heavy_n, 8);
+        HS_LAUNCH_CHECK(ctx);
+        k_merge_heavy<C><<<ctx.sm_count, HEAVY_THREADS, 0, st>>>(b.seg_off, b.heavy, b.heavy_n, b.seg_sum);
+        HS_LAUNCH_CHECK(ctx);
+    }
+    // 4. reduction levels
+    uint32_t T = p.B / p.m0;
+    {
+        const uint32_t total = p.W * T;
+        const int threads = 128;
+        k_reduce0<C><<<(total + threads - 1) / threads, threads, 0, st>>>(b.seg_off, b.seg_sum, p.W, p.B, p.m0,
+                                                                       b.redA, b.redR);
+        HS_LAUNCH_CHECK(ctx);
+    }
+    uint4 *inA = b.redA, *inR = b.redR, *outA = b.redA2, *outR = b.redR2;
+    uint32_t log2M = 0;
+    for (uint32_t m = p.m0; m > 1; m >>= 1)
+        log2M++;
+    while (T > 1) {
+        const uint32_t m = T < p.mr ? T : p.mr;
+        const uint32_t total = p.W * (T / m);
+        const int threads = 64;
+        k_reduce_level<C><<<(total + threads - 1) / threads, threads, 0, st>>>(inA, inR, p.W, T, m, log2M, outA,
+                                                                            outR);
+        HS_LAUNCH_CHECK(ctx);
+        for (uint32_t mm = m; mm > 1; mm >>= 1)
+            log2M++;
+        T /= m;
+        uint4 *ta = inA, *tr = inR;
+        inA = outA;
+        inR = outR;
+        outA = ta;
+        outR = tr;
+    }
+    // 5. Horner over windows
+    k_combine<C><<<1, 32, 0, st>>>(inA, p.W, (uint32_t)p.c, b.out_jac);
+    HS_LAUNCH_CHECK(ctx);
+    return cudaSuccess;
+}
+
+// ---------------------------------------------------------------------------
+// input conversion: radix-2^51 limbs -> 8 x 32-bit words (weakly reduced)
+// ---------------------------------------------------------------------------
+template <class C>
+__device__ Fe fe_from_51(const uint64_t *l)
+{
+    using F = typename C::F;
+    // sum l_i * 2^(51 i) into five 64-bit words (limbs may exceed 51 bits)
+    unsigned __int128 acc = 0;
+    uint64_t w[5];
+    // word j covers bits [64j, 64j+64)
+    unsigned __int128 v0 = (unsigned __int128)l[0];
+    unsigned __int128 v1 = (unsigned __int128)l[1] << 51;  // bits 51..115
+    unsigned __int128 v2 = (unsigned __int128)l[2] << 38;  // 102 = 64 + 38
+    unsigned __int128 v3 = (unsigned __int128)l[3] << 25;  // 153 = 128 + 25
+    unsigned __int128 v4 = (unsigned __int128)l[4] << 12;  // 204 = 192 + 12
+    acc = (unsigned __int128)(uint64_t)v0 + (uint64_t)v1;
+    w[0] = (uint64_t)acc;
+    acc = (acc >> 64) + (uint64_t)(v0 >> 64) + (uint64_t)(v1 >> 64) + (uint64_t)v2;
+    w[1] = (uint64_t)acc;
+    acc = (acc >> 64) + (uint64_t)(v2 >> 64) + (uint64_t)v3;
+    w[2] = (uint64_t)acc;
+    acc = (acc >> 64) + (uint64_t)(v3 >> 64) + (uint64_t)v4;
+    w[3] = (uint64_t)acc;
+    acc = (acc >> 64) + (uint64_t)(v4 >> 64);
+    w[4] = (uint64_t)acc;  // < 2^13
+    Fe r;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        r.w[2 * i] = (uint32_t)w[i];
+        r.w[2 * i + 1] = (uint32_t)(w[i] >> 32);
+    }
+    // fold w[4] * 2^256 == w[4] * c, one bit at a time (w[4] is tiny, usually 0)
+    uint64_t top = w[4];
+    Fe c1 = F::zero();
+    F::add_c_masked(c1, 0xffffffffu);  // c1 = c = 2^256 mod m
+    while (top) {
+        if (top & 1)
+            r = F::add(r, c1);
+        c1 = F::dbl(c1);
+        top >>= 1;
+    }
+    return r;
+}
+
+template <class C>
+__device__ void fe_to_51(uint64_t *l, const Fe &canon)
+{
+    uint64_t w[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+        w[i] = (uint64_t)canon.w[2 * i] | ((uint64_t)canon.w[2 * i + 1] << 32);
+    const uint64_t M51 = (1ull << 51) - 1;
+    l[0] = w[0] & M51;
+    l[1] = ((w[0] >> 51) | (w[1] << 13)) & M51;
+    l[2] = ((w[1] >> 38) | (w[2] << 26)) & M51;
+    l[3] = ((w[2] >> 25) | (w[3] << 39)) & M51;
+    l[4] = (w[3] >> 12) & M51;
+}
+
+// batch Jacobian -> affine: each thread owns a chunk, multiplies the Z values
+// that are neither 0 nor 1 (Montgomery's trick, fp/include/fp_batch_invert.h:61-114),
+// inverts the chunk product once and walks back.  Identity (Z == 0) -> (0,0).
+constexpr int AFF_CHUNK = 16;
+
+template <class C>
+__global__ void k_jac_to_affine(const uint64_t *__restrict__ in, int fmt, size_t n, uint4 *__restrict__ out,
+                                uint4 *__restrict__ scratch)
+{
+    using F = typename C::F;
+    const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const size_t lo = t * AFF_CHUNK;
+    if (lo >= n)
+        return;
+    const size_t hi = lo + AFF_CHUNK < n ? lo + AFF_CHUNK : n;
+    const size_t stride = (fmt == HS_FMT_JACOBIAN51) ? 15 : (fmt == HS_FMT_AFFINE51 ? 10 : 8);
+    // pass 1: prefix products of the Z values that need inverting
+    Fe run = F::one();
+    bool any = false;
+    for (size_t i = lo; i < hi; i++) {
+        Fe z;
+        if (fmt == HS_FMT_JACOBIAN51) {
+            z = fe_from_51<C>(in + stride * i + 10);
+            Fe zc = F::canon(z);
+            bool is0 = F::is_exact_zero(zc);
+            Fe one = F::one();
+            bool is1 = true;
+#pragma unroll
+            for (int k = 0; k < 8; k++)
+                is1 = is1 && (zc.w[k] == one.w[k]);
+            if (!is0 && !is1) {
+                run = F::mul(run, z);
+                any = true;
+            }
+        }
+        store_fe(scratch + 2 * i, run);
+    }
+    Fe inv = any ? F::inv(run) : F::one();
+    // pass 2: walk back
+    for (size_t i = hi; i-- > lo;) {
+        Fe x, y;
+        if (fmt == HS_FMT_JACOBIAN51) {
+            x = fe_from_51<C>(in + stride * i);
+            y = fe_from_51<C>(in + stride * i + 5);
+        } else if (fmt == HS_FMT_AFFINE51) {
+            x = fe_from_51<C>(in + stride * i);
+            y = fe_from_51<C>(in + stride * i + 5);
+        } else {
+            const uint4 *src = reinterpret_cast<const uint4 *>(in) + 4 * i;
+            x = load_fe(src);
+            y = load_fe(src + 2);
+        }
+        bool ident = false;
+        if (fmt == HS_FMT_JACOBIAN51) {
+            Fe z = fe_from_51<C>(in + stride * i + 10);
+            Fe zc = F::canon(z);
+            bool is0 = F::is_exact_zero(zc);
+            Fe one = F::one();
+            bool is1 = true;
+#pragma unroll
+            for (int k = 0; k < 8; k++)
+                is1 = is1 && (zc.w[k] == one.w[k]);
+            if (is0) {
+                ident = true;
+            } else if (!is1) {
+                Fe prev = (i > lo) ? load_fe(scratch + 2 * (i - 1)) : F::one();
+                Fe zi = F::mul(inv, prev);  // 1/z
+                inv = F::mul(inv, z);
+                Fe zi2 = F::sqr(zi);
+                x = F::mul(x, zi2);
+                y = F::mul(y, F::mul(zi2, zi));
+            }
+        } else {
+            Fe xc = F::canon(x), yc = F::canon(y);
+            ident = F::is_exact_zero(xc) && F::is_exact_zero(yc);
+        }
+        if (ident) {
+            x = F::zero();
+            y = F::zero();
+        }
+        store_fe(out + 4 * i, F::canon(x));
+        store_fe(out + 4 * i + 2, F::canon(y));
+    }
+}
+
+template <class C>
+cudaError_t to_affine(Context &ctx, const void *d_in, int fmt, size_t n, uint4 *d_out, void *scratch)
+{
+    if (n == 0)
+        return cudaSuccess;
+    const size_t chunks = (n + AFF_CHUNK - 1) / AFF_CHUNK;
+    const int threads = 128;
+    k_jac_to_affine<C><<<(unsigned)((chunks + threads - 1) / threads), threads, 0, ctx.stream>>>(
+        reinterpret_cast<const uint64_t *>(d_in), fmt, n, d_out, reinterpret_cast<uint4 *>(scratch));
+    HS_LAUNCH_CHECK(ctx);
+    return cudaSuccess;
+}
+
+inline size_t to_affine_scratch(size_t n) { return n * 32; }
+
+// ---------------------------------------------------------------------------
+// output formatting of canonical Jacobians (24 words each)
+// ---------------------------------------------------------------------------
+template <class C>
+__global__ void k_format_out(const uint32_t *__restrict__ jac, size_t count, int fmt, void *__restrict__ out)
+{
+    using F = typename C::F;
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= count)
+        return;
+    Fe X, Y, Z;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        X.w[k] = jac[24 * i + k];
+        Y.w[k] = jac[24 * i + 8 + k];
+        Z.w[k] = jac[24 * i + 16 + k];
+    }
+    const bool ident = F::is_zero(Z);
+    if (fmt == HS_FMT_JACOBIAN51) {
+        uint64_t *o = reinterpret_cast<uint64_t *>(out) + 15 * i;
+        fe_to_51<C>(o, F::canon(X));
+        fe_to_51<C>(o + 5, F::canon(Y));
+        fe_to_51<C>(o + 10, F::canon(Z));
+        return;
+    }
+    Fe x = F::zero(), y = F::zero();
+    Fe zc = F::canon(Z);
+    bool z_one = zc.w[0] == 1u;
+#pragma unroll
+    for (int k = 1; k < 8; k++)
+        z_one = z_one && zc.w[k] == 0u;
+    if (z_one) {
+        x = F::canon(X);
+        y = F::canon(Y);
+    } else if (!ident) {
+        Fe zi = F::inv(Z);
+        Fe zi2 = F::sqr(zi);
+        x = F::canon(F::mul(X, zi2));
+        y = F::canon(F::mul(Y, F::mul(zi2, zi)));
+    }
+    if (fmt == HS_FMT_AFFINE51) {
+        uint64_t *o = reinterpret_cast<uint64_t *>(out) + 10 * i;
+        fe_to_51<C>(o, x);
+        fe_to_51<C>(o + 5, y);
+    } else if (fmt == HS_FMT_AFFINE) {
+        uint4 *o = reinterpret_cast<uint4 *>(out) + 4 * i;
+        store_fe(o, x);
+        store_fe(o + 2, y);
+    } else {  // compressed: x with parity of y in bit 255
+        uint32_t *o = reinterpret_cast<uint32_t *>(out) + 8 * i;
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+            o[k] = x.w[k];
+        if (!ident)
+            o[7] |= (y.w[0] & 1u) << 31;
+    }
+}
+
+template <class C>
+cudaError_t format_out(Context &ctx, const uint32_t *d_jac, size_t count, int out_fmt, void *d_out)
+{
+    if (count == 0)
+        return cudaSuccess;
+    const int threads = 64;
+    k_format_out<C><<<(unsigned)((count + threads - 1) / threads), threads, 0, ctx.stream>>>(d_jac, count, out_fmt,
+                                                                                           d_out);
+    HS_LAUNCH_CHECK(ctx);
+    return cudaSuccess;
+}
+
+// ---------------------------------------------------------------------------
+// simplified SWU map (RFC 9380 6.6.2) as the reference computes it
+// (helios/src/x64/helios_map_to_curve.cpp:98-198): output affine, Z = 1.
+// ---------------------------------------------------------------------------
+template <class C>
+__device__ bool fsqrt(Fe &r, const Fe &a);
+
+template <>
+__device__ inline bool fsqrt<HeliosCurve>(Fe &r, const Fe &a)
+{
+    // p = 5 (mod 8): x = a^((p+3)/8); if x^2 = -a multiply by sqrt(-1) = 2^((p-1)/4)
+    const uint32_t e[8] = {0xfffffffeu, 0xffffffffu, 0xffffffffu, 0xffffffffu,
+                           0xffffffffu, 0xffffffffu, 0xffffffffu, 0x0fffffffu};
+    const Fe sqrtm1 = {{0x4a0ea0b0u, 0xc4ee1b27u, 0xad2fe478u, 0x2f431806u,
+                        0x3dfbd7a7u, 0x2b4d0099u, 0x4fc1df0bu, 0x2b832480u}};
+    Fe x = Fp::pow(a, e);
+    Fe x2 = Fp::sqr(x);
+    if (!Fp::eq(x2, a)) {
+        if (!Fp::eq(x2, Fp::neg(a)))
+            return false;
+        x = Fp::mul(x, sqrtm1);
+    }
+    r = x;
+    return true;
+}
+
+template <>
+__device__ inline bool fsqrt<SeleneCurve>(Fe &r, const Fe &a)
+{
+    // q = 3 (mod 4): x = a^((q+1)/4)
+    const uint32_t e[8] = {0x9e49f1e8u, 0x1badb49cu, 0x2dd95ad6u, 0xefdfde0bu,
+                           0xffffffffu, 0xffffffffu, 0xffffffffu, 0x1fffffffu};
+    Fe x = Fq::pow(a, e);
+    if (!Fq::eq(Fq::sqr(x), a))
+        return false;
+    r = x;
+    return true;
+}
+
+template <class C>
+__global__ void k_map_to_curve(const uint4 *__restrict__ u, size_t n, uint4 *__restrict__ out)
+{
+    using F = typename C::F;
+    using G = Group<C>;
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    Fe uu = load_fe(u + 2 * i);
+    uu.w[7] &= 0x7fffffffu;  // fp_frombytes masks bit 255
+    const Fe A = F::neg(F::from_u32(3));
+    const Fe Z = (C::SSWU_Z < 0) ? F::neg(F::from_u32((uint32_t)(-C::SSWU_Z))) : F::from_u32((uint32_t)C::SSWU_Z);
+    const Fe B = G::b();
+    Fe u2 = F::sqr(uu);
+    Fe Zu2 = F::mul(Z, u2);
+    Fe den = F::add(F::sqr(Zu2), Zu2);
+    Fe x1;
+    if (F::is_zero(den)) {
+        x1 = F::mul(B, F::inv(F::mul(Z, A)));  // B / (Z A)
+    } else {
+        // x1 = (-B/A) (1 + 1/den) = -B (den + 1) / (A den)
+        Fe num = F::neg(F::mul(B, F::add(den, F::one())));
+        x1 = F::mul(num, F::inv(F::mul(A, den)));
+    }
+    Fe gx1 = F::add(F::sub(F::mul(F::sqr(x1), x1), F::add(F::dbl(x1), x1)), B);
+    Fe x, y;
+    if (fsqrt<C>(y, gx1)) {
+        x = x1;
+    } else {
+        x = F::mul(Zu2, x1);
+        Fe gx2 = F::add(F::sub(F::mul(F::sqr(x), x), F::add(F::dbl(x), x)), B);
+        fsqrt<C>(y, gx2);
+    }
+    y = F::canon(y);
+    Fe uc = F::canon(uu);
+    if ((uc.w[0] & 1u) != (y.w[0] & 1u))
+        y = F::canon(F::neg(y));
+    store_fe(out + 4 * i, F::canon(x));
+    store_fe(out + 4 * i + 2, y);
+}
+
+template <class C>
+cudaError_t map_to_curve(Context &ctx, const void *d_u, size_t n, uint4 *d_out)
+{
+    if (n == 0)
+        return cudaSuccess;
+    const int threads = 64;
+    k_map_to_curve<C><<<(unsigned)((n + threads - 1) / threads), threads, 0, ctx.stream>>>(
+        reinterpret_cast<const uint4 *>(d_u), n, d_out);
+    HS_LAUNCH_CHECK(ctx);
+    return cudaSuccess;
+}
+
+// any input format -> canonical Jacobian (24 words); affine inputs get Z = 1,
+// the affine identity (0,0) becomes (1:1:0)
+template <class C>
+__global__ void k_to_jac24(const uint64_t *__restrict__ in, int fmt, size_t n, uint32_t *__restrict__ out)
+{
+    using F = typename C::F;
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    Fe X, Y, Z;
+    if (fmt == HS_FMT_JACOBIAN51) {
+        X = fe_from_51<C>(in + 15 * i);
+        Y = fe_from_51<C>(in + 15 * i + 5);
+        Z = fe_from_51<C>(in + 15 * i + 10);
+    } else {
+        if (fmt == HS_FMT_AFFINE51) {
+            X = fe_from_51<C>(in + 10 * i);
+            Y = fe_from_51<C>(in + 10 * i + 5);
+        } else {
+            const uint4 *src = reinterpret_cast<const uint4 *>(in) + 4 * i;
+            X = load_fe(src);
+            Y = load_fe(src + 2);
+        }
+        const bool ident = F::is_zero(X) && F::is_zero(Y);
+        Z = ident ? F::zero() : F::one();
+        if (ident) {
+            X = F::one();
+            Y = F::one();
+        }
+    }
+    X = F::canon(X);
+    Y = F::canon(Y);
+    Z = F::canon(Z);
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        out[24 * i + k] = X.w[k];
+        out[24 * i + 8 + k] = Y.w[k];
+        out[24 * i + 16 + k] = Z.w[k];
+    }
+}
+
+template <class C>
+cudaError_t to_jac24(Context &ctx, const void *d_in, int fmt, size_t n, uint32_t *d_out)
+{
+    if (n == 0)
+        return cudaSuccess;
+    const int threads = 128;
+    k_to_jac24<C><<<(unsigned)((n + threads - 1) / threads), threads, 0, ctx.stream>>>(
+        reinterpret_cast<const uint64_t *>(d_in), fmt, n, d_out);
+    HS_LAUNCH_CHECK(ctx);
+    return cudaSuccess;
+}
+
+template <class C>
+CurveOps make_ops()
+{
+    return CurveOps{&msm_tail<C>, &to_affine<C>, &to_affine_scratch, &format_out<C>, &map_to_curve<C>, &to_jac24<C>};
+}
+
+}  // namespace hs

@@ -1,0 +1,994 @@
+// hs_runtime.cu -- context, workspace, signed-digit recode + counting sort, and the C ABI.
+//
+// The recode follows encode_signed_wbit (helios/src/x64/helios_msm_vartime.cpp:127-162)
+// with one difference: W = ceil(257/c) windows, so the carry out of the last
+// full window is kept (the reference drops it when 256 % c == 0, i.e. c = 8).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <new>
+
+#include "hs_internal.h"
+
+struct hs_context {
+    hs::Context c;
+};
+
+namespace hs {
+
+// ---------------------------------------------------------------------------
+// arena
+// ---------------------------------------------------------------------------
+cudaError_t DeviceArena::reserve(size_t bytes)
+{
+    off = 0;
+    if (bytes <= cap)
+        return cudaSuccess;
+    if (base) {
+        cudaError_t e = cudaFree(base);
+        base = nullptr;
+        cap = 0;
+        if (e != cudaSuccess)
+            return e;
+    }
+    size_t want = bytes + bytes / 8;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void **>(&base), want);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        base = nullptr;
+        return e;
+    }
+    cap = want;
+    return cudaSuccess;
+}
+
+void *DeviceArena::take(size_t bytes)
+{
+    size_t o = (off + 255) & ~size_t(255);
+    if (o + bytes > cap)
+        return nullptr;
+    off = o + bytes;
+    return base + o;
+}
+
+void DeviceArena::release()
+{
+    if (base)
+        cudaFree(base);
+    base = nullptr;
+    cap = off = 0;
+}
+
+static size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+size_t fmt_bytes(int fmt)
+{
+    switch (fmt) {
+    case HS_FMT_JACOBIAN51:
+        return 120;
+    case HS_FMT_AFFINE51:
+        return 80;
+    case HS_FMT_AFFINE:
+        return 64;
+    case HS_FMT_COMPRESSED:
+        return 32;
+    default:
+        return 0;
+    }
+}
+
+const CurveOps &curve_ops(int curve) { return curve == HS_SELENE ? selene_ops : helios_ops; }
+
+// ---------------------------------------------------------------------------
+// planning
+// ---------------------------------------------------------------------------
+static int model_window(size_t n)
+{
+    // cost ~ W(c) * (n * madd + 2^(c-1) * 2 adds), madd ~ 10 M, add ~ 14 M
+    int best = 8;
+    double best_cost = 1e300;
+    for (int c = 4; c <= 20; c++) {
+        const double W = (257 + c - 1) / c;
+        const double cost = W * (10.0 * (double)n + 28.0 * (double)(1u << (c - 1)));
+        if (cost < best_cost) {
+            best_cost = cost;
+            best = c;
+        }
+    }
+    return best;
+}
+
+MsmPlan make_plan(const Context &ctx, int curve, size_t n)
+{
+    MsmPlan p;
+    p.curve = curve;
+    p.n = (uint32_t)n;
+    int c = 0;
+    for (const WindowRule &r : ctx.rules[curve == HS_SELENE ? 1 : 0])
+        if (n >= r.n_min && n <= r.n_max)
+            c = r.c;
+    if (c < 4 || c > 20)
+        c = model_window(n);
+    p.c = c;
+    p.W = (uint32_t)((257 + c - 1) / c);
+    p.B = 1u << (c - 1);
+    p.NB = p.W * p.B;
+    const uint32_t avg = (uint32_t)((n + p.B - 1) / p.B);
+    p.L = std::max<uint32_t>(16, std::min<uint32_t>(128, 2 * avg));
+    p.max_entries = (uint32_t)std::max<size_t>(1, n * p.W);
+    p.max_segs = p.max_entries / p.L + p.NB + 1;
+    p.m0 = std::min<uint32_t>(8, p.B);
+    p.mr = 8;
+    return p;
+}
+
+static constexpr int SCAN_THREADS = 1024;
+static constexpr int SCAN_ITEMS = 4;
+static constexpr uint32_t SCAN_BLOCK = SCAN_THREADS * SCAN_ITEMS;
+
+static uint32_t scan_blocks(uint32_t NB) { return (NB + SCAN_BLOCK - 1) / SCAN_BLOCK; }
+
+size_t plan_bytes(const MsmPlan &p)
+{
+    size_t b = 0;
+    b += 3 * align256((size_t)(p.NB + 1) * 4);                  // counts, offsets, seg_off
+    b += align256((size_t)2 * scan_blocks(p.NB) * 4 + 64);      // scan partials
+    b += align256((size_t)p.max_entries * 4);                   // sorted
+    b += align256((size_t)p.max_segs * 8);                      // segs
+    b += align256((size_t)p.max_segs * 128);                    // seg_sum
+    b += align256((size_t)p.NB * 4) + 256;                      // heavy list + counter
+    const size_t r0 = (size_t)p.W * (p.B / p.m0) * 128;
+    const size_t r1 = (size_t)p.W * std::max<uint32_t>(1, p.B / p.m0 / p.mr) * 128;
+    b += 2 * align256(r0) + 2 * align256(r1);
+    b += 256;                                                   // out_jac
+    return b + 16 * 256;
+}
+
+void carve(DeviceArena &a, const MsmPlan &p, MsmBuffers &b)
+{
+    b.counts = (uint32_t *)a.take((size_t)(p.NB + 1) * 4);
+    b.offsets = (uint32_t *)a.take((size_t)(p.NB + 1) * 4);
+    b.seg_off = (uint32_t *)a.take((size_t)(p.NB + 1) * 4);
+    b.scan_tmp = (uint32_t *)a.take((size_t)2 * scan_blocks(p.NB) * 4 + 64);
+    b.sorted = (uint32_t *)a.take((size_t)p.max_entries * 4);
+    b.segs = (uint2 *)a.take((size_t)p.max_segs * 8);
+    b.seg_sum = (uint4 *)a.take((size_t)p.max_segs * 128);
+    b.heavy = (uint32_t *)a.take((size_t)p.NB * 4);
+    b.heavy_n = (uint32_t *)a.take(4);
+    const size_t r0 = (size_t)p.W * (p.B / p.m0) * 128;
+    const size_t r1 = (size_t)p.W * std::max<uint32_t>(1, p.B / p.m0 / p.mr) * 128;
+    b.redA = (uint4 *)a.take(r0);
+    b.redR = (uint4 *)a.take(r0);
+    b.redA2 = (uint4 *)a.take(r1);
+    b.redR2 = (uint4 *)a.take(r1);
+    b.out_jac = (uint32_t *)a.take(96);
+}
+
+// ---------------------------------------------------------------------------
+// 1. signed-digit recode and counting sort
+// ---------------------------------------------------------------------------
+template <int CB>
+__device__ __forceinline__ uint32_t window_bits(const uint32_t s[8], int k)
+{
+    const int o = k * CB;
+    const int wi = o >> 5, sh = o & 31;
+    const uint32_t lo = (wi < 8) ? s[wi] : 0u;
+    const uint32_t hi = (wi + 1 < 8) ? s[wi + 1] : 0u;
+    return __funnelshift_r(lo, hi, sh) & ((1u << CB) - 1u);
+}
+
+// One thread per scalar.  Digits in [-2^(c-1), 2^(c-1)) except the top one,
+// which keeps the final carry and is at most 2^(c-1) because W*c >= 257.
+// count pass: histogram of (window, |digit|) keys; scatter pass: place
+// "index | sign" at offsets[key] + running fill.
+template <int CB, bool SCATTER>
+__global__ void k_recode(const uint4 *__restrict__ scalars, uint32_t n, uint32_t *__restrict__ counts,
+                         const uint32_t *__restrict__ offsets, uint32_t *__restrict__ sorted)
+{
+    constexpr int W = (257 + CB - 1) / CB;
+    constexpr uint32_t B = 1u << (CB - 1);
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const uint4 a = __ldg(scalars + 2 * (size_t)i), b = __ldg(scalars + 2 * (size_t)i + 1);
+    const uint32_t s[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+    uint32_t carry = 0;
+#pragma unroll
+    for (int k = 0; k < W; k++) {
+        const uint32_t v = window_bits<CB>(s, k) + carry;
+        uint32_t mag;
+        bool neg = false;
+        if (k < W - 1 && v >= B) {
+            mag = (1u << CB) - v;  // digit v - 2^c < 0
+            neg = mag != 0;
+            carry = 1;
+        } else {
+            mag = v;
+            carry = 0;
+        }
+        if (mag != 0) {
+            const uint32_t kb = (uint32_t)k * B + mag - 1u;
+            if (!SCATTER) {
+                atomicAdd(counts + kb, 1u);
+            } else {
+                const uint32_t pos = offsets[kb] + atomicAdd(counts + kb, 1u);
+                sorted[pos] = i | (neg ? 0x80000000u : 0u);
+            }
+        }
+    }
+}
+
+// exclusive scan of (count, ceil(count / L)) pairs, three phases
+__device__ __forceinline__ uint2 warp_incl_scan(uint2 v)
+{
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t x = __shfl_up_sync(0xffffffffu, v.x, d);
+        const uint32_t y = __shfl_up_sync(0xffffffffu, v.y, d);
+        if (lane >= d) {
+            v.x += x;
+            v.y += y;
+        }
+    }
+    return v;
+}
+
+// block-wide exclusive scan of one pair per thread; returns the prefix, sets *total
+__device__ __forceinline__ uint2 block_excl_scan(uint2 v, uint2 *total)
+{
+    __shared__ uint2 warp_tot[SCAN_THREADS / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint2 inc = warp_incl_scan(v);
+    if (lane == 31)
+        warp_tot[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        uint2 t = (lane < (int)(blockDim.x >> 5)) ? warp_tot[lane] : make_uint2(0, 0);
+        const uint2 ti = warp_incl_scan(t);
+        warp_tot[lane] = make_uint2(ti.x - t.x, ti.y - t.y);  // exclusive warp prefix
+        if (lane == 31)
+            *total = ti;
+    }
+    __syncthreads();
+    const uint2 wp = warp_tot[warp];
+    return make_uint2(wp.x + inc.x - v.x, wp.y + inc.y - v.y);
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_a(const uint32_t *__restrict__ counts, uint32_t NB, uint32_t L,
+                                                        uint32_t *__restrict__ offsets, uint32_t *__restrict__ seg_off,
+                                                        uint32_t *__restrict__ tmp)
+{
+    __shared__ uint2 tot;
+    const uint32_t base = blockIdx.x * SCAN_BLOCK + threadIdx.x * SCAN_ITEMS;
+    uint32_t c[SCAN_ITEMS], s[SCAN_ITEMS];
+    uint2 v = make_uint2(0, 0);
+#pragma unroll
+    for (int j = 0; j < SCAN_ITEMS; j++) {
+        const uint32_t idx = base + j;
+        c[j] = idx < NB ? counts[idx] : 0u;
+        s[j] = (c[j] + L - 1) / L;
+        v.x += c[j];
+        v.y += s[j];
+    }
+    uint2 pre = block_excl_scan(v, &tot);
+#pragma unroll
+    for (int j = 0; j < SCAN_ITEMS; j++) {
+        const uint32_t idx = base + j;
+        if (idx < NB) {
+            offsets[idx] = pre.x;
+            seg_off[idx] = pre.y;
+        }
+        pre.x += c[j];
+        pre.y += s[j];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        tmp[2 * blockIdx.x] = tot.x;
+        tmp[2 * blockIdx.x + 1] = tot.y;
+    }
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_b(uint32_t *__restrict__ tmp, uint32_t nblocks,
+                                                        uint32_t *__restrict__ off_total,
+                                                        uint32_t *__restrict__ seg_total)
+{
+    __shared__ uint2 tot;
+    const uint32_t base = threadIdx.x * SCAN_ITEMS;
+    uint2 it[SCAN_ITEMS];
+    uint2 v = make_uint2(0, 0);
+#pragma unroll
+    for (int j = 0; j < SCAN_ITEMS; j++) {
+        const uint32_t idx = base + j;
+        it[j] = idx < nblocks ? make_uint2(tmp[2 * idx], tmp[2 * idx + 1]) : make_uint2(0, 0);
+        v.x += it[j].x;
+        v.y += it[j].y;
+    }
+    uint2 pre = block_excl_scan(v, &tot);
+#pragma unroll
+    for (int j = 0; j < SCAN_ITEMS; j++) {
+        const uint32_t idx = base + j;
+        if (idx < nblocks) {
+            tmp[2 * idx] = pre.x;
+            tmp[2 * idx + 1] = pre.y;
+        }
+        pre.x += it[j].x;
+        pre.y += it[j].y;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        *off_total = tot.x;
+        *seg_total = tot.y;
+    }
+}
+
+__global__ void k_scan_c(uint32_t *__restrict__ offsets, uint32_t *__restrict__ seg_off, uint32_t NB,
+                         const uint32_t *__restrict__ tmp)
+{
+    const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= NB)
+        return;
+    const uint32_t blk = idx / SCAN_BLOCK;
+    offsets[idx] += tmp[2 * blk];
+    seg_off[idx] += tmp[2 * blk + 1];
+}
+
+__global__ void k_segments(const uint32_t *__restrict__ offsets, const uint32_t *__restrict__ seg_off, uint32_t NB,
+                           uint32_t L, uint2 *__restrict__ segs)
+{
+    const uint32_t kb = blockIdx.x * blockDim.x + threadIdx.x;
+    if (kb >= NB)
+        return;
+    const uint32_t start = offsets[kb], cnt = offsets[kb + 1] - start;
+    uint32_t s = seg_off[kb];
+    for (uint32_t j = 0; j < cnt; j += L, s++)
+        segs[s] = make_uint2(start + j, min(L, cnt - j));
+}
+
+template <int CB>
+static cudaError_t launch_recode(Context &ctx, const MsmPlan &p, const MsmBuffers &b, bool scatter)
+{
+    const int threads = 256;
+    const unsigned blocks = (p.n + threads - 1) / threads;
+    const uint4 *sc = reinterpret_cast<const uint4 *>(b.scalars);
+    if (scatter)
+        k_recode<CB, true><<<blocks, threads, 0, ctx.stream>>>(sc, p.n, b.counts, b.offsets, b.sorted);
+    else
+        k_recode<CB, false><<<blocks, threads, 0, ctx.stream>>>(sc, p.n, b.counts, b.offsets, b.sorted);
+    HS_LAUNCH_CHECK(ctx);
+    return cudaSuccess;
+}
+
+static cudaError_t recode_dispatch(Context &ctx, const MsmPlan &p, const MsmBuffers &b, bool scatter)
+{
+    switch (p.c) {
+#define HS_CASE(v) \
+    case v:        \
+        return launch_recode<v>(ctx, p, b, scatter);
+        HS_CASE(4)
+        HS_CASE(5)
+        HS_CASE(6)
+        HS_CASE(7)
+        HS_CASE(8)
+        HS_CASE(9)
+        HS_CASE(10)
+        HS_CASE(11)
+        HS_CASE(12)
+        HS_CASE(13)
+        HS_CASE(14)
+        HS_CASE(15)
+        HS_CASE(16)
+        HS_CASE(17)
+        HS_CASE(18)
+        HS_CASE(19)
+        HS_CASE(20)
+#undef HS_CASE
+    default:
+        return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_sort(Context &ctx, const MsmPlan &p, const MsmBuffers &b)
+{
+    cudaStream_t st = ctx.stream;
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(b.counts, 0, (size_t)(p.NB + 1) * 4, st)) != cudaSuccess)
+        return e;
+    if ((e = recode_dispatch(ctx, p, b, false)) != cudaSuccess)
+        return e;
+    const uint32_t nblk = scan_blocks(p.NB);
+    k_scan_a<<<nblk, SCAN_THREADS, 0, st>>>(b.counts, p.NB, p.L, b.offsets, b.seg_off, b.scan_tmp);
+    HS_LAUNCH_CHECK(ctx);
+    if (nblk > SCAN_BLOCK)
+        return cudaErrorInvalidValue;
+    k_scan_b<<<1, SCAN_THREADS, 0, st>>>(b.scan_tmp, nblk, b.offsets + p.NB, b.seg_off + p.NB);
+    HS_LAUNCH_CHECK(ctx);
+    k_scan_c<<<(p.NB + 255) / 256, 256, 0, st>>>(b.offsets, b.seg_off, p.NB, b.scan_tmp);
+    HS_LAUNCH_CHECK(ctx);
+    if ((e = cudaMemsetAsync(b.counts, 0, (size_t)(p.NB + 1) * 4, st)) != cudaSuccess)
+        return e;
+    if ((e = recode_dispatch(ctx, p, b, true)) != cudaSuccess)
+        return e;
+    k_segments<<<(p.NB + 255) / 256, 256, 0, st>>>(b.offsets, b.seg_off, p.NB, p.L, b.segs);
+    HS_LAUNCH_CHECK(ctx);
+    return cudaSuccess;
+}
+
+// ---------------------------------------------------------------------------
+// instrumentation
+// ---------------------------------------------------------------------------
+void prof_begin(Context &ctx, cudaEvent_t *ev)
+{
+    *ev = nullptr;
+    if (!ctx.profile)
+        return;
+    if (cudaEventCreate(ev) != cudaSuccess) {
+        *ev = nullptr;
+        return;
+    }
+    cudaEventRecord(*ev, ctx.stream);
+}
+
+void prof_end(Context &ctx, cudaEvent_t ev0, uint64_t entries)
+{
+    if (!ev0)
+        return;
+    cudaEvent_t ev1;
+    if (cudaEventCreate(&ev1) != cudaSuccess)
+        return;
+    cudaEventRecord(ev1, ctx.stream);
+    ctx.prof_events.emplace_back(ev0, ev1);
+    ctx.prof_entries += entries;
+    ctx.prof_launches++;
+}
+
+// Independent multiply-add chains: 8 accumulators per thread, each step one
+// mad.lo and one mad.hi per accumulator.
+__global__ void k_imad_peak(uint32_t seed, int iters, uint32_t *out)
+{
+    uint32_t a[8], b = seed ^ (threadIdx.x * 0x9e3779b9u) ^ blockIdx.x;
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+        a[k] = b + (uint32_t)k * 0x85ebca6bu;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(a[k]) : "r"(b), "r"((uint32_t)k));
+            asm volatile("mad.hi.u32 %0, %0, %1, %0;" : "+r"(a[k]) : "r"(b));
+        }
+    }
+    uint32_t r = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+        r ^= a[k];
+    if (r == 0x12345678u)
+        out[blockIdx.x * blockDim.x + threadIdx.x] = r;
+}
+
+// ---------------------------------------------------------------------------
+// host helpers for the C ABI
+// ---------------------------------------------------------------------------
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev)
+    {
+        cudaGetDevice(&prev);
+        if (prev != dev)
+            cudaSetDevice(dev);
+    }
+    ~DeviceGuard()
+    {
+        if (prev >= 0)
+            cudaSetDevice(prev);
+    }
+};
+
+static int fail(Context &ctx, cudaError_t e, const char *what)
+{
+    ctx.last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    cudaGetLastError();
+    return e == cudaErrorMemoryAllocation ? HS_ENOMEM : HS_ECUDA;
+}
+
+static int fail_msg(Context &ctx, int code, const char *what)
+{
+    ctx.last_error = what;
+    return code;
+}
+
+#define HS_CU(call, what)                        \
+    do {                                         \
+        cudaError_t e_ = (call);                 \
+        if (e_ != cudaSuccess)                   \
+            return fail(ctx, e_, what);          \
+    } while (0)
+
+static void identity_out(int curve, int out_fmt, void *out)
+{
+    (void)curve;
+    std::memset(out, 0, fmt_bytes(out_fmt));
+    if (out_fmt == HS_FMT_JACOBIAN51) {
+        uint64_t *o = static_cast<uint64_t *>(out);
+        o[0] = 1;  // X = 1
+        o[5] = 1;  // Y = 1, Z = 0 (helios/include/helios_ops.h:45-50)
+    }
+}
+
+static bool valid_curve(int c) { return c == HS_HELIOS || c == HS_SELENE; }
+static bool valid_in_fmt(int f) { return f == HS_FMT_JACOBIAN51 || f == HS_FMT_AFFINE51 || f == HS_FMT_AFFINE; }
+static bool valid_out_fmt(int f) { return f >= HS_FMT_JACOBIAN51 && f <= HS_FMT_COMPRESSED; }
+
+// device MSM over resident affine points; result in out_fmt at d_out
+static int msm_on_device(Context &ctx, int curve, const void *d_scalars, const void *d_points, size_t n,
+                         void *d_out, int out_fmt, size_t extra_bytes, void **extra)
+{
+    const MsmPlan p = make_plan(ctx, curve, n);
+    HS_CU(ctx.arena.reserve(plan_bytes(p) + align256(extra_bytes) + 512), "workspace allocation");
+    MsmBuffers b;
+    carve(ctx.arena, p, b);
+    if (extra)
+        *extra = extra_bytes ? ctx.arena.take(extra_bytes) : nullptr;
+    b.scalars = static_cast<const uint32_t *>(d_scalars);
+    b.points = static_cast<const uint4 *>(d_points);
+    HS_CU(launch_sort(ctx, p, b), "recode/sort");
+    const CurveOps &ops = curve_ops(curve);
+    HS_CU(ops.msm_tail(ctx, p, b), "bucket accumulation");
+    HS_CU(ops.format_out(ctx, b.out_jac, 1, out_fmt, d_out), "output formatting");
+    return HS_OK;
+}
+
+}  // namespace hs
+
+using namespace hs;
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+static thread_local std::string g_tls_error;
+
+int hs_abi_version(void) { return 1; }
+
+const char *hs_strerror(int s)
+{
+    switch (s) {
+    case HS_OK:
+        return "ok";
+    case HS_EINVAL:
+        return "invalid argument";
+    case HS_ENOMEM:
+        return "out of memory";
+    case HS_ECUDA:
+        return "CUDA error";
+    case HS_ETIMEDOUT:
+        return "timed out";
+    case HS_EBUSY:
+        return "busy";
+    case HS_ERANGE:
+        return "size out of range";
+    default:
+        return "unknown status";
+    }
+}
+
+int hs_context_create(hs_context **out, int device)
+{
+    if (!out)
+        return HS_EINVAL;
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || device < 0 || device >= count) {
+        g_tls_error = std::string("no such CUDA device: ") + (e != cudaSuccess ? cudaGetErrorString(e) : "index");
+        cudaGetLastError();
+        return e != cudaSuccess ? HS_ECUDA : HS_EINVAL;
+    }
+    hs_context *h = new (std::nothrow) hs_context();
+    if (!h)
+        return HS_ENOMEM;
+    Context &ctx = h->c;
+    ctx.device = device;
+    DeviceGuard g(device);
+    e = cudaStreamCreateWithFlags(&ctx.stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(&ctx.sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (e != cudaSuccess) {
+        g_tls_error = std::string("context creation: ") + cudaGetErrorString(e);
+        cudaGetLastError();
+        delete h;
+        return HS_ECUDA;
+    }
+    *out = h;
+    return HS_OK;
+}
+
+void hs_context_destroy(hs_context *h)
+{
+    if (!h)
+        return;
+    {
+        DeviceGuard g(h->c.device);
+        cudaStreamSynchronize(h->c.stream);
+        h->c.arena.release();
+        cudaStreamDestroy(h->c.stream);
+    }
+    delete h;
+}
+
+const char *hs_last_error(const hs_context *h) { return h ? h->c.last_error.c_str() : g_tls_error.c_str(); }
+
+uint64_t hs_context_launches(const hs_context *h) { return h ? h->c.launches : 0; }
+
+void *hs_context_stream(hs_context *h) { return h ? (void *)h->c.stream : nullptr; }
+
+int hs_context_set_window(hs_context *h, int curve, size_t n_min, size_t n_max, int window)
+{
+    if (!h || !valid_curve(curve) || n_min > n_max || (window != 0 && (window < 4 || window > 20)))
+        return HS_EINVAL;
+    std::lock_guard<std::mutex> lk(h->c.mu);
+    auto &rules = h->c.rules[curve == HS_SELENE ? 1 : 0];
+    if (window == 0) {
+        rules.clear();
+        return HS_OK;
+    }
+    rules.push_back(WindowRule{n_min, n_max, window});
+    return HS_OK;
+}
+
+int hs_msm_device(hs_context *h, int curve, const void *d_scalars, const void *d_points, size_t n, void *d_out,
+                  int out_fmt)
+{
+    if (!h || !valid_curve(curve) || !valid_out_fmt(out_fmt) || !d_out || (n && (!d_scalars || !d_points)))
+        return HS_EINVAL;
+    if (n >= 0x80000000ull)
+        return HS_ERANGE;
+    Context &ctx = h->c;
+    std::lock_guard<std::mutex> lk(ctx.mu);
+    DeviceGuard g(ctx.device);
+    if (n == 0) {
+        unsigned char idb[128];
+        identity_out(curve, out_fmt, idb);
+        HS_CU(cudaMemcpyAsync(d_out, idb, fmt_bytes(out_fmt), cudaMemcpyHostToDevice, ctx.stream), "copy");
+        HS_CU(cudaStreamSynchronize(ctx.stream), "sync");
+        return HS_OK;
+    }
+    return msm_on_device(ctx, curve, d_scalars, d_points, n, d_out, out_fmt, 0, nullptr);
+}
+
+// Stage host inputs (scalars and points in any format) and run one MSM of
+// n_total terms whose first `lead` terms come from (lead_scalar, lead_point).
+static int msm_host(Context &ctx, int curve, const uint8_t *lead_scalar, const void *lead_point, const uint8_t *scalars,
+                    const void *points, int point_fmt, size_t n, void *out, int out_fmt)
+{
+    const size_t lead = lead_scalar ? 1 : 0;
+    const size_t total = n + lead;
+    if (total == 0) {
+        identity_out(curve, out_fmt, out);
+        return HS_OK;
+    }
+    if (total >= 0x80000000ull)
+        return fail_msg(ctx, HS_ERANGE, "n too large");
+    DeviceGuard g(ctx.device);
+    const size_t pb = fmt_bytes(point_fmt);
+    const CurveOps &ops = curve_ops(curve);
+    const MsmPlan p = make_plan(ctx, curve, total);
+    const size_t need_in = align256(total * 32) + align256(total * 64) +
+                           (point_fmt == HS_FMT_AFFINE ? 0 : align256(total * pb)) +
+                           align256(ops.to_affine_scratch(total)) + 256;
+    HS_CU(ctx.arena.reserve(plan_bytes(p) + need_in + 1024), "workspace allocation");
+    MsmBuffers b;
+    carve(ctx.arena, p, b);
+    uint8_t *d_sc = (uint8_t *)ctx.arena.take(total * 32);
+    uint8_t *d_pts = (uint8_t *)ctx.arena.take(total * 64);
+    uint8_t *d_raw = point_fmt == HS_FMT_AFFINE ? d_pts : (uint8_t *)ctx.arena.take(total * pb);
+    void *d_scratch = ctx.arena.take(ops.to_affine_scratch(total));
+    void *d_out = ctx.arena.take(128);
+    if (!d_sc || !d_pts || !d_raw || !d_scratch || !d_out)
+        return fail_msg(ctx, HS_ENOMEM, "workspace carve");
+    cudaStream_t st = ctx.stream;
+    if (lead) {
+        HS_CU(cudaMemcpyAsync(d_sc, lead_scalar, 32, cudaMemcpyHostToDevice, st), "H2D scalars");
+        HS_CU(cudaMemcpyAsync(d_raw, lead_point, pb, cudaMemcpyHostToDevice, st), "H2D points");
+    }
+    if (n) {
+        HS_CU(cudaMemcpyAsync(d_sc + 32 * lead, scalars, n * 32, cudaMemcpyHostToDevice, st), "H2D scalars");
+        HS_CU(cudaMemcpyAsync(d_raw + pb * lead, points, n * pb, cudaMemcpyHostToDevice, st), "H2D points");
+    }
+    if (point_fmt != HS_FMT_AFFINE)
+        HS_CU(ops.to_affine(ctx, d_raw, point_fmt, total, (uint4 *)d_pts, d_scratch), "input conversion");
+    b.scalars = (const uint32_t *)d_sc;
+    b.points = (const uint4 *)d_pts;
+    HS_CU(launch_sort(ctx, p, b), "recode/sort");
+    HS_CU(ops.msm_tail(ctx, p, b), "bucket accumulation");
+    HS_CU(ops.format_out(ctx, b.out_jac, 1, out_fmt, d_out), "output formatting");
+    HS_CU(cudaMemcpyAsync(out, d_out, fmt_bytes(out_fmt), cudaMemcpyDeviceToHost, st), "D2H result");
+    HS_CU(cudaStreamSynchronize(st), "MSM");
+    return HS_OK;
+}
+
+int hs_msm(hs_context *h, int curve, const uint8_t *scalars, const void *points, int point_fmt, size_t n, void *out,
+           int out_fmt)
+{
+    if (!h || !valid_curve(curve) || !valid_in_fmt(point_fmt) || !valid_out_fmt(out_fmt) || !out ||
+        (n && (!scalars || !points)))
+        return HS_EINVAL;
+    Context &ctx = h->c;
+    std::lock_guard<std::mutex> lk(ctx.mu);
+    return msm_host(ctx, curve, nullptr, nullptr, scalars, points, point_fmt, n, out, out_fmt);
+}
+
+int hs_pedersen(hs_context *h, int curve, const uint8_t blinding[32], const void *H, const uint8_t *values,
+                const void *generators, int point_fmt, size_t n, void *out, int out_fmt)
+{
+    if (!h || !valid_curve(curve) || !valid_in_fmt(point_fmt) || !valid_out_fmt(out_fmt) || !out || !blinding ||
+        !H || (n && (!values || !generators)))
+        return HS_EINVAL;
+    Context &ctx = h->c;
+    std::lock_guard<std::mutex> lk(ctx.mu);
+    return msm_host(ctx, curve, blinding, H, values, generators, point_fmt, n, out, out_fmt);
+}
+
+int hs_batch_to_affine(hs_context *h, int curve, const void *in, size_t n, void *out, int out_fmt)
+{
+    if (!h || !valid_curve(curve) || (out_fmt != HS_FMT_AFFINE && out_fmt != HS_FMT_AFFINE51) ||
+        (n && (!in || !out)))
+        return HS_EINVAL;
+    if (n == 0)
+        return HS_OK;
+    Context &ctx = h->c;
+    std::lock_guard<std::mutex> lk(ctx.mu);
+    DeviceGuard g(ctx.device);
+    const CurveOps &ops = curve_ops(curve);
+    HS_CU(ctx.arena.reserve(align256(n * 120) + align256(n * 64) + align256(ops.to_affine_scratch(n)) +
+                            align256(n * 80) + 1024),
+          "workspace allocation");
+    void *d_in = ctx.arena.take(n * 120);
+    uint4 *d_aff = (uint4 *)ctx.arena.take(n * 64);
+    void *d_scr = ctx.arena.take(ops.to_affine_scratch(n));
+    void *d_o51 = ctx.arena.take(n * 80);
+    cudaStream_t st = ctx.stream;
+    HS_CU(cudaMemcpyAsync(d_in, in, n * 120, cudaMemcpyHostToDevice, st), "H2D");
+    HS_CU(ops.to_affine(ctx, d_in, HS_FMT_JACOBIAN51, n, d_aff, d_scr), "batch to affine");
+    if (out_fmt == HS_FMT_AFFINE) {
+        HS_CU(cudaMemcpyAsync(out, d_aff, n * 64, cudaMemcpyDeviceToHost, st), "D2H");
+    } else {
+        // affine -> canonical Jacobian with Z = 1 -> radix-2^51 (x, y) pairs
+        uint32_t *d_j = (uint32_t *)d_in;  // n*120 bytes >= n*96
+        HS_CU(ops.to_jac24(ctx, d_aff, HS_FMT_AFFINE, n, d_j), "affine pack");
+        HS_CU(ops.format_out(ctx, d_j, n, HS_FMT_AFFINE51, d_o51), "affine pack");
+        HS_CU(cudaMemcpyAsync(out, d_o51, n * 80, cudaMemcpyDeviceToHost, st), "D2H");
+    }
+    HS_CU(cudaStreamSynchronize(st), "batch to affine");
+    return HS_OK;
+}
+
+int hs_compress(hs_context *h, int curve, const void *in, int in_fmt, size_t n, uint8_t *out)
+{
+    if (!h || !valid_curve(curve) || !valid_in_fmt(in_fmt) || (n && (!in || !out)))
+        return HS_EINVAL;
+    if (n == 0)
+        return HS_OK;
+    Context &ctx = h->c;
+    std::lock_guard<std::mutex> lk(ctx.mu);
+    DeviceGuard g(ctx.device);
+    const CurveOps &ops = curve_ops(curve);
+    const size_t pb = fmt_bytes(in_fmt);
+    HS_CU(ctx.arena.reserve(align256(n * pb) + align256(n * 96) + align256(n * 32) + 1024), "workspace allocation");
+    void *d_in = ctx.arena.take(n * pb);
+    uint32_t *d_j = (uint32_t *)ctx.arena.take(n * 96);
+    void *d_o = ctx.arena.take(n * 32);
+    cudaStream_t st = ctx.stream;
+    HS_CU(cudaMemcpyAsync(d_in, in, n * pb, cudaMemcpyHostToDevice, st), "H2D");
+    HS_CU(ops.to_jac24(ctx, d_in, in_fmt, n, d_j), "unpack");
+    HS_CU(ops.format_out(ctx, d_j, n, HS_FMT_COMPRESSED, d_o), "compress");
+    HS_CU(cudaMemcpyAsync(out, d_o, n * 32, cudaMemcpyDeviceToHost, st), "D2H");
+    HS_CU(cudaStreamSynchronize(st), "compress");
+    return HS_OK;
+}
+
+int hs_map_to_curve_device(hs_context *h, int curve, const void *d_u, size_t n, void *d_out_affine)
+{
+    if (!h || !valid_curve(curve) || (n && (!d_u || !d_out_affine)))
+        return HS_EINVAL;
+    Context &ctx = h->c;
+    std::lock_guard<std::mutex> lk(ctx.mu);
+    DeviceGuard g(ctx.device);
+    HS_CU(curve_ops(curve).map_to_curve(ctx, d_u, n, (uint4 *)d_out_affine), "map to curve");
+    return HS_OK;
+}
+
+int hs_map_to_curve(hs_context *h, int curve, const uint8_t *u, size_t n, void *out, int out_fmt)
+{
+    if (!h || !valid_curve(curve) || (out_fmt != HS_FMT_AFFINE && out_fmt != HS_FMT_COMPRESSED &&
+                                      out_fmt != HS_FMT_JACOBIAN51) ||
+        (n && (!u || !out)))
+        return HS_EINVAL;
+    if (n == 0)
+        return HS_OK;
+    Context &ctx = h->c;
+    std::lock_guard<std::mutex> lk(ctx.mu);
+    DeviceGuard g(ctx.device);
+    const CurveOps &ops = curve_ops(curve);
+    HS_CU(ctx.arena.reserve(align256(n * 32) + align256(n * 64) + align256(n * 96) + align256(n * 120) + 1024),
+          "workspace allocation");
+    void *d_u = ctx.arena.take(n * 32);
+    uint4 *d_aff = (uint4 *)ctx.arena.take(n * 64);
+    uint32_t *d_j = (uint32_t *)ctx.arena.take(n * 96);
+    void *d_o = ctx.arena.take(n * 120);
+    cudaStream_t st = ctx.stream;
+    HS_CU(cudaMemcpyAsync(d_u, u, n * 32, cudaMemcpyHostToDevice, st), "H2D");
+    HS_CU(ops.map_to_curve(ctx, d_u, n, d_aff), "map to curve");
+    if (out_fmt == HS_FMT_AFFINE) {
+        HS_CU(cudaMemcpyAsync(out, d_aff, n * 64, cudaMemcpyDeviceToHost, st), "D2H");
+    } else {
+        HS_CU(ops.to_jac24(ctx, d_aff, HS_FMT_AFFINE, n, d_j), "pack");
+        HS_CU(ops.format_out(ctx, d_j, n, out_fmt, d_o), "format");
+        HS_CU(cudaMemcpyAsync(out, d_o, n * fmt_bytes(out_fmt), cudaMemcpyDeviceToHost, st), "D2H");
+    }
+    HS_CU(cudaStreamSynchronize(st), "map to curve");
+    return HS_OK;
+}
+
+int hs_msm_batch(hs_context *h, const hs_msm_desc *descs, size_t count, int point_fmt, int out_fmt)
+{
+    if (!h || (count && !descs) || !valid_in_fmt(point_fmt) || !valid_out_fmt(out_fmt))
+        return HS_EINVAL;
+    for (size_t i = 0; i < count; i++) {
+        const int rc = hs_msm(h, descs[i].curve, descs[i].scalars, descs[i].points, point_fmt, descs[i].n,
+                              descs[i].out, out_fmt);
+        if (rc != HS_OK)
+            return rc;
+    }
+    return HS_OK;
+}
+
+int hs_profile_enable(hs_context *h, int on)
+{
+    if (!h)
+        return HS_EINVAL;
+    std::lock_guard<std::mutex> lk(h->c.mu);
+    h->c.profile = on != 0;
+    return HS_OK;
+}
+
+int hs_profile_read(hs_context *h, double *ms, uint64_t *launches, uint64_t *entries, int reset)
+{
+    if (!h)
+        return HS_EINVAL;
+    Context &ctx = h->c;
+    std::lock_guard<std::mutex> lk(ctx.mu);
+    DeviceGuard g(ctx.device);
+    HS_CU(cudaStreamSynchronize(ctx.stream), "profile sync");
+    for (auto &pr : ctx.prof_events) {
+        float t = 0.f;
+        if (cudaEventElapsedTime(&t, pr.first, pr.second) == cudaSuccess)
+            ctx.prof_ms += t;
+        cudaEventDestroy(pr.first);
+        cudaEventDestroy(pr.second);
+    }
+    ctx.prof_events.clear();
+    if (ms)
+        *ms = ctx.prof_ms;
+    if (launches)
+        *launches = ctx.prof_launches;
+    if (entries)
+        *entries = ctx.prof_entries;
+    if (reset) {
+        ctx.prof_ms = 0.0;
+        ctx.prof_launches = 0;
+        ctx.prof_entries = 0;
+    }
+    return HS_OK;
+}
+
+int hs_measure_imad_peak(hs_context *h, double *imad_per_s)
+{
+    if (!h || !imad_per_s)
+        return HS_EINVAL;
+    Context &ctx = h->c;
+    std::lock_guard<std::mutex> lk(ctx.mu);
+    DeviceGuard g(ctx.device);
+    HS_CU(ctx.arena.reserve(1 << 20), "workspace allocation");
+    uint32_t *d = (uint32_t *)ctx.arena.take(1 << 20);
+    const int threads = 256, blocks = ctx.sm_count * 8, iters = 4096;
+    cudaEvent_t e0, e1;
+    HS_CU(cudaEventCreate(&e0), "event");
+    HS_CU(cudaEventCreate(&e1), "event");
+    k_imad_peak<<<blocks, threads, 0, ctx.stream>>>(1u, 64, d);  // warm-up
+    ctx.launches++;
+    float best = 1e30f;
+    for (int rep = 0; rep < 5; rep++) {
+        cudaEventRecord(e0, ctx.stream);
+        k_imad_peak<<<blocks, threads, 0, ctx.stream>>>((uint32_t)rep, iters, d);
+        ctx.launches++;
+        cudaEventRecord(e1, ctx.stream);
+        HS_CU(cudaEventSynchronize(e1), "imad peak");
+        float t = 0.f;
+        cudaEventElapsedTime(&t, e0, e1);
+        best = std::min(best, t);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    HS_CU(cudaGetLastError(), "imad peak");
+    const double ops = (double)blocks * threads * iters * 8.0 * 2.0;
+    *imad_per_s = ops / (best * 1e-3);
+    return HS_OK;
+}
+
+// ---- reference-signature drop-ins on a process-wide context ----
+static hs_context *g_ctx = nullptr;
+static std::once_flag g_ctx_once;
+static int g_ctx_rc = HS_OK;
+
+static hs_context *global_ctx()
+{
+    std::call_once(g_ctx_once, [] { g_ctx_rc = hs_context_create(&g_ctx, 0); });
+    if (g_ctx_rc != HS_OK || !g_ctx) {
+        std::fprintf(stderr, "helioselene_gb300: cannot create the device context (%s: %s)\n",
+                     hs_strerror(g_ctx_rc), hs_last_error(nullptr));
+        std::abort();
+    }
+    return g_ctx;
+}
+
+static void must(int rc, const char *what)
+{
+    if (rc != HS_OK) {
+        std::fprintf(stderr, "helioselene_gb300: %s failed (%s: %s)\n", what, hs_strerror(rc),
+                     hs_last_error(g_ctx));
+        std::abort();
+    }
+}
+
+void hs_helios_msm_vartime(hs_jacobian51 *result, const unsigned char *scalars, const hs_jacobian51 *points, size_t n)
+{
+    if (n == 0 || !scalars || !points) {
+        identity_out(HS_HELIOS, HS_FMT_JACOBIAN51, result);
+        return;
+    }
+    must(hs_msm(global_ctx(), HS_HELIOS, scalars, points, HS_FMT_JACOBIAN51, n, result, HS_FMT_JACOBIAN51),
+         "helios MSM");
+}
+
+void hs_selene_msm_vartime(hs_jacobian51 *result, const unsigned char *scalars, const hs_jacobian51 *points, size_t n)
+{
+    if (n == 0 || !scalars || !points) {
+        identity_out(HS_SELENE, HS_FMT_JACOBIAN51, result);
+        return;
+    }
+    must(hs_msm(global_ctx(), HS_SELENE, scalars, points, HS_FMT_JACOBIAN51, n, result, HS_FMT_JACOBIAN51),
+         "selene MSM");
+}
+
+void hs_helios_pedersen_commit(hs_jacobian51 *result, const unsigned char *blinding, const hs_jacobian51 *H,
+                               const unsigned char *values, const hs_jacobian51 *generators, size_t n)
+{
+    must(hs_pedersen(global_ctx(), HS_HELIOS, blinding, H, values, generators, HS_FMT_JACOBIAN51, n, result,
+                     HS_FMT_JACOBIAN51),
+         "helios Pedersen commitment");
+}
+
+void hs_selene_pedersen_commit(hs_jacobian51 *result, const unsigned char *blinding, const hs_jacobian51 *H,
+                               const unsigned char *values, const hs_jacobian51 *generators, size_t n)
+{
+    must(hs_pedersen(global_ctx(), HS_SELENE, blinding, H, values, generators, HS_FMT_JACOBIAN51, n, result,
+                     HS_FMT_JACOBIAN51),
+         "selene Pedersen commitment");
+}
+
+void hs_helios_batch_to_affine(hs_affine51 *out, const hs_jacobian51 *points, size_t n)
+{
+    must(hs_batch_to_affine(global_ctx(), HS_HELIOS, points, n, out, HS_FMT_AFFINE51), "helios batch to affine");
+}
+
+void hs_selene_batch_to_affine(hs_affine51 *out, const hs_jacobian51 *points, size_t n)
+{
+    must(hs_batch_to_affine(global_ctx(), HS_SELENE, points, n, out, HS_FMT_AFFINE51), "selene batch to affine");
+}
+
+}  // extern "C"

@@ -1,0 +1,183 @@
+/*
+ * helioselene_gb300.h -- C ABI of the GB300 variable-time MSM for the
+ * Helios/Selene curve cycle.
+ *
+ * Drop-in boundary for helioselene's public-data MSM path.  Every entry point
+ * takes plain pointers and sizes; nothing here exposes CUDA or any framework
+ * type.  The library computes on one CUDA device and never falls back to
+ * the CPU: if the device work fails, the call returns an error status (or,
+ * for the void-returning reference-signature entry points, prints the
+ * reason and aborts).
+ *
+ * Point formats (per point, little endian):
+ *   HS_FMT_JACOBIAN51  120 bytes: X[5], Y[5], Z[5] uint64 radix-2^51 limbs,
+ *                      the layout of helios_jacobian / selene_jacobian on
+ *                      64-bit hosts (helios/include/helios.h:41-46,
+ *                      fp/include/fp.h:42-46).  Limbs may be non-canonical;
+ *                      Z may be anything; Z == 0 is the identity.
+ *   HS_FMT_AFFINE51     80 bytes: x[5], y[5] radix-2^51 limbs
+ *                      (helios_affine, helios/include/helios.h:48-52);
+ *                      (0,0) is the identity.
+ *   HS_FMT_AFFINE       64 bytes: x || y as 32-byte little-endian integers;
+ *                      64 zero bytes are the identity.  The device-resident
+ *                      layout.
+ *   HS_FMT_COMPRESSED   32 bytes: the reference serialization (x with the
+ *                      parity of y in bit 255; identity = 32 zero bytes,
+ *                      helios/src/x64/helios_tobytes.cpp:42-66).  Output only.
+ * Scalars are 32-byte little-endian integers; any 256-bit value is accepted
+ * and the result is the exact sum (the reference additionally drops a
+ * recode carry for 864 <= n < 2592, helios/src/x64/helios_msm_vartime.cpp:
+ * 127-162 and 248-263; this library does not reproduce that defect).
+ */
+#ifndef HELIOSELENE_GB300_H
+#define HELIOSELENE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define HS_OK 0
+#define HS_EINVAL (-1)    /* bad argument (null pointer with n > 0, unknown format/curve) */
+#define HS_ENOMEM (-2)    /* device or pinned-host allocation refused */
+#define HS_ECUDA (-3)     /* a CUDA call failed; hs_last_error() has the text */
+#define HS_ETIMEDOUT (-4) /* a bounded device wait ran out */
+#define HS_EBUSY (-5)     /* serving queue full / admission refused */
+#define HS_ERANGE (-6)    /* size beyond a documented maximum */
+
+/* ---- curves and formats ---- */
+#define HS_HELIOS 0
+#define HS_SELENE 1
+
+#define HS_FMT_JACOBIAN51 0
+#define HS_FMT_AFFINE51 1
+#define HS_FMT_AFFINE 2
+#define HS_FMT_COMPRESSED 3
+
+/* The reference's point structs on 64-bit hosts (helios/include/helios.h:41-52,
+ * selene/include/selene.h:41-52). */
+typedef struct hs_jacobian51 {
+    uint64_t X[5];
+    uint64_t Y[5];
+    uint64_t Z[5];
+} hs_jacobian51;
+
+typedef struct hs_affine51 {
+    uint64_t x[5];
+    uint64_t y[5];
+} hs_affine51;
+
+typedef struct hs_context hs_context;
+
+/* ---- context ----
+ * A context owns one CUDA stream, a grow-only device workspace and pinned
+ * staging buffers on one device.  Calls on one context are serialised by an
+ * internal lock; use one context per host thread for concurrency. */
+int hs_context_create(hs_context **ctx, int device);
+void hs_context_destroy(hs_context *ctx);
+/* last error text of this context (or of the process when ctx is NULL) */
+const char *hs_last_error(const hs_context *ctx);
+const char *hs_strerror(int status);
+/* kernels launched on this context since creation (instrumentation) */
+uint64_t hs_context_launches(const hs_context *ctx);
+/* the context's cudaStream_t, as an opaque pointer */
+void *hs_context_stream(hs_context *ctx);
+/* set the Pippenger window width for one curve; 0 restores the built-in
+ * cost model (the autotuner writes this) */
+int hs_context_set_window(hs_context *ctx, int curve, size_t n_min, size_t n_max, int window);
+
+/* ---- MSM: sum of scalars[i] * points[i] ----
+ * Replaces helios_msm_vartime / selene_msm_vartime
+ * (helios/include/helios_msm_vartime.h:45-71, selene/include/selene_msm_vartime.h)
+ * and HeliosPoint/SelenePoint::multi_scalar_mul (include/helioselene_point.h:166-167,
+ * src/api_point.cpp:98-116, 202-220).
+ * Host buffers.  out: one point in out_fmt (JACOBIAN51 or COMPRESSED or AFFINE).
+ * n == 0 gives the identity, as in the reference (helios_msm_vartime.cpp:402-406). */
+int hs_msm(hs_context *ctx, int curve, const uint8_t *scalars, const void *points, int point_fmt, size_t n,
+           void *out, int out_fmt);
+
+/* Same on device-resident data: d_scalars n*32 bytes, d_points n*64 bytes
+ * (HS_FMT_AFFINE), d_out one point in out_fmt, all device pointers; runs on
+ * the context stream and does not synchronise. */
+int hs_msm_device(hs_context *ctx, int curve, const void *d_scalars, const void *d_points, size_t n, void *d_out,
+                  int out_fmt);
+
+/* ---- Pedersen commitment r*H + sum values[i] * generators[i] ----
+ * Replaces helios_pedersen_commit / selene_pedersen_commit
+ * (helios/include/helios_pedersen.h:55-86) and HeliosPoint::pedersen_commit
+ * (include/helioselene_point.h:170-174, src/api_point.cpp:118-144).
+ * H and generators use point_fmt; one MSM of n+1 terms. */
+int hs_pedersen(hs_context *ctx, int curve, const uint8_t blinding[32], const void *H, const uint8_t *values,
+                const void *generators, int point_fmt, size_t n, void *out, int out_fmt);
+
+/* ---- batch Jacobian -> affine with one shared inversion per chunk ----
+ * Replaces helios_batch_to_affine / selene_batch_to_affine
+ * (helios/include/helios_batch_affine.h:55-98): identity -> (0,0).
+ * in: n points in HS_FMT_JACOBIAN51; out: n points in HS_FMT_AFFINE51 or HS_FMT_AFFINE. */
+int hs_batch_to_affine(hs_context *ctx, int curve, const void *in, size_t n, void *out, int out_fmt);
+
+/* ---- serialization of n points (the reference's to_bytes, helios_tobytes.cpp:42-66) ----
+ * in: n points in in_fmt (JACOBIAN51, AFFINE51 or AFFINE); out: n*32 bytes. */
+int hs_compress(hs_context *ctx, int curve, const void *in, int in_fmt, size_t n, uint8_t *out);
+
+/* ---- simplified SWU map of n field elements (helios/src/x64/helios_map_to_curve.cpp:98-198,
+ * selene twin); u: n*32 bytes (bit 255 ignored); out: n points in out_fmt ----
+ * Used to derive bases / generators (HeliosPoint::map_to_curve, api_point.cpp:146-151). */
+int hs_map_to_curve(hs_context *ctx, int curve, const uint8_t *u, size_t n, void *out, int out_fmt);
+int hs_map_to_curve_device(hs_context *ctx, int curve, const void *d_u, size_t n, void *d_out_affine);
+
+/* ---- batched MSMs: many independent MSMs of uneven size, either curve ----
+ * One fused launch sequence over all of them (captured in a CUDA graph and
+ * replayed when the same shape is submitted again).  descs[i] names MSM i;
+ * all pointers are host pointers; outputs are written in out_fmt. */
+typedef struct hs_msm_desc {
+    int curve;
+    size_t n;
+    const uint8_t *scalars;
+    const void *points; /* point_fmt of the call */
+    void *out;
+} hs_msm_desc;
+int hs_msm_batch(hs_context *ctx, const hs_msm_desc *descs, size_t count, int point_fmt, int out_fmt);
+
+/* ---- drop-in entry points with the reference's exact signatures ----
+ * Same arguments and meaning as helios_msm_vartime / selene_msm_vartime
+ * (helios/include/helios_msm_vartime.h:45-49) and the dispatch-table slots
+ * helioselene_dispatch_table::{helios,selene}_msm_vartime
+ * (include/helioselene_dispatch.h:49-57).  They use a process-wide context on
+ * device 0 (created on first use, thread-safe).  The reference returns void;
+ * on a device failure these print the error and abort -- there is no CPU
+ * fallback. */
+void hs_helios_msm_vartime(hs_jacobian51 *result, const unsigned char *scalars, const hs_jacobian51 *points,
+                           size_t n);
+void hs_selene_msm_vartime(hs_jacobian51 *result, const unsigned char *scalars, const hs_jacobian51 *points,
+                           size_t n);
+void hs_helios_pedersen_commit(hs_jacobian51 *result, const unsigned char *blinding, const hs_jacobian51 *H,
+                               const unsigned char *values, const hs_jacobian51 *generators, size_t n);
+void hs_selene_pedersen_commit(hs_jacobian51 *result, const unsigned char *blinding, const hs_jacobian51 *H,
+                               const unsigned char *values, const hs_jacobian51 *generators, size_t n);
+void hs_helios_batch_to_affine(hs_affine51 *out, const hs_jacobian51 *points, size_t n);
+void hs_selene_batch_to_affine(hs_affine51 *out, const hs_jacobian51 *points, size_t n);
+
+/* ---- instrumentation ----
+ * With profiling on, the context records CUDA events around its bucket
+ * accumulation launches (the dominant kernel).  hs_profile_read synchronises
+ * the context stream and returns the summed device time and launch count
+ * since the last reset, plus the entries (point-window pairs) accumulated. */
+int hs_profile_enable(hs_context *ctx, int on);
+int hs_profile_read(hs_context *ctx, double *accumulate_ms, uint64_t *accumulate_launches, uint64_t *entries,
+                    int reset);
+/* Integer multiply-add throughput of this device: a kernel of independent
+ * mad.lo/mad.hi chains on every SM, timed with CUDA events.  Returns
+ * multiply-add instructions per second (one 32x32 half-product each). */
+int hs_measure_imad_peak(hs_context *ctx, double *imad_per_s);
+
+/* ---- library info ---- */
+int hs_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HELIOSELENE_GB300_H */

@@ -393,6 +393,57 @@ int hso_map_to_curve(int curve, uint8_t *out64, const uint8_t *u32s, size_t n)
     return 0;
 }
 
+typedef struct
+{
+    int curve;
+    uint8_t *out64;
+    const uint8_t *u32s;
+    size_t n;
+} map_task;
+
+static void *map_worker(void *arg)
+{
+    map_task *t = (map_task *)arg;
+    hso_map_to_curve(t->curve, t->out64, t->u32s, t->n);
+    return NULL;
+}
+
+int hso_map_to_curve_mt(int curve, uint8_t *out64, const uint8_t *u32s, size_t n, int nthreads)
+{
+    pthread_once(&g_once, init_consts);
+    if (curve != HSO_HELIOS && curve != HSO_SELENE)
+        return -1;
+    if (nthreads < 1)
+        nthreads = 1;
+    map_task *tasks = (map_task *)calloc((size_t)nthreads, sizeof(map_task));
+    pthread_t *tids = (pthread_t *)calloc((size_t)nthreads, sizeof(pthread_t));
+    if (!tasks || !tids)
+    {
+        free(tasks);
+        free(tids);
+        return -2;
+    }
+    size_t chunk = (n + (size_t)nthreads - 1) / (size_t)nthreads;
+    for (int t = 0; t < nthreads; t++)
+    {
+        size_t lo = (size_t)t * chunk, hi = lo + chunk;
+        if (lo > n)
+            lo = n;
+        if (hi > n)
+            hi = n;
+        tasks[t].curve = curve;
+        tasks[t].out64 = out64 + 64 * lo;
+        tasks[t].u32s = u32s + 32 * lo;
+        tasks[t].n = hi - lo;
+        pthread_create(&tids[t], NULL, map_worker, &tasks[t]);
+    }
+    for (int t = 0; t < nthreads; t++)
+        pthread_join(tids[t], NULL);
+    free(tasks);
+    free(tids);
+    return 0;
+}
+
 #define BODY_DEC(C)                                  \
     for (size_t i = 0; i < n; i++)                   \
     {                                                \

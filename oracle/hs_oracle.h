@@ -31,6 +31,7 @@ int hso_msm_mt(int curve, uint8_t out32[32], const uint8_t *scalars, const uint8
 int hso_pedersen(int curve, uint8_t out32[32], const uint8_t blinding[32], const uint8_t H64[64],
                  const uint8_t *values, const uint8_t *gens64, size_t n, int keep_carry);
 int hso_map_to_curve(int curve, uint8_t *out64, const uint8_t *u32s, size_t n);
+int hso_map_to_curve_mt(int curve, uint8_t *out64, const uint8_t *u32s, size_t n, int nthreads);
 int hso_decompress(int curve, uint8_t *out64, const uint8_t *in32, size_t n);
 int hso_compress(int curve, uint8_t *out32, const uint8_t *in64, size_t n);
 int hso_compress_jac(int curve, uint8_t *out32, const uint8_t *in96, size_t n);

@@ -46,6 +46,7 @@ def lib():
             "hso_msm_mt": [c.c_int, u8p, u8p, u8p, sz, c.c_int],
             "hso_pedersen": [c.c_int, u8p, u8p, u8p, u8p, u8p, sz, c.c_int],
             "hso_map_to_curve": [c.c_int, u8p, u8p, sz],
+            "hso_map_to_curve_mt": [c.c_int, u8p, u8p, sz, c.c_int],
             "hso_decompress": [c.c_int, u8p, u8p, sz],
             "hso_compress": [c.c_int, u8p, u8p, sz],
             "hso_compress_jac": [c.c_int, u8p, u8p, sz],
@@ -138,6 +139,14 @@ def map_to_curve(curve, us) -> np.ndarray:
     n = u.size // 32
     out = np.zeros(64 * n, np.uint8)
     assert lib().hso_map_to_curve(_cid(curve), _p(out), _p(u), n) == 0
+    return out
+
+
+def map_to_curve_mt(curve, us, nthreads) -> np.ndarray:
+    u = _buf(us)
+    n = u.size // 32
+    out = np.zeros(64 * n, np.uint8)
+    assert lib().hso_map_to_curve_mt(_cid(curve), _p(out), _p(u), n, int(nthreads)) == 0
     return out
 
 

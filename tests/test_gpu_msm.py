@@ -1,0 +1,276 @@
+"""GPU parity: the CUDA MSM path (through the C ABI) against the oracle.
+
+Integer work, so every comparison is bit-exact on the 32-byte serialization
+(helios/src/x64/helios_tobytes.cpp:42-66).  The oracle runs in exact mode
+(carry kept); where the reference itself is defective (w = 8 band) the GPU
+matches the exact sum, which the oracle tests pin to the reference's own
+code called on sub-864 chunks.
+"""
+
+import ctypes
+import random
+
+import numpy as np
+import pytest
+
+import oracle
+import pyref
+from conftest import CURVES, oracle_inputs
+
+pytestmark = pytest.mark.gpu
+
+HS_COMPRESSED, HS_JAC51, HS_AFF51, HS_AFF = 3, 0, 1, 2
+
+
+def hx(s):
+    return bytes.fromhex(s)
+
+
+def jac51_to_bytes(curve, rec: bytes) -> bytes:
+    """encode a 120-byte helios_jacobian record with the oracle"""
+    import helioselene_gb300 as hs
+    F = pyref.CURVES["helios" if curve == 0 else "selene"].F
+    limbs = np.frombuffer(rec, dtype=np.uint64)
+    X, Y, Z = (hs.fe51_to_int(limbs[5 * k:5 * k + 5]) % F for k in range(3))
+    j96 = X.to_bytes(32, "little") + Y.to_bytes(32, "little") + Z.to_bytes(32, "little")
+    return oracle.compress_jac(curve, j96).tobytes()
+
+
+@pytest.mark.parametrize("curve", [0, 1])
+def test_golden_vectors_on_gpu(ctx, golden, curve):
+    name = "helios" if curve == 0 else "selene"
+    for v in golden[name + "_point"]["msm"]:
+        sc = b"".join(hx(s) for s in v["scalars"])
+        pts, bad = oracle.decompress(curve, b"".join(hx(s) for s in v["points"]))
+        assert ctx.msm(curve, sc, pts, HS_AFF, HS_COMPRESSED).hex() == v["result"], v["label"]
+    for v in golden[name + "_point"]["pedersen_commit"]:
+        H, _ = oracle.decompress(curve, hx(v["H"]))
+        gens, _ = oracle.decompress(curve, b"".join(hx(s) for s in v["generators"]))
+        vals = b"".join(hx(s) for s in v["values"])
+        assert ctx.pedersen(curve, hx(v["blinding"]), H, vals, gens).hex() == v["result"], v["label"]
+    for v in golden[name + "_point"]["map_to_curve_single"]:
+        assert ctx.map_to_curve(curve, hx(v["u"]), HS_COMPRESSED).tobytes().hex() == v["result"], v["label"]
+
+
+@pytest.mark.parametrize("curve", [0, 1])
+@pytest.mark.parametrize("n", [1, 2, 7, 16, 17, 33, 64, 100, 257, 1000, 1024, 2048, 4096, 9000])
+def test_msm_random(ctx, curve, n):
+    sc, pts, _ = oracle_inputs(curve, n, seed=n * 31 + curve)
+    assert ctx.msm(curve, sc, pts) == oracle.msm(curve, sc, pts)
+
+
+@pytest.mark.parametrize("curve", [0, 1])
+def test_msm_edge_slices(ctx, curve):
+    """zero scalars, order-1, one base repeated with one scalar (bucket doubling), top-window-only"""
+    n = 4096
+    sc, pts, w = oracle_inputs(curve, n, seed=77, edge_fraction=0.08)
+    assert len(w.edge["repeated"]) > 10
+    assert ctx.msm(curve, sc, pts) == oracle.msm(curve, sc, pts)
+
+
+@pytest.mark.parametrize("curve", [0, 1])
+def test_msm_degenerate(ctx, curve):
+    n = 300
+    sc, pts, _ = oracle_inputs(curve, n, seed=5)
+    # all-zero scalars -> identity
+    assert ctx.msm(curve, np.zeros_like(sc), pts) == bytes(32)
+    # n == 0 -> identity in every output format
+    assert ctx.msm(curve, sc[:0], pts[:0]) == bytes(32)
+    jid = np.frombuffer(ctx.msm(curve, sc[:0], pts[:0], HS_AFF, HS_JAC51), np.uint64)
+    assert list(jid) == [1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0]
+    # identity bases mixed in, P and -P pairs, duplicated points with different scalars,
+    # unreduced scalars (bit 255 set, 2^256 - 1)
+    pts2 = pts.copy()
+    pts2[10:20] = 0
+    F = pyref.CURVES["helios" if curve == 0 else "selene"].F
+    for i in range(30, 40):
+        y = int.from_bytes(pts2[i - 10, 32:].tobytes(), "little")
+        pts2[i, :32] = pts2[i - 10, :32]
+        pts2[i, 32:] = np.frombuffer(((F - y) % F).to_bytes(32, "little"), np.uint8)
+        sc[i] = sc[i - 10]
+    pts2[50:60] = pts2[60:70]
+    sc[100:110] = 0xFF
+    sc[110:120, 31] |= 0x80
+    assert ctx.msm(curve, sc, pts2) == oracle.msm(curve, sc, pts2)
+    # a sum that cancels to the identity: s*P + s*(-P)
+    P = pts[:1].copy()
+    mP = P.copy()
+    y = int.from_bytes(P[0, 32:].tobytes(), "little")
+    mP[0, 32:] = np.frombuffer(((F - y) % F).to_bytes(32, "little"), np.uint8)
+    two = np.concatenate([sc[:1], sc[:1]])
+    assert ctx.msm(curve, two, np.concatenate([P, mP])) == bytes(32)
+
+
+@pytest.mark.parametrize("curve", [0, 1])
+def test_every_window_width(ctx, curve):
+    """the recode is compiled per window width: exercise each c against the oracle"""
+    n = 700
+    sc, pts, _ = oracle_inputs(curve, n, seed=123, edge_fraction=0.05)
+    sc[:7] = 0xFF
+    want = oracle.msm(curve, sc, pts)
+    try:
+        for c in range(4, 21):
+            ctx.set_window(curve, 1, 1 << 30, c)
+            assert ctx.msm(curve, sc, pts) == want, f"c={c}"
+            ctx.set_window(curve, 0, 0, 0)
+    finally:
+        ctx.set_window(curve, 0, 0, 0)
+
+
+@pytest.mark.parametrize("curve", [0, 1])
+def test_reference_struct_inputs_and_outputs(ctx, curve):
+    """helios_jacobian inputs with Z != 1, Z == 0 and lazy limbs; Jacobian output"""
+    import helioselene_gb300 as hs
+    n = 500
+    sc, pts, _ = oracle_inputs(curve, n, seed=8)
+    F = pyref.CURVES["helios" if curve == 0 else "selene"].F
+    rng = random.Random(4)
+    recs, j96 = [], []
+    for i in range(n):
+        x = int.from_bytes(pts[i, :32].tobytes(), "little")
+        y = int.from_bytes(pts[i, 32:].tobytes(), "little")
+        if i % 11 == 4:
+            X, Y, Z = 1, 1, 0
+        elif i % 3 == 0:
+            X, Y, Z = x, y, 1
+        else:
+            z = rng.randrange(2, F)
+            X, Y, Z = x * z * z % F, y * z * z * z % F, z
+        limbs = hs.int_to_fe51(X) + hs.int_to_fe51(Y) + hs.int_to_fe51(Z)
+        if i % 5 == 1 and limbs[1] > 0:
+            limbs[1] -= 1
+            limbs[0] += 1 << 51
+        recs.append(limbs)
+        j96.append(X.to_bytes(32, "little") + Y.to_bytes(32, "little") + Z.to_bytes(32, "little"))
+    arr = np.array(recs, dtype=np.uint64).view(np.uint8)
+    want = oracle.msm_jac(curve, sc, b"".join(j96))
+    assert ctx.msm(curve, sc, arr, HS_JAC51, HS_COMPRESSED) == want
+    out = ctx.msm(curve, sc, arr, HS_JAC51, HS_JAC51)
+    assert jac51_to_bytes(curve, out) == want
+    aff = ctx.msm(curve, sc, arr, HS_JAC51, HS_AFF)
+    assert oracle.compress(curve, aff).tobytes() == want
+    # batch to affine, both output layouts
+    got = ctx.batch_to_affine(curve, arr, HS_AFF)
+    assert (got == oracle.batch_to_affine(curve, b"".join(j96))).all()
+    got51 = ctx.batch_to_affine(curve, arr, HS_AFF51).view(np.uint64).reshape(n, 10)
+    for i in range(0, n, 37):
+        x = hs.fe51_to_int(got51[i, :5])
+        y = hs.fe51_to_int(got51[i, 5:])
+        assert x.to_bytes(32, "little") + y.to_bytes(32, "little") == got[64 * i:64 * i + 64].tobytes()
+    # compression of Jacobian records
+    comp = ctx.compress(curve, arr, HS_JAC51)
+    assert (comp == oracle.compress_jac(curve, b"".join(j96))).all()
+
+
+@pytest.mark.parametrize("curve", [0, 1])
+def test_pedersen_random(ctx, curve):
+    for n in (1, 16, 1000, 5000):
+        sc, pts, _ = oracle_inputs(curve, n + 1, seed=n)
+        want = oracle.pedersen(curve, sc[0], pts[0], sc[1:], pts[1:])
+        assert ctx.pedersen(curve, sc[0], pts[0], sc[1:], pts[1:]) == want
+
+
+@pytest.mark.parametrize("curve", [0, 1])
+def test_map_to_curve_matches_oracle(ctx, curve):
+    from helioselene_gb300.workload import random_field_bytes
+    u = random_field_bytes(np.random.default_rng(curve + 40), 2048)
+    u[0] = 0
+    u[1] = 0xFF  # bit 255 masked by the map
+    got = ctx.map_to_curve(curve, u, HS_AFF)
+    assert (got == oracle.map_to_curve(curve, u.reshape(-1))).all()
+
+
+@pytest.mark.parametrize("curve", [0, 1])
+def test_reference_signature_dropins(ctx, curve):
+    """hs_{helios,selene}_msm_vartime with the reference's argument list"""
+    import helioselene_gb300 as hs
+    lib = hs.load()
+    n = 64
+    sc, pts, _ = oracle_inputs(curve, n, seed=64)
+    recs = hs.affine64_to_jac51(pts)
+    res = np.zeros(15, np.uint64)
+    fn = lib.hs_helios_msm_vartime if curve == 0 else lib.hs_selene_msm_vartime
+    fn(res.ctypes.data, sc.ctypes.data, recs.ctypes.data, n)
+    assert jac51_to_bytes(curve, res.tobytes()) == oracle.msm(curve, sc, pts)
+    # n == 0: identity (1:1:0)
+    fn(res.ctypes.data, sc.ctypes.data, recs.ctypes.data, 0)
+    assert list(res) == [1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0]
+    # Pedersen drop-in
+    ped = lib.hs_helios_pedersen_commit if curve == 0 else lib.hs_selene_pedersen_commit
+    ped(res.ctypes.data, sc[0].ctypes.data, recs[:120].ctypes.data, np.ascontiguousarray(sc[1:]).ctypes.data,
+        np.ascontiguousarray(recs[120:]).ctypes.data, n - 1)
+    assert jac51_to_bytes(curve, res.tobytes()) == oracle.pedersen(curve, sc[0], pts[0], sc[1:], pts[1:])
+
+
+@pytest.mark.parametrize("curve", [0, 1])
+def test_point_api_mirror(ctx, curve):
+    import helioselene_gb300 as hs
+    Pt = hs.HeliosPoint if curve == 0 else hs.SelenePoint
+    n = 40
+    sc, pts, _ = oracle_inputs(curve, n, seed=9)
+    points = [Pt.from_affine_bytes(pts[i]) for i in range(n)]
+    scalars = [sc[i].tobytes() for i in range(n)]
+    r = Pt.multi_scalar_mul(scalars, points, ctx)
+    assert r.to_bytes(ctx) == oracle.msm(curve, sc, pts)
+    assert Pt.multi_scalar_mul([], [], ctx).to_bytes(ctx) == bytes(32)
+    c = Pt.pedersen_commit(scalars[0], points[0], scalars[1:], points[1:], ctx)
+    assert c.to_bytes(ctx) == oracle.pedersen(curve, sc[0], pts[0], sc[1:], pts[1:])
+    aff = (hs.helios_batch_to_affine if curve == 0 else hs.selene_batch_to_affine)(points[:5], ctx)
+    assert b"".join(aff) == pts[:5].tobytes()
+
+
+@pytest.mark.parametrize("curve", [0, 1])
+def test_msm_large_vs_threaded_oracle(ctx, curve):
+    """n = 2^18 with edge slices, against the oracle run on all host cores"""
+    import helioselene_gb300 as hs
+    from helioselene_gb300.workload import make_workload
+    n = 1 << 18
+    w = make_workload(curve, n, seed=2024 + curve, edge_fraction=0.01)
+    pts = ctx.map_to_curve(curve, w.u, HS_AFF)
+    # the GPU SWU map is itself checked against the oracle on a sample
+    idx = np.arange(0, n, 997)
+    assert (pts.reshape(n, 64)[idx] == oracle.map_to_curve(curve, w.u[idx].reshape(-1)).reshape(-1, 64)).all()
+    got = ctx.msm(curve, w.scalars, pts)
+    assert got == oracle.msm_mt(curve, w.scalars, pts, oracle.default_threads())
+
+
+@pytest.mark.parametrize("curve", [0, 1])
+def test_linearity_at_full_size(ctx, curve):
+    """size-independent property at n = 2^20: MSM(a) + MSM(b) == MSM(a + b mod order)"""
+    from helioselene_gb300.workload import ORDER, make_workload, random_scalars
+    n = 1 << 20
+    w = make_workload(curve, n, seed=31337 + curve, edge_fraction=0.01)
+    pts = ctx.map_to_curve(curve, w.u, HS_AFF)
+    a = w.scalars
+    b = random_scalars(np.random.default_rng(5), n, ORDER[curve])
+    order = ORDER[curve]
+    ai = a.view(np.uint64).reshape(n, 4)
+    bi = b.view(np.uint64).reshape(n, 4)
+    s = np.zeros((n, 4), np.uint64)
+    carry = np.zeros(n, np.uint64)
+    for i in range(4):
+        t = ai[:, i] + bi[:, i]
+        c1 = (t < ai[:, i]).astype(np.uint64)
+        t2 = t + carry
+        c2 = (t2 < t).astype(np.uint64)
+        s[:, i] = t2
+        carry = c1 | c2
+    from helioselene_gb300.workload import below
+    over = ~below(s, order)
+    o = np.array([(order >> (64 * i)) & (2**64 - 1) for i in range(4)], dtype=np.uint64)
+    borrow = np.zeros(n, np.uint64)
+    for i in range(4):
+        t = s[over, i] - o[i]
+        b1 = (s[over, i] < o[i]).astype(np.uint64)
+        t2 = t - borrow[over]
+        b2 = (t < borrow[over]).astype(np.uint64)
+        s[over, i] = t2
+        borrow[over] = b1 | b2
+    ra = ctx.msm(curve, a, pts, HS_AFF, HS_AFF)
+    rb = ctx.msm(curve, b, pts, HS_AFF, HS_AFF)
+    rs = ctx.msm(curve, s.view(np.uint8).reshape(n, 32), pts, HS_AFF, HS_COMPRESSED)
+    one = np.zeros((2, 32), np.uint8)
+    one[:, 0] = 1
+    pair = np.frombuffer(ra + rb, np.uint8)
+    assert ctx.msm(curve, one, pair) == rs
+    assert oracle.compress(curve, oracle.point_add(curve, ra, rb)).tobytes() == rs
