@@ -52,6 +52,7 @@ SIGNATURES = {
     "hs_profile_read": (_int, [_vp, _c.POINTER(_c.c_double), _c.POINTER(_c.c_uint64), _c.POINTER(_c.c_uint64),
                                _int]),
     "hs_measure_imad_peak": (_int, [_vp, _c.POINTER(_c.c_double)]),
+    "hs_field_op": (_int, [_vp, _int, _int, _vp, _vp, _sz, _vp]),
     "hs_helios_msm_vartime": (None, [_vp, _vp, _vp, _sz]),
     "hs_selene_msm_vartime": (None, [_vp, _vp, _vp, _sz]),
     "hs_helios_pedersen_commit": (None, [_vp, _vp, _vp, _vp, _vp, _sz]),

@@ -102,6 +102,15 @@ class Context:
         self._check(self._lib.hs_measure_imad_peak(self._h, ctypes.byref(v)), "hs_measure_imad_peak")
         return v.value
 
+    def field_op(self, field: int, op: int, a, b=None) -> np.ndarray:
+        """Element-wise device field arithmetic (0 mul, 1 sqr, 2 add, 3 sub, 4 canon, 5 inv, 6 neg)."""
+        x = _u8(a)
+        y = _u8(b) if b is not None else x
+        n = x.size // 32
+        out = np.zeros(32 * n, np.uint8)
+        self._check(self._lib.hs_field_op(self._h, field, op, _ptr(x), _ptr(y), n, _ptr(out)), "hs_field_op")
+        return out
+
     # -- MSM --
     def msm(self, curve: int, scalars, points, point_fmt: int = L.FMT_AFFINE,
             out_fmt: int = L.FMT_COMPRESSED) -> bytes:

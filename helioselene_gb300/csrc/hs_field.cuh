@@ -99,6 +99,72 @@ __device__ __forceinline__ void mul_wide_8x8(uint32_t t[16], const uint32_t a[8]
     }
 }
 
+// Squaring: the 28 cross products a_i a_j (i < j) once, doubled, plus the 8
+// squares -- 72 half-products instead of 128.  Cross products go in rows
+// (row i: a_i * a_j, j > i), split by the parity of j so that each chain
+// covers contiguous words; the partial sum after row i is below 2^(32(i+9)),
+// so carries are propagated only up to word i+8.  Single-instruction asm
+// statements are volatile to keep the carry chains in order.
+__device__ __forceinline__ void sqr_wide_8(uint32_t t[16], const uint32_t a[8])
+{
+#pragma unroll
+    for (int k = 0; k < 16; k++)
+        t[k] = 0;
+#pragma unroll
+    for (int i = 0; i < 7; i++) {
+#pragma unroll
+        for (int par = 1; par <= 2; par++) {
+            const int j0 = i + par;
+            if (j0 > 7)
+                continue;
+            int top = 0;
+#pragma unroll
+            for (int j = j0; j <= 7; j += 2) {
+                if (j == j0)
+                    asm volatile("mad.lo.cc.u32 %0, %1, %2, %0;" : "+r"(t[i + j]) : "r"(a[i]), "r"(a[j]));
+                else
+                    asm volatile("madc.lo.cc.u32 %0, %1, %2, %0;" : "+r"(t[i + j]) : "r"(a[i]), "r"(a[j]));
+                asm volatile("madc.hi.cc.u32 %0, %1, %2, %0;" : "+r"(t[i + j + 1]) : "r"(a[i]), "r"(a[j]));
+                top = i + j + 1;
+            }
+#pragma unroll
+            for (int k = top + 1; k <= i + 8; k++) {
+                if (k < i + 8)
+                    asm volatile("addc.cc.u32 %0, %0, 0;" : "+r"(t[k]));
+                else
+                    asm volatile("addc.u32 %0, %0, 0;" : "+r"(t[k]));
+            }
+        }
+    }
+    // double the cross sum (< 2^511, so nothing leaves word 15)
+#pragma unroll
+    for (int k = 15; k > 0; k--)
+        t[k] = __funnelshift_l(t[k - 1], t[k], 1);
+    t[0] <<= 1;
+    // add the squares a_i^2 at words 2i, 2i+1
+    asm("{\n\t"
+        "mad.lo.cc.u32  %0, %16, %16, %0;\n\t"
+        "madc.hi.cc.u32 %1, %16, %16, %1;\n\t"
+        "madc.lo.cc.u32 %2, %17, %17, %2;\n\t"
+        "madc.hi.cc.u32 %3, %17, %17, %3;\n\t"
+        "madc.lo.cc.u32 %4, %18, %18, %4;\n\t"
+        "madc.hi.cc.u32 %5, %18, %18, %5;\n\t"
+        "madc.lo.cc.u32 %6, %19, %19, %6;\n\t"
+        "madc.hi.cc.u32 %7, %19, %19, %7;\n\t"
+        "madc.lo.cc.u32 %8, %20, %20, %8;\n\t"
+        "madc.hi.cc.u32 %9, %20, %20, %9;\n\t"
+        "madc.lo.cc.u32 %10, %21, %21, %10;\n\t"
+        "madc.hi.cc.u32 %11, %21, %21, %11;\n\t"
+        "madc.lo.cc.u32 %12, %22, %22, %12;\n\t"
+        "madc.hi.cc.u32 %13, %22, %22, %13;\n\t"
+        "madc.lo.cc.u32 %14, %23, %23, %14;\n\t"
+        "madc.hi.u32    %15, %23, %23, %15;\n\t"
+        "}"
+        : "+r"(t[0]), "+r"(t[1]), "+r"(t[2]), "+r"(t[3]), "+r"(t[4]), "+r"(t[5]), "+r"(t[6]), "+r"(t[7]),
+          "+r"(t[8]), "+r"(t[9]), "+r"(t[10]), "+r"(t[11]), "+r"(t[12]), "+r"(t[13]), "+r"(t[14]), "+r"(t[15])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(a[4]), "r"(a[5]), "r"(a[6]), "r"(a[7]));
+}
+
 template <class P>
 struct Field {
     static constexpr uint32_t M0 = P::M[0], M1 = P::M[1], M2 = P::M[2], M3 = P::M[3];
@@ -378,7 +444,12 @@ struct Field {
         return reduce_wide(t);
     }
 
-    __device__ __forceinline__ static Fe sqr(const Fe &a) { return mul(a, a); }
+    __device__ __forceinline__ static Fe sqr(const Fe &a)
+    {
+        uint32_t t[16];
+        sqr_wide_8(t, a.w);
+        return reduce_wide(t);
+    }
 
     // canonical representative in [0, m): a < 2^256 = 2m + c
     __device__ __forceinline__ static Fe canon(const Fe &a)

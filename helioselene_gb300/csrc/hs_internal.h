@@ -62,6 +62,7 @@ struct MsmPlan {
     uint32_t L = 0;      // max entries per accumulation segment
     uint32_t max_entries = 0;
     uint32_t max_segs = 0;
+    uint32_t hist_blocks = 0;  // blocks of the segment-length histogram
     uint32_t m0 = 0;     // buckets per thread in the first reduction level
     uint32_t mr = 0;     // group size of the later reduction levels
 };
@@ -75,7 +76,9 @@ struct MsmBuffers {
     uint32_t *seg_off = nullptr;        // NB + 1, exclusive scan of segment counts
     uint32_t *scan_tmp = nullptr;       // per-block partials of the scan
     uint32_t *sorted = nullptr;         // max_entries: point index | sign << 31
-    uint2 *segs = nullptr;              // max_segs: (start, length)
+    uint4 *segs = nullptr;              // max_segs: (start, length, destination slot, 0), longest first
+    uint32_t *len_hist = nullptr;       // (L+1) x hist blocks: segment-length histogram, then its scan
+    uint32_t *len_scan = nullptr;       // exclusive scan of len_hist (+1 total)
     uint4 *seg_sum = nullptr;           // max_segs XYZZ sums (8 uint4 each)
     uint32_t *heavy = nullptr;          // NB heavy-bucket list
     uint32_t *heavy_n = nullptr;        // 1 counter
@@ -103,6 +106,8 @@ struct CurveOps {
     cudaError_t (*map_to_curve)(Context &ctx, const void *d_u, size_t n, uint4 *d_out);
     // any point format -> canonical Jacobian, 24 words per point
     cudaError_t (*to_jac24)(Context &ctx, const void *d_in, int fmt, size_t n, uint32_t *d_out);
+    // element-wise field op over n 32-byte values (validation hook)
+    cudaError_t (*field_op)(Context &ctx, int op, const void *d_a, const void *d_b, size_t n, void *d_out);
 };
 extern const CurveOps helios_ops;
 extern const CurveOps selene_ops;

@@ -68,10 +68,11 @@ __device__ __forceinline__ Xyzz load_xyzz(const uint4 *o)
 }
 
 // ---------------------------------------------------------------------------
-// 2. bucket accumulation: one thread per segment of <= L entries
+// 2. bucket accumulation: one thread per segment of <= L entries (segments come
+//    longest first, so the lanes of a warp do equal work)
 // ---------------------------------------------------------------------------
 template <class C>
-__global__ void __launch_bounds__(128) k_accumulate(const uint2 *__restrict__ segs, const uint32_t *__restrict__ seg_total,
+__global__ void __launch_bounds__(128) k_accumulate(const uint4 *__restrict__ segs, const uint32_t *__restrict__ seg_total,
                                                    const uint32_t *__restrict__ sorted, const uint4 *__restrict__ pts,
                                                    uint4 *__restrict__ seg_sum)
 {
@@ -79,7 +80,7 @@ __global__ void __launch_bounds__(128) k_accumulate(const uint2 *__restrict__ se
     using F = typename C::F;
     const uint32_t S = *seg_total;
     for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < S; s += gridDim.x * blockDim.x) {
-        const uint2 d = segs[s];
+        const uint4 d = segs[s];  // start, length, destination slot
         Xyzz acc = G::inf();
         for (uint32_t i = 0; i < d.y; i++) {
             const uint32_t e = __ldg(sorted + d.x + i);
@@ -91,7 +92,7 @@ __global__ void __launch_bounds__(128) k_accumulate(const uint2 *__restrict__ se
                 y = F::neg(y);
             G::add_affine(acc, x, y);
         }
-        store_xyzz(seg_sum + 8 * (size_t)s, acc);
+        store_xyzz(seg_sum + 8 * (size_t)d.z, acc);
     }
 }
 
@@ -681,9 +682,45 @@ cudaError_t to_jac24(Context &ctx, const void *d_in, int fmt, size_t n, uint32_t
 }
 
 template <class C>
+__global__ void k_field_op(int op, const uint4 *__restrict__ a, const uint4 *__restrict__ b, size_t n,
+                           uint4 *__restrict__ out)
+{
+    using F = typename C::F;
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const Fe x = load_fe(a + 2 * i);
+    const Fe y = (op == 2 || op == 3 || op == 0) ? load_fe(b + 2 * i) : F::zero();
+    Fe r;
+    switch (op) {
+    case 0: r = F::mul(x, y); break;
+    case 1: r = F::sqr(x); break;
+    case 2: r = F::add(x, y); break;
+    case 3: r = F::sub(x, y); break;
+    case 4: r = x; break;
+    case 5: r = F::inv(x); break;
+    default: r = F::neg(x); break;
+    }
+    store_fe(out + 2 * i, F::canon(r));
+}
+
+template <class C>
+cudaError_t field_op(Context &ctx, int op, const void *d_a, const void *d_b, size_t n, void *d_out)
+{
+    if (n == 0)
+        return cudaSuccess;
+    const int threads = 128;
+    k_field_op<C><<<(unsigned)((n + threads - 1) / threads), threads, 0, ctx.stream>>>(
+        op, (const uint4 *)d_a, (const uint4 *)d_b, n, (uint4 *)d_out);
+    HS_LAUNCH_CHECK(ctx);
+    return cudaSuccess;
+}
+
+template <class C>
 CurveOps make_ops()
 {
-    return CurveOps{&msm_tail<C>, &to_affine<C>, &to_affine_scratch, &format_out<C>, &map_to_curve<C>, &to_jac24<C>};
+    return CurveOps{&msm_tail<C>, &to_affine<C>,   &to_affine_scratch, &format_out<C>,
+                    &map_to_curve<C>, &to_jac24<C>, &field_op<C>};
 }
 
 }  // namespace hs

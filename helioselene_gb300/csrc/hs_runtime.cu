@@ -86,6 +86,8 @@ const CurveOps &curve_ops(int curve) { return curve == HS_SELENE ? selene_ops : 
 // ---------------------------------------------------------------------------
 // planning
 // ---------------------------------------------------------------------------
+static constexpr uint32_t SEG_HIST_THREADS = 256;
+
 static int model_window(size_t n)
 {
     // cost ~ W(c) * (n * madd + 2^(c-1) * 2 adds), madd ~ 10 M, add ~ 14 M
@@ -121,6 +123,7 @@ MsmPlan make_plan(const Context &ctx, int curve, size_t n)
     p.L = std::max<uint32_t>(16, std::min<uint32_t>(128, 2 * avg));
     p.max_entries = (uint32_t)std::max<size_t>(1, n * p.W);
     p.max_segs = p.max_entries / p.L + p.NB + 1;
+    p.hist_blocks = (p.NB + SEG_HIST_THREADS - 1) / SEG_HIST_THREADS;
     p.m0 = std::min<uint32_t>(8, p.B);
     p.mr = 8;
     return p;
@@ -136,9 +139,11 @@ size_t plan_bytes(const MsmPlan &p)
 {
     size_t b = 0;
     b += 3 * align256((size_t)(p.NB + 1) * 4);                  // counts, offsets, seg_off
-    b += align256((size_t)2 * scan_blocks(p.NB) * 4 + 64);      // scan partials
+    const size_t nh = (size_t)(p.L + 1) * p.hist_blocks;
+    b += align256((size_t)2 * scan_blocks((uint32_t)std::max<size_t>(p.NB, nh)) * 4 + 64);  // scan partials
+    b += 2 * align256((nh + 1) * 4);                            // segment-length histogram + scan
     b += align256((size_t)p.max_entries * 4);                   // sorted
-    b += align256((size_t)p.max_segs * 8);                      // segs
+    b += align256((size_t)p.max_segs * 16);                     // segs
     b += align256((size_t)p.max_segs * 128);                    // seg_sum
     b += align256((size_t)p.NB * 4) + 256;                      // heavy list + counter
     const size_t r0 = (size_t)p.W * (p.B / p.m0) * 128;
@@ -153,9 +158,12 @@ void carve(DeviceArena &a, const MsmPlan &p, MsmBuffers &b)
     b.counts = (uint32_t *)a.take((size_t)(p.NB + 1) * 4);
     b.offsets = (uint32_t *)a.take((size_t)(p.NB + 1) * 4);
     b.seg_off = (uint32_t *)a.take((size_t)(p.NB + 1) * 4);
-    b.scan_tmp = (uint32_t *)a.take((size_t)2 * scan_blocks(p.NB) * 4 + 64);
+    const size_t nh = (size_t)(p.L + 1) * p.hist_blocks;
+    b.scan_tmp = (uint32_t *)a.take((size_t)2 * scan_blocks((uint32_t)std::max<size_t>(p.NB, nh)) * 4 + 64);
+    b.len_hist = (uint32_t *)a.take((nh + 1) * 4);
+    b.len_scan = (uint32_t *)a.take((nh + 1) * 4);
     b.sorted = (uint32_t *)a.take((size_t)p.max_entries * 4);
-    b.segs = (uint2 *)a.take((size_t)p.max_segs * 8);
+    b.segs = (uint4 *)a.take((size_t)p.max_segs * 16);
     b.seg_sum = (uint4 *)a.take((size_t)p.max_segs * 128);
     b.heavy = (uint32_t *)a.take((size_t)p.NB * 4);
     b.heavy_n = (uint32_t *)a.take(4);
@@ -281,7 +289,8 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_a(const uint32_t *__restr
         const uint32_t idx = base + j;
         if (idx < NB) {
             offsets[idx] = pre.x;
-            seg_off[idx] = pre.y;
+            if (seg_off)
+                seg_off[idx] = pre.y;
         }
         pre.x += c[j];
         pre.y += s[j];
@@ -322,7 +331,8 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_b(uint32_t *__restrict__ 
     __syncthreads();
     if (threadIdx.x == 0) {
         *off_total = tot.x;
-        *seg_total = tot.y;
+        if (seg_total)
+            *seg_total = tot.y;
     }
 }
 
@@ -334,19 +344,60 @@ __global__ void k_scan_c(uint32_t *__restrict__ offsets, uint32_t *__restrict__ 
         return;
     const uint32_t blk = idx / SCAN_BLOCK;
     offsets[idx] += tmp[2 * blk];
-    seg_off[idx] += tmp[2 * blk + 1];
+    if (seg_off)
+        seg_off[idx] += tmp[2 * blk + 1];
 }
 
-__global__ void k_segments(const uint32_t *__restrict__ offsets, const uint32_t *__restrict__ seg_off, uint32_t NB,
-                           uint32_t L, uint2 *__restrict__ segs)
+// Segments (<= L entries of one bucket) are emitted longest first so that the
+// 32 lanes of a warp in k_accumulate get equal work: a per-block histogram of
+// segment lengths, a scan over (length descending, block), and a scatter
+// through block-local cursors.  Each descriptor carries its destination slot
+// seg_off[bucket] + j, so a bucket's partial sums stay contiguous.
+__global__ void __launch_bounds__(SEG_HIST_THREADS) k_seg_hist(const uint32_t *__restrict__ offsets, uint32_t NB,
+                                                              uint32_t L, uint32_t nblk, uint32_t *__restrict__ hist)
 {
+    extern __shared__ uint32_t h[];
+    for (uint32_t i = threadIdx.x; i <= L; i += blockDim.x)
+        h[i] = 0;
+    __syncthreads();
+    const uint32_t kb = blockIdx.x * blockDim.x + threadIdx.x;
+    if (kb < NB) {
+        const uint32_t cnt = offsets[kb + 1] - offsets[kb];
+        const uint32_t nfull = cnt / L, rem = cnt % L;
+        if (nfull)
+            atomicAdd(&h[L], nfull);
+        if (rem)
+            atomicAdd(&h[rem], 1u);
+    }
+    __syncthreads();
+    for (uint32_t len = threadIdx.x; len <= L; len += blockDim.x)
+        hist[(size_t)(L - len) * nblk + blockIdx.x] = h[len];
+}
+
+__global__ void __launch_bounds__(SEG_HIST_THREADS) k_seg_scatter(const uint32_t *__restrict__ offsets,
+                                                                 const uint32_t *__restrict__ seg_off, uint32_t NB,
+                                                                 uint32_t L, uint32_t nblk,
+                                                                 const uint32_t *__restrict__ hist_scan,
+                                                                 uint4 *__restrict__ segs)
+{
+    extern __shared__ uint32_t cur[];
+    for (uint32_t len = threadIdx.x; len <= L; len += blockDim.x)
+        cur[len] = hist_scan[(size_t)(L - len) * nblk + blockIdx.x];
+    __syncthreads();
     const uint32_t kb = blockIdx.x * blockDim.x + threadIdx.x;
     if (kb >= NB)
         return;
     const uint32_t start = offsets[kb], cnt = offsets[kb + 1] - start;
-    uint32_t s = seg_off[kb];
-    for (uint32_t j = 0; j < cnt; j += L, s++)
-        segs[s] = make_uint2(start + j, min(L, cnt - j));
+    const uint32_t nfull = cnt / L, rem = cnt % L, dest = seg_off[kb];
+    if (nfull) {
+        const uint32_t p = atomicAdd(&cur[L], nfull);
+        for (uint32_t j = 0; j < nfull; j++)
+            segs[p + j] = make_uint4(start + j * L, L, dest + j, 0u);
+    }
+    if (rem) {
+        const uint32_t p = atomicAdd(&cur[rem], 1u);
+        segs[p] = make_uint4(start + nfull * L, rem, dest + nfull, 0u);
+    }
 }
 
 template <int CB>
@@ -413,7 +464,22 @@ cudaError_t launch_sort(Context &ctx, const MsmPlan &p, const MsmBuffers &b)
         return e;
     if ((e = recode_dispatch(ctx, p, b, true)) != cudaSuccess)
         return e;
-    k_segments<<<(p.NB + 255) / 256, 256, 0, st>>>(b.offsets, b.seg_off, p.NB, p.L, b.segs);
+    // segments, longest first
+    const uint32_t nh = (p.L + 1) * p.hist_blocks;
+    const size_t hsm = (size_t)(p.L + 1) * 4;
+    k_seg_hist<<<p.hist_blocks, SEG_HIST_THREADS, hsm, st>>>(b.offsets, p.NB, p.L, p.hist_blocks, b.len_hist);
+    HS_LAUNCH_CHECK(ctx);
+    const uint32_t nblk2 = scan_blocks(nh);
+    if (nblk2 > SCAN_BLOCK)
+        return cudaErrorInvalidValue;
+    k_scan_a<<<nblk2, SCAN_THREADS, 0, st>>>(b.len_hist, nh, 1u, b.len_scan, nullptr, b.scan_tmp);
+    HS_LAUNCH_CHECK(ctx);
+    k_scan_b<<<1, SCAN_THREADS, 0, st>>>(b.scan_tmp, nblk2, b.len_scan + nh, nullptr);
+    HS_LAUNCH_CHECK(ctx);
+    k_scan_c<<<(nh + 255) / 256, 256, 0, st>>>(b.len_scan, nullptr, nh, b.scan_tmp);
+    HS_LAUNCH_CHECK(ctx);
+    k_seg_scatter<<<p.hist_blocks, SEG_HIST_THREADS, hsm, st>>>(b.offsets, b.seg_off, p.NB, p.L, p.hist_blocks,
+                                                                 b.len_scan, b.segs);
     HS_LAUNCH_CHECK(ctx);
     return cudaSuccess;
 }
@@ -831,6 +897,28 @@ int hs_map_to_curve(hs_context *h, int curve, const uint8_t *u, size_t n, void *
         HS_CU(cudaMemcpyAsync(out, d_o, n * fmt_bytes(out_fmt), cudaMemcpyDeviceToHost, st), "D2H");
     }
     HS_CU(cudaStreamSynchronize(st), "map to curve");
+    return HS_OK;
+}
+
+int hs_field_op(hs_context *h, int field, int op, const uint8_t *a, const uint8_t *b, size_t n, uint8_t *out)
+{
+    const bool binary = op == 0 || op == 2 || op == 3;
+    if (!h || !valid_curve(field) || op < 0 || op > 6 || (n && (!a || !out || (binary && !b))))
+        return HS_EINVAL;
+    if (n == 0)
+        return HS_OK;
+    Context &ctx = h->c;
+    std::lock_guard<std::mutex> lk(ctx.mu);
+    DeviceGuard g(ctx.device);
+    HS_CU(ctx.arena.reserve(3 * align256(n * 32) + 1024), "workspace allocation");
+    void *da = ctx.arena.take(n * 32), *db = ctx.arena.take(n * 32), *dout = ctx.arena.take(n * 32);
+    cudaStream_t st = ctx.stream;
+    HS_CU(cudaMemcpyAsync(da, a, n * 32, cudaMemcpyHostToDevice, st), "H2D");
+    if (binary)
+        HS_CU(cudaMemcpyAsync(db, b, n * 32, cudaMemcpyHostToDevice, st), "H2D");
+    HS_CU(curve_ops(field).field_op(ctx, op, da, db, n, dout), "field op");
+    HS_CU(cudaMemcpyAsync(out, dout, n * 32, cudaMemcpyDeviceToHost, st), "D2H");
+    HS_CU(cudaStreamSynchronize(st), "field op");
     return HS_OK;
 }
 

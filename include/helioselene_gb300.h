@@ -174,6 +174,13 @@ int hs_profile_read(hs_context *ctx, double *accumulate_ms, uint64_t *accumulate
  * multiply-add instructions per second (one 32x32 half-product each). */
 int hs_measure_imad_peak(hs_context *ctx, double *imad_per_s);
 
+/* Field arithmetic on the device, for validation of the field layer:
+ * field HS_HELIOS selects F_p (2^255-19), HS_SELENE selects F_q (2^255-gamma).
+ * op: 0 mul, 1 square, 2 add, 3 sub, 4 canonical reduce, 5 invert (0 -> 0), 6 negate.
+ * a, b, out: n little-endian 32-byte values in host memory (b unused for unary ops);
+ * inputs may be any 256-bit value, outputs are canonical. */
+int hs_field_op(hs_context *ctx, int field, int op, const uint8_t *a, const uint8_t *b, size_t n, uint8_t *out);
+
 /* ---- library info ---- */
 int hs_abi_version(void);
 
