@@ -63,8 +63,7 @@ struct MsmPlan {
     uint32_t max_entries = 0;
     uint32_t max_segs = 0;
     uint32_t hist_blocks = 0;  // blocks of the segment-length histogram
-    uint32_t m0 = 0;     // buckets per thread in the first reduction level
-    uint32_t mr = 0;     // group size of the later reduction levels
+    uint32_t m0 = 0;     // buckets per thread in the bucket reduction
 };
 
 // Device buffers of one MSM (all carved from the arena).
@@ -82,7 +81,8 @@ struct MsmBuffers {
     uint4 *seg_sum = nullptr;           // max_segs XYZZ sums (8 uint4 each)
     uint32_t *heavy = nullptr;          // NB heavy-bucket list
     uint32_t *heavy_n = nullptr;        // 1 counter
-    uint4 *redA = nullptr, *redR = nullptr, *redA2 = nullptr, *redR2 = nullptr;
+    uint4 *redA = nullptr;              // W * (B / m0) weighted group sums
+    uint4 *redR = nullptr;              // W window sums
     uint32_t *out_jac = nullptr;        // 24 words: canonical Jacobian X, Y, Z
 };
 

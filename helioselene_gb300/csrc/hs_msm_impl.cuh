@@ -10,10 +10,10 @@
 //      thread sums one segment of affine bases into an XYZZ point;
 //   3. k_merge_light / k_merge_heavy: buckets with several segments are folded
 //      (sequentially when few, by a block-wide tree when many);
-//   4. k_reduce0 / k_reduce_level: per window S = sum_j (j+1) B_j by running
-//      sums over groups of buckets, recursively over the group results;
+//   4. k_reduce_abs / k_window_sum: per window S = sum_j (j+1) B_j by running
+//      sums over groups of buckets carrying absolute weights, then a tree sum;
 //   5. k_combine: Horner over the windows, S = 2^c S + S_k (the reference's
-//      per-window doublings, :285-289), result as canonical Jacobian.
+//      per-window doublings, :285-289) on one warp, result as canonical Jacobian.
 #pragma once
 
 #include "hs_curve.cuh"
@@ -156,13 +156,30 @@ __global__ void __launch_bounds__(HEAVY_THREADS) k_merge_heavy(const uint32_t *_
 // ---------------------------------------------------------------------------
 // 4. bucket reduction: S_k = sum_j (j+1) * B_{k,j}
 // ---------------------------------------------------------------------------
-// Level 0: thread (k, t) owns buckets [t*m, (t+1)*m) of window k and returns
-//   A = sum_j (j - t*m + 1) B_j   and   R = sum_j B_j
-// (running sum from the top, as the reference does over the whole window,
-// helios_msm_vartime.cpp:334-361), so that S_k = sum_t (A_t + t*m*R_t).
+// Thread (k, t) owns buckets [lo, lo+m) of window k, lo = t*m.  A running sum
+// from the top (as the reference does over the whole window,
+// helios_msm_vartime.cpp:334-361) gives acc = sum_j (j - lo + 1) B_j and
+// run = sum_j B_j; the thread then adds lo*run (double-and-add on t, then
+// log2(m) doublings) so that its output carries absolute weights and the
+// window sum is a plain sum: S_k = sum_t A_t.
 template <class C>
-__global__ void k_reduce0(const uint32_t *__restrict__ seg_off, const uint4 *__restrict__ seg_sum, uint32_t W,
-                          uint32_t B, uint32_t m, uint4 *__restrict__ outA, uint4 *__restrict__ outR)
+__device__ Xyzz mul_small(const Xyzz &P, uint32_t t)
+{
+    using G = Group<C>;
+    if (t == 0 || G::is_inf(P))
+        return G::inf();
+    Xyzz Q = P;
+    for (int b = 30 - __clz(t); b >= 0; b--) {
+        Q = G::dbl(Q);
+        if ((t >> b) & 1u)
+            Q = G::add(Q, P);
+    }
+    return Q;
+}
+
+template <class C>
+__global__ void k_reduce_abs(const uint32_t *__restrict__ seg_off, const uint4 *__restrict__ seg_sum, uint32_t W,
+                             uint32_t B, uint32_t m, uint32_t log2m, uint4 *__restrict__ outA)
 {
     using G = Group<C>;
     const uint32_t T = B / m;
@@ -178,40 +195,47 @@ __global__ void k_reduce0(const uint32_t *__restrict__ seg_off, const uint4 *__r
             run = G::add(run, load_xyzz(seg_sum + 8 * (size_t)s0));
         acc = G::add(acc, run);
     }
-    store_xyzz(outA + 8 * (size_t)tid, acc);
-    store_xyzz(outR + 8 * (size_t)tid, run);
+    Xyzz off = mul_small<C>(run, t);
+    for (uint32_t i = 0; i < log2m; i++)
+        off = G::dbl(off);
+    store_xyzz(outA + 8 * (size_t)tid, G::add(acc, off));
 }
 
-// Level l: the window sum is S = sum_t (A_t + t*M*R_t) over T pairs.  Group
-// t = u*m + r:  A'_u = sum_r A + M * sum_r r*R,  R'_u = sum_r R,  M' = m*M.
+// S_k = sum over the T outputs of window k: one block per window, strided
+// per-thread sums, then a shared-memory tree.
+constexpr int WSUM_THREADS = 256;
+
 template <class C>
-__global__ void k_reduce_level(const uint4 *__restrict__ inA, const uint4 *__restrict__ inR, uint32_t W, uint32_t T,
-                               uint32_t m, uint32_t log2M, uint4 *__restrict__ outA, uint4 *__restrict__ outR)
+__global__ void __launch_bounds__(WSUM_THREADS) k_window_sum(const uint4 *__restrict__ inA, uint32_t T,
+                                                            uint4 *__restrict__ S)
 {
     using G = Group<C>;
-    const uint32_t U = T / m;
-    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-    if (tid >= W * U)
-        return;
-    const uint32_t k = tid / U, u = tid % U;
-    const size_t base = (size_t)k * T + (size_t)u * m;
-    Xyzz run = G::inf(), acc = G::inf(), asum = G::inf();
-    for (int r = (int)m - 1; r >= 1; r--) {
-        run = G::add(run, load_xyzz(inR + 8 * (base + r)));
-        acc = G::add(acc, run);
-        asum = G::add(asum, load_xyzz(inA + 8 * (base + r)));
+    __shared__ uint4 sh[WSUM_THREADS * 8];
+    const uint32_t k = blockIdx.x;
+    Xyzz acc = G::inf();
+    for (uint32_t i = threadIdx.x; i < T; i += WSUM_THREADS)
+        acc = G::add(acc, load_xyzz(inA + 8 * ((size_t)k * T + i)));
+    store_xyzz(sh + 8 * threadIdx.x, acc);
+    __syncthreads();
+    for (uint32_t stride = WSUM_THREADS / 2; stride > 0; stride >>= 1) {
+        if (threadIdx.x < stride)
+            store_xyzz(sh + 8 * threadIdx.x,
+                       G::add(load_xyzz(sh + 8 * threadIdx.x), load_xyzz(sh + 8 * (threadIdx.x + stride))));
+        __syncthreads();
     }
-    run = G::add(run, load_xyzz(inR + 8 * base));
-    asum = G::add(asum, load_xyzz(inA + 8 * base));
-    for (uint32_t i = 0; i < log2M; i++)
-        acc = G::dbl(acc);
-    store_xyzz(outA + 8 * (size_t)tid, G::add(asum, acc));
-    store_xyzz(outR + 8 * (size_t)tid, run);
+    if (threadIdx.x == 0)
+        store_xyzz(S + 8 * (size_t)k, load_xyzz(sh));
 }
 
 // ---------------------------------------------------------------------------
 // 5. window combination (Horner) -> canonical Jacobian
 // ---------------------------------------------------------------------------
+// The 256 doublings of the Horner chain are inherently sequential, so each
+// doubling and addition is spread over the lanes of one warp: in every stage
+// the active lanes compute one independent product each (operands picked from
+// a shared-memory slot file by lane), with the linear steps in between done
+// by lane 0.  This turns the 9 (dbl) and 14 (add) sequential products into 3
+// and 4 product stages.
 template <class C>
 __device__ void store_jacobian_canon(uint32_t *out, const Xyzz &p)
 {
@@ -230,19 +254,181 @@ __device__ void store_jacobian_canon(uint32_t *out, const Xyzz &p)
     }
 }
 
+enum Slot : int {
+    sX, sY, sZZ, sZZZ,          // running total
+    sX2, sY2, sZZ2, sZZZ2,      // addend
+    sU, sV, sA, sB, sT, sW, sS, sM, sM2, sD, sYa, sYb, sXn, sZZn, sZZZn,
+    sU1, sU2, sS1, sS2, sZ12, sZZZ12, sP, sR, sPP, sRR, sPPP, sQ,
+    sZERO, sNSLOTS
+};
+
+struct SlotFile {
+    Fe f[sNSLOTS];
+    int flag;
+};
+
+// every lane < width computes f[dst[lane]] = f[a[lane]] * f[b[lane]]
 template <class C>
-__global__ void k_combine(const uint4 *__restrict__ S, uint32_t W, uint32_t c, uint32_t *__restrict__ out)
+__device__ __forceinline__ void lane_products(SlotFile &sf, int width, const int *a, const int *b, const int *dst)
 {
-    using G = Group<C>;
-    if (blockIdx.x != 0 || threadIdx.x != 0)
+    using F = typename C::F;
+    const int lane = threadIdx.x & 31;
+    __syncwarp();
+    if (lane < width) {
+        const Fe x = sf.f[a[lane]], y = sf.f[b[lane]];
+        const Fe r = F::mul(x, y);
+        sf.f[dst[lane]] = r;
+    }
+    __syncwarp();
+}
+
+template <class C>
+__device__ void coop_dbl(SlotFile &sf)
+{
+    using F = typename C::F;
+    const int lane = threadIdx.x & 31;
+    if (F::is_exact_zero(sf.f[sZZ]))
+        return;  // identity
+    if (lane == 0) {
+        sf.f[sU] = F::dbl(sf.f[sY]);
+        sf.f[sA] = F::sub(sf.f[sX], sf.f[sZZ]);
+        sf.f[sB] = F::add(sf.f[sX], sf.f[sZZ]);
+    }
+    {
+        const int a[2] = {sU, sA}, b[2] = {sU, sB}, d[2] = {sV, sT};
+        lane_products<C>(sf, 2, a, b, d);  // V = U^2, T = (X-ZZ)(X+ZZ)
+    }
+    if (lane == 0) {
+        const Fe t = sf.f[sT];
+        sf.f[sM] = F::add(F::dbl(t), t);  // M = 3(X^2 - ZZ^2), a = -3
+    }
+    {
+        const int a[4] = {sU, sX, sM, sV}, b[4] = {sV, sV, sM, sZZ}, d[4] = {sW, sS, sM2, sZZn};
+        lane_products<C>(sf, 4, a, b, d);  // W = U V, S = X V, M^2, ZZ' = V ZZ
+    }
+    if (lane == 0) {
+        const Fe xn = F::sub(sf.f[sM2], F::dbl(sf.f[sS]));
+        sf.f[sXn] = xn;
+        sf.f[sD] = F::sub(sf.f[sS], xn);
+    }
+    {
+        const int a[3] = {sM, sW, sW}, b[3] = {sD, sZZZ, sY}, d[3] = {sYa, sZZZn, sYb};
+        lane_products<C>(sf, 3, a, b, d);  // M (S - X'), W ZZZ, W Y
+    }
+    if (lane == 0) {
+        sf.f[sX] = sf.f[sXn];
+        sf.f[sY] = F::sub(sf.f[sYa], sf.f[sYb]);
+        sf.f[sZZ] = sf.f[sZZn];
+        sf.f[sZZZ] = sf.f[sZZZn];
+        if (F::is_zero(sf.f[sZZ])) {  // y == 0: no such point on a prime-order curve, kept complete
+            sf.f[sX] = sf.f[sY] = sf.f[sZZ] = sf.f[sZZZ] = F::zero();
+        }
+    }
+    __syncwarp();
+}
+
+// total += addend (slots sX2..sZZZ2), complete
+template <class C>
+__device__ void coop_add(SlotFile &sf)
+{
+    using F = typename C::F;
+    const int lane = threadIdx.x & 31;
+    if (F::is_exact_zero(sf.f[sZZ2]))
         return;
-    Xyzz total = load_xyzz(S + 8 * (size_t)(W - 1));
+    if (F::is_exact_zero(sf.f[sZZ])) {
+        __syncwarp();
+        if (lane == 0) {
+            sf.f[sX] = sf.f[sX2];
+            sf.f[sY] = sf.f[sY2];
+            sf.f[sZZ] = sf.f[sZZ2];
+            sf.f[sZZZ] = sf.f[sZZZ2];
+        }
+        __syncwarp();
+        return;
+    }
+    {
+        const int a[6] = {sX, sX2, sY, sY2, sZZ, sZZZ}, b[6] = {sZZ2, sZZ, sZZZ2, sZZZ, sZZ2, sZZZ2};
+        const int d[6] = {sU1, sU2, sS1, sS2, sZ12, sZZZ12};
+        lane_products<C>(sf, 6, a, b, d);
+    }
+    if (lane == 0) {
+        sf.f[sP] = F::sub(sf.f[sU2], sf.f[sU1]);
+        sf.f[sR] = F::sub(sf.f[sS2], sf.f[sS1]);
+        sf.flag = F::is_zero(sf.f[sP]) ? (F::is_zero(sf.f[sR]) ? 1 : 2) : 0;
+    }
+    __syncwarp();
+    const int flag = sf.flag;
+    if (flag == 1) {  // same point: double
+        coop_dbl<C>(sf);
+        return;
+    }
+    if (flag == 2) {  // opposite points
+        if (lane == 0)
+            sf.f[sX] = sf.f[sY] = sf.f[sZZ] = sf.f[sZZZ] = F::zero();
+        __syncwarp();
+        return;
+    }
+    {
+        const int a[2] = {sP, sR}, b[2] = {sP, sR}, d[2] = {sPP, sRR};
+        lane_products<C>(sf, 2, a, b, d);
+    }
+    {
+        const int a[3] = {sP, sU1, sZ12}, b[3] = {sPP, sPP, sPP}, d[3] = {sPPP, sQ, sZZn};
+        lane_products<C>(sf, 3, a, b, d);
+    }
+    if (lane == 0) {
+        const Fe xn = F::sub(F::sub(sf.f[sRR], sf.f[sPPP]), F::dbl(sf.f[sQ]));
+        sf.f[sXn] = xn;
+        sf.f[sD] = F::sub(sf.f[sQ], xn);
+    }
+    {
+        const int a[3] = {sR, sS1, sZZZ12}, b[3] = {sD, sPPP, sPPP}, d[3] = {sYa, sYb, sZZZn};
+        lane_products<C>(sf, 3, a, b, d);
+    }
+    if (lane == 0) {
+        sf.f[sX] = sf.f[sXn];
+        sf.f[sY] = F::sub(sf.f[sYa], sf.f[sYb]);
+        sf.f[sZZ] = sf.f[sZZn];
+        sf.f[sZZZ] = sf.f[sZZZn];
+    }
+    __syncwarp();
+}
+
+template <class C>
+__global__ void __launch_bounds__(32) k_combine(const uint4 *__restrict__ S, uint32_t W, uint32_t c,
+                                               uint32_t *__restrict__ out)
+{
+    __shared__ SlotFile sf;
+    const int lane = threadIdx.x & 31;
+    if (lane == 0) {
+        const Xyzz top = load_xyzz(S + 8 * (size_t)(W - 1));
+        sf.f[sX] = top.X;
+        sf.f[sY] = top.Y;
+        sf.f[sZZ] = top.ZZ;
+        sf.f[sZZZ] = top.ZZZ;
+    }
+    __syncwarp();
     for (int k = (int)W - 2; k >= 0; k--) {
         for (uint32_t d = 0; d < c; d++)
-            total = G::dbl(total);
-        total = G::add(total, load_xyzz(S + 8 * (size_t)k));
+            coop_dbl<C>(sf);
+        if (lane == 0) {
+            const Xyzz a = load_xyzz(S + 8 * (size_t)k);
+            sf.f[sX2] = a.X;
+            sf.f[sY2] = a.Y;
+            sf.f[sZZ2] = a.ZZ;
+            sf.f[sZZZ2] = a.ZZZ;
+        }
+        __syncwarp();
+        coop_add<C>(sf);
     }
-    store_jacobian_canon<C>(out, total);
+    if (lane == 0) {
+        Xyzz t;
+        t.X = sf.f[sX];
+        t.Y = sf.f[sY];
+        t.ZZ = sf.f[sZZ];
+        t.ZZZ = sf.f[sZZZ];
+        store_jacobian_canon<C>(out, t);
+    }
 }
 
 template <class C>
@@ -271,37 +457,22 @@ cudaError_t msm_tail(Context &ctx, const MsmPlan &p, const MsmBuffers &b)
         k_merge_heavy<C><<<ctx.sm_count, HEAVY_THREADS, 0, st>>>(b.seg_off, b.heavy, b.heavy_n, b.seg_sum);
         HS_LAUNCH_CHECK(ctx);
     }
-    // 4. reduction levels
-    uint32_t T = p.B / p.m0;
+    // 4. bucket reduction with absolute weights, then one plain sum per window
+    const uint32_t T = p.B / p.m0;
     {
+        uint32_t log2m = 0;
+        while ((1u << log2m) < p.m0)
+            log2m++;
         const uint32_t total = p.W * T;
-        const int threads = 128;
-        k_reduce0<C><<<(total + threads - 1) / threads, threads, 0, st>>>(b.seg_off, b.seg_sum, p.W, p.B, p.m0,
-                                                                       b.redA, b.redR);
-        HS_LAUNCH_CHECK(ctx);
-    }
-    uint4 *inA = b.redA, *inR = b.redR, *outA = b.redA2, *outR = b.redR2;
-    uint32_t log2M = 0;
-    for (uint32_t m = p.m0; m > 1; m >>= 1)
-        log2M++;
-    while (T > 1) {
-        const uint32_t m = T < p.mr ? T : p.mr;
-        const uint32_t total = p.W * (T / m);
         const int threads = 64;
-        k_reduce_level<C><<<(total + threads - 1) / threads, threads, 0, st>>>(inA, inR, p.W, T, m, log2M, outA,
-                                                                            outR);
+        k_reduce_abs<C><<<(total + threads - 1) / threads, threads, 0, st>>>(b.seg_off, b.seg_sum, p.W, p.B, p.m0,
+                                                                           log2m, b.redA);
         HS_LAUNCH_CHECK(ctx);
-        for (uint32_t mm = m; mm > 1; mm >>= 1)
-            log2M++;
-        T /= m;
-        uint4 *ta = inA, *tr = inR;
-        inA = outA;
-        inR = outR;
-        outA = ta;
-        outR = tr;
+        k_window_sum<C><<<p.W, WSUM_THREADS, 0, st>>>(b.redA, T, b.redR);
+        HS_LAUNCH_CHECK(ctx);
     }
     // 5. Horner over windows
-    k_combine<C><<<1, 32, 0, st>>>(inA, p.W, (uint32_t)p.c, b.out_jac);
+    k_combine<C><<<1, 32, 0, st>>>(b.redR, p.W, (uint32_t)p.c, b.out_jac);
     HS_LAUNCH_CHECK(ctx);
     return cudaSuccess;
 }

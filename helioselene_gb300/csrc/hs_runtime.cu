@@ -124,8 +124,7 @@ MsmPlan make_plan(const Context &ctx, int curve, size_t n)
     p.max_entries = (uint32_t)std::max<size_t>(1, n * p.W);
     p.max_segs = p.max_entries / p.L + p.NB + 1;
     p.hist_blocks = (p.NB + SEG_HIST_THREADS - 1) / SEG_HIST_THREADS;
-    p.m0 = std::min<uint32_t>(8, p.B);
-    p.mr = 8;
+    p.m0 = std::min<uint32_t>(16, p.B);
     return p;
 }
 
@@ -147,8 +146,7 @@ size_t plan_bytes(const MsmPlan &p)
     b += align256((size_t)p.max_segs * 128);                    // seg_sum
     b += align256((size_t)p.NB * 4) + 256;                      // heavy list + counter
     const size_t r0 = (size_t)p.W * (p.B / p.m0) * 128;
-    const size_t r1 = (size_t)p.W * std::max<uint32_t>(1, p.B / p.m0 / p.mr) * 128;
-    b += 2 * align256(r0) + 2 * align256(r1);
+    b += align256(r0) + align256((size_t)p.W * 128);
     b += 256;                                                   // out_jac
     return b + 16 * 256;
 }
@@ -168,11 +166,8 @@ void carve(DeviceArena &a, const MsmPlan &p, MsmBuffers &b)
     b.heavy = (uint32_t *)a.take((size_t)p.NB * 4);
     b.heavy_n = (uint32_t *)a.take(4);
     const size_t r0 = (size_t)p.W * (p.B / p.m0) * 128;
-    const size_t r1 = (size_t)p.W * std::max<uint32_t>(1, p.B / p.m0 / p.mr) * 128;
     b.redA = (uint4 *)a.take(r0);
-    b.redR = (uint4 *)a.take(r0);
-    b.redA2 = (uint4 *)a.take(r1);
-    b.redR2 = (uint4 *)a.take(r1);
+    b.redR = (uint4 *)a.take((size_t)p.W * 128);
     b.out_jac = (uint32_t *)a.take(96);
 }
 
