@@ -164,6 +164,197 @@ def affine_to_jac51_fast(aff: np.ndarray, n: int) -> np.ndarray:
     return out.view(np.uint8).reshape(-1)
 
 
+def run_batched(hs, torch, device: str, local: int, steps: int) -> dict:
+    """Config 3: 1024 independent MSMs, sizes log-uniform in [64, 65536], curve
+    Bernoulli(0.5), as one batched launch sequence per curve (two contexts, so the
+    two curve groups overlap) against the plain per-call path on the same MSMs."""
+    from helioselene_gb300 import autotune
+    from helioselene_gb300.workload import ORDER, random_field_bytes, random_scalars
+    rng = np.random.default_rng(SEED + 3)
+    count = 1024
+    sizes = np.exp(rng.uniform(np.log(64), np.log(65536), count)).astype(np.int64)
+    curves = rng.integers(0, 2, count)
+    ctxs = [hs.Context(local), hs.Context(local)]
+    t0 = time.time()
+    tuned = autotune.load_or_tune(ctxs[0], cache=Path.home() / ".cache" / "helioselene_gb300_autotune.json",
+                                  n_max=65536, points_per_class=1 << 18, reps=2)
+    for c, name in ((hs.HELIOS, "helios"), (hs.SELENE, "selene")):
+        autotune.apply(ctxs[1], c, tuned[name])
+    tune_s = time.time() - t0
+    groups = {}
+    for curve in (hs.HELIOS, hs.SELENE):
+        idx = np.nonzero(curves == curve)[0]
+        sz = [int(sizes[i]) for i in idx]
+        total = sum(sz)
+        d_u = torch.from_numpy(random_field_bytes(rng, total).reshape(-1)).to(device)
+        d_pts = torch.empty(total * 64, dtype=torch.uint8, device=device)
+        d_sc = torch.from_numpy(random_scalars(rng, total, ORDER[curve]).reshape(-1)).to(device)
+        d_out = torch.empty(len(sz) * 120, dtype=torch.uint8, device=device)
+        d_out_plain = torch.empty(len(sz) * 120, dtype=torch.uint8, device=device)
+        torch.cuda.synchronize()
+        ctxs[0].map_to_curve_device(curve, d_u.data_ptr(), total, d_pts.data_ptr())
+        torch.cuda.synchronize()
+        offs = np.concatenate([[0], np.cumsum(sz)])
+        groups[curve] = {"idx": idx, "sizes": sz, "offs": offs, "d_sc": d_sc, "d_pts": d_pts, "d_out": d_out,
+                         "d_out_plain": d_out_plain}
+    streams = [torch.cuda.ExternalStream(c.stream, device=device) for c in ctxs]
+
+    def batched_once():
+        start = torch.cuda.Event(enable_timing=True)
+        ends = [torch.cuda.Event(enable_timing=True) for _ in streams]
+        start.record(streams[0])
+        streams[1].wait_event(start)
+        for k, curve in enumerate((hs.HELIOS, hs.SELENE)):
+            g = groups[curve]
+            ctxs[k].msm_batch_device(curve, g["sizes"], g["d_sc"].data_ptr(), g["d_pts"].data_ptr(),
+                                     g["d_out"].data_ptr(), hs.FMT_JACOBIAN51)
+            ends[k].record(streams[k])
+        for s in streams:
+            s.synchronize()
+        return max(start.elapsed_time(e) for e in ends)
+
+    batched_once()  # capture the graphs
+    times = [batched_once() for _ in range(max(3, steps))]
+    batched_ms = statistics.median(times)
+    # plain per-call path, the MSMs in stream order on one context, direct launches
+    plain_ctx = ctxs[0]
+    plain_ctx.set_graphs(False)
+    order = np.argsort(np.concatenate([groups[0]["idx"], groups[1]["idx"]]), kind="stable")
+    seq = [(0, j) for j in range(len(groups[0]["idx"]))] + [(1, j) for j in range(len(groups[1]["idx"]))]
+    seq = [seq[i] for i in order]
+
+    def plain_once():
+        s = streams[0]
+        a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(s)
+        for curve, j in seq:
+            g = groups[curve]
+            o = int(g["offs"][j])
+            plain_ctx.msm_device(curve, g["d_sc"].data_ptr() + 32 * o, g["d_pts"].data_ptr() + 64 * o,
+                                 g["sizes"][j], g["d_out_plain"].data_ptr() + 120 * j, hs.FMT_JACOBIAN51)
+        e.record(s)
+        s.synchronize()
+        return a.elapsed_time(e)
+
+    plain_once()
+    plain_ms = min(plain_once() for _ in range(2))
+    plain_ctx.set_graphs(True)
+    # same points? compare the serialized 32-byte encodings (Jacobian Z depends on summation order)
+    same = True
+    for c in (0, 1):
+        a = plain_ctx.compress(c, groups[c]["d_out"].cpu().numpy(), hs.FMT_JACOBIAN51)
+        p = plain_ctx.compress(c, groups[c]["d_out_plain"].cpu().numpy(), hs.FMT_JACOBIAN51)
+        same = same and bool((a == p).all())
+    total_pts = int(sizes.sum())
+    res = {"msms": count, "points": total_pts, "sizes": "log-uniform [64, 65536], seed-fixed",
+           "curves": {"helios": int((curves == 0).sum()), "selene": int((curves == 1).sum())},
+           "msms_per_s": count / (batched_ms * 1e-3), "ms": batched_ms,
+           "plain_msms_per_s": count / (plain_ms * 1e-3), "plain_ms": plain_ms,
+           "speedup_vs_plain": plain_ms / batched_ms, "points_per_s": total_pts / (batched_ms * 1e-3),
+           "bit_exact_vs_plain": bool(same), "autotune": {"seconds": round(tune_s, 2), **tuned},
+           "graph": "one captured launch sequence per curve group, replayed"}
+    for c in ctxs:
+        c.close()
+    return res
+
+
+def run_serving(hs, torch, device: str, local: int, requests_per_rate: int = 1000) -> dict:
+    """Config 4: Poisson arrivals of MSM requests, sizes from the mixture 70%
+    log-uniform [256, 4096], 25% [4096, 65536], 5% 2^18, curves alternating;
+    75% of each request's bases come from a 2^18-point resident pool per curve,
+    25% are fresh points sent with the request.  Continuous batching (4 slots)
+    against the plain path: the same requests one MSM per launch sequence, one
+    at a time (a server with one slot and one request per batch)."""
+    from helioselene_gb300.workload import ORDER, random_field_bytes, random_scalars
+    rng = np.random.default_rng(SEED + 4)
+    pool_n = 1 << 18
+    res_n = 1 << 19
+    pools, fresh, scal = {}, {}, {}
+    ctx = hs.Context(local)
+    for curve in (hs.HELIOS, hs.SELENE):
+        d_u = torch.from_numpy(random_field_bytes(rng, pool_n + res_n).reshape(-1)).to(device)
+        d_p = torch.empty((pool_n + res_n) * 64, dtype=torch.uint8, device=device)
+        torch.cuda.synchronize()
+        ctx.map_to_curve_device(curve, d_u.data_ptr(), pool_n + res_n, d_p.data_ptr())
+        torch.cuda.synchronize()
+        allp = d_p.cpu().numpy().reshape(-1, 64)
+        pools[curve] = np.ascontiguousarray(allp[:pool_n])
+        f = torch.empty(res_n * 64, dtype=torch.uint8, pin_memory=True)
+        f.numpy()[:] = allp[pool_n:].reshape(-1)
+        fresh[curve] = f
+        s = torch.empty(res_n * 2 * 32, dtype=torch.uint8, pin_memory=True)
+        s.numpy()[:] = random_scalars(rng, 2 * res_n, ORDER[curve]).reshape(-1)
+        scal[curve] = s
+    ctx.close()
+    perm = torch.empty(2 * res_n * 4, dtype=torch.uint8, pin_memory=True)
+    perm.numpy().view(np.uint32)[:] = rng.integers(0, pool_n, 2 * res_n).astype(np.uint32)
+
+    def draw(count):
+        u = rng.random(count)
+        n = np.where(u < 0.70, np.exp(rng.uniform(np.log(256), np.log(4096), count)),
+                     np.where(u < 0.95, np.exp(rng.uniform(np.log(4096), np.log(65536), count)), 2.0**18))
+        n = n.astype(np.int64)
+        reqs = []
+        for i in range(count):
+            curve = i % 2
+            k = int(n[i])
+            npool = (3 * k) // 4
+            nfresh = k - npool
+            so = int(rng.integers(0, 2 * res_n - k))
+            fo = int(rng.integers(0, res_n - nfresh + 1))
+            io = int(rng.integers(0, 2 * res_n - npool))
+            reqs.append((curve, so, k, io, npool, fo, nfresh))
+        return reqs
+
+    def views(r):
+        curve, so, k, io, npool, fo, nfresh = r
+        sc = scal[curve].numpy()[32 * so:32 * (so + k)]
+        idx = perm.numpy().view(np.uint32)[io:io + npool]
+        fr = fresh[curve].numpy()[64 * fo:64 * (fo + nfresh)]
+        return curve, sc, idx, fr
+
+    def run(srv, reqs, rate):
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, len(reqs))) if rate else np.zeros(len(reqs))
+        tickets = []
+        t0 = time.perf_counter()
+        for r, at in zip(reqs, arrivals):
+            delay = at - (time.perf_counter() - t0)
+            if delay > 0:
+                time.sleep(delay)
+            curve, sc, idx, fr = views(r)
+            tickets.append(srv.submit(curve, sc, idx, fr))
+        lat = [srv.wait(t, 600000)[1] for t in tickets]
+        wall = time.perf_counter() - t0
+        return {"rate_offered": rate or "all-at-once", "requests": len(reqs), "msms_per_s": len(reqs) / wall,
+                "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                "mean_points": float(np.mean([r[2] for r in reqs]))}
+
+    out = {"requests_per_rate": requests_per_rate, "pool_points_per_curve": pool_n,
+           "mix": "70% [256,4096], 25% [4096,65536], 5% 2^18 log-uniform; 75% pool bases, 25% fresh",
+           "plain": "same requests, one MSM per launch sequence, one at a time", "rates": []}
+    srv = hs.Server(local, slots=4, max_batch_points=1 << 22, max_batch_msms=1024)
+    plain = hs.Server(local, slots=1, max_batch_msms=1)
+    for s in (srv, plain):
+        for c in (hs.HELIOS, hs.SELENE):
+            s.set_pool(c, pools[c])
+    warm = draw(64)
+    run(srv, warm, 0)
+    run(plain, warm[:16], 0)
+    for rate in (1000, 3000, 9000, 0):
+        reqs = draw(requests_per_rate)
+        a = run(srv, reqs, rate)
+        bsec = run(plain, reqs[: max(100, requests_per_rate // 5)], rate)
+        out["rates"].append({"serving": a, "plain": bsec})
+    out["server_stats"] = srv.stats()
+    peak = out["rates"][-1]
+    out["msms_per_s"] = peak["serving"]["msms_per_s"]
+    out["plain_msms_per_s"] = peak["plain"]["msms_per_s"]
+    out["speedup_vs_plain"] = out["msms_per_s"] / out["plain_msms_per_s"]
+    srv.close()
+    plain.close()
+    return out
+
+
 def cpu_baseline_leg(data, n: int, gpu_results: dict) -> dict:
     """The oracle port on all host cores, on the same workload; also checks the GPU results."""
     sys.path.insert(0, str(ROOT / "oracle"))
@@ -195,48 +386,51 @@ def run_ours(args) -> None:
     torch.cuda.set_device(local)
     device = f"cuda:{local}"
     ctx = hs.Context(local)
+    ctx2 = hs.Context(local)  # the Selene MSM of a step runs on its own stream, overlapping the Helios one
+    ctxs = {hs.HELIOS: ctx, hs.SELENE: ctx2}
     n = args.n
     data = make_inputs(hs, ctx, torch, n, device)
-    stream = torch.cuda.ExternalStream(ctx.stream, device=device)
+    streams = {c: torch.cuda.ExternalStream(x.stream, device=device) for c, x in ctxs.items()}
+    stream = streams[hs.HELIOS]
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=device)
     d_out = torch.empty(2 * 128, dtype=torch.uint8, device=device)
     torch.cuda.synchronize()
 
-    def step():
-        for curve in (hs.HELIOS, hs.SELENE):
-            ctx.msm_device(curve, data[curve]["d_sc"].data_ptr(), data[curve]["d_pts"].data_ptr(), n,
-                           d_out.data_ptr() + 128 * curve, hs.FMT_COMPRESSED)
-
-    for _ in range(args.warmup):
+    def step(ev_pair=None):
+        start = torch.cuda.Event(enable_timing=True)
         with torch.cuda.stream(stream):
             flush.zero_()
+        start.record(stream)
+        streams[hs.SELENE].wait_event(start)
+        ends = []
+        for curve in (hs.HELIOS, hs.SELENE):
+            ctxs[curve].msm_device(curve, data[curve]["d_sc"].data_ptr(), data[curve]["d_pts"].data_ptr(), n,
+                                   d_out.data_ptr() + 128 * curve, hs.FMT_JACOBIAN51)
+            e = torch.cuda.Event(enable_timing=True)
+            e.record(streams[curve])
+            ends.append(e)
+        return start, ends
+
+    for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
-    results = {hs.HELIOS: None, hs.SELENE: None}
+    # results as the reference returns them (Jacobian records), serialized for the bit-exact check
     out_host = d_out.cpu().numpy()
-    results[hs.HELIOS] = out_host[:32].tobytes()
-    results[hs.SELENE] = out_host[128:160].tobytes()
+    results = {c: ctx.compress(c, out_host[128 * c:128 * c + 120], hs.FMT_JACOBIAN51).tobytes()
+               for c in (hs.HELIOS, hs.SELENE)}
 
-    # ---- timed region: device-resident inputs ----
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    # ---- timed region: device-resident inputs, both curves per step ----
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    ctx.profile(True)
-    ctx.profile_read(reset=True)
-    launches0 = ctx.launches
+    launches0 = ctx.launches + ctx2.launches
+    marks = []
     with ClockSampler(local) as clocks:
         for i in range(args.steps):
-            with torch.cuda.stream(stream):
-                flush.zero_()
-            ev[i][0].record(stream)
-            step()
-            ev[i][1].record(stream)
+            marks.append(step())
         torch.cuda.synchronize()
-    launches = ctx.launches - launches0
-    prof = ctx.profile_read(reset=True)
-    ctx.profile(False)
-    ms = sum(a.elapsed_time(b) for a, b in ev)
+    launches = ctx.launches + ctx2.launches - launches0
+    ms = sum(max(s.elapsed_time(e) for e in ends) for s, ends in marks)
     if dist:
         t = torch.tensor([ms], dtype=torch.float64, device=device)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -244,35 +438,52 @@ def run_ours(args) -> None:
     ms_per_step = ms / args.steps
     value = ws * 2 * n / (ms_per_step * 1e-3)
 
-    # per-curve split (untimed in the headline; same method)
+    # per-curve latency, one MSM at a time (also the roofline pass: accumulation
+    # launches timed with events on the context stream)
     per_curve = {}
+    prof_total = {"ms": 0.0, "work": 0.0, "launches": 0}
     for curve, name in ((hs.HELIOS, "helios"), (hs.SELENE, "selene")):
         ts = []
+        c = ctxs[curve]
+        s = streams[curve]
+        c.profile(True)
+        c.profile_read(reset=True)
         for _ in range(3):
-            with torch.cuda.stream(stream):
+            with torch.cuda.stream(s):
                 flush.zero_()
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            ctx.msm_device(curve, data[curve]["d_sc"].data_ptr(), data[curve]["d_pts"].data_ptr(), n,
-                           d_out.data_ptr(), hs.FMT_COMPRESSED)
-            b.record(stream)
+            a.record(s)
+            c.msm_device(curve, data[curve]["d_sc"].data_ptr(), data[curve]["d_pts"].data_ptr(), n,
+                         d_out.data_ptr(), hs.FMT_JACOBIAN51)
+            b.record(s)
             torch.cuda.synchronize()
             ts.append(a.elapsed_time(b))
-        per_curve[name] = {"ms": min(ts), "points_per_s": n / (min(ts) * 1e-3)}
+        pr = c.profile_read(reset=True)
+        c.profile(False)
+        per_curve[name] = {"ms": min(ts), "points_per_s": n / (min(ts) * 1e-3),
+                           "accumulate_ms": pr["accumulate_ms"] / max(1, pr["accumulate_launches"])}
+        prof_total["ms"] += pr["accumulate_ms"]
+        prof_total["launches"] += pr["accumulate_launches"]
+        prof_total["work"] += pr["entries"] * 6 * IMAD_PER_MODMUL[curve]
 
     # ---- e2e: reference-facing call with host buffers ----
     e2e_steps = max(3, min(args.steps, 10))
     for _ in range(2):
         for curve in (hs.HELIOS, hs.SELENE):
-            ctx.msm(curve, data[curve]["h_sc"].numpy(), data[curve]["h_jac"].numpy(), hs.FMT_JACOBIAN51,
-                    hs.FMT_JACOBIAN51)
+            ctxs[curve].msm(curve, data[curve]["h_sc"].numpy(), data[curve]["h_jac"].numpy(), hs.FMT_JACOBIAN51,
+                            hs.FMT_JACOBIAN51)
     if dist:
         dist.barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        for curve in (hs.HELIOS, hs.SELENE):
-            ctx.msm(curve, data[curve]["h_sc"].numpy(), data[curve]["h_jac"].numpy(), hs.FMT_JACOBIAN51,
-                    hs.FMT_JACOBIAN51)
+        # the two curves from two host threads (one context each), as a caller would overlap them
+        ths = [threading.Thread(target=ctxs[c].msm, args=(c, data[c]["h_sc"].numpy(), data[c]["h_jac"].numpy(),
+                                                         hs.FMT_JACOBIAN51, hs.FMT_JACOBIAN51))
+               for c in (hs.HELIOS, hs.SELENE)]
+        for t in ths:
+            t.start()
+        for t in ths:
+            t.join()
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     if dist:
         t = torch.tensor([e2e_s], dtype=torch.float64, device=device)
@@ -281,11 +492,14 @@ def run_ours(args) -> None:
 
     # ---- roofline of the dominant kernel (bucket accumulation) ----
     imad_peak = ctx.measure_imad_peak()
-    # algorithmic work of one accumulation launch: entries x 6 modmul (batch-affine add)
-    acc_ms = prof["accumulate_ms"] / max(1, prof["accumulate_launches"])
-    entries_per_launch = prof["entries"] / max(1, prof["accumulate_launches"])
-    imad_eq = entries_per_launch * 6 * (IMAD_PER_MODMUL[0] + IMAD_PER_MODMUL[1]) / 2
-    achieved = imad_eq / (acc_ms * 1e-3) if acc_ms > 0 else 0.0
+    achieved = prof_total["work"] / (prof_total["ms"] * 1e-3) if prof_total["ms"] > 0 else 0.0
+    acc_ms = prof_total["ms"] / max(1, prof_total["launches"])
+    batched = None
+    if not args.no_batched:
+        batched = run_batched(hs, torch, device, local, args.steps)
+    serving = None
+    if not args.no_serving:
+        serving = run_serving(hs, torch, device, local)
     m_n, c_star = modmul_count(n)
     whole = m_n * (IMAD_PER_MODMUL[0] + IMAD_PER_MODMUL[1]) / (ms_per_step * 1e-3)
 
@@ -306,11 +520,16 @@ def run_ours(args) -> None:
             "roofline": {"bound": "imad", "achieved": achieved / 1e12, "peak": imad_peak / 1e12,
                          "unit": "T IMAD/s", "frac": achieved / imad_peak if imad_peak else None,
                          "traffic": None, "kernel": "k_accumulate",
-                         "work": "entries x 6 modmul (batch-affine bucket add) x 188 IMAD-eq (mean of F_p 144, F_q 232)",
+                         "work": "point-window entries x 6 modmul (batch-affine bucket add) x IMAD-eq per modmul "
+                                 "(F_p 144, F_q 232), summed over one Helios and one Selene launch",
                          "peak_source": "measured in this run by hs_measure_imad_peak (mad.lo/mad.hi chains)",
                          "accumulate_ms_per_launch": acc_ms,
                          "whole_msm_frac": whole / imad_peak if imad_peak else None},
         }
+        if not args.no_batched:
+            line["batched"] = batched
+        if not args.no_serving:
+            line["serving"] = serving
         if ws == 1 and not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline_leg(data, n, results)
         print(json.dumps(line), flush=True)
@@ -318,6 +537,7 @@ def run_ours(args) -> None:
         dist.barrier()
         dist.destroy_process_group()
     ctx.close()
+    ctx2.close()
 
 
 def run_reference(args) -> None:
@@ -364,6 +584,8 @@ def main() -> None:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=1 << 20)
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched (1024 uneven MSMs) section")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving (Poisson arrivals) section")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

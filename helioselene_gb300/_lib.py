@@ -28,6 +28,23 @@ class hs_msm_desc(ctypes.Structure):
                 ("points", ctypes.c_void_p), ("out", ctypes.c_void_p)]
 
 
+class hs_server_config(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("slots", ctypes.c_int), ("hbm_budget", ctypes.c_size_t),
+                ("max_batch_points", ctypes.c_size_t), ("max_batch_msms", ctypes.c_size_t), ("out_fmt", ctypes.c_int)]
+
+
+class hs_request(ctypes.Structure):
+    _fields_ = [("curve", ctypes.c_int), ("n_pool", ctypes.c_size_t), ("pool_idx", ctypes.c_void_p),
+                ("n_fresh", ctypes.c_size_t), ("fresh_points", ctypes.c_void_p), ("scalars", ctypes.c_void_p),
+                ("out", ctypes.c_void_p)]
+
+
+class hs_server_stats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("failed", ctypes.c_uint64),
+                ("batches", ctypes.c_uint64), ("max_batch_msms", ctypes.c_uint64), ("peak_bytes", ctypes.c_uint64),
+                ("deferred", ctypes.c_uint64)]
+
+
 # name -> (restype, argtypes); mirrors include/helioselene_gb300.h
 _c = ctypes
 _vp, _sz, _int = _c.c_void_p, _c.c_size_t, _c.c_int
@@ -40,6 +57,7 @@ SIGNATURES = {
     "hs_context_launches": (_c.c_uint64, [_vp]),
     "hs_context_stream": (_vp, [_vp]),
     "hs_context_set_window": (_int, [_vp, _int, _sz, _sz, _int]),
+    "hs_context_set_graphs": (_int, [_vp, _int]),
     "hs_msm": (_int, [_vp, _int, _vp, _vp, _int, _sz, _vp, _int]),
     "hs_msm_device": (_int, [_vp, _int, _vp, _vp, _sz, _vp, _int]),
     "hs_pedersen": (_int, [_vp, _int, _vp, _vp, _vp, _vp, _int, _sz, _vp, _int]),
@@ -48,11 +66,18 @@ SIGNATURES = {
     "hs_map_to_curve": (_int, [_vp, _int, _vp, _sz, _vp, _int]),
     "hs_map_to_curve_device": (_int, [_vp, _int, _vp, _sz, _vp]),
     "hs_msm_batch": (_int, [_vp, _c.POINTER(hs_msm_desc), _sz, _int, _int]),
+    "hs_msm_batch_device": (_int, [_vp, _int, _vp, _sz, _vp, _vp, _vp, _int]),
     "hs_profile_enable": (_int, [_vp, _int]),
     "hs_profile_read": (_int, [_vp, _c.POINTER(_c.c_double), _c.POINTER(_c.c_uint64), _c.POINTER(_c.c_uint64),
                                _int]),
     "hs_measure_imad_peak": (_int, [_vp, _c.POINTER(_c.c_double)]),
     "hs_field_op": (_int, [_vp, _int, _int, _vp, _vp, _sz, _vp]),
+    "hs_server_create": (_int, [_c.POINTER(_vp), _c.POINTER(hs_server_config)]),
+    "hs_server_set_pool": (_int, [_vp, _int, _vp, _sz]),
+    "hs_server_submit": (_int, [_vp, _c.POINTER(hs_request), _c.POINTER(_c.c_uint64)]),
+    "hs_server_wait": (_int, [_vp, _c.c_uint64, _int, _c.POINTER(_c.c_double)]),
+    "hs_server_get_stats": (_int, [_vp, _c.POINTER(hs_server_stats)]),
+    "hs_server_destroy": (None, [_vp]),
     "hs_helios_msm_vartime": (None, [_vp, _vp, _vp, _sz]),
     "hs_selene_msm_vartime": (None, [_vp, _vp, _vp, _sz]),
     "hs_helios_pedersen_commit": (None, [_vp, _vp, _vp, _vp, _vp, _sz]),

@@ -87,6 +87,9 @@ class Context:
     def set_window(self, curve: int, n_min: int, n_max: int, window: int) -> None:
         self._check(self._lib.hs_context_set_window(self._h, curve, n_min, n_max, window), "set_window")
 
+    def set_graphs(self, on: bool) -> None:
+        self._check(self._lib.hs_context_set_graphs(self._h, int(on)), "set_graphs")
+
     # -- instrumentation --
     def profile(self, on: bool = True) -> None:
         self._check(self._lib.hs_profile_enable(self._h, int(on)), "hs_profile_enable")
@@ -151,6 +154,14 @@ class Context:
         self._check(self._lib.hs_msm_batch(self._h, descs, len(items), point_fmt, out_fmt), "hs_msm_batch")
         return [o.tobytes() for o in outs]
 
+    def msm_batch_device(self, curve: int, sizes: Sequence[int], d_scalars: int, d_points: int, d_out: int,
+                         out_fmt: int = L.FMT_JACOBIAN51) -> None:
+        """Batched MSMs on one curve over concatenated device arrays (hs_msm_batch_device)."""
+        sz = np.ascontiguousarray(np.asarray(sizes, dtype=np.uint64))
+        self._check(self._lib.hs_msm_batch_device(self._h, curve, sz.ctypes.data_as(ctypes.c_void_p), len(sizes),
+                                                  ctypes.c_void_p(d_scalars), ctypes.c_void_p(d_points),
+                                                  ctypes.c_void_p(d_out), out_fmt), "hs_msm_batch_device")
+
     # -- conversions --
     def batch_to_affine(self, curve: int, jac51, out_fmt: int = L.FMT_AFFINE) -> np.ndarray:
         j = _u8(jac51)
@@ -177,6 +188,78 @@ class Context:
     def map_to_curve_device(self, curve: int, d_u: int, n: int, d_out: int) -> None:
         self._check(self._lib.hs_map_to_curve_device(self._h, curve, ctypes.c_void_p(d_u), n,
                                                      ctypes.c_void_p(d_out)), "hs_map_to_curve_device")
+
+
+class Server:
+    """Continuous-batching MSM server (hs_server_*): submit requests as they
+    arrive, wait for each; the native scheduler batches whatever is queued onto
+    free slots within the HBM budget."""
+
+    def __init__(self, device: int = 0, slots: int = 4, hbm_budget: int = 0, max_batch_points: int = 0,
+                 max_batch_msms: int = 0, out_fmt: int = L.FMT_COMPRESSED):
+        self._lib = L.load()
+        cfg = L.hs_server_config(device, slots, hbm_budget, max_batch_points, max_batch_msms, out_fmt)
+        h = ctypes.c_void_p()
+        rc = self._lib.hs_server_create(ctypes.byref(h), ctypes.byref(cfg))
+        if rc != L.HS_OK:
+            raise L.HsError(rc, "hs_server_create")
+        self._h = h
+        self.out_bytes = L.FMT_BYTES[out_fmt]
+        self._live = {}
+
+    def set_pool(self, curve: int, affine_points) -> None:
+        p = _u8(affine_points)
+        rc = self._lib.hs_server_set_pool(self._h, curve, _ptr(p), p.size // 64)
+        if rc != L.HS_OK:
+            raise L.HsError(rc, "hs_server_set_pool")
+
+    def submit(self, curve: int, scalars, pool_idx=None, fresh_points=None) -> int:
+        s = _u8(scalars)
+        idx = np.ascontiguousarray(pool_idx, dtype=np.uint32) if pool_idx is not None else None
+        fr = _u8(fresh_points) if fresh_points is not None else None
+        out = np.zeros(self.out_bytes, np.uint8)
+        req = L.hs_request(curve, 0 if idx is None else idx.size, None if idx is None else idx.ctypes.data,
+                           0 if fr is None else fr.size // 64, None if fr is None else fr.ctypes.data,
+                           s.ctypes.data, out.ctypes.data)
+        t = ctypes.c_uint64()
+        rc = self._lib.hs_server_submit(self._h, ctypes.byref(req), ctypes.byref(t))
+        if rc != L.HS_OK:
+            raise L.HsError(rc, "hs_server_submit")
+        self._live[t.value] = (s, idx, fr, out)
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = 60000):
+        """-> (result bytes, latency_ms from submit to completion)"""
+        lat = ctypes.c_double()
+        rc = self._lib.hs_server_wait(self._h, ticket, timeout_ms, ctypes.byref(lat))
+        if rc == L.HS_ETIMEDOUT:
+            raise TimeoutError(f"request {ticket} not done after {timeout_ms} ms")
+        bufs = self._live.pop(ticket)
+        if rc != L.HS_OK:
+            raise L.HsError(rc, "hs_server_wait")
+        return bufs[3].tobytes(), lat.value
+
+    def stats(self) -> dict:
+        st = L.hs_server_stats()
+        self._lib.hs_server_get_stats(self._h, ctypes.byref(st))
+        return {f: int(getattr(st, f)) for f, _ in L.hs_server_stats._fields_}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.hs_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 _default = None

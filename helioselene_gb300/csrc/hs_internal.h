@@ -30,10 +30,21 @@ struct WindowRule {
     int c;
 };
 
+// A captured launch sequence, replayed when the same batch shape runs again on
+// the same buffers.
+struct GraphEntry {
+    std::vector<uint64_t> key;
+    cudaGraphExec_t exec = nullptr;
+    uint64_t kernels = 0;
+};
+
 struct Context {
     int device = 0;
     int sm_count = 0;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;   // the stream every launch goes to
+    cudaStream_t stream2 = nullptr;  // second curve group of a mixed batch
+    bool use_graphs = true;
+    std::vector<GraphEntry> graphs;
     DeviceArena arena;
     std::mutex mu;
     std::string last_error;
@@ -51,52 +62,92 @@ struct Context {
 void prof_begin(Context &ctx, cudaEvent_t *ev);
 void prof_end(Context &ctx, cudaEvent_t ev0, uint64_t entries);
 
-// Pippenger plan for one MSM of n points with c-bit signed windows.
-struct MsmPlan {
-    int curve = 0;
-    uint32_t n = 0;
-    int c = 0;           // window bits
-    uint32_t W = 0;      // windows = ceil(257 / c)
-    uint32_t B = 0;      // buckets per window = 2^(c-1)
-    uint32_t NB = 0;     // W * B
-    uint32_t L = 0;      // max entries per accumulation segment
-    uint32_t max_entries = 0;
-    uint32_t max_segs = 0;
-    uint32_t hist_blocks = 0;  // blocks of the segment-length histogram
-    uint32_t m0 = 0;     // buckets per thread in the bucket reduction
+// One MSM inside a batch (device-visible; every MSM of a batch is on the same curve).
+// Its points and scalars sit at [pt_off, pt_off + n) of the batch's concatenated
+// arrays; its W x B buckets at [bucket_base, bucket_base + W*B) of the batch's
+// bucket space; its W * (B/m0) reduction groups at group_base; its W window
+// sums at win_base.
+struct MsmDesc {
+    uint32_t pt_off, n;
+    uint32_t c, W, B;
+    uint32_t bucket_base;
+    uint32_t group_base, m0, log2m0, T;  // T = B / m0 groups per window
+    uint32_t win_base;
+    uint32_t pad;
 };
 
-// Device buffers of one MSM (all carved from the arena).
-struct MsmBuffers {
-    const uint32_t *scalars = nullptr;  // n * 8 words
-    const uint4 *points = nullptr;      // n * 4 uint4 (affine x || y)
+// A run of MSMs sharing one window width (one templated recode launch).
+struct WindowClass {
+    int c;
+    uint32_t first, count;       // MSM indices
+    uint32_t pt_begin, pt_end;   // concatenated point range
+};
+
+// Pippenger plan for a batch of MSMs on one curve (a single MSM is a batch of one).
+struct BatchPlan {
+    int curve = 0;
+    std::vector<MsmDesc> msms;
+    std::vector<WindowClass> classes;
+    uint32_t M = 0;             // MSMs
+    uint32_t n_total = 0;       // points
+    uint32_t NB = 0;            // buckets (all MSMs, all windows)
+    uint32_t G = 0;             // reduction groups
+    uint32_t WS = 0;            // window sums
+    uint32_t L = 0;             // max entries per accumulation segment
+    uint32_t max_entries = 0;
+    uint32_t max_segs = 0;
+    uint32_t hist_blocks = 0;   // blocks of the segment-length histogram
+    uint64_t entries_bound = 0; // sum n_i * W_i
+};
+
+// Device buffers of one batch (carved from the arena).
+struct BatchBuffers {
+    const uint32_t *scalars = nullptr;  // n_total * 8 words
+    const uint4 *points = nullptr;      // n_total * 4 uint4 (affine x || y)
+    MsmDesc *desc = nullptr;            // M descriptors
     uint32_t *counts = nullptr;         // NB + 1 (later reused as fill cursors)
     uint32_t *offsets = nullptr;        // NB + 1, exclusive scan of counts
     uint32_t *seg_off = nullptr;        // NB + 1, exclusive scan of segment counts
-    uint32_t *scan_tmp = nullptr;       // per-block partials of the scan
+    uint32_t *scan_tmp = nullptr;       // per-block partials of the scans
+    uint32_t *len_hist = nullptr;       // (L+1) x hist_blocks segment-length histogram
+    uint32_t *len_scan = nullptr;       // its exclusive scan (+1 total)
     uint32_t *sorted = nullptr;         // max_entries: point index | sign << 31
     uint4 *segs = nullptr;              // max_segs: (start, length, destination slot, 0), longest first
-    uint32_t *len_hist = nullptr;       // (L+1) x hist blocks: segment-length histogram, then its scan
-    uint32_t *len_scan = nullptr;       // exclusive scan of len_hist (+1 total)
     uint4 *seg_sum = nullptr;           // max_segs XYZZ sums (8 uint4 each)
     uint32_t *heavy = nullptr;          // NB heavy-bucket list
     uint32_t *heavy_n = nullptr;        // 1 counter
-    uint4 *redA = nullptr;              // W * (B / m0) weighted group sums
-    uint4 *redR = nullptr;              // W window sums
-    uint32_t *out_jac = nullptr;        // 24 words: canonical Jacobian X, Y, Z
+    uint4 *redA = nullptr;              // G weighted group sums
+    uint4 *redS = nullptr;              // WS window sums
+    uint32_t *out_jac = nullptr;        // M x 24 words: canonical Jacobian X, Y, Z
 };
 
-MsmPlan make_plan(const Context &ctx, int curve, size_t n);
-size_t plan_bytes(const MsmPlan &p);
-void carve(DeviceArena &a, const MsmPlan &p, MsmBuffers &b);
+// index of the MSM owning element x of a batch: the largest m with key(m) <= x
+template <class KeyFn>
+__device__ __forceinline__ uint32_t find_msm(uint32_t M, uint32_t x, KeyFn key)
+{
+    uint32_t lo = 0, hi = M - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (key(mid) <= x)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
 
-// curve-independent launches (hs_runtime.cu)
-cudaError_t launch_sort(Context &ctx, const MsmPlan &p, const MsmBuffers &b);
+int choose_window(const Context &ctx, int curve, size_t n);
+BatchPlan make_batch_plan(const Context &ctx, int curve, const size_t *sizes, uint32_t M);
+size_t batch_bytes(const BatchPlan &p);
+bool carve(DeviceArena &a, const BatchPlan &p, BatchBuffers &b);
+
+// curve-independent launches (hs_runtime.cu): descriptor upload, recode, sort, segments
+cudaError_t launch_sort(Context &ctx, const BatchPlan &p, const BatchBuffers &b);
 
 // per-curve entry points (hs_curve_helios.cu / hs_curve_selene.cu)
 struct CurveOps {
-    // buckets -> window sums -> canonical Jacobian in b.out_jac (after launch_sort)
-    cudaError_t (*msm_tail)(Context &ctx, const MsmPlan &p, const MsmBuffers &b);
+    // buckets -> window sums -> canonical Jacobians in b.out_jac (after launch_sort)
+    cudaError_t (*msm_tail)(Context &ctx, const BatchPlan &p, const BatchBuffers &b);
     // jac51 / affine51 / affine input -> device affine (n * 64 bytes); scalars of
     // identity points are left alone (the accumulator skips (0,0) bases)
     cudaError_t (*to_affine)(Context &ctx, const void *d_in, int fmt, size_t n, uint4 *d_out, void *scratch);
@@ -114,6 +165,30 @@ extern const CurveOps selene_ops;
 const CurveOps &curve_ops(int curve);
 
 size_t fmt_bytes(int fmt);
+size_t align256(size_t b);
+
+// make `dev` current for a scope
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev)
+    {
+        cudaGetDevice(&prev);
+        if (prev != dev)
+            cudaSetDevice(dev);
+    }
+    ~DeviceGuard()
+    {
+        if (prev >= 0)
+            cudaSetDevice(prev);
+    }
+};
+
+// batch execution helpers shared with the serving loop (hs_runtime.cu)
+int reserve_batch(Context &ctx, const BatchPlan &p, size_t extra_bytes, BatchBuffers &b, void **extra);
+int execute_batch(Context &ctx, const BatchPlan &p, const BatchBuffers &b, void *d_out, int out_fmt);
+void drop_graphs(Context &ctx);
+int fail(Context &ctx, cudaError_t e, const char *what);
+int fail_msg(Context &ctx, int code, const char *what);
 
 #define HS_LAUNCH_CHECK(ctx)                                 \
     do {                                                     \

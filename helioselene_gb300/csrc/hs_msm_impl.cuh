@@ -178,43 +178,51 @@ __device__ Xyzz mul_small(const Xyzz &P, uint32_t t)
 }
 
 template <class C>
-__global__ void k_reduce_abs(const uint32_t *__restrict__ seg_off, const uint4 *__restrict__ seg_sum, uint32_t W,
-                             uint32_t B, uint32_t m, uint32_t log2m, uint4 *__restrict__ outA)
+__global__ void k_reduce_abs(const uint32_t *__restrict__ seg_off, const uint4 *__restrict__ seg_sum,
+                             const MsmDesc *__restrict__ desc, uint32_t M, uint32_t G, uint4 *__restrict__ outA)
 {
-    using G = Group<C>;
-    const uint32_t T = B / m;
-    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-    if (tid >= W * T)
+    using G_ = Group<C>;
+    const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= G)
         return;
-    const uint32_t k = tid / T, t = tid % T;
-    Xyzz run = G::inf(), acc = G::inf();
+    const uint32_t mi = find_msm(M, gid, [&](uint32_t k) { return desc[k].group_base; });
+    const MsmDesc d = desc[mi];
+    const uint32_t local = gid - d.group_base;
+    const uint32_t k = local / d.T, t = local % d.T;
+    const uint32_t m = d.m0;
+    Xyzz run = G_::inf(), acc = G_::inf();
     for (int j = (int)((t + 1) * m) - 1; j >= (int)(t * m); j--) {
-        const uint32_t kb = k * B + (uint32_t)j;
+        const uint32_t kb = d.bucket_base + k * d.B + (uint32_t)j;
         const uint32_t s0 = seg_off[kb];
         if (seg_off[kb + 1] != s0)
-            run = G::add(run, load_xyzz(seg_sum + 8 * (size_t)s0));
-        acc = G::add(acc, run);
+            run = G_::add(run, load_xyzz(seg_sum + 8 * (size_t)s0));
+        acc = G_::add(acc, run);
     }
     Xyzz off = mul_small<C>(run, t);
-    for (uint32_t i = 0; i < log2m; i++)
-        off = G::dbl(off);
-    store_xyzz(outA + 8 * (size_t)tid, G::add(acc, off));
+    for (uint32_t i = 0; i < d.log2m0; i++)
+        off = G_::dbl(off);
+    store_xyzz(outA + 8 * (size_t)gid, G_::add(acc, off));
 }
 
-// S_k = sum over the T outputs of window k: one block per window, strided
-// per-thread sums, then a shared-memory tree.
-constexpr int WSUM_THREADS = 256;
+// S_k = sum over the T group outputs of window k of one MSM: one block per
+// window (all windows of all MSMs), strided per-thread sums, then a
+// shared-memory tree.
+constexpr int WSUM_THREADS = 128;
 
 template <class C>
-__global__ void __launch_bounds__(WSUM_THREADS) k_window_sum(const uint4 *__restrict__ inA, uint32_t T,
+__global__ void __launch_bounds__(WSUM_THREADS) k_window_sum(const uint4 *__restrict__ inA,
+                                                            const MsmDesc *__restrict__ desc, uint32_t M,
                                                             uint4 *__restrict__ S)
 {
     using G = Group<C>;
     __shared__ uint4 sh[WSUM_THREADS * 8];
-    const uint32_t k = blockIdx.x;
+    const uint32_t s = blockIdx.x;
+    const uint32_t mi = find_msm(M, s, [&](uint32_t k) { return desc[k].win_base; });
+    const MsmDesc d = desc[mi];
+    const size_t base = (size_t)d.group_base + (size_t)(s - d.win_base) * d.T;
     Xyzz acc = G::inf();
-    for (uint32_t i = threadIdx.x; i < T; i += WSUM_THREADS)
-        acc = G::add(acc, load_xyzz(inA + 8 * ((size_t)k * T + i)));
+    for (uint32_t i = threadIdx.x; i < d.T; i += WSUM_THREADS)
+        acc = G::add(acc, load_xyzz(inA + 8 * (base + i)));
     store_xyzz(sh + 8 * threadIdx.x, acc);
     __syncthreads();
     for (uint32_t stride = WSUM_THREADS / 2; stride > 0; stride >>= 1) {
@@ -224,7 +232,7 @@ __global__ void __launch_bounds__(WSUM_THREADS) k_window_sum(const uint4 *__rest
         __syncthreads();
     }
     if (threadIdx.x == 0)
-        store_xyzz(S + 8 * (size_t)k, load_xyzz(sh));
+        store_xyzz(S + 8 * (size_t)s, load_xyzz(sh));
 }
 
 // ---------------------------------------------------------------------------
@@ -394,25 +402,28 @@ __device__ void coop_add(SlotFile &sf)
     __syncwarp();
 }
 
+// one warp per MSM of the batch
 template <class C>
-__global__ void __launch_bounds__(32) k_combine(const uint4 *__restrict__ S, uint32_t W, uint32_t c,
+__global__ void __launch_bounds__(32) k_combine(const uint4 *__restrict__ S, const MsmDesc *__restrict__ desc,
                                                uint32_t *__restrict__ out)
 {
     __shared__ SlotFile sf;
     const int lane = threadIdx.x & 31;
+    const MsmDesc d = desc[blockIdx.x];
+    const uint4 *Sm = S + 8 * (size_t)d.win_base;
     if (lane == 0) {
-        const Xyzz top = load_xyzz(S + 8 * (size_t)(W - 1));
+        const Xyzz top = load_xyzz(Sm + 8 * (size_t)(d.W - 1));
         sf.f[sX] = top.X;
         sf.f[sY] = top.Y;
         sf.f[sZZ] = top.ZZ;
         sf.f[sZZZ] = top.ZZZ;
     }
     __syncwarp();
-    for (int k = (int)W - 2; k >= 0; k--) {
-        for (uint32_t d = 0; d < c; d++)
+    for (int k = (int)d.W - 2; k >= 0; k--) {
+        for (uint32_t i = 0; i < d.c; i++)
             coop_dbl<C>(sf);
         if (lane == 0) {
-            const Xyzz a = load_xyzz(S + 8 * (size_t)k);
+            const Xyzz a = load_xyzz(Sm + 8 * (size_t)k);
             sf.f[sX2] = a.X;
             sf.f[sY2] = a.Y;
             sf.f[sZZ2] = a.ZZ;
@@ -427,12 +438,12 @@ __global__ void __launch_bounds__(32) k_combine(const uint4 *__restrict__ S, uin
         t.Y = sf.f[sY];
         t.ZZ = sf.f[sZZ];
         t.ZZZ = sf.f[sZZZ];
-        store_jacobian_canon<C>(out, t);
+        store_jacobian_canon<C>(out + 24 * (size_t)blockIdx.x, t);
     }
 }
 
 template <class C>
-cudaError_t msm_tail(Context &ctx, const MsmPlan &p, const MsmBuffers &b)
+cudaError_t msm_tail(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
 {
     cudaStream_t st = ctx.stream;
     // 2. accumulate: persistent grid over the device-side segment count
@@ -443,7 +454,7 @@ cudaError_t msm_tail(Context &ctx, const MsmPlan &p, const MsmBuffers &b)
         prof_begin(ctx, &ev0);
         k_accumulate<C><<<blocks, threads, 0, st>>>(b.segs, b.seg_off + p.NB, b.sorted, b.points, b.seg_sum);
         HS_LAUNCH_CHECK(ctx);
-        prof_end(ctx, ev0, (uint64_t)p.n * p.W);
+        prof_end(ctx, ev0, p.entries_bound);
     }
     // 3. merge multi-segment buckets
     {
@@ -458,21 +469,16 @@ cudaError_t msm_tail(Context &ctx, const MsmPlan &p, const MsmBuffers &b)
         HS_LAUNCH_CHECK(ctx);
     }
     // 4. bucket reduction with absolute weights, then one plain sum per window
-    const uint32_t T = p.B / p.m0;
     {
-        uint32_t log2m = 0;
-        while ((1u << log2m) < p.m0)
-            log2m++;
-        const uint32_t total = p.W * T;
         const int threads = 64;
-        k_reduce_abs<C><<<(total + threads - 1) / threads, threads, 0, st>>>(b.seg_off, b.seg_sum, p.W, p.B, p.m0,
-                                                                           log2m, b.redA);
+        k_reduce_abs<C><<<(p.G + threads - 1) / threads, threads, 0, st>>>(b.seg_off, b.seg_sum, b.desc, p.M, p.G,
+                                                                         b.redA);
         HS_LAUNCH_CHECK(ctx);
-        k_window_sum<C><<<p.W, WSUM_THREADS, 0, st>>>(b.redA, T, b.redR);
+        k_window_sum<C><<<p.WS, WSUM_THREADS, 0, st>>>(b.redA, b.desc, p.M, b.redS);
         HS_LAUNCH_CHECK(ctx);
     }
-    // 5. Horner over windows
-    k_combine<C><<<1, 32, 0, st>>>(b.redR, p.W, (uint32_t)p.c, b.out_jac);
+    // 5. Horner over windows, one warp per MSM
+    k_combine<C><<<p.M, 32, 0, st>>>(b.redS, b.desc, b.out_jac);
     HS_LAUNCH_CHECK(ctx);
     return cudaSuccess;
 }

@@ -63,7 +63,7 @@ void DeviceArena::release()
     cap = off = 0;
 }
 
-static size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
 size_t fmt_bytes(int fmt)
 {
@@ -104,27 +104,58 @@ static int model_window(size_t n)
     return best;
 }
 
-MsmPlan make_plan(const Context &ctx, int curve, size_t n)
+int choose_window(const Context &ctx, int curve, size_t n)
 {
-    MsmPlan p;
-    p.curve = curve;
-    p.n = (uint32_t)n;
     int c = 0;
     for (const WindowRule &r : ctx.rules[curve == HS_SELENE ? 1 : 0])
         if (n >= r.n_min && n <= r.n_max)
             c = r.c;
     if (c < 4 || c > 20)
         c = model_window(n);
-    p.c = c;
-    p.W = (uint32_t)((257 + c - 1) / c);
-    p.B = 1u << (c - 1);
-    p.NB = p.W * p.B;
-    const uint32_t avg = (uint32_t)((n + p.B - 1) / p.B);
-    p.L = std::max<uint32_t>(16, std::min<uint32_t>(128, 2 * avg));
-    p.max_entries = (uint32_t)std::max<size_t>(1, n * p.W);
-    p.max_segs = p.max_entries / p.L + p.NB + 1;
+    return c;
+}
+
+BatchPlan make_batch_plan(const Context &ctx, int curve, const size_t *sizes, uint32_t M)
+{
+    BatchPlan p;
+    p.curve = curve;
+    p.M = M;
+    p.msms.resize(M);
+    uint64_t pt = 0, nb = 0, g = 0, ws = 0, ent = 0;
+    for (uint32_t i = 0; i < M; i++) {
+        MsmDesc &d = p.msms[i];
+        const size_t n = sizes[i];
+        const int c = choose_window(ctx, curve, n ? n : 1);
+        d.pt_off = (uint32_t)pt;
+        d.n = (uint32_t)n;
+        d.c = (uint32_t)c;
+        d.W = (uint32_t)((257 + c - 1) / c);
+        d.B = 1u << (c - 1);
+        d.m0 = std::min<uint32_t>(16, d.B);
+        d.log2m0 = 0;
+        while ((1u << d.log2m0) < d.m0)
+            d.log2m0++;
+        d.T = d.B / d.m0;
+        d.bucket_base = (uint32_t)nb;
+        d.group_base = (uint32_t)g;
+        d.win_base = (uint32_t)ws;
+        d.pad = 0;
+        pt += n;
+        nb += (uint64_t)d.W * d.B;
+        g += (uint64_t)d.W * d.T;
+        ws += d.W;
+        ent += (uint64_t)n * d.W;
+    }
+    p.n_total = (uint32_t)pt;
+    p.NB = (uint32_t)nb;
+    p.G = (uint32_t)g;
+    p.WS = (uint32_t)ws;
+    p.entries_bound = ent;
+    p.max_entries = (uint32_t)std::max<uint64_t>(1, ent);
+    const uint64_t avg = nb ? (ent + nb - 1) / nb : 1;
+    p.L = (uint32_t)std::max<uint64_t>(16, std::min<uint64_t>(128, 2 * avg));
+    p.max_segs = (uint32_t)(std::min<uint64_t>(ent, nb) + ent / p.L + 1);
     p.hist_blocks = (p.NB + SEG_HIST_THREADS - 1) / SEG_HIST_THREADS;
-    p.m0 = std::min<uint32_t>(16, p.B);
     return p;
 }
 
@@ -134,29 +165,33 @@ static constexpr uint32_t SCAN_BLOCK = SCAN_THREADS * SCAN_ITEMS;
 
 static uint32_t scan_blocks(uint32_t NB) { return (NB + SCAN_BLOCK - 1) / SCAN_BLOCK; }
 
-size_t plan_bytes(const MsmPlan &p)
+static size_t hist_len(const BatchPlan &p) { return (size_t)(p.L + 1) * p.hist_blocks; }
+
+size_t batch_bytes(const BatchPlan &p)
 {
     size_t b = 0;
-    b += 3 * align256((size_t)(p.NB + 1) * 4);                  // counts, offsets, seg_off
-    const size_t nh = (size_t)(p.L + 1) * p.hist_blocks;
+    const size_t nh = hist_len(p);
+    b += align256((size_t)p.M * sizeof(MsmDesc));
+    b += 3 * align256((size_t)(p.NB + 1) * 4);                                             // counts, offsets, seg_off
     b += align256((size_t)2 * scan_blocks((uint32_t)std::max<size_t>(p.NB, nh)) * 4 + 64);  // scan partials
-    b += 2 * align256((nh + 1) * 4);                            // segment-length histogram + scan
-    b += align256((size_t)p.max_entries * 4);                   // sorted
-    b += align256((size_t)p.max_segs * 16);                     // segs
-    b += align256((size_t)p.max_segs * 128);                    // seg_sum
-    b += align256((size_t)p.NB * 4) + 256;                      // heavy list + counter
-    const size_t r0 = (size_t)p.W * (p.B / p.m0) * 128;
-    b += align256(r0) + align256((size_t)p.W * 128);
-    b += 256;                                                   // out_jac
+    b += 2 * align256((nh + 1) * 4);                                                       // length histogram + scan
+    b += align256((size_t)p.max_entries * 4);                                              // sorted
+    b += align256((size_t)p.max_segs * 16);                                                // segs
+    b += align256((size_t)p.max_segs * 128);                                               // seg_sum
+    b += align256((size_t)p.NB * 4) + 256;                                                 // heavy list + counter
+    b += align256((size_t)std::max<uint32_t>(1, p.G) * 128);                               // group sums
+    b += align256((size_t)std::max<uint32_t>(1, p.WS) * 128);                              // window sums
+    b += align256((size_t)std::max<uint32_t>(1, p.M) * 96);                                // results
     return b + 16 * 256;
 }
 
-void carve(DeviceArena &a, const MsmPlan &p, MsmBuffers &b)
+bool carve(DeviceArena &a, const BatchPlan &p, BatchBuffers &b)
 {
+    const size_t nh = hist_len(p);
+    b.desc = (MsmDesc *)a.take((size_t)p.M * sizeof(MsmDesc));
     b.counts = (uint32_t *)a.take((size_t)(p.NB + 1) * 4);
     b.offsets = (uint32_t *)a.take((size_t)(p.NB + 1) * 4);
     b.seg_off = (uint32_t *)a.take((size_t)(p.NB + 1) * 4);
-    const size_t nh = (size_t)(p.L + 1) * p.hist_blocks;
     b.scan_tmp = (uint32_t *)a.take((size_t)2 * scan_blocks((uint32_t)std::max<size_t>(p.NB, nh)) * 4 + 64);
     b.len_hist = (uint32_t *)a.take((nh + 1) * 4);
     b.len_scan = (uint32_t *)a.take((nh + 1) * 4);
@@ -165,10 +200,11 @@ void carve(DeviceArena &a, const MsmPlan &p, MsmBuffers &b)
     b.seg_sum = (uint4 *)a.take((size_t)p.max_segs * 128);
     b.heavy = (uint32_t *)a.take((size_t)p.NB * 4);
     b.heavy_n = (uint32_t *)a.take(4);
-    const size_t r0 = (size_t)p.W * (p.B / p.m0) * 128;
-    b.redA = (uint4 *)a.take(r0);
-    b.redR = (uint4 *)a.take((size_t)p.W * 128);
-    b.out_jac = (uint32_t *)a.take(96);
+    b.redA = (uint4 *)a.take((size_t)std::max<uint32_t>(1, p.G) * 128);
+    b.redS = (uint4 *)a.take((size_t)std::max<uint32_t>(1, p.WS) * 128);
+    b.out_jac = (uint32_t *)a.take((size_t)std::max<uint32_t>(1, p.M) * 96);
+    return b.desc && b.counts && b.offsets && b.seg_off && b.scan_tmp && b.len_hist && b.len_scan && b.sorted &&
+           b.segs && b.seg_sum && b.heavy && b.heavy_n && b.redA && b.redS && b.out_jac;
 }
 
 // ---------------------------------------------------------------------------
@@ -184,21 +220,16 @@ __device__ __forceinline__ uint32_t window_bits(const uint32_t s[8], int k)
     return __funnelshift_r(lo, hi, sh) & ((1u << CB) - 1u);
 }
 
-// One thread per scalar.  Digits in [-2^(c-1), 2^(c-1)) except the top one,
-// which keeps the final carry and is at most 2^(c-1) because W*c >= 257.
-// count pass: histogram of (window, |digit|) keys; scatter pass: place
-// "index | sign" at offsets[key] + running fill.
+// Digits in [-2^(c-1), 2^(c-1)) except the top one, which keeps the final
+// carry and is at most 2^(c-1) because W*c >= 257.  count pass: histogram of
+// bucket keys; scatter pass: place "index | sign" at offsets[key] + running fill.
 template <int CB, bool SCATTER>
-__global__ void k_recode(const uint4 *__restrict__ scalars, uint32_t n, uint32_t *__restrict__ counts,
-                         const uint32_t *__restrict__ offsets, uint32_t *__restrict__ sorted)
+__device__ __forceinline__ void recode_one(const uint32_t s[8], uint32_t i, uint32_t bucket_base,
+                                           uint32_t *__restrict__ counts, const uint32_t *__restrict__ offsets,
+                                           uint32_t *__restrict__ sorted)
 {
     constexpr int W = (257 + CB - 1) / CB;
     constexpr uint32_t B = 1u << (CB - 1);
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n)
-        return;
-    const uint4 a = __ldg(scalars + 2 * (size_t)i), b = __ldg(scalars + 2 * (size_t)i + 1);
-    const uint32_t s[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
     uint32_t carry = 0;
 #pragma unroll
     for (int k = 0; k < W; k++) {
@@ -214,7 +245,7 @@ __global__ void k_recode(const uint4 *__restrict__ scalars, uint32_t n, uint32_t
             carry = 0;
         }
         if (mag != 0) {
-            const uint32_t kb = (uint32_t)k * B + mag - 1u;
+            const uint32_t kb = bucket_base + (uint32_t)k * B + mag - 1u;
             if (!SCATTER) {
                 atomicAdd(counts + kb, 1u);
             } else {
@@ -222,6 +253,47 @@ __global__ void k_recode(const uint4 *__restrict__ scalars, uint32_t n, uint32_t
                 sorted[pos] = i | (neg ? 0x80000000u : 0u);
             }
         }
+    }
+}
+
+// One thread per point of the batch; the window width is per MSM.
+template <bool SCATTER>
+__global__ void k_recode(const uint4 *__restrict__ scalars, uint32_t n_total, const MsmDesc *__restrict__ desc,
+                         uint32_t M, uint32_t *__restrict__ counts, const uint32_t *__restrict__ offsets,
+                         uint32_t *__restrict__ sorted)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_total)
+        return;
+    const uint32_t m = find_msm(M, i, [&](uint32_t k) { return desc[k].pt_off; });
+    const uint32_t c = desc[m].c, base = desc[m].bucket_base;
+    const uint4 a = __ldg(scalars + 2 * (size_t)i), b = __ldg(scalars + 2 * (size_t)i + 1);
+    const uint32_t s[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+    switch (c) {
+#define HS_CASE(v)                                                       \
+    case v:                                                              \
+        recode_one<v, SCATTER>(s, i, base, counts, offsets, sorted);     \
+        break;
+        HS_CASE(4)
+        HS_CASE(5)
+        HS_CASE(6)
+        HS_CASE(7)
+        HS_CASE(8)
+        HS_CASE(9)
+        HS_CASE(10)
+        HS_CASE(11)
+        HS_CASE(12)
+        HS_CASE(13)
+        HS_CASE(14)
+        HS_CASE(15)
+        HS_CASE(16)
+        HS_CASE(17)
+        HS_CASE(18)
+        HS_CASE(19)
+        HS_CASE(20)
+#undef HS_CASE
+    default:
+        break;
     }
 }
 
@@ -247,6 +319,7 @@ __device__ __forceinline__ uint2 block_excl_scan(uint2 v, uint2 *total)
     __shared__ uint2 warp_tot[SCAN_THREADS / 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint2 inc = warp_incl_scan(v);
+    __syncthreads();
     if (lane == 31)
         warp_tot[warp] = inc;
     __syncthreads();
@@ -297,37 +370,46 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_a(const uint32_t *__restr
     }
 }
 
+// scan of the block partials, in chunks of SCAN_BLOCK with a running carry
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_b(uint32_t *__restrict__ tmp, uint32_t nblocks,
                                                         uint32_t *__restrict__ off_total,
                                                         uint32_t *__restrict__ seg_total)
 {
     __shared__ uint2 tot;
-    const uint32_t base = threadIdx.x * SCAN_ITEMS;
-    uint2 it[SCAN_ITEMS];
-    uint2 v = make_uint2(0, 0);
+    uint2 carry = make_uint2(0, 0);
+    for (uint32_t chunk = 0; chunk < nblocks; chunk += SCAN_BLOCK) {
+        const uint32_t base = chunk + threadIdx.x * SCAN_ITEMS;
+        uint2 it[SCAN_ITEMS];
+        uint2 v = make_uint2(0, 0);
 #pragma unroll
-    for (int j = 0; j < SCAN_ITEMS; j++) {
-        const uint32_t idx = base + j;
-        it[j] = idx < nblocks ? make_uint2(tmp[2 * idx], tmp[2 * idx + 1]) : make_uint2(0, 0);
-        v.x += it[j].x;
-        v.y += it[j].y;
-    }
-    uint2 pre = block_excl_scan(v, &tot);
-#pragma unroll
-    for (int j = 0; j < SCAN_ITEMS; j++) {
-        const uint32_t idx = base + j;
-        if (idx < nblocks) {
-            tmp[2 * idx] = pre.x;
-            tmp[2 * idx + 1] = pre.y;
+        for (int j = 0; j < SCAN_ITEMS; j++) {
+            const uint32_t idx = base + j;
+            it[j] = idx < nblocks ? make_uint2(tmp[2 * idx], tmp[2 * idx + 1]) : make_uint2(0, 0);
+            v.x += it[j].x;
+            v.y += it[j].y;
         }
-        pre.x += it[j].x;
-        pre.y += it[j].y;
+        uint2 pre = block_excl_scan(v, &tot);
+        pre.x += carry.x;
+        pre.y += carry.y;
+#pragma unroll
+        for (int j = 0; j < SCAN_ITEMS; j++) {
+            const uint32_t idx = base + j;
+            if (idx < nblocks) {
+                tmp[2 * idx] = pre.x;
+                tmp[2 * idx + 1] = pre.y;
+            }
+            pre.x += it[j].x;
+            pre.y += it[j].y;
+        }
+        __syncthreads();
+        carry.x += tot.x;
+        carry.y += tot.y;
+        __syncthreads();
     }
-    __syncthreads();
     if (threadIdx.x == 0) {
-        *off_total = tot.x;
+        *off_total = carry.x;
         if (seg_total)
-            *seg_total = tot.y;
+            *seg_total = carry.y;
     }
 }
 
@@ -395,84 +477,50 @@ __global__ void __launch_bounds__(SEG_HIST_THREADS) k_seg_scatter(const uint32_t
     }
 }
 
-template <int CB>
-static cudaError_t launch_recode(Context &ctx, const MsmPlan &p, const MsmBuffers &b, bool scatter)
+static cudaError_t launch_scan(Context &ctx, const uint32_t *in, uint32_t n, uint32_t L, uint32_t *out,
+                               uint32_t *out2, uint32_t *tmp)
 {
-    const int threads = 256;
-    const unsigned blocks = (p.n + threads - 1) / threads;
-    const uint4 *sc = reinterpret_cast<const uint4 *>(b.scalars);
-    if (scatter)
-        k_recode<CB, true><<<blocks, threads, 0, ctx.stream>>>(sc, p.n, b.counts, b.offsets, b.sorted);
-    else
-        k_recode<CB, false><<<blocks, threads, 0, ctx.stream>>>(sc, p.n, b.counts, b.offsets, b.sorted);
+    cudaStream_t st = ctx.stream;
+    const uint32_t nblk = std::max<uint32_t>(1, scan_blocks(n));
+    k_scan_a<<<nblk, SCAN_THREADS, 0, st>>>(in, n, L, out, out2, tmp);
     HS_LAUNCH_CHECK(ctx);
+    k_scan_b<<<1, SCAN_THREADS, 0, st>>>(tmp, nblk, out + n, out2 ? out2 + n : nullptr);
+    HS_LAUNCH_CHECK(ctx);
+    if (n) {
+        k_scan_c<<<(n + 255) / 256, 256, 0, st>>>(out, out2, n, tmp);
+        HS_LAUNCH_CHECK(ctx);
+    }
     return cudaSuccess;
 }
 
-static cudaError_t recode_dispatch(Context &ctx, const MsmPlan &p, const MsmBuffers &b, bool scatter)
-{
-    switch (p.c) {
-#define HS_CASE(v) \
-    case v:        \
-        return launch_recode<v>(ctx, p, b, scatter);
-        HS_CASE(4)
-        HS_CASE(5)
-        HS_CASE(6)
-        HS_CASE(7)
-        HS_CASE(8)
-        HS_CASE(9)
-        HS_CASE(10)
-        HS_CASE(11)
-        HS_CASE(12)
-        HS_CASE(13)
-        HS_CASE(14)
-        HS_CASE(15)
-        HS_CASE(16)
-        HS_CASE(17)
-        HS_CASE(18)
-        HS_CASE(19)
-        HS_CASE(20)
-#undef HS_CASE
-    default:
-        return cudaErrorInvalidValue;
-    }
-}
-
-cudaError_t launch_sort(Context &ctx, const MsmPlan &p, const MsmBuffers &b)
+// recode + counting sort + segments of a whole batch (descriptors already on the device)
+cudaError_t launch_sort(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
 {
     cudaStream_t st = ctx.stream;
     cudaError_t e;
     if ((e = cudaMemsetAsync(b.counts, 0, (size_t)(p.NB + 1) * 4, st)) != cudaSuccess)
         return e;
-    if ((e = recode_dispatch(ctx, p, b, false)) != cudaSuccess)
+    const uint4 *sc = reinterpret_cast<const uint4 *>(b.scalars);
+    const unsigned rblocks = (p.n_total + 255) / 256;
+    if (p.n_total) {
+        k_recode<false><<<rblocks, 256, 0, st>>>(sc, p.n_total, b.desc, p.M, b.counts, b.offsets, b.sorted);
+        HS_LAUNCH_CHECK(ctx);
+    }
+    if ((e = launch_scan(ctx, b.counts, p.NB, p.L, b.offsets, b.seg_off, b.scan_tmp)) != cudaSuccess)
         return e;
-    const uint32_t nblk = scan_blocks(p.NB);
-    k_scan_a<<<nblk, SCAN_THREADS, 0, st>>>(b.counts, p.NB, p.L, b.offsets, b.seg_off, b.scan_tmp);
-    HS_LAUNCH_CHECK(ctx);
-    if (nblk > SCAN_BLOCK)
-        return cudaErrorInvalidValue;
-    k_scan_b<<<1, SCAN_THREADS, 0, st>>>(b.scan_tmp, nblk, b.offsets + p.NB, b.seg_off + p.NB);
-    HS_LAUNCH_CHECK(ctx);
-    k_scan_c<<<(p.NB + 255) / 256, 256, 0, st>>>(b.offsets, b.seg_off, p.NB, b.scan_tmp);
-    HS_LAUNCH_CHECK(ctx);
     if ((e = cudaMemsetAsync(b.counts, 0, (size_t)(p.NB + 1) * 4, st)) != cudaSuccess)
         return e;
-    if ((e = recode_dispatch(ctx, p, b, true)) != cudaSuccess)
-        return e;
+    if (p.n_total) {
+        k_recode<true><<<rblocks, 256, 0, st>>>(sc, p.n_total, b.desc, p.M, b.counts, b.offsets, b.sorted);
+        HS_LAUNCH_CHECK(ctx);
+    }
     // segments, longest first
-    const uint32_t nh = (p.L + 1) * p.hist_blocks;
+    const uint32_t nh = (uint32_t)hist_len(p);
     const size_t hsm = (size_t)(p.L + 1) * 4;
     k_seg_hist<<<p.hist_blocks, SEG_HIST_THREADS, hsm, st>>>(b.offsets, p.NB, p.L, p.hist_blocks, b.len_hist);
     HS_LAUNCH_CHECK(ctx);
-    const uint32_t nblk2 = scan_blocks(nh);
-    if (nblk2 > SCAN_BLOCK)
-        return cudaErrorInvalidValue;
-    k_scan_a<<<nblk2, SCAN_THREADS, 0, st>>>(b.len_hist, nh, 1u, b.len_scan, nullptr, b.scan_tmp);
-    HS_LAUNCH_CHECK(ctx);
-    k_scan_b<<<1, SCAN_THREADS, 0, st>>>(b.scan_tmp, nblk2, b.len_scan + nh, nullptr);
-    HS_LAUNCH_CHECK(ctx);
-    k_scan_c<<<(nh + 255) / 256, 256, 0, st>>>(b.len_scan, nullptr, nh, b.scan_tmp);
-    HS_LAUNCH_CHECK(ctx);
+    if ((e = launch_scan(ctx, b.len_hist, nh, 1u, b.len_scan, nullptr, b.scan_tmp)) != cudaSuccess)
+        return e;
     k_seg_scatter<<<p.hist_blocks, SEG_HIST_THREADS, hsm, st>>>(b.offsets, b.seg_off, p.NB, p.L, p.hist_blocks,
                                                                  b.len_scan, b.segs);
     HS_LAUNCH_CHECK(ctx);
@@ -533,29 +581,14 @@ __global__ void k_imad_peak(uint32_t seed, int iters, uint32_t *out)
 // ---------------------------------------------------------------------------
 // host helpers for the C ABI
 // ---------------------------------------------------------------------------
-struct DeviceGuard {
-    int prev = -1;
-    explicit DeviceGuard(int dev)
-    {
-        cudaGetDevice(&prev);
-        if (prev != dev)
-            cudaSetDevice(dev);
-    }
-    ~DeviceGuard()
-    {
-        if (prev >= 0)
-            cudaSetDevice(prev);
-    }
-};
-
-static int fail(Context &ctx, cudaError_t e, const char *what)
+int fail(Context &ctx, cudaError_t e, const char *what)
 {
     ctx.last_error = std::string(what) + ": " + cudaGetErrorString(e);
     cudaGetLastError();
     return e == cudaErrorMemoryAllocation ? HS_ENOMEM : HS_ECUDA;
 }
 
-static int fail_msg(Context &ctx, int code, const char *what)
+int fail_msg(Context &ctx, int code, const char *what)
 {
     ctx.last_error = what;
     return code;
@@ -583,23 +616,99 @@ static bool valid_curve(int c) { return c == HS_HELIOS || c == HS_SELENE; }
 static bool valid_in_fmt(int f) { return f == HS_FMT_JACOBIAN51 || f == HS_FMT_AFFINE51 || f == HS_FMT_AFFINE; }
 static bool valid_out_fmt(int f) { return f >= HS_FMT_JACOBIAN51 && f <= HS_FMT_COMPRESSED; }
 
-// device MSM over resident affine points; result in out_fmt at d_out
-static int msm_on_device(Context &ctx, int curve, const void *d_scalars, const void *d_points, size_t n,
-                         void *d_out, int out_fmt, size_t extra_bytes, void **extra)
+// Reserve the arena for one batch plus extra_bytes of call-specific staging
+// (one reservation: a later reserve could move the arena).
+int reserve_batch(Context &ctx, const BatchPlan &p, size_t extra_bytes, BatchBuffers &b, void **extra)
 {
-    const MsmPlan p = make_plan(ctx, curve, n);
-    HS_CU(ctx.arena.reserve(plan_bytes(p) + align256(extra_bytes) + 512), "workspace allocation");
-    MsmBuffers b;
-    carve(ctx.arena, p, b);
-    if (extra)
+    HS_CU(ctx.arena.reserve(batch_bytes(p) + align256(extra_bytes) + 1024), "workspace allocation");
+    if (!carve(ctx.arena, p, b))
+        return fail_msg(ctx, HS_ENOMEM, "workspace carve");
+    if (extra) {
         *extra = extra_bytes ? ctx.arena.take(extra_bytes) : nullptr;
-    b.scalars = static_cast<const uint32_t *>(d_scalars);
-    b.points = static_cast<const uint4 *>(d_points);
-    HS_CU(launch_sort(ctx, p, b), "recode/sort");
-    const CurveOps &ops = curve_ops(curve);
-    HS_CU(ops.msm_tail(ctx, p, b), "bucket accumulation");
-    HS_CU(ops.format_out(ctx, b.out_jac, 1, out_fmt, d_out), "output formatting");
+        if (extra_bytes && !*extra)
+            return fail_msg(ctx, HS_ENOMEM, "workspace carve");
+    }
     return HS_OK;
+}
+
+static cudaError_t launch_batch(Context &ctx, const BatchPlan &p, const BatchBuffers &b, void *d_out, int out_fmt)
+{
+    cudaError_t e;
+    if ((e = launch_sort(ctx, p, b)) != cudaSuccess)
+        return e;
+    const CurveOps &ops = curve_ops(p.curve);
+    if ((e = ops.msm_tail(ctx, p, b)) != cudaSuccess)
+        return e;
+    return ops.format_out(ctx, b.out_jac, p.M, out_fmt, d_out);
+}
+
+// Run a batch plan whose inputs are in b.scalars / b.points (device, concatenated),
+// results (M records of out_fmt) to d_out.  The descriptors are uploaded every
+// time; the launch sequence is captured once per (shape, buffers) and replayed.
+int execute_batch(Context &ctx, const BatchPlan &p, const BatchBuffers &b, void *d_out, int out_fmt)
+{
+    cudaStream_t st = ctx.stream;
+    HS_CU(cudaMemcpyAsync(b.desc, p.msms.data(), (size_t)p.M * sizeof(MsmDesc), cudaMemcpyHostToDevice, st),
+          "descriptor upload");
+    if (!ctx.use_graphs || ctx.profile) {
+        HS_CU(launch_batch(ctx, p, b, d_out, out_fmt), "MSM launch");
+        return HS_OK;
+    }
+    std::vector<uint64_t> key;
+    key.reserve(12 + 2 * p.M);
+    key.push_back((uint64_t)p.curve);
+    key.push_back((uint64_t)p.M);
+    key.push_back((uint64_t)out_fmt);
+    key.push_back((uint64_t)(uintptr_t)ctx.arena.base);
+    key.push_back((uint64_t)ctx.arena.cap);
+    key.push_back((uint64_t)(uintptr_t)b.desc);
+    key.push_back((uint64_t)(uintptr_t)b.scalars);
+    key.push_back((uint64_t)(uintptr_t)b.points);
+    key.push_back((uint64_t)(uintptr_t)d_out);
+    key.push_back((uint64_t)(uintptr_t)st);
+    for (const MsmDesc &d : p.msms) {
+        key.push_back(((uint64_t)d.n << 8) | d.c);
+    }
+    for (GraphEntry &g : ctx.graphs) {
+        if (g.key == key) {
+            HS_CU(cudaGraphLaunch(g.exec, st), "graph launch");
+            ctx.launches += g.kernels;
+            return HS_OK;
+        }
+    }
+    cudaGraph_t graph = nullptr;
+    const uint64_t before = ctx.launches;
+    HS_CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "graph capture");
+    cudaError_t le = launch_batch(ctx, p, b, d_out, out_fmt);
+    cudaError_t ce = cudaStreamEndCapture(st, &graph);
+    if (le != cudaSuccess || ce != cudaSuccess) {
+        if (graph)
+            cudaGraphDestroy(graph);
+        return fail(ctx, le != cudaSuccess ? le : ce, "graph capture");
+    }
+    cudaGraphExec_t exec = nullptr;
+    cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess)
+        return fail(ctx, ie, "graph instantiate");
+    GraphEntry ent;
+    ent.key = std::move(key);
+    ent.exec = exec;
+    ent.kernels = ctx.launches - before;
+    if (ctx.graphs.size() >= 64) {
+        cudaGraphExecDestroy(ctx.graphs.front().exec);
+        ctx.graphs.erase(ctx.graphs.begin());
+    }
+    ctx.graphs.push_back(std::move(ent));
+    HS_CU(cudaGraphLaunch(exec, st), "graph launch");
+    return HS_OK;
+}
+
+void drop_graphs(Context &ctx)
+{
+    for (GraphEntry &g : ctx.graphs)
+        cudaGraphExecDestroy(g.exec);
+    ctx.graphs.clear();
 }
 
 }  // namespace hs
@@ -675,8 +784,11 @@ void hs_context_destroy(hs_context *h)
     {
         DeviceGuard g(h->c.device);
         cudaStreamSynchronize(h->c.stream);
+        drop_graphs(h->c);
         h->c.arena.release();
         cudaStreamDestroy(h->c.stream);
+        if (h->c.stream2)
+            cudaStreamDestroy(h->c.stream2);
     }
     delete h;
 }
@@ -701,6 +813,18 @@ int hs_context_set_window(hs_context *h, int curve, size_t n_min, size_t n_max, 
     return HS_OK;
 }
 
+int hs_context_set_graphs(hs_context *h, int on)
+{
+    if (!h)
+        return HS_EINVAL;
+    std::lock_guard<std::mutex> lk(h->c.mu);
+    DeviceGuard g(h->c.device);
+    h->c.use_graphs = on != 0;
+    if (!on)
+        drop_graphs(h->c);
+    return HS_OK;
+}
+
 int hs_msm_device(hs_context *h, int curve, const void *d_scalars, const void *d_points, size_t n, void *d_out,
                   int out_fmt)
 {
@@ -718,7 +842,15 @@ int hs_msm_device(hs_context *h, int curve, const void *d_scalars, const void *d
         HS_CU(cudaStreamSynchronize(ctx.stream), "sync");
         return HS_OK;
     }
-    return msm_on_device(ctx, curve, d_scalars, d_points, n, d_out, out_fmt, 0, nullptr);
+    const size_t sizes[1] = {n};
+    const BatchPlan p = make_batch_plan(ctx, curve, sizes, 1);
+    BatchBuffers b;
+    int rc = reserve_batch(ctx, p, 0, b, nullptr);
+    if (rc != HS_OK)
+        return rc;
+    b.scalars = static_cast<const uint32_t *>(d_scalars);
+    b.points = static_cast<const uint4 *>(d_points);
+    return execute_batch(ctx, p, b, d_out, out_fmt);
 }
 
 // Stage host inputs (scalars and points in any format) and run one MSM of
@@ -737,20 +869,21 @@ static int msm_host(Context &ctx, int curve, const uint8_t *lead_scalar, const v
     DeviceGuard g(ctx.device);
     const size_t pb = fmt_bytes(point_fmt);
     const CurveOps &ops = curve_ops(curve);
-    const MsmPlan p = make_plan(ctx, curve, total);
+    const size_t sizes[1] = {total};
+    const BatchPlan p = make_batch_plan(ctx, curve, sizes, 1);
     const size_t need_in = align256(total * 32) + align256(total * 64) +
                            (point_fmt == HS_FMT_AFFINE ? 0 : align256(total * pb)) +
                            align256(ops.to_affine_scratch(total)) + 256;
-    HS_CU(ctx.arena.reserve(plan_bytes(p) + need_in + 1024), "workspace allocation");
-    MsmBuffers b;
-    carve(ctx.arena, p, b);
-    uint8_t *d_sc = (uint8_t *)ctx.arena.take(total * 32);
-    uint8_t *d_pts = (uint8_t *)ctx.arena.take(total * 64);
-    uint8_t *d_raw = point_fmt == HS_FMT_AFFINE ? d_pts : (uint8_t *)ctx.arena.take(total * pb);
-    void *d_scratch = ctx.arena.take(ops.to_affine_scratch(total));
-    void *d_out = ctx.arena.take(128);
-    if (!d_sc || !d_pts || !d_raw || !d_scratch || !d_out)
-        return fail_msg(ctx, HS_ENOMEM, "workspace carve");
+    BatchBuffers b;
+    void *extra = nullptr;
+    int rc = reserve_batch(ctx, p, need_in, b, &extra);
+    if (rc != HS_OK)
+        return rc;
+    uint8_t *d_sc = (uint8_t *)extra;
+    uint8_t *d_pts = d_sc + align256(total * 32);
+    uint8_t *d_raw = point_fmt == HS_FMT_AFFINE ? d_pts : d_pts + align256(total * 64);
+    uint8_t *d_scratch = (point_fmt == HS_FMT_AFFINE ? d_pts + align256(total * 64) : d_raw + align256(total * pb));
+    uint8_t *d_out = d_scratch + align256(ops.to_affine_scratch(total));
     cudaStream_t st = ctx.stream;
     if (lead) {
         HS_CU(cudaMemcpyAsync(d_sc, lead_scalar, 32, cudaMemcpyHostToDevice, st), "H2D scalars");
@@ -764,9 +897,9 @@ static int msm_host(Context &ctx, int curve, const uint8_t *lead_scalar, const v
         HS_CU(ops.to_affine(ctx, d_raw, point_fmt, total, (uint4 *)d_pts, d_scratch), "input conversion");
     b.scalars = (const uint32_t *)d_sc;
     b.points = (const uint4 *)d_pts;
-    HS_CU(launch_sort(ctx, p, b), "recode/sort");
-    HS_CU(ops.msm_tail(ctx, p, b), "bucket accumulation");
-    HS_CU(ops.format_out(ctx, b.out_jac, 1, out_fmt, d_out), "output formatting");
+    rc = execute_batch(ctx, p, b, d_out, out_fmt);
+    if (rc != HS_OK)
+        return rc;
     HS_CU(cudaMemcpyAsync(out, d_out, fmt_bytes(out_fmt), cudaMemcpyDeviceToHost, st), "D2H result");
     HS_CU(cudaStreamSynchronize(st), "MSM");
     return HS_OK;
@@ -917,16 +1050,151 @@ int hs_field_op(hs_context *h, int field, int op, const uint8_t *a, const uint8_
     return HS_OK;
 }
 
+int hs_msm_batch_device(hs_context *h, int curve, const size_t *sizes, size_t count, const void *d_scalars,
+                        const void *d_points, void *d_out, int out_fmt)
+{
+    if (!h || !valid_curve(curve) || !valid_out_fmt(out_fmt) || (count && (!sizes || !d_out)))
+        return HS_EINVAL;
+    if (count == 0)
+        return HS_OK;
+    if (count >= 0x1000000ull)
+        return HS_ERANGE;
+    uint64_t total = 0;
+    for (size_t i = 0; i < count; i++)
+        total += sizes[i];
+    if (total >= 0x80000000ull)
+        return HS_ERANGE;
+    if (total && (!d_scalars || !d_points))
+        return HS_EINVAL;
+    Context &ctx = h->c;
+    std::lock_guard<std::mutex> lk(ctx.mu);
+    DeviceGuard g(ctx.device);
+    const BatchPlan p = make_batch_plan(ctx, curve, sizes, (uint32_t)count);
+    if ((uint64_t)p.NB >= 0x80000000ull || p.entries_bound >= 0x80000000ull)
+        return fail_msg(ctx, HS_ERANGE, "batch too large for one launch sequence");
+    BatchBuffers b;
+    int rc = reserve_batch(ctx, p, 0, b, nullptr);
+    if (rc != HS_OK)
+        return rc;
+    b.scalars = static_cast<const uint32_t *>(d_scalars);
+    b.points = static_cast<const uint4 *>(d_points);
+    return execute_batch(ctx, p, b, d_out, out_fmt);
+}
+
+// Host-buffer batch of MSMs on either curve: the MSMs are grouped by curve,
+// each group is staged into concatenated device arrays and runs as one batch;
+// the Selene group runs on a second stream concurrently with the Helios group.
 int hs_msm_batch(hs_context *h, const hs_msm_desc *descs, size_t count, int point_fmt, int out_fmt)
 {
     if (!h || (count && !descs) || !valid_in_fmt(point_fmt) || !valid_out_fmt(out_fmt))
         return HS_EINVAL;
+    for (size_t i = 0; i < count; i++)
+        if (!valid_curve(descs[i].curve) || !descs[i].out || (descs[i].n && (!descs[i].scalars || !descs[i].points)))
+            return HS_EINVAL;
+    if (count == 0)
+        return HS_OK;
+    Context &ctx = h->c;
+    std::lock_guard<std::mutex> lk(ctx.mu);
+    DeviceGuard g(ctx.device);
+    const size_t pb = fmt_bytes(point_fmt), ob = fmt_bytes(out_fmt);
+    std::vector<size_t> idx[2];
+    std::vector<size_t> sizes[2];
+    size_t totals[2] = {0, 0};
     for (size_t i = 0; i < count; i++) {
-        const int rc = hs_msm(h, descs[i].curve, descs[i].scalars, descs[i].points, point_fmt, descs[i].n,
-                              descs[i].out, out_fmt);
-        if (rc != HS_OK)
-            return rc;
+        const int k = descs[i].curve == HS_SELENE ? 1 : 0;
+        idx[k].push_back(i);
+        sizes[k].push_back(descs[i].n);
+        totals[k] += descs[i].n;
     }
+    if (totals[0] >= 0x80000000ull || totals[1] >= 0x80000000ull)
+        return fail_msg(ctx, HS_ERANGE, "batch too large");
+    BatchPlan plans[2];
+    size_t bytes = 1024, stage[2] = {0, 0};
+    for (int k = 0; k < 2; k++) {
+        if (idx[k].empty())
+            continue;
+        plans[k] = make_batch_plan(ctx, k, sizes[k].data(), (uint32_t)idx[k].size());
+        if (plans[k].entries_bound >= 0x80000000ull)
+            return fail_msg(ctx, HS_ERANGE, "batch too large for one launch sequence");
+        const size_t t = std::max<size_t>(1, totals[k]);
+        stage[k] = align256(t * 32) + align256(t * 64) + (point_fmt == HS_FMT_AFFINE ? 0 : align256(t * pb)) +
+                   align256(curve_ops(k).to_affine_scratch(t)) + align256(idx[k].size() * ob);
+        bytes += batch_bytes(plans[k]) + stage[k] + 1024;
+    }
+    HS_CU(ctx.arena.reserve(bytes), "workspace allocation");
+    BatchBuffers bufs[2];
+    uint8_t *st_base[2] = {nullptr, nullptr};
+    for (int k = 0; k < 2; k++) {
+        if (idx[k].empty())
+            continue;
+        if (!carve(ctx.arena, plans[k], bufs[k]) || !(st_base[k] = (uint8_t *)ctx.arena.take(stage[k])))
+            return fail_msg(ctx, HS_ENOMEM, "workspace carve");
+    }
+    if (!ctx.stream2)
+        HS_CU(cudaStreamCreateWithFlags(&ctx.stream2, cudaStreamNonBlocking), "stream creation");
+    cudaStream_t s1 = ctx.stream;
+    cudaEvent_t ev_in = nullptr, ev_done = nullptr;
+    HS_CU(cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming), "event");
+    HS_CU(cudaEventCreateWithFlags(&ev_done, cudaEventDisableTiming), "event");
+    struct EvGuard {
+        cudaEvent_t a, b;
+        ~EvGuard()
+        {
+            cudaEventDestroy(a);
+            cudaEventDestroy(b);
+        }
+    } evg{ev_in, ev_done};
+    uint8_t *d_out[2] = {nullptr, nullptr};
+    // stage inputs (all copies on the first stream)
+    for (int k = 0; k < 2; k++) {
+        if (idx[k].empty())
+            continue;
+        const size_t t = std::max<size_t>(1, totals[k]);
+        uint8_t *d_sc = st_base[k];
+        uint8_t *d_pts = d_sc + align256(t * 32);
+        uint8_t *d_raw = point_fmt == HS_FMT_AFFINE ? d_pts : d_pts + align256(t * 64);
+        uint8_t *d_scr = point_fmt == HS_FMT_AFFINE ? d_pts + align256(t * 64) : d_raw + align256(t * pb);
+        d_out[k] = d_scr + align256(curve_ops(k).to_affine_scratch(t));
+        size_t off = 0;
+        for (size_t j = 0; j < idx[k].size(); j++) {
+            const hs_msm_desc &d = descs[idx[k][j]];
+            if (d.n) {
+                HS_CU(cudaMemcpyAsync(d_sc + 32 * off, d.scalars, d.n * 32, cudaMemcpyHostToDevice, s1), "H2D");
+                HS_CU(cudaMemcpyAsync(d_raw + pb * off, d.points, d.n * pb, cudaMemcpyHostToDevice, s1), "H2D");
+            }
+            off += d.n;
+        }
+        if (point_fmt != HS_FMT_AFFINE && totals[k])
+            HS_CU(curve_ops(k).to_affine(ctx, d_raw, point_fmt, totals[k], (uint4 *)d_pts, d_scr), "conversion");
+        bufs[k].scalars = (const uint32_t *)d_sc;
+        bufs[k].points = (const uint4 *)d_pts;
+    }
+    HS_CU(cudaEventRecord(ev_in, s1), "event");
+    // Helios group on the first stream, Selene group on the second
+    int rc = HS_OK;
+    if (!idx[0].empty())
+        rc = execute_batch(ctx, plans[0], bufs[0], d_out[0], out_fmt);
+    if (rc == HS_OK && !idx[1].empty()) {
+        HS_CU(cudaStreamWaitEvent(ctx.stream2, ev_in, 0), "stream wait");
+        ctx.stream = ctx.stream2;
+        rc = execute_batch(ctx, plans[1], bufs[1], d_out[1], out_fmt);
+        ctx.stream = s1;
+        HS_CU(cudaEventRecord(ev_done, ctx.stream2), "event");
+        HS_CU(cudaStreamWaitEvent(s1, ev_done, 0), "stream wait");
+    }
+    if (rc != HS_OK)
+        return rc;
+    std::vector<uint8_t> host_out[2];
+    for (int k = 0; k < 2; k++) {
+        if (idx[k].empty())
+            continue;
+        host_out[k].resize(idx[k].size() * ob);
+        HS_CU(cudaMemcpyAsync(host_out[k].data(), d_out[k], host_out[k].size(), cudaMemcpyDeviceToHost, s1), "D2H");
+    }
+    HS_CU(cudaStreamSynchronize(s1), "MSM batch");
+    for (int k = 0; k < 2; k++)
+        for (size_t j = 0; j < idx[k].size(); j++)
+            std::memcpy(descs[idx[k][j]].out, host_out[k].data() + j * ob, ob);
     return HS_OK;
 }
 

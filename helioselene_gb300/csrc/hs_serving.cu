@@ -1,0 +1,492 @@
+// hs_serving.cu -- continuous-batching request loop for MSMs (hs_server_*).
+//
+// The reference has no serving layer; this is the GB300 form of "many
+// independent public-data MSMs arriving over time" (FCMP++ alternates Helios
+// and Selene layers).  One scheduler thread owns `slots` execution slots
+// (stream + workspace each).  Each pass it (1) retires slots whose completion
+// event fired, copying results out and waking waiters; (2) while a slot is
+// free and requests are queued, takes the oldest request's curve, collects up
+// to the caps of queued requests of that curve (FIFO), checks the batch's
+// workspace against the HBM budget, stages scalars / fresh bases, gathers pool
+// bases on the device, and launches the batched MSM pipeline on that slot.
+// All waits are host-side and bounded.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "hs_internal.h"
+
+namespace hs {
+
+// out[dst[p]] = pool[src[p]] (64-byte affine points)
+__global__ void k_gather_pool(const uint4 *__restrict__ pool, const uint32_t *__restrict__ src,
+                              const uint32_t *__restrict__ dst, uint32_t count, uint4 *__restrict__ out)
+{
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= count)
+        return;
+    const uint4 *s = pool + 4 * (size_t)src[p];
+    uint4 *d = out + 4 * (size_t)dst[p];
+    d[0] = s[0];
+    d[1] = s[1];
+    d[2] = s[2];
+    d[3] = s[3];
+}
+
+using Clock = std::chrono::steady_clock;
+
+struct ReqState {
+    hs_request req;
+    size_t n = 0;
+    Clock::time_point submitted;
+    double latency_ms = 0.0;
+    int status = 1;  // 1 = pending, else HS_OK / error
+};
+
+struct Slot {
+    Context ctx;
+    cudaEvent_t done = nullptr;
+    bool busy = false;
+    int curve = 0;
+    size_t bytes = 0;
+    std::vector<uint64_t> tickets;
+    uint8_t *pinned_out = nullptr;
+    size_t pinned_cap = 0;
+    std::vector<uint32_t> h_src, h_dst;  // staging of the pool gather (kept alive until retire)
+};
+
+struct Pool {
+    uint4 *d = nullptr;
+    size_t n = 0;
+};
+
+struct Server {
+    hs_server_config cfg{};
+    std::vector<std::unique_ptr<Slot>> slots;
+    Pool pools[2];
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<uint64_t> queue;
+    std::unordered_map<uint64_t, ReqState> reqs;
+    uint64_t next_ticket = 1;
+    size_t in_flight = 0;
+    bool stop = false;
+    hs_server_stats stats{};
+    std::thread thr;
+    std::string last_error;
+};
+
+static size_t batch_stage_bytes(size_t total, size_t total_pool, size_t msms, size_t ob)
+{
+    return align256(std::max<size_t>(1, total) * 32) + align256(std::max<size_t>(1, total) * 64) +
+           2 * align256(std::max<size_t>(1, total_pool) * 4) + align256(std::max<size_t>(1, msms) * ob);
+}
+
+// launch one batch on slot s; called with the server lock held; false = deferred (budget)
+static bool launch(Server &S, Slot &s, std::vector<uint64_t> &batch, int curve)
+{
+    const size_t ob = fmt_bytes(S.cfg.out_fmt);
+    std::vector<size_t> sizes;
+    size_t total = 0, total_pool = 0;
+    for (uint64_t t : batch) {
+        const ReqState &r = S.reqs[t];
+        sizes.push_back(r.n);
+        total += r.n;
+        total_pool += r.req.n_pool;
+    }
+    Context &ctx = s.ctx;
+    const BatchPlan p = make_batch_plan(ctx, curve, sizes.data(), (uint32_t)sizes.size());
+    const size_t extra = batch_stage_bytes(total, total_pool, batch.size(), ob);
+    const size_t bytes = batch_bytes(p) + extra + 2048;
+    if (S.in_flight > 0 && S.in_flight + bytes > S.cfg.hbm_budget) {
+        S.stats.deferred++;
+        return false;
+    }
+    auto fail_batch = [&](int code) {
+        for (uint64_t t : batch) {
+            ReqState &r = S.reqs[t];
+            r.status = code;
+            S.stats.failed++;
+        }
+        S.last_error = ctx.last_error;
+        S.cv_done.notify_all();
+        return true;
+    };
+    BatchBuffers b;
+    void *ext = nullptr;
+    if (reserve_batch(ctx, p, extra, b, &ext) != HS_OK)
+        return fail_batch(HS_ENOMEM);
+    uint8_t *d_sc = (uint8_t *)ext;
+    uint8_t *d_pts = d_sc + align256(std::max<size_t>(1, total) * 32);
+    uint32_t *d_src = (uint32_t *)(d_pts + align256(std::max<size_t>(1, total) * 64));
+    uint32_t *d_dst = d_src + align256(std::max<size_t>(1, total_pool) * 4) / 4;
+    uint8_t *d_out = (uint8_t *)(d_dst) + align256(std::max<size_t>(1, total_pool) * 4);
+    if (s.pinned_cap < batch.size() * ob) {
+        if (s.pinned_out)
+            cudaFreeHost(s.pinned_out);
+        s.pinned_cap = std::max<size_t>(batch.size() * ob, 1024 * 120);
+        if (cudaMallocHost((void **)&s.pinned_out, s.pinned_cap) != cudaSuccess) {
+            s.pinned_out = nullptr;
+            s.pinned_cap = 0;
+            cudaGetLastError();
+            return fail_batch(HS_ENOMEM);
+        }
+    }
+    cudaStream_t st = ctx.stream;
+    s.h_src.clear();
+    s.h_dst.clear();
+    size_t off = 0;
+    cudaError_t e = cudaSuccess;
+    for (uint64_t t : batch) {
+        const hs_request &q = S.reqs[t].req;
+        const size_t n = q.n_pool + q.n_fresh;
+        if (n && e == cudaSuccess)
+            e = cudaMemcpyAsync(d_sc + 32 * off, q.scalars, 32 * n, cudaMemcpyHostToDevice, st);
+        if (q.n_fresh && e == cudaSuccess)
+            e = cudaMemcpyAsync(d_pts + 64 * (off + q.n_pool), q.fresh_points, 64 * q.n_fresh,
+                                cudaMemcpyHostToDevice, st);
+        for (size_t j = 0; j < q.n_pool; j++) {
+            s.h_src.push_back(q.pool_idx[j]);
+            s.h_dst.push_back((uint32_t)(off + j));
+        }
+        off += n;
+    }
+    if (total_pool && e == cudaSuccess) {
+        e = cudaMemcpyAsync(d_src, s.h_src.data(), 4 * total_pool, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(d_dst, s.h_dst.data(), 4 * total_pool, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) {
+            k_gather_pool<<<(unsigned)((total_pool + 255) / 256), 256, 0, st>>>(S.pools[curve].d, d_src, d_dst,
+                                                                              (uint32_t)total_pool, (uint4 *)d_pts);
+            ctx.launches++;
+            e = cudaGetLastError();
+        }
+    }
+    if (e != cudaSuccess) {
+        ctx.last_error = std::string("staging: ") + cudaGetErrorString(e);
+        return fail_batch(HS_ECUDA);
+    }
+    b.scalars = (const uint32_t *)d_sc;
+    b.points = (const uint4 *)d_pts;
+    if (execute_batch(ctx, p, b, d_out, S.cfg.out_fmt) != HS_OK)
+        return fail_batch(HS_ECUDA);
+    e = cudaMemcpyAsync(s.pinned_out, d_out, batch.size() * ob, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+        e = cudaEventRecord(s.done, st);
+    if (e != cudaSuccess) {
+        ctx.last_error = std::string("result copy: ") + cudaGetErrorString(e);
+        return fail_batch(HS_ECUDA);
+    }
+    s.busy = true;
+    s.curve = curve;
+    s.bytes = bytes;
+    s.tickets = batch;
+    S.in_flight += bytes;
+    S.stats.peak_bytes = std::max<uint64_t>(S.stats.peak_bytes, S.in_flight);
+    S.stats.batches++;
+    S.stats.max_batch_msms = std::max<uint64_t>(S.stats.max_batch_msms, batch.size());
+    return true;
+}
+
+static void retire(Server &S, Slot &s, cudaError_t status)
+{
+    const size_t ob = fmt_bytes(S.cfg.out_fmt);
+    const auto now = Clock::now();
+    for (size_t j = 0; j < s.tickets.size(); j++) {
+        auto it = S.reqs.find(s.tickets[j]);
+        if (it == S.reqs.end())
+            continue;
+        ReqState &r = it->second;
+        if (status == cudaSuccess) {
+            std::memcpy(r.req.out, s.pinned_out + j * ob, ob);
+            r.status = HS_OK;
+            S.stats.completed++;
+        } else {
+            r.status = HS_ECUDA;
+            S.stats.failed++;
+        }
+        r.latency_ms = std::chrono::duration<double, std::milli>(now - r.submitted).count();
+    }
+    if (status != cudaSuccess)
+        S.last_error = std::string("batch: ") + cudaGetErrorString(status);
+    S.in_flight -= s.bytes;
+    s.bytes = 0;
+    s.busy = false;
+    s.tickets.clear();
+    S.cv_done.notify_all();
+}
+
+static void scheduler(Server *Sp)
+{
+    Server &S = *Sp;
+    cudaSetDevice(S.cfg.device);
+    std::unique_lock<std::mutex> lk(S.mu);
+    while (true) {
+        bool progress = false;
+        for (auto &sp : S.slots) {
+            Slot &s = *sp;
+            if (!s.busy)
+                continue;
+            const cudaError_t q = cudaEventQuery(s.done);
+            if (q == cudaErrorNotReady)
+                continue;
+            if (q != cudaSuccess)
+                cudaGetLastError();
+            retire(S, s, q);
+            progress = true;
+        }
+        if (S.stop) {
+            bool any = false;
+            for (auto &sp : S.slots)
+                any = any || sp->busy;
+            if (!any)
+                break;
+        }
+        while (!S.stop && !S.queue.empty()) {
+            Slot *free_slot = nullptr;
+            for (auto &sp : S.slots)
+                if (!sp->busy) {
+                    free_slot = sp.get();
+                    break;
+                }
+            if (!free_slot)
+                break;
+            // oldest request decides the curve; take queued requests of that curve, FIFO, up to the caps
+            const int curve = S.reqs[S.queue.front()].req.curve;
+            std::vector<uint64_t> batch;
+            size_t pts = 0;
+            std::deque<uint64_t> rest;
+            while (!S.queue.empty()) {
+                const uint64_t t = S.queue.front();
+                S.queue.pop_front();
+                const ReqState &r = S.reqs[t];
+                if (r.req.curve == curve && batch.size() < S.cfg.max_batch_msms &&
+                    (batch.empty() || pts + r.n <= S.cfg.max_batch_points)) {
+                    batch.push_back(t);
+                    pts += r.n;
+                } else {
+                    rest.push_back(t);
+                }
+            }
+            S.queue.swap(rest);
+            if (!launch(S, *free_slot, batch, curve)) {
+                // over budget: put the batch back at the front and wait for a completion
+                for (auto it = batch.rbegin(); it != batch.rend(); ++it)
+                    S.queue.push_front(*it);
+                break;
+            }
+            progress = true;
+        }
+        if (!progress) {
+            bool busy = false;
+            for (auto &sp : S.slots)
+                busy = busy || sp->busy;
+            // poll the device every 50 us while batches are in flight, otherwise sleep until work arrives
+            S.cv_work.wait_for(lk, busy ? std::chrono::microseconds(50) : std::chrono::milliseconds(20));
+        }
+    }
+    // fail what is still queued
+    for (uint64_t t : S.queue) {
+        S.reqs[t].status = HS_EBUSY;
+        S.stats.failed++;
+    }
+    S.queue.clear();
+    S.cv_done.notify_all();
+}
+
+}  // namespace hs
+
+using namespace hs;
+
+struct hs_server {
+    Server s;
+};
+
+extern "C" {
+
+int hs_server_create(hs_server **out, const hs_server_config *cfg)
+{
+    if (!out || !cfg)
+        return HS_EINVAL;
+    *out = nullptr;
+    if (cfg->out_fmt < HS_FMT_JACOBIAN51 || cfg->out_fmt > HS_FMT_COMPRESSED || cfg->slots < 0 || cfg->slots > 16)
+        return HS_EINVAL;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || cfg->device < 0 || cfg->device >= count) {
+        cudaGetLastError();
+        return HS_EINVAL;
+    }
+    std::unique_ptr<hs_server> h(new (std::nothrow) hs_server());
+    if (!h)
+        return HS_ENOMEM;
+    Server &S = h->s;
+    S.cfg = *cfg;
+    if (S.cfg.slots == 0)
+        S.cfg.slots = 4;
+    if (S.cfg.max_batch_points == 0)
+        S.cfg.max_batch_points = size_t(1) << 22;
+    if (S.cfg.max_batch_msms == 0)
+        S.cfg.max_batch_msms = 1024;
+    DeviceGuard g(S.cfg.device);
+    if (S.cfg.hbm_budget == 0) {
+        size_t fr = 0, tot = 0;
+        if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+            cudaGetLastError();
+            return HS_ECUDA;
+        }
+        S.cfg.hbm_budget = fr / 2;
+    }
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, S.cfg.device);
+    for (int i = 0; i < S.cfg.slots; i++) {
+        auto sl = std::make_unique<Slot>();
+        sl->ctx.device = S.cfg.device;
+        sl->ctx.sm_count = sms;
+        sl->ctx.use_graphs = false;  // request shapes rarely repeat
+        if (cudaStreamCreateWithFlags(&sl->ctx.stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&sl->done, cudaEventDisableTiming) != cudaSuccess) {
+            cudaGetLastError();
+            return HS_ECUDA;
+        }
+        S.slots.push_back(std::move(sl));
+    }
+    S.thr = std::thread(scheduler, &S);
+    *out = h.release();
+    return HS_OK;
+}
+
+int hs_server_set_pool(hs_server *h, int curve, const void *pts, size_t n)
+{
+    if (!h || (curve != HS_HELIOS && curve != HS_SELENE) || (n && !pts) || n >= 0x80000000ull)
+        return HS_EINVAL;
+    Server &S = h->s;
+    std::lock_guard<std::mutex> lk(S.mu);
+    for (auto &sp : S.slots)
+        if (sp->busy || !S.queue.empty())
+            return HS_EBUSY;  // replace pools only while idle
+    DeviceGuard g(S.cfg.device);
+    Pool &p = S.pools[curve];
+    if (p.d)
+        cudaFree(p.d);
+    p.d = nullptr;
+    p.n = 0;
+    if (!n)
+        return HS_OK;
+    if (cudaMalloc((void **)&p.d, n * 64) != cudaSuccess) {
+        cudaGetLastError();
+        p.d = nullptr;
+        return HS_ENOMEM;
+    }
+    if (cudaMemcpy(p.d, pts, n * 64, cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaGetLastError();
+        return HS_ECUDA;
+    }
+    p.n = n;
+    return HS_OK;
+}
+
+int hs_server_submit(hs_server *h, const hs_request *req, uint64_t *ticket)
+{
+    if (!h || !req || !ticket || (req->curve != HS_HELIOS && req->curve != HS_SELENE) || !req->out)
+        return HS_EINVAL;
+    const size_t n = req->n_pool + req->n_fresh;
+    if ((n && !req->scalars) || (req->n_pool && !req->pool_idx) || (req->n_fresh && !req->fresh_points))
+        return HS_EINVAL;
+    Server &S = h->s;
+    if (n > S.cfg.max_batch_points)
+        return HS_ERANGE;
+    std::lock_guard<std::mutex> lk(S.mu);
+    if (S.stop)
+        return HS_EBUSY;
+    if (req->n_pool) {
+        const Pool &p = S.pools[req->curve];
+        for (size_t j = 0; j < req->n_pool; j++)
+            if (req->pool_idx[j] >= p.n)
+                return HS_EINVAL;
+    }
+    const uint64_t t = S.next_ticket++;
+    ReqState &r = S.reqs[t];
+    r.req = *req;
+    r.n = n;
+    r.submitted = Clock::now();
+    S.queue.push_back(t);
+    S.stats.submitted++;
+    *ticket = t;
+    S.cv_work.notify_one();
+    return HS_OK;
+}
+
+int hs_server_wait(hs_server *h, uint64_t ticket, int timeout_ms, double *latency_ms)
+{
+    if (!h)
+        return HS_EINVAL;
+    Server &S = h->s;
+    std::unique_lock<std::mutex> lk(S.mu);
+    auto it = S.reqs.find(ticket);
+    if (it == S.reqs.end())
+        return HS_EINVAL;
+    const auto deadline = Clock::now() + std::chrono::milliseconds(std::max(0, timeout_ms));
+    while (it->second.status == 1) {
+        if (S.cv_done.wait_until(lk, deadline) == std::cv_status::timeout && it->second.status == 1)
+            return HS_ETIMEDOUT;
+        it = S.reqs.find(ticket);
+        if (it == S.reqs.end())
+            return HS_EINVAL;
+    }
+    const int st = it->second.status;
+    if (latency_ms)
+        *latency_ms = it->second.latency_ms;
+    S.reqs.erase(it);
+    return st;
+}
+
+int hs_server_get_stats(hs_server *h, hs_server_stats *st)
+{
+    if (!h || !st)
+        return HS_EINVAL;
+    std::lock_guard<std::mutex> lk(h->s.mu);
+    *st = h->s.stats;
+    return HS_OK;
+}
+
+void hs_server_destroy(hs_server *h)
+{
+    if (!h)
+        return;
+    Server &S = h->s;
+    {
+        std::lock_guard<std::mutex> lk(S.mu);
+        S.stop = true;
+        S.cv_work.notify_all();
+    }
+    if (S.thr.joinable())
+        S.thr.join();
+    {
+        DeviceGuard g(S.cfg.device);
+        for (auto &sp : S.slots) {
+            Slot &s = *sp;
+            cudaStreamSynchronize(s.ctx.stream);
+            drop_graphs(s.ctx);
+            s.ctx.arena.release();
+            cudaStreamDestroy(s.ctx.stream);
+            cudaEventDestroy(s.done);
+            if (s.pinned_out)
+                cudaFreeHost(s.pinned_out);
+        }
+        for (Pool &p : S.pools)
+            if (p.d)
+                cudaFree(p.d);
+    }
+    delete h;
+}
+
+}  // extern "C"

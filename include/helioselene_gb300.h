@@ -88,6 +88,9 @@ void *hs_context_stream(hs_context *ctx);
 /* set the Pippenger window width for one curve; 0 restores the built-in
  * cost model (the autotuner writes this) */
 int hs_context_set_window(hs_context *ctx, int curve, size_t n_min, size_t n_max, int window);
+/* capture launch sequences as CUDA graphs and replay them for repeated shapes
+ * (on by default); off launches every kernel directly */
+int hs_context_set_graphs(hs_context *ctx, int on);
 
 /* ---- MSM: sum of scalars[i] * points[i] ----
  * Replaces helios_msm_vartime / selene_msm_vartime
@@ -141,6 +144,70 @@ typedef struct hs_msm_desc {
     void *out;
 } hs_msm_desc;
 int hs_msm_batch(hs_context *ctx, const hs_msm_desc *descs, size_t count, int point_fmt, int out_fmt);
+
+/* Batched MSMs on device-resident data, all on one curve: MSM i has sizes[i]
+ * points whose scalars (32 bytes each) and HS_FMT_AFFINE points (64 bytes each)
+ * follow those of MSM i-1 in d_scalars / d_points; d_out receives count
+ * records of out_fmt.  One launch sequence serves the whole batch: recode and
+ * counting sort over all MSMs' buckets, one accumulation launch, reductions
+ * indexed by MSM, and one warp per MSM for the window combination.  Window
+ * widths come from the context's rules (hs_context_set_window) or the cost
+ * model, per MSM size.  Runs on the context stream; does not synchronise. */
+int hs_msm_batch_device(hs_context *ctx, int curve, const size_t *sizes, size_t count, const void *d_scalars,
+                        const void *d_points, void *d_out, int out_fmt);
+
+/* ---- serving: continuous batching of MSM requests ----
+ * A server owns `slots` CUDA streams, each with its own workspace, a request
+ * queue and one scheduler thread.  Requests that arrive while others are on
+ * the GPU are admitted as soon as a slot and enough of the HBM budget are
+ * free: the scheduler groups queued requests by curve (up to the batch caps),
+ * gathers their pool bases on the device, and runs each group as one batched
+ * launch sequence (the hs_msm_batch_device pipeline) on a free slot, so
+ * batches overlap on the device.  Completion is detected with CUDA events and
+ * bounded host waits only.  A request's buffers (scalars, indices, fresh
+ * points, out) must stay valid until hs_server_wait has returned for it;
+ * page-locked buffers let the copies run asynchronously.  Results are the
+ * same whichever requests share a batch: with HS_FMT_COMPRESSED or
+ * HS_FMT_AFFINE the bytes are identical alone and in the mix (a Jacobian
+ * result is the same point, its Z depends on the summation order). */
+typedef struct hs_server hs_server;
+
+typedef struct hs_server_config {
+    int device;
+    int slots;               /* batches in flight at once, 1..16; 0 selects 4 */
+    size_t hbm_budget;       /* device bytes the in-flight batches may hold; 0 selects half the free memory */
+    size_t max_batch_points; /* points per launched batch; 0 selects 2^22 */
+    size_t max_batch_msms;   /* requests per launched batch; 0 selects 1024 */
+    int out_fmt;             /* result format of every request */
+} hs_server_config;
+
+typedef struct hs_request {
+    int curve;
+    size_t n_pool;            /* leading bases taken from the curve's resident pool */
+    const uint32_t *pool_idx; /* n_pool indices into that pool */
+    size_t n_fresh;           /* trailing bases given with the request */
+    const void *fresh_points; /* n_fresh HS_FMT_AFFINE points */
+    const uint8_t *scalars;   /* (n_pool + n_fresh) * 32 bytes */
+    void *out;                /* one out_fmt record, written before the request completes */
+} hs_request;
+
+typedef struct hs_server_stats {
+    uint64_t submitted, completed, failed, batches, max_batch_msms;
+    uint64_t peak_bytes;   /* peak device workspace held by in-flight batches */
+    uint64_t deferred;     /* launches postponed by the HBM budget */
+} hs_server_stats;
+
+int hs_server_create(hs_server **srv, const hs_server_config *cfg);
+/* upload (replace) the resident base pool of one curve: n HS_FMT_AFFINE points */
+int hs_server_set_pool(hs_server *srv, int curve, const void *affine_points, size_t n);
+/* queue a request; HS_ERANGE if it alone exceeds the batch caps or the budget */
+int hs_server_submit(hs_server *srv, const hs_request *req, uint64_t *ticket);
+/* wait up to timeout_ms for a request: HS_OK (result written, latency from
+ * submit to completion in *latency_ms), HS_ETIMEDOUT, or the failure status */
+int hs_server_wait(hs_server *srv, uint64_t ticket, int timeout_ms, double *latency_ms);
+int hs_server_get_stats(hs_server *srv, hs_server_stats *st);
+/* stops the scheduler after the in-flight batches finish; queued requests fail */
+void hs_server_destroy(hs_server *srv);
 
 /* ---- drop-in entry points with the reference's exact signatures ----
  * Same arguments and meaning as helios_msm_vartime / selene_msm_vartime
