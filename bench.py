@@ -355,6 +355,77 @@ def run_serving(hs, torch, device: str, local: int, requests_per_rate: int = 100
     return out
 
 
+def run_fixed(hs, torch, device: str, local: int, count: int = 64) -> dict:
+    """Config 5: Pedersen-style commitments r*H + sum v_i G_i over n = 2^20 resident
+    generators per curve with device window tables; scalars uniform mod order
+    (< 2^255, bit 255 cleared) with 10% of the commitments sparse (one 16-bit value
+    per scalar, <= 16 set bits); all outputs normalised to affine with one shared
+    inversion per 16 commitments.  Against the plain per-call MSM of n + 1 terms."""
+    from helioselene_gb300.workload import random_field_bytes
+    n = 1 << 20
+    rng = np.random.default_rng(SEED + 5)
+    gen = torch.Generator(device=device)
+    gen.manual_seed(SEED + 5)
+    ctx = hs.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=device)
+    out = {"generators": n, "commitments": count, "sparse_fraction": 0.1}
+    for curve, name in ((hs.HELIOS, "helios"), (hs.SELENE, "selene")):
+        d_u = torch.from_numpy(random_field_bytes(rng, n + 1).reshape(-1)).to(device)
+        d_pts = torch.empty((n + 1) * 64, dtype=torch.uint8, device=device)
+        torch.cuda.synchronize()
+        ctx.map_to_curve_device(curve, d_u.data_ptr(), n + 1, d_pts.data_ptr())
+        torch.cuda.synchronize()
+        gens = d_pts.cpu().numpy().reshape(n + 1, 64)
+        t0 = time.perf_counter()
+        fb = hs.FixedBase(ctx, curve, gens[:n], H=gens[n])
+        table_s = time.perf_counter() - t0
+        sc = torch.randint(0, 256, (count, n + 1, 32), dtype=torch.uint8, device=device, generator=gen)
+        sc[:, :, 31] &= 0x7F
+        nsparse = max(1, count // 10)
+        sp = sc[:nsparse]
+        sp.zero_()
+        v16 = torch.randint(0, 65536, (nsparse, n + 1), device=device, generator=gen)
+        off = torch.randint(0, 30, (nsparse, n + 1), device=device, generator=gen)
+        lo = (v16 & 0xFF).to(torch.uint8)
+        hi = (v16 >> 8).to(torch.uint8)
+        sp.scatter_(2, off.unsqueeze(2), lo.unsqueeze(2))
+        sp.scatter_(2, (off + 1).unsqueeze(2), hi.unsqueeze(2))
+        d_out = torch.empty(count * 64, dtype=torch.uint8, device=device)
+        torch.cuda.synchronize()
+        fb.commit_device(sc.data_ptr(), count, d_out.data_ptr(), hs.FMT_AFFINE)  # warm-up / graph capture
+        stream.synchronize()
+        a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fb.commit_device(sc.data_ptr(), count, d_out.data_ptr(), hs.FMT_AFFINE)
+        e.record(stream)
+        stream.synchronize()
+        fixed_ms = a.elapsed_time(e)
+        # plain path: one MSM of n + 1 terms per commitment, on the same device data
+        k = 3
+        d_plain = torch.empty(k * 120, dtype=torch.uint8, device=device)
+        ctx.msm_device(curve, sc[nsparse].data_ptr(), d_pts.data_ptr(), n + 1, d_plain.data_ptr())
+        stream.synchronize()
+        a.record(stream)
+        for j in range(k):
+            ctx.msm_device(curve, sc[nsparse + j].data_ptr(), d_pts.data_ptr(), n + 1, d_plain.data_ptr() + 120 * j)
+        e.record(stream)
+        stream.synchronize()
+        plain_ms = a.elapsed_time(e) / k
+        aff = d_out.cpu().numpy().reshape(count, 64)
+        got = ctx.compress(curve, aff[nsparse:nsparse + k], hs.FMT_AFFINE)
+        want = ctx.compress(curve, d_plain.cpu().numpy(), hs.FMT_JACOBIAN51)
+        out[name] = {"window": fb.window, "table_bytes": fb.table_bytes, "table_build_s": table_s,
+                     "commitments_per_s": count / (fixed_ms * 1e-3), "ms": fixed_ms,
+                     "plain_ms_per_commitment": plain_ms,
+                     "speedup_vs_plain": plain_ms * count / fixed_ms,
+                     "bit_exact_vs_plain": bool((got == want).all())}
+        fb.close()
+        del sc, d_out, d_pts, d_u
+        torch.cuda.empty_cache()
+    ctx.close()
+    return out
+
+
 def cpu_baseline_leg(data, n: int, gpu_results: dict) -> dict:
     """The oracle port on all host cores, on the same workload; also checks the GPU results."""
     sys.path.insert(0, str(ROOT / "oracle"))
@@ -500,6 +571,9 @@ def run_ours(args) -> None:
     serving = None
     if not args.no_serving:
         serving = run_serving(hs, torch, device, local)
+    fixed = None
+    if not args.no_fixed:
+        fixed = run_fixed(hs, torch, device, local)
     m_n, c_star = modmul_count(n)
     whole = m_n * (IMAD_PER_MODMUL[0] + IMAD_PER_MODMUL[1]) / (ms_per_step * 1e-3)
 
@@ -530,6 +604,8 @@ def run_ours(args) -> None:
             line["batched"] = batched
         if not args.no_serving:
             line["serving"] = serving
+        if not args.no_fixed:
+            line["fixed_base"] = fixed
         if ws == 1 and not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline_leg(data, n, results)
         print(json.dumps(line), flush=True)
@@ -586,6 +662,7 @@ def main() -> None:
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched (1024 uneven MSMs) section")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving (Poisson arrivals) section")
+    ap.add_argument("--no-fixed", action="store_true", help="skip the fixed-base commitment section")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -72,6 +72,11 @@ SIGNATURES = {
                                _int]),
     "hs_measure_imad_peak": (_int, [_vp, _c.POINTER(_c.c_double)]),
     "hs_field_op": (_int, [_vp, _int, _int, _vp, _vp, _sz, _vp]),
+    "hs_fixed_base_create": (_int, [_vp, _int, _vp, _int, _sz, _vp, _int, _c.POINTER(_vp)]),
+    "hs_fixed_base_commit": (_int, [_vp, _vp, _vp, _vp, _sz, _vp, _int]),
+    "hs_fixed_base_commit_device": (_int, [_vp, _vp, _vp, _sz, _vp, _int]),
+    "hs_fixed_base_info": (_int, [_vp, _c.POINTER(_int), _c.POINTER(_sz)]),
+    "hs_fixed_base_destroy": (None, [_vp]),
     "hs_server_create": (_int, [_c.POINTER(_vp), _c.POINTER(hs_server_config)]),
     "hs_server_set_pool": (_int, [_vp, _int, _vp, _sz]),
     "hs_server_submit": (_int, [_vp, _c.POINTER(hs_request), _c.POINTER(_c.c_uint64)]),

@@ -190,6 +190,54 @@ class Context:
                                                      ctypes.c_void_p(d_out)), "hs_map_to_curve_device")
 
 
+class FixedBase:
+    """Resident generator set with device window tables (hs_fixed_base_*):
+    commitments r*H + sum v_i G_i over the same generators."""
+
+    def __init__(self, ctx: Context, curve: int, generators, H=None, point_fmt: int = L.FMT_AFFINE, window: int = 0):
+        self.ctx, self.curve = ctx, curve
+        g = _u8(generators)
+        self.n = g.size // L.FMT_BYTES[point_fmt]
+        h = _u8(H) if H is not None else None
+        fb = ctypes.c_void_p()
+        ctx._check(ctx._lib.hs_fixed_base_create(ctx.handle, curve, _ptr(g), point_fmt, self.n,
+                                                 None if h is None else _ptr(h), window, ctypes.byref(fb)),
+                   "hs_fixed_base_create")
+        self._fb = fb
+        self.has_H = H is not None
+        w, tb = ctypes.c_int(), ctypes.c_size_t()
+        ctx._lib.hs_fixed_base_info(fb, ctypes.byref(w), ctypes.byref(tb))
+        self.window, self.table_bytes = w.value, tb.value
+
+    def commit(self, values, blindings=None, out_fmt: int = L.FMT_COMPRESSED) -> List[bytes]:
+        v = _u8(values)
+        count = v.size // (32 * self.n) if self.n else (len(blindings) // 32 if blindings is not None else 0)
+        b = _u8(blindings) if blindings is not None else None
+        out = np.zeros(count * L.FMT_BYTES[out_fmt], np.uint8)
+        self.ctx._check(self.ctx._lib.hs_fixed_base_commit(self.ctx.handle, self._fb, _ptr(v),
+                                                           None if b is None else _ptr(b), count, _ptr(out),
+                                                           out_fmt), "hs_fixed_base_commit")
+        ob = L.FMT_BYTES[out_fmt]
+        return [out[ob * i:ob * (i + 1)].tobytes() for i in range(count)]
+
+    def commit_device(self, d_scalars: int, count: int, d_out: int, out_fmt: int = L.FMT_JACOBIAN51) -> None:
+        self.ctx._check(self.ctx._lib.hs_fixed_base_commit_device(self.ctx.handle, self._fb,
+                                                                  ctypes.c_void_p(d_scalars), count,
+                                                                  ctypes.c_void_p(d_out), out_fmt),
+                        "hs_fixed_base_commit_device")
+
+    def close(self) -> None:
+        if getattr(self, "_fb", None):
+            self.ctx._lib.hs_fixed_base_destroy(self._fb)
+            self._fb = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Server:
     """Continuous-batching MSM server (hs_server_*): submit requests as they
     arrive, wait for each; the native scheduler batches whatever is queued onto

@@ -36,6 +36,7 @@ struct GraphEntry {
     std::vector<uint64_t> key;
     cudaGraphExec_t exec = nullptr;
     uint64_t kernels = 0;
+    void *d_desc = nullptr;  // the batch descriptors, uploaded once at capture
 };
 
 struct Context {
@@ -67,13 +68,18 @@ void prof_end(Context &ctx, cudaEvent_t ev0, uint64_t entries);
 // arrays; its W x B buckets at [bucket_base, bucket_base + W*B) of the batch's
 // bucket space; its W * (B/m0) reduction groups at group_base; its W window
 // sums at win_base.
+// A fixed-base MSM (fixed = 1) reads its bases from a table of window
+// multiples 2^(c k) G_i stored at index i*W + k: every window then adds into
+// the same B buckets, so it reduces Wr = 1 window and needs no Horner step.
 struct MsmDesc {
     uint32_t pt_off, n;
     uint32_t c, W, B;
     uint32_t bucket_base;
     uint32_t group_base, m0, log2m0, T;  // T = B / m0 groups per window
     uint32_t win_base;
-    uint32_t pad;
+    uint32_t fixed;   // 1: bases from a window-multiple table
+    uint32_t Wr;      // windows that are reduced and combined (W, or 1 for fixed-base)
+    uint32_t pad0, pad1, pad2;
 };
 
 // A run of MSMs sharing one window width (one templated recode launch).
@@ -138,6 +144,8 @@ __device__ __forceinline__ uint32_t find_msm(uint32_t M, uint32_t x, KeyFn key)
 
 int choose_window(const Context &ctx, int curve, size_t n);
 BatchPlan make_batch_plan(const Context &ctx, int curve, const size_t *sizes, uint32_t M);
+// count fixed-base MSMs of n table generators each (window c), scalars back to back
+BatchPlan make_fixed_plan(int curve, size_t n, int c, uint32_t count);
 size_t batch_bytes(const BatchPlan &p);
 bool carve(DeviceArena &a, const BatchPlan &p, BatchBuffers &b);
 
@@ -159,6 +167,9 @@ struct CurveOps {
     cudaError_t (*to_jac24)(Context &ctx, const void *d_in, int fmt, size_t n, uint32_t *d_out);
     // element-wise field op over n 32-byte values (validation hook)
     cudaError_t (*field_op)(Context &ctx, int op, const void *d_a, const void *d_b, size_t n, void *d_out);
+    // window-multiple table: table[i*W + k] = 2^(c k) * gens[i] (affine), tmp holds n*W XYZZ points
+    cudaError_t (*fixed_table)(Context &ctx, const uint4 *d_gens, size_t n, int c, int W, uint4 *d_tmp,
+                               uint4 *d_table);
 };
 extern const CurveOps helios_ops;
 extern const CurveOps selene_ops;

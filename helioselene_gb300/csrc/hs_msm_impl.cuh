@@ -412,14 +412,14 @@ __global__ void __launch_bounds__(32) k_combine(const uint4 *__restrict__ S, con
     const MsmDesc d = desc[blockIdx.x];
     const uint4 *Sm = S + 8 * (size_t)d.win_base;
     if (lane == 0) {
-        const Xyzz top = load_xyzz(Sm + 8 * (size_t)(d.W - 1));
+        const Xyzz top = load_xyzz(Sm + 8 * (size_t)(d.Wr - 1));
         sf.f[sX] = top.X;
         sf.f[sY] = top.Y;
         sf.f[sZZ] = top.ZZ;
         sf.f[sZZZ] = top.ZZZ;
     }
     __syncwarp();
-    for (int k = (int)d.W - 2; k >= 0; k--) {
+    for (int k = (int)d.Wr - 2; k >= 0; k--) {
         for (uint32_t i = 0; i < d.c; i++)
             coop_dbl<C>(sf);
         if (lane == 0) {
@@ -893,11 +893,85 @@ cudaError_t field_op(Context &ctx, int op, const void *d_a, const void *d_b, siz
     return cudaSuccess;
 }
 
+// ---------------------------------------------------------------------------
+// fixed-base window tables: table[i*W + k] = 2^(c k) * G_i, affine
+// ---------------------------------------------------------------------------
+template <class C>
+__global__ void k_fb_expand(const uint4 *__restrict__ gens, size_t n, int c, int W, uint4 *__restrict__ tmp)
+{
+    using G = Group<C>;
+    using F = typename C::F;
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    Fe x, y;
+    load_affine(gens, (uint32_t)i, x, y);
+    Xyzz acc = (F::is_exact_zero(x) && F::is_exact_zero(y)) ? G::inf() : G::from_affine(x, y);
+    for (int k = 0; k < W; k++) {
+        store_xyzz(tmp + 8 * ((size_t)i * W + k), acc);
+        if (k + 1 < W)
+            for (int d = 0; d < c; d++)
+                acc = G::dbl(acc);
+    }
+}
+
+// XYZZ -> affine in chunks of 16 with one inversion per chunk (Montgomery's
+// trick on ZZ*ZZZ); identity -> (0,0)
+template <class C>
+__global__ void k_fb_normalize(const uint4 *__restrict__ tmp, size_t m, uint4 *__restrict__ table,
+                               uint4 *__restrict__ prefix)
+{
+    using G = Group<C>;
+    using F = typename C::F;
+    const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const size_t lo = t * AFF_CHUNK;
+    if (lo >= m)
+        return;
+    const size_t hi = lo + AFF_CHUNK < m ? lo + AFF_CHUNK : m;
+    Fe run = F::one();
+    for (size_t i = lo; i < hi; i++) {
+        const Xyzz p = load_xyzz(tmp + 8 * i);
+        if (!G::is_inf(p))
+            run = F::mul(run, F::mul(p.ZZ, p.ZZZ));
+        store_fe(prefix + 2 * i, run);
+    }
+    Fe inv = F::inv(run);
+    for (size_t i = hi; i-- > lo;) {
+        const Xyzz p = load_xyzz(tmp + 8 * i);
+        Fe x = F::zero(), y = F::zero();
+        if (!G::is_inf(p)) {
+            const Fe z = F::mul(p.ZZ, p.ZZZ);
+            const Fe prev = (i > lo) ? load_fe(prefix + 2 * (i - 1)) : F::one();
+            const Fe zi = F::mul(inv, prev);  // 1 / (ZZ ZZZ)
+            inv = F::mul(inv, z);
+            x = F::canon(F::mul(p.X, F::mul(p.ZZZ, zi)));
+            y = F::canon(F::mul(p.Y, F::mul(p.ZZ, zi)));
+        }
+        store_fe(table + 4 * i, x);
+        store_fe(table + 4 * i + 2, y);
+    }
+}
+
+template <class C>
+cudaError_t fixed_table(Context &ctx, const uint4 *d_gens, size_t n, int c, int W, uint4 *d_tmp, uint4 *d_table)
+{
+    if (n == 0)
+        return cudaSuccess;
+    const size_t m = n * (size_t)W;
+    uint4 *prefix = d_tmp + 8 * m;  // tmp holds m XYZZ points then m prefix products
+    k_fb_expand<C><<<(unsigned)((n + 127) / 128), 128, 0, ctx.stream>>>(d_gens, n, c, W, d_tmp);
+    HS_LAUNCH_CHECK(ctx);
+    const size_t chunks = (m + AFF_CHUNK - 1) / AFF_CHUNK;
+    k_fb_normalize<C><<<(unsigned)((chunks + 127) / 128), 128, 0, ctx.stream>>>(d_tmp, m, d_table, prefix);
+    HS_LAUNCH_CHECK(ctx);
+    return cudaSuccess;
+}
+
 template <class C>
 CurveOps make_ops()
 {
-    return CurveOps{&msm_tail<C>, &to_affine<C>,   &to_affine_scratch, &format_out<C>,
-                    &map_to_curve<C>, &to_jac24<C>, &field_op<C>};
+    return CurveOps{&msm_tail<C>,   &to_affine<C>, &to_affine_scratch, &format_out<C>,
+                    &map_to_curve<C>, &to_jac24<C>, &field_op<C>,       &fixed_table<C>};
 }
 
 }  // namespace hs

@@ -18,6 +18,17 @@ struct hs_context {
     hs::Context c;
 };
 
+struct hs_fixed_base {
+    int curve = 0;
+    int device = 0;
+    int c = 0;
+    int W = 0;
+    size_t n_user = 0;  // generators given
+    size_t n_gen = 0;   // + H when present
+    bool has_H = false;
+    uint4 *d_table = nullptr;
+};
+
 namespace hs {
 
 // ---------------------------------------------------------------------------
@@ -90,7 +101,11 @@ static constexpr uint32_t SEG_HIST_THREADS = 256;
 
 static int model_window(size_t n)
 {
-    // cost ~ W(c) * (n * madd + 2^(c-1) * 2 adds), madd ~ 10 M, add ~ 14 M
+    // cost ~ W(c) * (n * madd + 2^(c-1) * 2 adds), madd ~ 10 M, add ~ 14 M.  A
+    // first guess only: the autotuner (helioselene_gb300.autotune) measures each
+    // size class on the device and installs rules that override it.  On GB300 at
+    // n = 2^20 the measured optimum agrees (c = 16: 16 full windows plus a
+    // carry window that is almost empty).
     int best = 8;
     double best_cost = 1e300;
     for (int c = 4; c <= 20; c++) {
@@ -139,7 +154,9 @@ BatchPlan make_batch_plan(const Context &ctx, int curve, const size_t *sizes, ui
         d.bucket_base = (uint32_t)nb;
         d.group_base = (uint32_t)g;
         d.win_base = (uint32_t)ws;
-        d.pad = 0;
+        d.fixed = 0;
+        d.Wr = d.W;
+        d.pad0 = d.pad1 = d.pad2 = 0;
         pt += n;
         nb += (uint64_t)d.W * d.B;
         g += (uint64_t)d.W * d.T;
@@ -155,6 +172,48 @@ BatchPlan make_batch_plan(const Context &ctx, int curve, const size_t *sizes, ui
     const uint64_t avg = nb ? (ent + nb - 1) / nb : 1;
     p.L = (uint32_t)std::max<uint64_t>(16, std::min<uint64_t>(128, 2 * avg));
     p.max_segs = (uint32_t)(std::min<uint64_t>(ent, nb) + ent / p.L + 1);
+    p.hist_blocks = (p.NB + SEG_HIST_THREADS - 1) / SEG_HIST_THREADS;
+    return p;
+}
+
+BatchPlan make_fixed_plan(int curve, size_t n, int c, uint32_t count)
+{
+    BatchPlan p;
+    p.curve = curve;
+    p.M = count;
+    p.msms.resize(count);
+    const uint32_t W = (uint32_t)((257 + c - 1) / c), B = 1u << (c - 1);
+    const uint32_t m0 = std::min<uint32_t>(16, B);
+    uint32_t log2m0 = 0;
+    while ((1u << log2m0) < m0)
+        log2m0++;
+    for (uint32_t j = 0; j < count; j++) {
+        MsmDesc &d = p.msms[j];
+        d.pt_off = (uint32_t)(j * n);
+        d.n = (uint32_t)n;
+        d.c = (uint32_t)c;
+        d.W = W;
+        d.B = B;
+        d.m0 = m0;
+        d.log2m0 = log2m0;
+        d.T = B / m0;
+        d.bucket_base = j * B;
+        d.group_base = j * d.T;
+        d.win_base = j;
+        d.fixed = 1;
+        d.Wr = 1;
+        d.pad0 = d.pad1 = d.pad2 = 0;
+    }
+    const uint64_t ent = (uint64_t)count * n * W;
+    p.n_total = (uint32_t)(count * n);
+    p.NB = count * B;
+    p.G = count * (B / m0);
+    p.WS = count;
+    p.entries_bound = ent;
+    p.max_entries = (uint32_t)std::max<uint64_t>(1, ent);
+    const uint64_t avg = (ent + p.NB - 1) / p.NB;
+    p.L = (uint32_t)std::max<uint64_t>(16, std::min<uint64_t>(128, 2 * avg));
+    p.max_segs = (uint32_t)(std::min<uint64_t>(ent, p.NB) + ent / p.L + 1);
     p.hist_blocks = (p.NB + SEG_HIST_THREADS - 1) / SEG_HIST_THREADS;
     return p;
 }
@@ -223,10 +282,13 @@ __device__ __forceinline__ uint32_t window_bits(const uint32_t s[8], int k)
 // Digits in [-2^(c-1), 2^(c-1)) except the top one, which keeps the final
 // carry and is at most 2^(c-1) because W*c >= 257.  count pass: histogram of
 // bucket keys; scatter pass: place "index | sign" at offsets[key] + running fill.
+// Normal MSMs: window k uses buckets bucket_base + k*B + ..., entries name the
+// point (pbase = i, pstep = 0).  Fixed-base MSMs: every window uses the same B
+// buckets (wstep = 0), entries name table row (i - pt_off)*W + k (pstep = 1).
 template <int CB, bool SCATTER>
-__device__ __forceinline__ void recode_one(const uint32_t s[8], uint32_t i, uint32_t bucket_base,
-                                           uint32_t *__restrict__ counts, const uint32_t *__restrict__ offsets,
-                                           uint32_t *__restrict__ sorted)
+__device__ __forceinline__ void recode_one(const uint32_t s[8], uint32_t pbase, uint32_t pstep, uint32_t wstep,
+                                           uint32_t bucket_base, uint32_t *__restrict__ counts,
+                                           const uint32_t *__restrict__ offsets, uint32_t *__restrict__ sorted)
 {
     constexpr int W = (257 + CB - 1) / CB;
     constexpr uint32_t B = 1u << (CB - 1);
@@ -245,12 +307,12 @@ __device__ __forceinline__ void recode_one(const uint32_t s[8], uint32_t i, uint
             carry = 0;
         }
         if (mag != 0) {
-            const uint32_t kb = bucket_base + (uint32_t)k * B + mag - 1u;
+            const uint32_t kb = bucket_base + (uint32_t)k * wstep + mag - 1u;
             if (!SCATTER) {
                 atomicAdd(counts + kb, 1u);
             } else {
                 const uint32_t pos = offsets[kb] + atomicAdd(counts + kb, 1u);
-                sorted[pos] = i | (neg ? 0x80000000u : 0u);
+                sorted[pos] = (pbase + (uint32_t)k * pstep) | (neg ? 0x80000000u : 0u);
             }
         }
     }
@@ -267,12 +329,16 @@ __global__ void k_recode(const uint4 *__restrict__ scalars, uint32_t n_total, co
         return;
     const uint32_t m = find_msm(M, i, [&](uint32_t k) { return desc[k].pt_off; });
     const uint32_t c = desc[m].c, base = desc[m].bucket_base;
+    const bool fixed = desc[m].fixed != 0;
+    const uint32_t pbase = fixed ? (i - desc[m].pt_off) * desc[m].W : i;
+    const uint32_t pstep = fixed ? 1u : 0u;
+    const uint32_t wstep = fixed ? 0u : desc[m].B;
     const uint4 a = __ldg(scalars + 2 * (size_t)i), b = __ldg(scalars + 2 * (size_t)i + 1);
     const uint32_t s[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
     switch (c) {
 #define HS_CASE(v)                                                       \
     case v:                                                              \
-        recode_one<v, SCATTER>(s, i, base, counts, offsets, sorted);     \
+        recode_one<v, SCATTER>(s, pbase, pstep, wstep, base, counts, offsets, sorted); \
         break;
         HS_CASE(4)
         HS_CASE(5)
@@ -648,9 +714,9 @@ static cudaError_t launch_batch(Context &ctx, const BatchPlan &p, const BatchBuf
 int execute_batch(Context &ctx, const BatchPlan &p, const BatchBuffers &b, void *d_out, int out_fmt)
 {
     cudaStream_t st = ctx.stream;
-    HS_CU(cudaMemcpyAsync(b.desc, p.msms.data(), (size_t)p.M * sizeof(MsmDesc), cudaMemcpyHostToDevice, st),
-          "descriptor upload");
     if (!ctx.use_graphs || ctx.profile) {
+        HS_CU(cudaMemcpyAsync(b.desc, p.msms.data(), (size_t)p.M * sizeof(MsmDesc), cudaMemcpyHostToDevice, st),
+              "descriptor upload");
         HS_CU(launch_batch(ctx, p, b, d_out, out_fmt), "MSM launch");
         return HS_OK;
     }
@@ -661,13 +727,14 @@ int execute_batch(Context &ctx, const BatchPlan &p, const BatchBuffers &b, void 
     key.push_back((uint64_t)out_fmt);
     key.push_back((uint64_t)(uintptr_t)ctx.arena.base);
     key.push_back((uint64_t)ctx.arena.cap);
-    key.push_back((uint64_t)(uintptr_t)b.desc);
     key.push_back((uint64_t)(uintptr_t)b.scalars);
     key.push_back((uint64_t)(uintptr_t)b.points);
     key.push_back((uint64_t)(uintptr_t)d_out);
     key.push_back((uint64_t)(uintptr_t)st);
+    key.push_back((uint64_t)(uintptr_t)b.counts);
     for (const MsmDesc &d : p.msms) {
-        key.push_back(((uint64_t)d.n << 8) | d.c);
+        key.push_back(((uint64_t)d.n << 16) | ((uint64_t)d.fixed << 8) | d.c);
+        key.push_back(d.pt_off);
     }
     for (GraphEntry &g : ctx.graphs) {
         if (g.key == key) {
@@ -676,27 +743,44 @@ int execute_batch(Context &ctx, const BatchPlan &p, const BatchBuffers &b, void 
             return HS_OK;
         }
     }
+    // The descriptors of a captured shape live in a buffer owned by the graph:
+    // uploaded once here, so a replay needs no host copy (a pageable copy
+    // would synchronise the stream).
+    GraphEntry ent;
+    HS_CU(cudaMalloc(&ent.d_desc, (size_t)p.M * sizeof(MsmDesc)), "descriptor allocation");
+    cudaError_t ue = cudaMemcpy(ent.d_desc, p.msms.data(), (size_t)p.M * sizeof(MsmDesc), cudaMemcpyHostToDevice);
+    if (ue != cudaSuccess) {
+        cudaFree(ent.d_desc);
+        return fail(ctx, ue, "descriptor upload");
+    }
+    BatchBuffers bg = b;
+    bg.desc = (MsmDesc *)ent.d_desc;
     cudaGraph_t graph = nullptr;
     const uint64_t before = ctx.launches;
-    HS_CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "graph capture");
-    cudaError_t le = launch_batch(ctx, p, b, d_out, out_fmt);
-    cudaError_t ce = cudaStreamEndCapture(st, &graph);
+    cudaError_t ce = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    cudaError_t le = ce == cudaSuccess ? launch_batch(ctx, p, bg, d_out, out_fmt) : ce;
+    if (ce == cudaSuccess)
+        ce = cudaStreamEndCapture(st, &graph);
     if (le != cudaSuccess || ce != cudaSuccess) {
         if (graph)
             cudaGraphDestroy(graph);
+        cudaFree(ent.d_desc);
         return fail(ctx, le != cudaSuccess ? le : ce, "graph capture");
     }
     cudaGraphExec_t exec = nullptr;
     cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
     cudaGraphDestroy(graph);
-    if (ie != cudaSuccess)
+    if (ie != cudaSuccess) {
+        cudaFree(ent.d_desc);
         return fail(ctx, ie, "graph instantiate");
-    GraphEntry ent;
+    }
     ent.key = std::move(key);
     ent.exec = exec;
     ent.kernels = ctx.launches - before;
     if (ctx.graphs.size() >= 64) {
+        cudaStreamSynchronize(st);
         cudaGraphExecDestroy(ctx.graphs.front().exec);
+        cudaFree(ctx.graphs.front().d_desc);
         ctx.graphs.erase(ctx.graphs.begin());
     }
     ctx.graphs.push_back(std::move(ent));
@@ -706,8 +790,12 @@ int execute_batch(Context &ctx, const BatchPlan &p, const BatchBuffers &b, void 
 
 void drop_graphs(Context &ctx)
 {
-    for (GraphEntry &g : ctx.graphs)
+    if (!ctx.graphs.empty() && ctx.stream)
+        cudaStreamSynchronize(ctx.stream);
+    for (GraphEntry &g : ctx.graphs) {
         cudaGraphExecDestroy(g.exec);
+        cudaFree(g.d_desc);
+    }
     ctx.graphs.clear();
 }
 
@@ -1269,6 +1357,233 @@ int hs_measure_imad_peak(hs_context *h, double *imad_per_s)
     const double ops = (double)blocks * threads * iters * 8.0 * 2.0;
     *imad_per_s = ops / (best * 1e-3);
     return HS_OK;
+}
+
+// ---- fixed-base commitments ----
+static int fixed_window(size_t n)
+{
+    // one reduction window: cost ~ W(c) * n * madd + 2^(c-1) * 2 adds
+    int best = 8;
+    double best_cost = 1e300;
+    for (int c = 6; c <= 20; c++) {
+        const double W = (257 + c - 1) / c;
+        const double cost = W * 10.0 * (double)n + 28.0 * (double)(1u << (c - 1));
+        if (cost < best_cost) {
+            best_cost = cost;
+            best = c;
+        }
+    }
+    return best;
+}
+
+int hs_fixed_base_create(hs_context *h, int curve, const void *generators, int point_fmt, size_t n, const void *H,
+                         int window, hs_fixed_base **out)
+{
+    if (!h || !out || !valid_curve(curve) || !valid_in_fmt(point_fmt) || (n && !generators) ||
+        (window != 0 && (window < 4 || window > 20)))
+        return HS_EINVAL;
+    *out = nullptr;
+    const size_t n_gen = n + (H ? 1 : 0);
+    if (n_gen == 0)
+        return HS_EINVAL;
+    const int c = window ? window : fixed_window(n_gen);
+    const int W = (257 + c - 1) / c;
+    if (n_gen * (size_t)W >= 0x80000000ull)
+        return HS_ERANGE;
+    Context &ctx = h->c;
+    std::lock_guard<std::mutex> lk(ctx.mu);
+    DeviceGuard g(ctx.device);
+    const CurveOps &ops = curve_ops(curve);
+    const size_t pb = fmt_bytes(point_fmt);
+    const size_t m = n_gen * (size_t)W;
+    HS_CU(ctx.arena.reserve(align256(n_gen * pb) + align256(n_gen * 64) + align256(ops.to_affine_scratch(n_gen)) +
+                            align256(m * 160) + 1024),
+          "workspace allocation");
+    uint8_t *d_raw = (uint8_t *)ctx.arena.take(n_gen * pb);
+    uint4 *d_gens = (uint4 *)ctx.arena.take(n_gen * 64);
+    void *d_scr = ctx.arena.take(ops.to_affine_scratch(n_gen));
+    uint4 *d_tmp = (uint4 *)ctx.arena.take(m * 160);
+    if (!d_raw || !d_gens || !d_scr || !d_tmp)
+        return fail_msg(ctx, HS_ENOMEM, "workspace carve");
+    hs_fixed_base *fb = new (std::nothrow) hs_fixed_base();
+    if (!fb)
+        return HS_ENOMEM;
+    fb->curve = curve;
+    fb->device = ctx.device;
+    fb->c = c;
+    fb->W = W;
+    fb->n_user = n;
+    fb->n_gen = n_gen;
+    fb->has_H = H != nullptr;
+    cudaError_t e = cudaMalloc((void **)&fb->d_table, m * 64);
+    if (e != cudaSuccess) {
+        delete fb;
+        return fail(ctx, e, "fixed-base table allocation");
+    }
+    cudaStream_t st = ctx.stream;
+    auto bail = [&](cudaError_t err, const char *what) {
+        cudaFree(fb->d_table);
+        delete fb;
+        return fail(ctx, err, what);
+    };
+    if (n && (e = cudaMemcpyAsync(d_raw, generators, n * pb, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        return bail(e, "H2D generators");
+    if (H && (e = cudaMemcpyAsync(d_raw + n * pb, H, pb, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        return bail(e, "H2D H");
+    if (point_fmt != HS_FMT_AFFINE) {
+        if ((e = ops.to_affine(ctx, d_raw, point_fmt, n_gen, d_gens, d_scr)) != cudaSuccess)
+            return bail(e, "generator conversion");
+    } else if ((e = cudaMemcpyAsync(d_gens, d_raw, n_gen * 64, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) {
+        return bail(e, "generator copy");
+    }
+    if ((e = ops.fixed_table(ctx, d_gens, n_gen, c, W, d_tmp, fb->d_table)) != cudaSuccess)
+        return bail(e, "window table");
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess)
+        return bail(e, "window table");
+    *out = fb;
+    return HS_OK;
+}
+
+// Run count fixed-base commitments whose scalars are at d_scalars (count x n_gen
+// x 32 bytes on the device) in chunks bounded by the entry count; results to d_out.
+static int fixed_commit_chunks(Context &ctx, const hs_fixed_base *fb, const uint8_t *d_scalars, size_t count,
+                               uint8_t *d_out, int out_fmt)
+{
+    const uint64_t per = (uint64_t)fb->n_gen * fb->W;
+    const size_t chunk = (size_t)std::max<uint64_t>(1, std::min<uint64_t>(count, (1ull << 29) / per));
+    const BatchPlan big = make_fixed_plan(fb->curve, fb->n_gen, fb->c, (uint32_t)chunk);
+    const bool aff = out_fmt == HS_FMT_AFFINE;
+    // affine results: Jacobian first, then one shared inversion per 16 commitments
+    const size_t extra = aff ? align256(count * 120) + align256(count * 32) : 0;
+    HS_CU(ctx.arena.reserve(batch_bytes(big) + extra + 2048), "workspace allocation");
+    const size_t ob = aff ? 120 : fmt_bytes(out_fmt);
+    uint8_t *d_jac = nullptr;
+    void *d_scr = nullptr;
+    for (size_t j0 = 0; j0 < count; j0 += chunk) {
+        const size_t cnt = std::min(chunk, count - j0);
+        const BatchPlan p = make_fixed_plan(fb->curve, fb->n_gen, fb->c, (uint32_t)cnt);
+        ctx.arena.reset();
+        if (aff) {  // results and scratch live at the front of the arena, below the batch workspace
+            d_jac = (uint8_t *)ctx.arena.take(count * 120);
+            d_scr = ctx.arena.take(count * 32);
+        }
+        BatchBuffers b;
+        if (!carve(ctx.arena, p, b))
+            return fail_msg(ctx, HS_ENOMEM, "workspace carve");
+        b.scalars = (const uint32_t *)(d_scalars + 32 * fb->n_gen * j0);
+        b.points = fb->d_table;
+        const int rc = execute_batch(ctx, p, b, (aff ? d_jac : d_out) + ob * j0, aff ? HS_FMT_JACOBIAN51 : out_fmt);
+        if (rc != HS_OK)
+            return rc;
+    }
+    if (aff)
+        HS_CU(curve_ops(fb->curve).to_affine(ctx, d_jac, HS_FMT_JACOBIAN51, count, (uint4 *)d_out, d_scr),
+              "batch to affine");
+    return HS_OK;
+}
+
+int hs_fixed_base_commit_device(hs_context *h, const hs_fixed_base *fb, const void *d_scalars, size_t count,
+                                void *d_out, int out_fmt)
+{
+    if (!h || !fb || !valid_out_fmt(out_fmt) || (count && (!d_scalars || !d_out)))
+        return HS_EINVAL;
+    if (count == 0)
+        return HS_OK;
+    if ((uint64_t)count * fb->n_gen >= 0x80000000ull)
+        return HS_ERANGE;
+    Context &ctx = h->c;
+    if (ctx.device != fb->device)
+        return HS_EINVAL;
+    std::lock_guard<std::mutex> lk(ctx.mu);
+    DeviceGuard g(ctx.device);
+    return fixed_commit_chunks(ctx, fb, (const uint8_t *)d_scalars, count, (uint8_t *)d_out, out_fmt);
+}
+
+int hs_fixed_base_commit(hs_context *h, const hs_fixed_base *fb, const uint8_t *values, const uint8_t *blindings,
+                         size_t count, void *out, int out_fmt)
+{
+    if (!h || !fb || !valid_out_fmt(out_fmt) || (count && (!out || (fb->n_user && !values))) ||
+        (blindings && !fb->has_H))
+        return HS_EINVAL;
+    if (count == 0)
+        return HS_OK;
+    Context &ctx = h->c;
+    if (ctx.device != fb->device)
+        return HS_EINVAL;
+    std::lock_guard<std::mutex> lk(ctx.mu);
+    DeviceGuard g(ctx.device);
+    const CurveOps &ops = curve_ops(fb->curve);
+    const uint64_t per = (uint64_t)fb->n_gen * fb->W;
+    const size_t chunk = (size_t)std::max<uint64_t>(1, std::min<uint64_t>(count, (1ull << 29) / per));
+    const size_t ob = fmt_bytes(out_fmt);
+    // staging for one chunk: scalars in the device layout, Jacobian results, formatted results
+    const size_t sc_bytes = align256(chunk * fb->n_gen * 32);
+    const size_t extra = sc_bytes + align256(chunk * 120) + align256(chunk * ob) + align256(chunk * 32) + 256;
+    std::vector<uint8_t> host(count * ob);
+    for (size_t j0 = 0; j0 < count; j0 += chunk) {
+        const size_t cnt = std::min(chunk, count - j0);
+        const BatchPlan big = make_fixed_plan(fb->curve, fb->n_gen, fb->c, (uint32_t)chunk);
+        HS_CU(ctx.arena.reserve(batch_bytes(big) + align256(extra) + 1024), "workspace allocation");
+        const BatchPlan p = make_fixed_plan(fb->curve, fb->n_gen, fb->c, (uint32_t)cnt);
+        BatchBuffers b;
+        if (!carve(ctx.arena, p, b))
+            return fail_msg(ctx, HS_ENOMEM, "workspace carve");
+        uint8_t *d_sc = (uint8_t *)ctx.arena.take(sc_bytes);
+        uint8_t *d_jac = (uint8_t *)ctx.arena.take(align256(chunk * 120));
+        uint8_t *d_fmt = (uint8_t *)ctx.arena.take(align256(chunk * ob));
+        void *d_scr = ctx.arena.take(align256(chunk * 32));
+        if (!d_sc || !d_jac || !d_fmt || !d_scr)
+            return fail_msg(ctx, HS_ENOMEM, "workspace carve");
+        cudaStream_t st = ctx.stream;
+        const size_t g = fb->n_gen;
+        if (fb->n_user)
+            HS_CU(cudaMemcpy2DAsync(d_sc, g * 32, values + j0 * fb->n_user * 32, fb->n_user * 32, fb->n_user * 32,
+                                    cnt, cudaMemcpyHostToDevice, st),
+                  "H2D values");
+        if (fb->has_H) {
+            if (blindings)
+                HS_CU(cudaMemcpy2DAsync(d_sc + fb->n_user * 32, g * 32, blindings + j0 * 32, 32, 32, cnt,
+                                        cudaMemcpyHostToDevice, st),
+                      "H2D blindings");
+            else
+                HS_CU(cudaMemset2DAsync(d_sc + fb->n_user * 32, g * 32, 0, 32, cnt, st), "zero blindings");
+        }
+        b.scalars = (const uint32_t *)d_sc;
+        b.points = fb->d_table;
+        const bool aff = out_fmt == HS_FMT_AFFINE;
+        int rc = execute_batch(ctx, p, b, aff ? d_jac : d_fmt, aff ? HS_FMT_JACOBIAN51 : out_fmt);
+        if (rc != HS_OK)
+            return rc;
+        if (aff)  // normalise all results with one shared inversion per 16 (Montgomery's trick)
+            HS_CU(ops.to_affine(ctx, d_jac, HS_FMT_JACOBIAN51, cnt, (uint4 *)d_fmt, d_scr), "batch to affine");
+        HS_CU(cudaMemcpyAsync(host.data() + j0 * ob, d_fmt, cnt * ob, cudaMemcpyDeviceToHost, st), "D2H");
+        HS_CU(cudaStreamSynchronize(st), "fixed-base commit");
+    }
+    std::memcpy(out, host.data(), host.size());
+    return HS_OK;
+}
+
+int hs_fixed_base_info(const hs_fixed_base *fb, int *window, size_t *table_bytes)
+{
+    if (!fb)
+        return HS_EINVAL;
+    if (window)
+        *window = fb->c;
+    if (table_bytes)
+        *table_bytes = fb->n_gen * (size_t)fb->W * 64;
+    return HS_OK;
+}
+
+void hs_fixed_base_destroy(hs_fixed_base *fb)
+{
+    if (!fb)
+        return;
+    {
+        DeviceGuard g(fb->device);
+        cudaDeviceSynchronize();
+        cudaFree(fb->d_table);
+    }
+    delete fb;
 }
 
 // ---- reference-signature drop-ins on a process-wide context ----

@@ -156,6 +156,33 @@ int hs_msm_batch(hs_context *ctx, const hs_msm_desc *descs, size_t count, int po
 int hs_msm_batch_device(hs_context *ctx, int curve, const size_t *sizes, size_t count, const void *d_scalars,
                         const void *d_points, void *d_out, int out_fmt);
 
+/* ---- fixed-base commitments over a resident generator set ----
+ * Pedersen-style r*H + sum v_i G_i (helios/include/helios_pedersen.h:55-86) for
+ * many commitments over the same generators.  hs_fixed_base_create uploads the
+ * n generators (and H, appended as generator n when given), then precomputes on
+ * the device, for window width c, the table 2^(c k) G_i for every window k
+ * (the vartime counterpart of the reference's per-base multiple tables,
+ * helios/include/helios_scalarmult_fixed.h:54-63, helios_msm_fixed.h:60-155).
+ * A commitment then adds every (generator, window) digit into one set of
+ * 2^(c-1) buckets: one bucket reduction, no per-window doublings.  window 0
+ * picks c from the generator count.  The table stays resident until destroy. */
+typedef struct hs_fixed_base hs_fixed_base;
+int hs_fixed_base_create(hs_context *ctx, int curve, const void *generators, int point_fmt, size_t n, const void *H,
+                         int window, hs_fixed_base **fb);
+/* values: count x n scalars (32 bytes each, commitment-major); blindings:
+ * count scalars or NULL (then r = 0; required NULL when created without H);
+ * out: count records of out_fmt (HS_FMT_AFFINE outputs are normalised with
+ * one shared inversion per 16 commitments). */
+int hs_fixed_base_commit(hs_context *ctx, const hs_fixed_base *fb, const uint8_t *values, const uint8_t *blindings,
+                         size_t count, void *out, int out_fmt);
+/* device variant: d_scalars holds count x g scalars, g = n (+1 with H, the
+ * blinding last in each commitment); d_out count records; does not synchronise */
+int hs_fixed_base_commit_device(hs_context *ctx, const hs_fixed_base *fb, const void *d_scalars, size_t count,
+                                void *d_out, int out_fmt);
+/* window width and device bytes of the table */
+int hs_fixed_base_info(const hs_fixed_base *fb, int *window, size_t *table_bytes);
+void hs_fixed_base_destroy(hs_fixed_base *fb);
+
 /* ---- serving: continuous batching of MSM requests ----
  * A server owns `slots` CUDA streams, each with its own workspace, a request
  * queue and one scheduler thread.  Requests that arrive while others are on
