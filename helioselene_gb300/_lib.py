@@ -83,6 +83,8 @@ SIGNATURES = {
     "hs_server_wait": (_int, [_vp, _c.c_uint64, _int, _c.POINTER(_c.c_double)]),
     "hs_server_get_stats": (_int, [_vp, _c.POINTER(hs_server_stats)]),
     "hs_server_destroy": (None, [_vp]),
+    "hs_msm_device_noalloc": (_int, [_int, _vp, _vp, _sz, _vp, _int, _vp]),
+    "hs_msm_noalloc_scratch_bytes": (_sz, []),
     "hs_helios_msm_vartime": (None, [_vp, _vp, _vp, _sz]),
     "hs_selene_msm_vartime": (None, [_vp, _vp, _vp, _sz]),
     "hs_helios_pedersen_commit": (None, [_vp, _vp, _vp, _vp, _vp, _sz]),

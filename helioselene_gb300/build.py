@@ -18,7 +18,7 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libhelioselene_gb300.so"
-SOURCES = ["hs_runtime.cu", "hs_curve_helios.cu", "hs_curve_selene.cu", "hs_serving.cu"]
+SOURCES = ["hs_runtime.cu", "hs_curve_helios.cu", "hs_curve_selene.cu", "hs_serving.cu", "hs_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
                      "-Xptxas", "-warn-spills"]

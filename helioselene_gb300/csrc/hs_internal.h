@@ -197,6 +197,8 @@ struct DeviceGuard {
 // batch execution helpers shared with the serving loop (hs_runtime.cu)
 int reserve_batch(Context &ctx, const BatchPlan &p, size_t extra_bytes, BatchBuffers &b, void **extra);
 int execute_batch(Context &ctx, const BatchPlan &p, const BatchBuffers &b, void *d_out, int out_fmt);
+// recode, sort, accumulate, reduce, combine and format one batch with direct launches
+cudaError_t launch_batch(Context &ctx, const BatchPlan &p, const BatchBuffers &b, void *d_out, int out_fmt);
 void drop_graphs(Context &ctx);
 int fail(Context &ctx, cudaError_t e, const char *what);
 int fail_msg(Context &ctx, int code, const char *what);

@@ -697,7 +697,7 @@ int reserve_batch(Context &ctx, const BatchPlan &p, size_t extra_bytes, BatchBuf
     return HS_OK;
 }
 
-static cudaError_t launch_batch(Context &ctx, const BatchPlan &p, const BatchBuffers &b, void *d_out, int out_fmt)
+cudaError_t launch_batch(Context &ctx, const BatchPlan &p, const BatchBuffers &b, void *d_out, int out_fmt)
 {
     cudaError_t e;
     if ((e = launch_sort(ctx, p, b)) != cudaSuccess)

@@ -275,6 +275,28 @@ int hs_measure_imad_peak(hs_context *ctx, double *imad_per_s);
  * inputs may be any 256-bit value, outputs are canonical. */
 int hs_field_op(hs_context *ctx, int field, int op, const uint8_t *a, const uint8_t *b, size_t n, uint8_t *out);
 
+/* ---- MSM without device allocation ----
+ * For callers that cannot allocate device memory while they run: code under
+ * an allocator or memory pool that must not be bypassed, processes whose
+ * device memory is reserved up front, and latency-critical or graph-driven
+ * callers that must not reach cudaMalloc / cudaFree (both can synchronise the
+ * device).  This entry point has no counterpart in the reference.
+ * Same computation and arguments as hs_msm_device, but every scratch buffer
+ * comes from one fixed array of hs_msm_noalloc_scratch_bytes() (64 MiB) in
+ * device memory, which each device that loads this library holds until the
+ * process exits.  It needs no context: it runs on the current device and on
+ * `stream` (a cudaStream_t, NULL for the default stream) and does not
+ * synchronise.  n must be 1 .. HS_NOALLOC_MAX_POINTS; larger sizes, and any
+ * size whose workspace would not fit the array, return HS_ERANGE.
+ * All calls on a device share the one array and find the previous call's
+ * contents in it (each call clears what it needs cleared): calls whose work
+ * overlaps on the GPU -- on different streams, or from different threads --
+ * race and corrupt each other's results; run them one after another. */
+#define HS_NOALLOC_MAX_POINTS 262144
+int hs_msm_device_noalloc(int curve, const void *d_scalars, const void *d_points, size_t n, void *d_out, int out_fmt,
+                          void *stream);
+size_t hs_msm_noalloc_scratch_bytes(void);
+
 /* ---- library info ---- */
 int hs_abi_version(void);
 
