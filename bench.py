@@ -509,29 +509,37 @@ def run_ours(args) -> None:
     ms_per_step = ms / args.steps
     value = ws * 2 * n / (ms_per_step * 1e-3)
 
-    # per-curve latency, one MSM at a time (also the roofline pass: accumulation
-    # launches timed with events on the context stream)
+    # per-curve latency, one MSM at a time; then the roofline pass: the unsplit
+    # batch path of the same MSM with its accumulation launch timed by events on
+    # the context stream (a split MSM runs two accumulations concurrently, which
+    # per-launch events cannot separate)
     per_curve = {}
     prof_total = {"ms": 0.0, "work": 0.0, "launches": 0}
     for curve, name in ((hs.HELIOS, "helios"), (hs.SELENE, "selene")):
-        ts = []
         c = ctxs[curve]
         s = streams[curve]
+        args_dev = (data[curve]["d_sc"].data_ptr(), data[curve]["d_pts"].data_ptr())
+
+        def timed(fn):
+            ts = []
+            for _ in range(3):
+                with torch.cuda.stream(s):
+                    flush.zero_()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(s)
+                fn()
+                b.record(s)
+                torch.cuda.synchronize()
+                ts.append(a.elapsed_time(b))
+            return min(ts)
+
+        t_split = timed(lambda: c.msm_device(curve, *args_dev, n, d_out.data_ptr(), hs.FMT_JACOBIAN51))
         c.profile(True)
         c.profile_read(reset=True)
-        for _ in range(3):
-            with torch.cuda.stream(s):
-                flush.zero_()
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(s)
-            c.msm_device(curve, data[curve]["d_sc"].data_ptr(), data[curve]["d_pts"].data_ptr(), n,
-                         d_out.data_ptr(), hs.FMT_JACOBIAN51)
-            b.record(s)
-            torch.cuda.synchronize()
-            ts.append(a.elapsed_time(b))
+        t_plain = timed(lambda: c.msm_batch_device(curve, [n], *args_dev, d_out.data_ptr(), hs.FMT_JACOBIAN51))
         pr = c.profile_read(reset=True)
         c.profile(False)
-        per_curve[name] = {"ms": min(ts), "points_per_s": n / (min(ts) * 1e-3),
+        per_curve[name] = {"ms": t_split, "points_per_s": n / (t_split * 1e-3), "unsplit_ms": t_plain,
                            "accumulate_ms": pr["accumulate_ms"] / max(1, pr["accumulate_launches"])}
         prof_total["ms"] += pr["accumulate_ms"]
         prof_total["launches"] += pr["accumulate_launches"]

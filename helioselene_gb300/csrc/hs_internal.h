@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstddef>
 #include <cstdint>
 #include <mutex>
@@ -43,8 +44,10 @@ struct Context {
     int device = 0;
     int sm_count = 0;
     cudaStream_t stream = nullptr;   // the stream every launch goes to
-    cudaStream_t stream2 = nullptr;  // second curve group of a mixed batch
+    cudaStream_t stream2 = nullptr;  // second curve group of a mixed batch, lower window half of a split MSM
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;  // fork/join of the two streams (created with stream2)
     bool use_graphs = true;
+    size_t split_min = size_t(1) << 18;  // single MSMs this large run as two window halves (0: never)
     std::vector<GraphEntry> graphs;
     DeviceArena arena;
     std::mutex mu;
@@ -68,6 +71,11 @@ void prof_end(Context &ctx, cudaEvent_t ev0, uint64_t entries);
 // arrays; its W x B buckets at [bucket_base, bucket_base + W*B) of the batch's
 // bucket space; its W * (B/m0) reduction groups at group_base; its W window
 // sums at win_base.
+// buckets per level-1 reduction group (k_reduce_groups), and groups per
+// level-2 chunk (k_window_chunks)
+constexpr uint32_t RED_GROUP = 8;
+constexpr uint32_t RED_CHUNK = 256;
+
 // A fixed-base MSM (fixed = 1) reads its bases from a table of window
 // multiples 2^(c k) G_i stored at index i*W + k: every window then adds into
 // the same B buckets, so it reduces Wr = 1 window and needs no Horner step.
@@ -79,7 +87,10 @@ struct MsmDesc {
     uint32_t win_base;
     uint32_t fixed;   // 1: bases from a window-multiple table
     uint32_t Wr;      // windows that are reduced and combined (W, or 1 for fixed-base)
-    uint32_t pad0, pad1, pad2;
+    uint32_t w_lo;    // first window this descriptor emits (a window-split half starts above 0)
+    uint32_t w_cnt;   // windows emitted: [w_lo, w_lo + w_cnt)
+    uint32_t shift;   // doublings applied after the Horner step (c * w_lo for an upper half)
+    uint32_t chunk_base;  // first level-2 reduction chunk (Wr * max(1, T / RED_CHUNK) per MSM)
 };
 
 // A run of MSMs sharing one window width (one templated recode launch).
@@ -99,6 +110,9 @@ struct BatchPlan {
     uint32_t NB = 0;            // buckets (all MSMs, all windows)
     uint32_t G = 0;             // reduction groups
     uint32_t WS = 0;            // window sums
+    uint32_t CH = 0;            // level-2 reduction chunks
+    uint32_t max_T = 1;         // largest groups-per-window of the batch
+    uint32_t max_nbk = 1;       // largest chunks-per-window of the batch
     uint32_t L = 0;             // max entries per accumulation segment
     uint32_t max_entries = 0;
     uint32_t max_segs = 0;
@@ -122,7 +136,8 @@ struct BatchBuffers {
     uint4 *seg_sum = nullptr;           // max_segs XYZZ sums (8 uint4 each)
     uint32_t *heavy = nullptr;          // NB heavy-bucket list
     uint32_t *heavy_n = nullptr;        // 1 counter
-    uint4 *redA = nullptr;              // G weighted group sums
+    uint4 *redA = nullptr;              // G group (acc, run) pairs
+    uint4 *redC = nullptr;              // CH chunk (sum, run) pairs
     uint4 *redS = nullptr;              // WS window sums
     uint32_t *out_jac = nullptr;        // M x 24 words: canonical Jacobian X, Y, Z
 };
@@ -146,6 +161,8 @@ int choose_window(const Context &ctx, int curve, size_t n);
 BatchPlan make_batch_plan(const Context &ctx, int curve, const size_t *sizes, uint32_t M);
 // count fixed-base MSMs of n table generators each (window c), scalars back to back
 BatchPlan make_fixed_plan(int curve, size_t n, int c, uint32_t count);
+// one MSM of n points restricted to windows [w_lo, w_lo + w_cnt) of width c
+BatchPlan make_window_plan(int curve, size_t n, int c, uint32_t w_lo, uint32_t w_cnt);
 size_t batch_bytes(const BatchPlan &p);
 bool carve(DeviceArena &a, const BatchPlan &p, BatchBuffers &b);
 
@@ -170,6 +187,8 @@ struct CurveOps {
     // window-multiple table: table[i*W + k] = 2^(c k) * gens[i] (affine), tmp holds n*W XYZZ points
     cudaError_t (*fixed_table)(Context &ctx, const uint4 *d_gens, size_t n, int c, int W, uint4 *d_tmp,
                                uint4 *d_table);
+    // out = a + b for canonical Jacobians (24 words each)
+    cudaError_t (*join)(Context &ctx, const uint32_t *d_a, const uint32_t *d_b, uint32_t *d_out);
 };
 extern const CurveOps helios_ops;
 extern const CurveOps selene_ops;

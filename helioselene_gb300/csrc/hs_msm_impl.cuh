@@ -10,8 +10,9 @@
 //      thread sums one segment of affine bases into an XYZZ point;
 //   3. k_merge_light / k_merge_heavy: buckets with several segments are folded
 //      (sequentially when few, by a block-wide tree when many);
-//   4. k_reduce_abs / k_window_sum: per window S = sum_j (j+1) B_j by running
-//      sums over groups of buckets carrying absolute weights, then a tree sum;
+//   4. k_reduce_groups / k_window_chunks / k_window_sum: per window
+//      S = sum_j (j+1) B_j by running sums over groups of 8 buckets, then
+//      suffix scans and trees over the groups (no scalar multiples);
 //   5. k_combine: Horner over the windows, S = 2^c S + S_k (the reference's
 //      per-window doublings, :285-289) on one warp, result as canonical Jacobian.
 #pragma once
@@ -154,32 +155,18 @@ __global__ void __launch_bounds__(HEAVY_THREADS) k_merge_heavy(const uint32_t *_
 }
 
 // ---------------------------------------------------------------------------
-// 4. bucket reduction: S_k = sum_j (j+1) * B_{k,j}
+// 4. bucket reduction: S = sum_j (j+1) B_j per window, in two levels
 // ---------------------------------------------------------------------------
-// Thread (k, t) owns buckets [lo, lo+m) of window k, lo = t*m.  A running sum
-// from the top (as the reference does over the whole window,
-// helios_msm_vartime.cpp:334-361) gives acc = sum_j (j - lo + 1) B_j and
-// run = sum_j B_j; the thread then adds lo*run (double-and-add on t, then
-// log2(m) doublings) so that its output carries absolute weights and the
-// window sum is a plain sum: S_k = sum_t A_t.
+// Level 1, k_reduce_groups: thread (k, t) owns the m0 buckets [t m0, (t+1) m0)
+// of window k and runs the reference's top-down running sum over them
+// (helios_msm_vartime.cpp:334-361), giving
+//     run_t = sum_j B_j,   acc_t = sum_j (j - t m0 + 1) B_j,
+// so that S = sum_t acc_t + m0 sum_t t run_t.
 template <class C>
-__device__ Xyzz mul_small(const Xyzz &P, uint32_t t)
-{
-    using G = Group<C>;
-    if (t == 0 || G::is_inf(P))
-        return G::inf();
-    Xyzz Q = P;
-    for (int b = 30 - __clz(t); b >= 0; b--) {
-        Q = G::dbl(Q);
-        if ((t >> b) & 1u)
-            Q = G::add(Q, P);
-    }
-    return Q;
-}
-
-template <class C>
-__global__ void k_reduce_abs(const uint32_t *__restrict__ seg_off, const uint4 *__restrict__ seg_sum,
-                             const MsmDesc *__restrict__ desc, uint32_t M, uint32_t G, uint4 *__restrict__ outA)
+__global__ void __launch_bounds__(128, 4) k_reduce_groups(const uint32_t *__restrict__ seg_off,
+                                                      const uint4 *__restrict__ seg_sum,
+                                                      const MsmDesc *__restrict__ desc, uint32_t M, uint32_t G,
+                                                      uint4 *__restrict__ out)
 {
     using G_ = Group<C>;
     const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -198,40 +185,131 @@ __global__ void k_reduce_abs(const uint32_t *__restrict__ seg_off, const uint4 *
             run = G_::add(run, load_xyzz(seg_sum + 8 * (size_t)s0));
         acc = G_::add(acc, run);
     }
-    Xyzz off = mul_small<C>(run, t);
-    for (uint32_t i = 0; i < d.log2m0; i++)
-        off = G_::dbl(off);
-    store_xyzz(outA + 8 * (size_t)gid, G_::add(acc, off));
+    store_xyzz(out + 16 * (size_t)gid, acc);
+    store_xyzz(out + 16 * (size_t)gid + 8, run);
 }
 
-// S_k = sum over the T group outputs of window k of one MSM: one block per
-// window (all windows of all MSMs), strided per-thread sums, then a
-// shared-memory tree.
-constexpr int WSUM_THREADS = 128;
-
+// Level 2 spreads each window's T groups over chunks of up to RED_CHUNK groups,
+// one block per chunk (k_window_chunks), then adds the chunks of a window
+// (k_window_sum).  Both use one identity: for points x_0..x_{m-1},
+//     sum_i i x_i = sum_{i >= 1} X_i,   X_i = sum_{j >= i} x_j,
+// where the suffix sums X_i come from a scan over the threads of a block.
+// Chunk b of window k (groups from t0 = b RED_CHUNK) yields
+//     C_b = sum_t acc_t + m0 sum_t (t - t0) run_t,     R_b = sum_t run_t,
+// and the window sum is S = sum_b C_b + m0 RED_CHUNK sum_b b R_b.  Each step
+// is a short running sum, a log-depth scan or tree, and log2 of a power of two
+// doublings: no scalar multiples by group index.
 template <class C>
-__global__ void __launch_bounds__(WSUM_THREADS) k_window_sum(const uint4 *__restrict__ inA,
-                                                            const MsmDesc *__restrict__ desc, uint32_t M,
-                                                            uint4 *__restrict__ S)
+__device__ __forceinline__ Xyzz block_suffix_scan(uint4 *sh, Xyzz r, uint32_t i, uint32_t nt)
 {
     using G = Group<C>;
-    __shared__ uint4 sh[WSUM_THREADS * 8];
-    const uint32_t s = blockIdx.x;
-    const uint32_t mi = find_msm(M, s, [&](uint32_t k) { return desc[k].win_base; });
-    const MsmDesc d = desc[mi];
-    const size_t base = (size_t)d.group_base + (size_t)(s - d.win_base) * d.T;
-    Xyzz acc = G::inf();
-    for (uint32_t i = threadIdx.x; i < d.T; i += WSUM_THREADS)
-        acc = G::add(acc, load_xyzz(inA + 8 * (base + i)));
-    store_xyzz(sh + 8 * threadIdx.x, acc);
+    store_xyzz(sh + 8 * i, r);
     __syncthreads();
-    for (uint32_t stride = WSUM_THREADS / 2; stride > 0; stride >>= 1) {
-        if (threadIdx.x < stride)
-            store_xyzz(sh + 8 * threadIdx.x,
-                       G::add(load_xyzz(sh + 8 * threadIdx.x), load_xyzz(sh + 8 * (threadIdx.x + stride))));
+    for (uint32_t dl = 1; dl < nt; dl <<= 1) {
+        Xyzz o = G::inf();
+        const bool take = i + dl < nt;
+        if (take)
+            o = load_xyzz(sh + 8 * (i + dl));
+        __syncthreads();
+        if (take) {
+            r = G::add(r, o);
+            store_xyzz(sh + 8 * i, r);
+        }
         __syncthreads();
     }
-    if (threadIdx.x == 0)
+    return r;
+}
+
+// sum of v over the first nt (a power of two) threads, result in sh[0]
+template <class C>
+__device__ __forceinline__ void block_tree_sum(uint4 *sh, const Xyzz &v, uint32_t i, uint32_t nt)
+{
+    using G = Group<C>;
+    __syncthreads();
+    store_xyzz(sh + 8 * i, v);
+    __syncthreads();
+    for (uint32_t stride = nt / 2; stride > 0; stride >>= 1) {
+        if (i < stride)
+            store_xyzz(sh + 8 * i, G::add(load_xyzz(sh + 8 * i), load_xyzz(sh + 8 * (i + stride))));
+        __syncthreads();
+    }
+}
+
+// k_window_chunks: thread i of a chunk first runs a top-down running sum over
+// its q = 4 consecutive groups (lo = t0 + i q):
+//     r_i = sum run_t,  w_i = sum (t - lo) run_t,  a_i = sum acc_t,
+// then the block scans r (X_i = sum_{j >= i} r_j) and thread i contributes
+//     a_i + m0 (w_i + q X_i [i >= 1]),
+// which sums to C_b; X_0 is R_b.  Four groups per thread keep both the
+// sequential part and the scan's extra work small.
+constexpr uint32_t RED_CHUNK_Q = 4;
+constexpr uint32_t RED_CHUNK_THREADS = RED_CHUNK / RED_CHUNK_Q;
+
+template <class C>
+__global__ void __launch_bounds__(RED_CHUNK_THREADS) k_window_chunks(const uint4 *__restrict__ in,
+                                                                    const MsmDesc *__restrict__ desc, uint32_t M,
+                                                                    uint4 *__restrict__ outC)
+{
+    using G = Group<C>;
+    __shared__ uint4 sh[RED_CHUNK_THREADS * 8];
+    const uint32_t ch = blockIdx.x, i = threadIdx.x;
+    const uint32_t mi = find_msm(M, ch, [&](uint32_t k) { return desc[k].chunk_base; });
+    const MsmDesc d = desc[mi];
+    const uint32_t nbk = d.T > RED_CHUNK ? d.T / RED_CHUNK : 1;
+    const uint32_t nt = d.T < RED_CHUNK ? d.T : RED_CHUNK;
+    const uint32_t q = nt < RED_CHUNK_Q ? nt : RED_CHUNK_Q;
+    const uint32_t P = nt / q;
+    const uint32_t local = ch - d.chunk_base;
+    const uint32_t k = local / nbk, b = local % nbk;
+    Xyzz a = G::inf(), r = G::inf(), w = G::inf();
+    if (i < P) {
+        const size_t lo = (size_t)d.group_base + (size_t)k * d.T + (size_t)b * RED_CHUNK + (size_t)i * q;
+        for (int u = (int)q - 1; u >= 0; u--) {
+            a = G::add(a, load_xyzz(in + 16 * (lo + u)));
+            r = G::add(r, load_xyzz(in + 16 * (lo + u) + 8));
+            if (u > 0)
+                w = G::add(w, r);
+        }
+    }
+    r = block_suffix_scan<C>(sh, r, i, P);
+    Xyzz v = (i >= 1 && i < P) ? r : G::inf();
+    for (uint32_t m = q; m > 1; m >>= 1)
+        v = G::dbl(v);
+    v = G::add(v, w);
+    for (uint32_t m = d.m0; m > 1; m >>= 1)
+        v = G::dbl(v);
+    v = G::add(v, a);
+    block_tree_sum<C>(sh, v, i, P);
+    if (i == 0) {
+        store_xyzz(outC + 16 * (size_t)ch, load_xyzz(sh));
+        store_xyzz(outC + 16 * (size_t)ch + 8, r);  // thread 0's suffix sum is the chunk's run total
+    }
+}
+
+template <class C>
+__global__ void __launch_bounds__(RED_CHUNK) k_window_sum(const uint4 *__restrict__ inC,
+                                                         const MsmDesc *__restrict__ desc, uint32_t M,
+                                                         uint4 *__restrict__ S)
+{
+    using G = Group<C>;
+    __shared__ uint4 sh[RED_CHUNK * 8];
+    const uint32_t s = blockIdx.x, i = threadIdx.x;
+    const uint32_t mi = find_msm(M, s, [&](uint32_t k) { return desc[k].win_base; });
+    const MsmDesc d = desc[mi];
+    const uint32_t nbk = d.T > RED_CHUNK ? d.T / RED_CHUNK : 1;
+    Xyzz cb = G::inf(), r = G::inf();
+    if (i < nbk) {
+        const size_t c = (size_t)d.chunk_base + (size_t)(s - d.win_base) * nbk + i;
+        cb = load_xyzz(inC + 16 * c);
+        r = load_xyzz(inC + 16 * c + 8);
+    }
+    r = block_suffix_scan<C>(sh, r, i, nbk);
+    Xyzz v = (i >= 1 && i < nbk) ? r : G::inf();
+    for (uint32_t m = d.m0 * RED_CHUNK; m > 1 && nbk > 1; m >>= 1)
+        v = G::dbl(v);
+    v = G::add(v, cb);
+    block_tree_sum<C>(sh, v, i, nbk);
+    if (i == 0)
         store_xyzz(S + 8 * (size_t)s, load_xyzz(sh));
 }
 
@@ -432,6 +510,8 @@ __global__ void __launch_bounds__(32) k_combine(const uint4 *__restrict__ S, con
         __syncwarp();
         coop_add<C>(sf);
     }
+    for (uint32_t i = 0; i < d.shift; i++)  // upper window-split half: times 2^(c w_lo)
+        coop_dbl<C>(sf);
     if (lane == 0) {
         Xyzz t;
         t.X = sf.f[sX];
@@ -446,10 +526,13 @@ template <class C>
 cudaError_t msm_tail(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
 {
     cudaStream_t st = ctx.stream;
-    // 2. accumulate: persistent grid over the device-side segment count
+    // 2. accumulate: one thread per segment, the grid sized by the host bound on
+    //    the segment count (threads past the device-side count exit at once).
+    //    Blocks are short, so kernels of other streams (the tail of the other
+    //    window half or of another MSM) get SM slots while this one runs.
     {
         const int threads = 128;
-        const int blocks = ctx.sm_count * 8;
+        const int blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>((p.max_segs + threads - 1) / threads, 1u << 30));
         cudaEvent_t ev0 = nullptr;
         prof_begin(ctx, &ev0);
         k_accumulate<C><<<blocks, threads, 0, st>>>(b.segs, b.seg_off + p.NB, b.sorted, b.points, b.seg_sum);
@@ -468,13 +551,17 @@ cudaError_t msm_tail(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
         k_merge_heavy<C><<<ctx.sm_count, HEAVY_THREADS, 0, st>>>(b.seg_off, b.heavy, b.heavy_n, b.seg_sum);
         HS_LAUNCH_CHECK(ctx);
     }
-    // 4. bucket reduction with absolute weights, then one plain sum per window
+    // 4. bucket reduction: group running sums, then one block per window
     {
-        const int threads = 64;
-        k_reduce_abs<C><<<(p.G + threads - 1) / threads, threads, 0, st>>>(b.seg_off, b.seg_sum, b.desc, p.M, p.G,
-                                                                         b.redA);
+        const int threads = 128;
+        k_reduce_groups<C><<<(p.G + threads - 1) / threads, threads, 0, st>>>(b.seg_off, b.seg_sum, b.desc, p.M,
+                                                                            p.G, b.redA);
         HS_LAUNCH_CHECK(ctx);
-        k_window_sum<C><<<p.WS, WSUM_THREADS, 0, st>>>(b.redA, b.desc, p.M, b.redS);
+        const uint32_t t2 = std::max<uint32_t>(32, std::min<uint32_t>(RED_CHUNK_THREADS, p.max_T / RED_CHUNK_Q));
+        k_window_chunks<C><<<p.CH, t2, 0, st>>>(b.redA, b.desc, p.M, b.redC);
+        HS_LAUNCH_CHECK(ctx);
+        const uint32_t t3 = std::max<uint32_t>(32, std::min<uint32_t>(RED_CHUNK, p.max_nbk));
+        k_window_sum<C><<<p.WS, t3, 0, st>>>(b.redC, b.desc, p.M, b.redS);
         HS_LAUNCH_CHECK(ctx);
     }
     // 5. Horner over windows, one warp per MSM
@@ -967,11 +1054,51 @@ cudaError_t fixed_table(Context &ctx, const uint4 *d_gens, size_t n, int c, int 
     return cudaSuccess;
 }
 
+// out = a + b over canonical Jacobians (the two halves of a window-split MSM)
+template <class C>
+__device__ Xyzz xyzz_from_jac24(const uint32_t *j)
+{
+    using F = typename C::F;
+    using G = Group<C>;
+    Fe X, Y, Z;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        X.w[k] = j[k];
+        Y.w[k] = j[8 + k];
+        Z.w[k] = j[16 + k];
+    }
+    if (F::is_zero(Z))
+        return G::inf();
+    Xyzz p;
+    p.X = X;
+    p.Y = Y;
+    p.ZZ = F::sqr(Z);
+    p.ZZZ = F::mul(p.ZZ, Z);
+    return p;
+}
+
+template <class C>
+__global__ void k_join(const uint32_t *__restrict__ a, const uint32_t *__restrict__ b, uint32_t *__restrict__ out)
+{
+    using G = Group<C>;
+    if (blockIdx.x != 0 || threadIdx.x != 0)
+        return;
+    store_jacobian_canon<C>(out, G::add(xyzz_from_jac24<C>(a), xyzz_from_jac24<C>(b)));
+}
+
+template <class C>
+cudaError_t join(Context &ctx, const uint32_t *d_a, const uint32_t *d_b, uint32_t *d_out)
+{
+    k_join<C><<<1, 32, 0, ctx.stream>>>(d_a, d_b, d_out);
+    HS_LAUNCH_CHECK(ctx);
+    return cudaSuccess;
+}
+
 template <class C>
 CurveOps make_ops()
 {
-    return CurveOps{&msm_tail<C>,   &to_affine<C>, &to_affine_scratch, &format_out<C>,
-                    &map_to_curve<C>, &to_jac24<C>, &field_op<C>,       &fixed_table<C>};
+    return CurveOps{&msm_tail<C>,     &to_affine<C>, &to_affine_scratch, &format_out<C>, &map_to_curve<C>,
+                    &to_jac24<C>,     &field_op<C>,  &fixed_table<C>,    &join<C>};
 }
 
 }  // namespace hs

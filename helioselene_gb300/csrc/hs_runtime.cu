@@ -130,6 +130,22 @@ int choose_window(const Context &ctx, int curve, size_t n)
     return c;
 }
 
+// level-2 reduction chunks: chunk_base per MSM and the plan totals
+static void plan_chunks(BatchPlan &p)
+{
+    uint64_t ch = 0;
+    p.max_T = 1;
+    p.max_nbk = 1;
+    for (MsmDesc &d : p.msms) {
+        const uint32_t nbk = d.T > RED_CHUNK ? d.T / RED_CHUNK : 1;
+        d.chunk_base = (uint32_t)ch;
+        ch += (uint64_t)d.Wr * nbk;
+        p.max_T = std::max(p.max_T, d.T);
+        p.max_nbk = std::max(p.max_nbk, nbk);
+    }
+    p.CH = (uint32_t)ch;
+}
+
 BatchPlan make_batch_plan(const Context &ctx, int curve, const size_t *sizes, uint32_t M)
 {
     BatchPlan p;
@@ -146,7 +162,7 @@ BatchPlan make_batch_plan(const Context &ctx, int curve, const size_t *sizes, ui
         d.c = (uint32_t)c;
         d.W = (uint32_t)((257 + c - 1) / c);
         d.B = 1u << (c - 1);
-        d.m0 = std::min<uint32_t>(16, d.B);
+        d.m0 = std::min<uint32_t>(RED_GROUP, d.B);
         d.log2m0 = 0;
         while ((1u << d.log2m0) < d.m0)
             d.log2m0++;
@@ -156,7 +172,9 @@ BatchPlan make_batch_plan(const Context &ctx, int curve, const size_t *sizes, ui
         d.win_base = (uint32_t)ws;
         d.fixed = 0;
         d.Wr = d.W;
-        d.pad0 = d.pad1 = d.pad2 = 0;
+        d.w_lo = 0;
+        d.w_cnt = d.W;
+        d.shift = 0;
         pt += n;
         nb += (uint64_t)d.W * d.B;
         g += (uint64_t)d.W * d.T;
@@ -173,6 +191,7 @@ BatchPlan make_batch_plan(const Context &ctx, int curve, const size_t *sizes, ui
     p.L = (uint32_t)std::max<uint64_t>(16, std::min<uint64_t>(128, 2 * avg));
     p.max_segs = (uint32_t)(std::min<uint64_t>(ent, nb) + ent / p.L + 1);
     p.hist_blocks = (p.NB + SEG_HIST_THREADS - 1) / SEG_HIST_THREADS;
+    plan_chunks(p);
     return p;
 }
 
@@ -183,7 +202,7 @@ BatchPlan make_fixed_plan(int curve, size_t n, int c, uint32_t count)
     p.M = count;
     p.msms.resize(count);
     const uint32_t W = (uint32_t)((257 + c - 1) / c), B = 1u << (c - 1);
-    const uint32_t m0 = std::min<uint32_t>(16, B);
+    const uint32_t m0 = std::min<uint32_t>(RED_GROUP, B);
     uint32_t log2m0 = 0;
     while ((1u << log2m0) < m0)
         log2m0++;
@@ -202,7 +221,9 @@ BatchPlan make_fixed_plan(int curve, size_t n, int c, uint32_t count)
         d.win_base = j;
         d.fixed = 1;
         d.Wr = 1;
-        d.pad0 = d.pad1 = d.pad2 = 0;
+        d.w_lo = 0;
+        d.w_cnt = W;
+        d.shift = 0;
     }
     const uint64_t ent = (uint64_t)count * n * W;
     p.n_total = (uint32_t)(count * n);
@@ -215,6 +236,47 @@ BatchPlan make_fixed_plan(int curve, size_t n, int c, uint32_t count)
     p.L = (uint32_t)std::max<uint64_t>(16, std::min<uint64_t>(128, 2 * avg));
     p.max_segs = (uint32_t)(std::min<uint64_t>(ent, p.NB) + ent / p.L + 1);
     p.hist_blocks = (p.NB + SEG_HIST_THREADS - 1) / SEG_HIST_THREADS;
+    plan_chunks(p);
+    return p;
+}
+
+BatchPlan make_window_plan(int curve, size_t n, int c, uint32_t w_lo, uint32_t w_cnt)
+{
+    BatchPlan p;
+    p.curve = curve;
+    p.M = 1;
+    p.msms.resize(1);
+    MsmDesc &d = p.msms[0];
+    d.pt_off = 0;
+    d.n = (uint32_t)n;
+    d.c = (uint32_t)c;
+    d.W = (uint32_t)((257 + c - 1) / c);
+    d.B = 1u << (c - 1);
+    d.m0 = std::min<uint32_t>(RED_GROUP, d.B);
+    d.log2m0 = 0;
+    while ((1u << d.log2m0) < d.m0)
+        d.log2m0++;
+    d.T = d.B / d.m0;
+    d.bucket_base = 0;
+    d.group_base = 0;
+    d.win_base = 0;
+    d.fixed = 0;
+    d.Wr = w_cnt;
+    d.w_lo = w_lo;
+    d.w_cnt = w_cnt;
+    d.shift = (uint32_t)c * w_lo;
+    const uint64_t ent = (uint64_t)n * w_cnt;
+    p.n_total = (uint32_t)n;
+    p.NB = w_cnt * d.B;
+    p.G = w_cnt * d.T;
+    p.WS = w_cnt;
+    p.entries_bound = ent;
+    p.max_entries = (uint32_t)std::max<uint64_t>(1, ent);
+    const uint64_t avg = (ent + p.NB - 1) / p.NB;
+    p.L = (uint32_t)std::max<uint64_t>(16, std::min<uint64_t>(128, 2 * avg));
+    p.max_segs = (uint32_t)(std::min<uint64_t>(ent, p.NB) + ent / p.L + 1);
+    p.hist_blocks = (p.NB + SEG_HIST_THREADS - 1) / SEG_HIST_THREADS;
+    plan_chunks(p);
     return p;
 }
 
@@ -238,7 +300,8 @@ size_t batch_bytes(const BatchPlan &p)
     b += align256((size_t)p.max_segs * 16);                                                // segs
     b += align256((size_t)p.max_segs * 128);                                               // seg_sum
     b += align256((size_t)p.NB * 4) + 256;                                                 // heavy list + counter
-    b += align256((size_t)std::max<uint32_t>(1, p.G) * 128);                               // group sums
+    b += align256((size_t)std::max<uint32_t>(1, p.G) * 256);                               // group (acc, run) pairs
+    b += align256((size_t)std::max<uint32_t>(1, p.CH) * 256);                              // chunk (sum, run) pairs
     b += align256((size_t)std::max<uint32_t>(1, p.WS) * 128);                              // window sums
     b += align256((size_t)std::max<uint32_t>(1, p.M) * 96);                                // results
     return b + 16 * 256;
@@ -259,11 +322,12 @@ bool carve(DeviceArena &a, const BatchPlan &p, BatchBuffers &b)
     b.seg_sum = (uint4 *)a.take((size_t)p.max_segs * 128);
     b.heavy = (uint32_t *)a.take((size_t)p.NB * 4);
     b.heavy_n = (uint32_t *)a.take(4);
-    b.redA = (uint4 *)a.take((size_t)std::max<uint32_t>(1, p.G) * 128);
+    b.redA = (uint4 *)a.take((size_t)std::max<uint32_t>(1, p.G) * 256);
+    b.redC = (uint4 *)a.take((size_t)std::max<uint32_t>(1, p.CH) * 256);
     b.redS = (uint4 *)a.take((size_t)std::max<uint32_t>(1, p.WS) * 128);
     b.out_jac = (uint32_t *)a.take((size_t)std::max<uint32_t>(1, p.M) * 96);
     return b.desc && b.counts && b.offsets && b.seg_off && b.scan_tmp && b.len_hist && b.len_scan && b.sorted &&
-           b.segs && b.seg_sum && b.heavy && b.heavy_n && b.redA && b.redS && b.out_jac;
+           b.segs && b.seg_sum && b.heavy && b.heavy_n && b.redA && b.redC && b.redS && b.out_jac;
 }
 
 // ---------------------------------------------------------------------------
@@ -285,10 +349,13 @@ __device__ __forceinline__ uint32_t window_bits(const uint32_t s[8], int k)
 // Normal MSMs: window k uses buckets bucket_base + k*B + ..., entries name the
 // point (pbase = i, pstep = 0).  Fixed-base MSMs: every window uses the same B
 // buckets (wstep = 0), entries name table row (i - pt_off)*W + k (pstep = 1).
+// The digits are always computed from window 0 (the carries run upward), but
+// only windows [w_lo, w_lo + w_cnt) are emitted (a window-split half).
 template <int CB, bool SCATTER>
 __device__ __forceinline__ void recode_one(const uint32_t s[8], uint32_t pbase, uint32_t pstep, uint32_t wstep,
-                                           uint32_t bucket_base, uint32_t *__restrict__ counts,
-                                           const uint32_t *__restrict__ offsets, uint32_t *__restrict__ sorted)
+                                           uint32_t bucket_base, uint32_t w_lo, uint32_t w_cnt,
+                                           uint32_t *__restrict__ counts, const uint32_t *__restrict__ offsets,
+                                           uint32_t *__restrict__ sorted)
 {
     constexpr int W = (257 + CB - 1) / CB;
     constexpr uint32_t B = 1u << (CB - 1);
@@ -306,8 +373,8 @@ __device__ __forceinline__ void recode_one(const uint32_t s[8], uint32_t pbase, 
             mag = v;
             carry = 0;
         }
-        if (mag != 0) {
-            const uint32_t kb = bucket_base + (uint32_t)k * wstep + mag - 1u;
+        if (mag != 0 && (uint32_t)k - w_lo < w_cnt) {
+            const uint32_t kb = bucket_base + ((uint32_t)k - w_lo) * wstep + mag - 1u;
             if (!SCATTER) {
                 atomicAdd(counts + kb, 1u);
             } else {
@@ -333,12 +400,13 @@ __global__ void k_recode(const uint4 *__restrict__ scalars, uint32_t n_total, co
     const uint32_t pbase = fixed ? (i - desc[m].pt_off) * desc[m].W : i;
     const uint32_t pstep = fixed ? 1u : 0u;
     const uint32_t wstep = fixed ? 0u : desc[m].B;
+    const uint32_t w_lo = desc[m].w_lo, w_cnt = desc[m].w_cnt;
     const uint4 a = __ldg(scalars + 2 * (size_t)i), b = __ldg(scalars + 2 * (size_t)i + 1);
     const uint32_t s[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
     switch (c) {
 #define HS_CASE(v)                                                       \
     case v:                                                              \
-        recode_one<v, SCATTER>(s, pbase, pstep, wstep, base, counts, offsets, sorted); \
+        recode_one<v, SCATTER>(s, pbase, pstep, wstep, base, w_lo, w_cnt, counts, offsets, sorted); \
         break;
         HS_CASE(4)
         HS_CASE(5)
@@ -788,6 +856,143 @@ int execute_batch(Context &ctx, const BatchPlan &p, const BatchBuffers &b, void 
     return HS_OK;
 }
 
+// ---------------------------------------------------------------------------
+// window-split MSM: the upper windows on the context stream, the lower windows
+// on a second, lower-priority stream, joined by one point addition.  The upper
+// half carries the long Horner chain (its extra c*w_lo doublings), so it starts
+// first and its chain runs while the lower half is still accumulating.
+// ---------------------------------------------------------------------------
+// the second stream gets the greatest priority: the upper window half goes there
+static cudaError_t ensure_stream2(Context &ctx)
+{
+    cudaError_t e = cudaSuccess;
+    if (!ctx.stream2) {
+        int least = 0, greatest = 0;
+        if ((e = cudaDeviceGetStreamPriorityRange(&least, &greatest)) != cudaSuccess)
+            return e;
+        if ((e = cudaStreamCreateWithPriority(&ctx.stream2, cudaStreamNonBlocking, greatest)) != cudaSuccess)
+            return e;
+    }
+    if (!ctx.ev_fork && (e = cudaEventCreateWithFlags(&ctx.ev_fork, cudaEventDisableTiming)) != cudaSuccess)
+        return e;
+    if (!ctx.ev_join && (e = cudaEventCreateWithFlags(&ctx.ev_join, cudaEventDisableTiming)) != cudaSuccess)
+        return e;
+    return e;
+}
+
+struct SplitPlan {
+    BatchPlan hi, lo;
+};
+
+static SplitPlan make_split(const Context &ctx, int curve, size_t n)
+{
+    const int c = choose_window(ctx, curve, n);
+    const uint32_t W = (uint32_t)((257 + c - 1) / c);
+    const uint32_t h = W / 2;
+    return SplitPlan{make_window_plan(curve, n, c, h, W - h), make_window_plan(curve, n, c, 0, h)};
+}
+
+static size_t split_bytes(const SplitPlan &s) { return batch_bytes(s.hi) + batch_bytes(s.lo) + 2048; }
+
+static cudaError_t launch_split(Context &ctx, const SplitPlan &s, const BatchBuffers &bh, const BatchBuffers &bl,
+                                uint32_t *d_final, void *d_out, int out_fmt)
+{
+    const CurveOps &ops = curve_ops(s.hi.curve);
+    cudaStream_t a = ctx.stream, b = ctx.stream2;
+    cudaError_t e;
+    if ((e = cudaEventRecord(ctx.ev_fork, a)) != cudaSuccess || (e = cudaStreamWaitEvent(b, ctx.ev_fork, 0)) != cudaSuccess)
+        return e;
+    ctx.stream = b;  // upper half on the high-priority stream
+    e = launch_sort(ctx, s.hi, bh);
+    if (e == cudaSuccess)
+        e = ops.msm_tail(ctx, s.hi, bh);
+    ctx.stream = a;
+    if (e != cudaSuccess)
+        return e;
+    if ((e = launch_sort(ctx, s.lo, bl)) != cudaSuccess || (e = ops.msm_tail(ctx, s.lo, bl)) != cudaSuccess)
+        return e;
+    if ((e = cudaEventRecord(ctx.ev_join, b)) != cudaSuccess || (e = cudaStreamWaitEvent(a, ctx.ev_join, 0)) != cudaSuccess)
+        return e;
+    if ((e = ops.join(ctx, bh.out_jac, bl.out_jac, d_final)) != cudaSuccess)
+        return e;
+    return ops.format_out(ctx, d_final, 1, out_fmt, d_out);
+}
+
+// buffers: both halves carved after one reservation made by the caller
+static int execute_split(Context &ctx, const SplitPlan &s, const void *d_scalars, const void *d_points, void *d_out,
+                         int out_fmt)
+{
+    HS_CU(ensure_stream2(ctx), "stream creation");
+    BatchBuffers bh, bl;
+    if (!carve(ctx.arena, s.hi, bh) || !carve(ctx.arena, s.lo, bl))
+        return fail_msg(ctx, HS_ENOMEM, "workspace carve");
+    uint32_t *d_final = (uint32_t *)ctx.arena.take(96);
+    if (!d_final)
+        return fail_msg(ctx, HS_ENOMEM, "workspace carve");
+    bh.scalars = bl.scalars = static_cast<const uint32_t *>(d_scalars);
+    bh.points = bl.points = static_cast<const uint4 *>(d_points);
+    cudaStream_t st = ctx.stream;
+    if (!ctx.use_graphs || ctx.profile) {
+        HS_CU(cudaMemcpyAsync(bh.desc, s.hi.msms.data(), sizeof(MsmDesc), cudaMemcpyHostToDevice, st), "descriptors");
+        HS_CU(cudaMemcpyAsync(bl.desc, s.lo.msms.data(), sizeof(MsmDesc), cudaMemcpyHostToDevice, st), "descriptors");
+        HS_CU(launch_split(ctx, s, bh, bl, d_final, d_out, out_fmt), "split MSM launch");
+        return HS_OK;
+    }
+    std::vector<uint64_t> key = {0x5350u, (uint64_t)s.hi.curve, (uint64_t)s.hi.msms[0].n, (uint64_t)s.hi.msms[0].c,
+                                 (uint64_t)out_fmt, (uint64_t)(uintptr_t)ctx.arena.base, (uint64_t)ctx.arena.cap,
+                                 (uint64_t)(uintptr_t)bh.counts, (uint64_t)(uintptr_t)d_scalars,
+                                 (uint64_t)(uintptr_t)d_points, (uint64_t)(uintptr_t)d_out, (uint64_t)(uintptr_t)st};
+    for (GraphEntry &g : ctx.graphs) {
+        if (g.key == key) {
+            HS_CU(cudaGraphLaunch(g.exec, st), "graph launch");
+            ctx.launches += g.kernels;
+            return HS_OK;
+        }
+    }
+    GraphEntry ent;
+    HS_CU(cudaMalloc(&ent.d_desc, 2 * sizeof(MsmDesc)), "descriptor allocation");
+    const MsmDesc both[2] = {s.hi.msms[0], s.lo.msms[0]};
+    cudaError_t ue = cudaMemcpy(ent.d_desc, both, sizeof(both), cudaMemcpyHostToDevice);
+    if (ue != cudaSuccess) {
+        cudaFree(ent.d_desc);
+        return fail(ctx, ue, "descriptor upload");
+    }
+    bh.desc = (MsmDesc *)ent.d_desc;
+    bl.desc = (MsmDesc *)ent.d_desc + 1;
+    cudaGraph_t graph = nullptr;
+    const uint64_t before = ctx.launches;
+    cudaError_t ce = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    cudaError_t le = ce == cudaSuccess ? launch_split(ctx, s, bh, bl, d_final, d_out, out_fmt) : ce;
+    if (ce == cudaSuccess)
+        ce = cudaStreamEndCapture(st, &graph);
+    if (le != cudaSuccess || ce != cudaSuccess) {
+        if (graph)
+            cudaGraphDestroy(graph);
+        cudaFree(ent.d_desc);
+        return fail(ctx, le != cudaSuccess ? le : ce, "graph capture");
+    }
+    cudaGraphExec_t exec = nullptr;
+    // the captured stream priorities stay on the kernel nodes: the upper half is scheduled first
+    cudaError_t ie = cudaGraphInstantiateWithFlags(&exec, graph, cudaGraphInstantiateFlagUseNodePriority);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) {
+        cudaFree(ent.d_desc);
+        return fail(ctx, ie, "graph instantiate");
+    }
+    ent.key = std::move(key);
+    ent.exec = exec;
+    ent.kernels = ctx.launches - before;
+    if (ctx.graphs.size() >= 64) {
+        cudaStreamSynchronize(st);
+        cudaGraphExecDestroy(ctx.graphs.front().exec);
+        cudaFree(ctx.graphs.front().d_desc);
+        ctx.graphs.erase(ctx.graphs.begin());
+    }
+    ctx.graphs.push_back(std::move(ent));
+    HS_CU(cudaGraphLaunch(exec, st), "graph launch");
+    return HS_OK;
+}
+
 void drop_graphs(Context &ctx)
 {
     if (!ctx.graphs.empty() && ctx.stream)
@@ -877,6 +1082,10 @@ void hs_context_destroy(hs_context *h)
         cudaStreamDestroy(h->c.stream);
         if (h->c.stream2)
             cudaStreamDestroy(h->c.stream2);
+        if (h->c.ev_fork)
+            cudaEventDestroy(h->c.ev_fork);
+        if (h->c.ev_join)
+            cudaEventDestroy(h->c.ev_join);
     }
     delete h;
 }
@@ -913,6 +1122,15 @@ int hs_context_set_graphs(hs_context *h, int on)
     return HS_OK;
 }
 
+int hs_context_set_split(hs_context *h, size_t min_points)
+{
+    if (!h)
+        return HS_EINVAL;
+    std::lock_guard<std::mutex> lk(h->c.mu);
+    h->c.split_min = min_points;
+    return HS_OK;
+}
+
 int hs_msm_device(hs_context *h, int curve, const void *d_scalars, const void *d_points, size_t n, void *d_out,
                   int out_fmt)
 {
@@ -929,6 +1147,11 @@ int hs_msm_device(hs_context *h, int curve, const void *d_scalars, const void *d
         HS_CU(cudaMemcpyAsync(d_out, idb, fmt_bytes(out_fmt), cudaMemcpyHostToDevice, ctx.stream), "copy");
         HS_CU(cudaStreamSynchronize(ctx.stream), "sync");
         return HS_OK;
+    }
+    if (ctx.split_min && n >= ctx.split_min) {
+        const SplitPlan s = make_split(ctx, curve, n);
+        HS_CU(ctx.arena.reserve(split_bytes(s)), "workspace allocation");
+        return execute_split(ctx, s, d_scalars, d_points, d_out, out_fmt);
     }
     const size_t sizes[1] = {n};
     const BatchPlan p = make_batch_plan(ctx, curve, sizes, 1);
@@ -957,17 +1180,22 @@ static int msm_host(Context &ctx, int curve, const uint8_t *lead_scalar, const v
     DeviceGuard g(ctx.device);
     const size_t pb = fmt_bytes(point_fmt);
     const CurveOps &ops = curve_ops(curve);
-    const size_t sizes[1] = {total};
-    const BatchPlan p = make_batch_plan(ctx, curve, sizes, 1);
+    const bool split = ctx.split_min && total >= ctx.split_min;
+    SplitPlan s;
+    BatchPlan p;
+    if (split)
+        s = make_split(ctx, curve, total);
+    else {
+        const size_t sizes[1] = {total};
+        p = make_batch_plan(ctx, curve, sizes, 1);
+    }
     const size_t need_in = align256(total * 32) + align256(total * 64) +
                            (point_fmt == HS_FMT_AFFINE ? 0 : align256(total * pb)) +
                            align256(ops.to_affine_scratch(total)) + 256;
-    BatchBuffers b;
-    void *extra = nullptr;
-    int rc = reserve_batch(ctx, p, need_in, b, &extra);
-    if (rc != HS_OK)
-        return rc;
-    uint8_t *d_sc = (uint8_t *)extra;
+    HS_CU(ctx.arena.reserve(need_in + (split ? split_bytes(s) : batch_bytes(p)) + 2048), "workspace allocation");
+    uint8_t *d_sc = (uint8_t *)ctx.arena.take(need_in);
+    if (!d_sc)
+        return fail_msg(ctx, HS_ENOMEM, "workspace carve");
     uint8_t *d_pts = d_sc + align256(total * 32);
     uint8_t *d_raw = point_fmt == HS_FMT_AFFINE ? d_pts : d_pts + align256(total * 64);
     uint8_t *d_scratch = (point_fmt == HS_FMT_AFFINE ? d_pts + align256(total * 64) : d_raw + align256(total * pb));
@@ -983,9 +1211,17 @@ static int msm_host(Context &ctx, int curve, const uint8_t *lead_scalar, const v
     }
     if (point_fmt != HS_FMT_AFFINE)
         HS_CU(ops.to_affine(ctx, d_raw, point_fmt, total, (uint4 *)d_pts, d_scratch), "input conversion");
-    b.scalars = (const uint32_t *)d_sc;
-    b.points = (const uint4 *)d_pts;
-    rc = execute_batch(ctx, p, b, d_out, out_fmt);
+    int rc;
+    if (split) {
+        rc = execute_split(ctx, s, d_sc, d_pts, d_out, out_fmt);
+    } else {
+        BatchBuffers b;
+        if (!carve(ctx.arena, p, b))
+            return fail_msg(ctx, HS_ENOMEM, "workspace carve");
+        b.scalars = (const uint32_t *)d_sc;
+        b.points = (const uint4 *)d_pts;
+        rc = execute_batch(ctx, p, b, d_out, out_fmt);
+    }
     if (rc != HS_OK)
         return rc;
     HS_CU(cudaMemcpyAsync(out, d_out, fmt_bytes(out_fmt), cudaMemcpyDeviceToHost, st), "D2H result");
@@ -1218,8 +1454,7 @@ int hs_msm_batch(hs_context *h, const hs_msm_desc *descs, size_t count, int poin
         if (!carve(ctx.arena, plans[k], bufs[k]) || !(st_base[k] = (uint8_t *)ctx.arena.take(stage[k])))
             return fail_msg(ctx, HS_ENOMEM, "workspace carve");
     }
-    if (!ctx.stream2)
-        HS_CU(cudaStreamCreateWithFlags(&ctx.stream2, cudaStreamNonBlocking), "stream creation");
+    HS_CU(ensure_stream2(ctx), "stream creation");
     cudaStream_t s1 = ctx.stream;
     cudaEvent_t ev_in = nullptr, ev_done = nullptr;
     HS_CU(cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming), "event");

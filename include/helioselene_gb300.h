@@ -91,6 +91,11 @@ int hs_context_set_window(hs_context *ctx, int curve, size_t n_min, size_t n_max
 /* capture launch sequences as CUDA graphs and replay them for repeated shapes
  * (on by default); off launches every kernel directly */
 int hs_context_set_graphs(hs_context *ctx, int on);
+/* single MSMs of at least min_points run as two window halves on two streams
+ * joined by one addition, so the long doubling chain of the upper half overlaps
+ * the accumulation of the lower half (default 2^18; 0 turns the split off, for
+ * callers that already overlap several MSMs on the device) */
+int hs_context_set_split(hs_context *ctx, size_t min_points);
 
 /* ---- MSM: sum of scalars[i] * points[i] ----
  * Replaces helios_msm_vartime / selene_msm_vartime

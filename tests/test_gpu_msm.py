@@ -274,3 +274,27 @@ def test_linearity_at_full_size(ctx, curve):
     pair = np.frombuffer(ra + rb, np.uint8)
     assert ctx.msm(curve, one, pair) == rs
     assert oracle.compress(curve, oracle.point_add(curve, ra, rb)).tobytes() == rs
+
+
+@pytest.mark.parametrize("curve", [0, 1])
+def test_window_split_matches_unsplit(ctx, curve):
+    """single MSMs of n >= 2^18 run as two window halves on two streams joined by
+    one addition; the batch path runs the same MSM unsplit.  Odd and even window
+    counts, empty upper halves (small scalars) and all-zero scalars."""
+    from helioselene_gb300.workload import make_workload
+    n = (1 << 18) + 3
+    w = make_workload(curve, n, seed=77 + curve, edge_fraction=0.01)
+    pts = ctx.map_to_curve(curve, w.u, HS_AFF)
+    small = w.scalars.copy()
+    small[:, 8:] = 0
+    zero = np.zeros_like(w.scalars)
+    try:
+        for c in (10, 13, 16, 17):
+            ctx.set_window(curve, 1, 1 << 30, c)
+            for sc in (w.scalars, small, zero):
+                split = ctx.msm(curve, sc, pts)
+                assert split == ctx.msm_batch([(curve, sc, pts)])[0], f"c={c}"
+            ctx.set_window(curve, 0, 0, 0)
+    finally:
+        ctx.set_window(curve, 0, 0, 0)
+    assert ctx.msm(curve, zero, pts) == bytes(32)
