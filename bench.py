@@ -42,6 +42,9 @@ WORKLOAD = ("Helios + Selene vartime Pippenger MSM, n=2^20 each; scalars uniform
             "SWU-derived affine bases; 1% edge slices (zero, order-1, repeated base, top-window-only)")
 SEED = 0x48454C494F53
 IMAD_PER_MODMUL = {0: 144, 1: 232}  # F_p, F_q: 2 IMAD per 32x32->64 product
+# dram__bytes_read.sum + dram__bytes_write.sum of one k_accumulate launch at
+# n = 2^20, mean of the Helios and Selene launches of one ncu capture
+ACC_TRAFFIC_BYTES = (477.2e6 + 497.5e6) / 2
 
 
 def modmul_count(n: int) -> tuple:
@@ -458,6 +461,9 @@ def run_ours(args) -> None:
     device = f"cuda:{local}"
     ctx = hs.Context(local)
     ctx2 = hs.Context(local)  # the Selene MSM of a step runs on its own stream, overlapping the Helios one
+    if args.split is not None:
+        ctx.set_split(args.split)
+        ctx2.set_split(args.split)
     ctxs = {hs.HELIOS: ctx, hs.SELENE: ctx2}
     n = args.n
     data = make_inputs(hs, ctx, torch, n, device)
@@ -468,9 +474,11 @@ def run_ours(args) -> None:
     torch.cuda.synchronize()
 
     def step(ev_pair=None):
+        # steps do not overlap: L2 flush, then a synchronize, then the timed events
         start = torch.cuda.Event(enable_timing=True)
         with torch.cuda.stream(stream):
             flush.zero_()
+        torch.cuda.synchronize()
         start.record(stream)
         streams[hs.SELENE].wait_event(start)
         ends = []
@@ -591,6 +599,7 @@ def run_ours(args) -> None:
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "n": n, "curves": ["helios", "selene"], "parallelism": f"replicas{ws}",
+                       "window_split_min_points": args.split if args.split is not None else "library default (2^18)",
                        "l2": "flushed before every step (256 MiB memset, outside the timed events)",
                        "inputs": "device-resident scalars + canonical affine bases"},
             "per_curve": per_curve,
@@ -601,7 +610,10 @@ def run_ours(args) -> None:
                     "api": "hs_msm(point_fmt=HS_FMT_JACOBIAN51, out_fmt=HS_FMT_JACOBIAN51), pinned host buffers"},
             "roofline": {"bound": "imad", "achieved": achieved / 1e12, "peak": imad_peak / 1e12,
                          "unit": "T IMAD/s", "frac": achieved / imad_peak if imad_peak else None,
-                         "traffic": None, "kernel": "k_accumulate",
+                         "traffic": ACC_TRAFFIC_BYTES, "traffic_unit": "bytes per launch (DRAM read + write)",
+                         "traffic_source": "ncu capture of k_accumulate at n=2^20 (Helios 477.2 MB, Selene 497.5 MB), "
+                                           "profiles/k_accumulate_msm_n2p20.md",
+                         "kernel": "k_accumulate",
                          "work": "point-window entries x 6 modmul (batch-affine bucket add) x IMAD-eq per modmul "
                                  "(F_p 144, F_q 232), summed over one Helios and one Selene launch",
                          "peak_source": "measured in this run by hs_measure_imad_peak (mad.lo/mad.hi chains)",
@@ -671,6 +683,8 @@ def main() -> None:
     ap.add_argument("--no-batched", action="store_true", help="skip the batched (1024 uneven MSMs) section")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving (Poisson arrivals) section")
     ap.add_argument("--no-fixed", action="store_true", help="skip the fixed-base commitment section")
+    ap.add_argument("--split", type=int, default=None,
+                    help="window-split threshold in points for single MSMs (0: off; default: the library's)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
