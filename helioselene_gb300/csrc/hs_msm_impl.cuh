@@ -245,7 +245,9 @@ __device__ __forceinline__ void block_tree_sum(uint4 *sh, const Xyzz &v, uint32_
 constexpr uint32_t RED_CHUNK_Q = 4;
 constexpr uint32_t RED_CHUNK_THREADS = RED_CHUNK / RED_CHUNK_Q;
 
-template <class C>
+// DIRECT: every window of the batch is one chunk (T <= RED_CHUNK), so C_b is
+// already the window sum and goes straight to S (k_window_sum is skipped).
+template <class C, bool DIRECT>
 __global__ void __launch_bounds__(RED_CHUNK_THREADS) k_window_chunks(const uint4 *__restrict__ in,
                                                                     const MsmDesc *__restrict__ desc, uint32_t M,
                                                                     uint4 *__restrict__ outC)
@@ -281,8 +283,12 @@ __global__ void __launch_bounds__(RED_CHUNK_THREADS) k_window_chunks(const uint4
     v = G::add(v, a);
     block_tree_sum<C>(sh, v, i, P);
     if (i == 0) {
-        store_xyzz(outC + 16 * (size_t)ch, load_xyzz(sh));
-        store_xyzz(outC + 16 * (size_t)ch + 8, r);  // thread 0's suffix sum is the chunk's run total
+        if (DIRECT) {
+            store_xyzz(outC + 8 * (size_t)ch, load_xyzz(sh));
+        } else {
+            store_xyzz(outC + 16 * (size_t)ch, load_xyzz(sh));
+            store_xyzz(outC + 16 * (size_t)ch + 8, r);  // thread 0's suffix sum is the chunk's run total
+        }
     }
 }
 
@@ -558,11 +564,16 @@ cudaError_t msm_tail(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
                                                                             p.G, b.redA);
         HS_LAUNCH_CHECK(ctx);
         const uint32_t t2 = std::max<uint32_t>(32, std::min<uint32_t>(RED_CHUNK_THREADS, p.max_T / RED_CHUNK_Q));
-        k_window_chunks<C><<<p.CH, t2, 0, st>>>(b.redA, b.desc, p.M, b.redC);
-        HS_LAUNCH_CHECK(ctx);
-        const uint32_t t3 = std::max<uint32_t>(32, std::min<uint32_t>(RED_CHUNK, p.max_nbk));
-        k_window_sum<C><<<p.WS, t3, 0, st>>>(b.redC, b.desc, p.M, b.redS);
-        HS_LAUNCH_CHECK(ctx);
+        if (p.max_nbk == 1) {  // one chunk per window: chunk index == window slot
+            k_window_chunks<C, true><<<p.CH, t2, 0, st>>>(b.redA, b.desc, p.M, b.redS);
+            HS_LAUNCH_CHECK(ctx);
+        } else {
+            k_window_chunks<C, false><<<p.CH, t2, 0, st>>>(b.redA, b.desc, p.M, b.redC);
+            HS_LAUNCH_CHECK(ctx);
+            const uint32_t t3 = std::max<uint32_t>(32, std::min<uint32_t>(RED_CHUNK, p.max_nbk));
+            k_window_sum<C><<<p.WS, t3, 0, st>>>(b.redC, b.desc, p.M, b.redS);
+            HS_LAUNCH_CHECK(ctx);
+        }
     }
     // 5. Horner over windows, one warp per MSM
     k_combine<C><<<p.M, 32, 0, st>>>(b.redS, b.desc, b.out_jac);
