@@ -64,6 +64,8 @@ SIGNATURES = {
     "hs_pedersen": (_int, [_vp, _int, _vp, _vp, _vp, _vp, _int, _sz, _vp, _int]),
     "hs_batch_to_affine": (_int, [_vp, _int, _vp, _sz, _vp, _int]),
     "hs_compress": (_int, [_vp, _int, _vp, _int, _sz, _vp]),
+    "hs_decompress": (_int, [_vp, _int, _vp, _sz, _vp, _int, _vp]),
+    "hs_decompress_device": (_int, [_vp, _int, _vp, _sz, _vp, _vp]),
     "hs_map_to_curve": (_int, [_vp, _int, _vp, _sz, _vp, _int]),
     "hs_map_to_curve_device": (_int, [_vp, _int, _vp, _sz, _vp]),
     "hs_msm_batch": (_int, [_vp, _c.POINTER(hs_msm_desc), _sz, _int, _int]),

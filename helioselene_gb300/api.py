@@ -182,6 +182,22 @@ class Context:
         self._check(self._lib.hs_compress(self._h, curve, _ptr(p), in_fmt, n, _ptr(out)), "hs_compress")
         return out
 
+    def decompress(self, curve: int, encodings, out_fmt: int = L.FMT_AFFINE, check: bool = True):
+        """32-byte encodings -> points in out_fmt and a validity mask (hs_decompress).
+        With check=False invalid encodings come back as the identity instead of raising."""
+        e = _u8(encodings)
+        n = e.size // 32
+        out = np.zeros(n * L.FMT_BYTES[out_fmt], np.uint8)
+        valid = np.zeros(n, np.uint8)
+        rc = self._lib.hs_decompress(self._h, curve, _ptr(e), n, _ptr(out), out_fmt, _ptr(valid))
+        if rc != L.HS_EINVAL or check:
+            self._check(rc, "hs_decompress")
+        return out, valid.astype(bool)
+
+    def decompress_device(self, curve: int, d_in: int, n: int, d_out: int, d_valid: int) -> None:
+        self._check(self._lib.hs_decompress_device(self._h, curve, ctypes.c_void_p(d_in), n, ctypes.c_void_p(d_out),
+                                                   ctypes.c_void_p(d_valid)), "hs_decompress_device")
+
     def map_to_curve(self, curve: int, u, out_fmt: int = L.FMT_AFFINE) -> np.ndarray:
         uu = _u8(u)
         n = uu.size // 32
@@ -372,6 +388,14 @@ class _PointBase:
     @classmethod
     def identity(cls):
         return cls(jac51_from_ints(1, 1, 0))
+
+    @classmethod
+    def from_bytes(cls, data: bytes, ctx: Context = None):
+        """Decode a 32-byte encoding on the device; None when the reference rejects
+        it (HeliosPoint::from_bytes, src/api_point.cpp:58-64)."""
+        ctx = ctx or default_context()
+        out, valid = ctx.decompress(cls.CURVE, bytes(data), L.FMT_JACOBIAN51, check=False)
+        return cls(out.tobytes()) if valid[0] else None
 
     @classmethod
     def from_affine_bytes(cls, aff64) -> "_PointBase":

@@ -189,6 +189,10 @@ struct CurveOps {
                                uint4 *d_table);
     // out = a + b for canonical Jacobians (24 words each)
     cudaError_t (*join)(Context &ctx, const uint32_t *d_a, const uint32_t *d_b, uint32_t *d_out);
+    // 32-byte encodings -> canonical affine; invalid ones give (0, 0), d_valid[i] = 0
+    // (d_valid may be null) and a count in *d_bad (not cleared here)
+    cudaError_t (*decompress)(Context &ctx, const void *d_in, size_t n, uint4 *d_out, uint8_t *d_valid,
+                              uint32_t *d_bad);
 };
 extern const CurveOps helios_ops;
 extern const CurveOps selene_ops;

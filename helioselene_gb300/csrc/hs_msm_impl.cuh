@@ -727,10 +727,21 @@ __global__ void k_jac_to_affine(const uint64_t *__restrict__ in, int fmt, size_t
 }
 
 template <class C>
+cudaError_t decompress(Context &ctx, const void *d_in, size_t n, uint4 *d_out, uint8_t *d_valid, uint32_t *d_bad);
+
+// HS_FMT_COMPRESSED input decodes on the device; the count of invalid
+// encodings is left in the first word of scratch for the caller to check.
+template <class C>
 cudaError_t to_affine(Context &ctx, const void *d_in, int fmt, size_t n, uint4 *d_out, void *scratch)
 {
     if (n == 0)
         return cudaSuccess;
+    if (fmt == HS_FMT_COMPRESSED) {
+        cudaError_t e = cudaMemsetAsync(scratch, 0, sizeof(uint32_t), ctx.stream);
+        if (e != cudaSuccess)
+            return e;
+        return decompress<C>(ctx, d_in, n, d_out, nullptr, static_cast<uint32_t *>(scratch));
+    }
     const size_t chunks = (n + AFF_CHUNK - 1) / AFF_CHUNK;
     const int threads = 128;
     k_jac_to_affine<C><<<(unsigned)((chunks + threads - 1) / threads), threads, 0, ctx.stream>>>(
@@ -899,6 +910,62 @@ cudaError_t map_to_curve(Context &ctx, const void *d_u, size_t n, uint4 *d_out)
     const int threads = 64;
     k_map_to_curve<C><<<(unsigned)((n + threads - 1) / threads), threads, 0, ctx.stream>>>(
         reinterpret_cast<const uint4 *>(d_u), n, d_out);
+    HS_LAUNCH_CHECK(ctx);
+    return cudaSuccess;
+}
+
+// ---------------------------------------------------------------------------
+// point decoding (helios/src/x64/helios_frombytes.cpp:59-109, selene twin):
+// bit 255 is the parity of y; x must be canonical (the reference re-encodes and
+// compares); y = sqrt(x^3 - 3x + b), negated when its parity differs.  An
+// invalid encoding (x >= m, or no square root: this includes the 32 zero bytes
+// of the identity's encoding) gives (0, 0), valid[i] = 0 and one count in *bad.
+// ---------------------------------------------------------------------------
+template <class C>
+__global__ void k_decompress(const uint4 *__restrict__ in, size_t n, uint4 *__restrict__ out,
+                             uint8_t *__restrict__ valid, uint32_t *__restrict__ bad)
+{
+    using F = typename C::F;
+    using G = Group<C>;
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    Fe x = load_fe(in + 2 * i);
+    const uint32_t parity = x.w[7] >> 31;
+    x.w[7] &= 0x7fffffffu;
+    const Fe xc = F::canon(x);
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+        ok = ok && (xc.w[k] == x.w[k]);
+    Fe y = F::zero();
+    if (ok) {
+        const Fe rhs = F::add(F::sub(F::mul(F::sqr(x), x), F::add(F::dbl(x), x)), G::b());
+        ok = fsqrt<C>(y, rhs);
+    }
+    if (ok) {
+        y = F::canon(y);
+        if ((y.w[0] & 1u) != parity)
+            y = F::canon(F::neg(y));
+    } else {
+        x = F::zero();
+        y = F::zero();
+        atomicAdd(bad, 1u);
+    }
+    store_fe(out + 4 * i, x);
+    store_fe(out + 4 * i + 2, y);
+    if (valid)
+        valid[i] = ok ? 1 : 0;
+}
+
+template <class C>
+cudaError_t decompress(Context &ctx, const void *d_in, size_t n, uint4 *d_out, uint8_t *d_valid, uint32_t *d_bad)
+{
+    if (n == 0)
+        return cudaSuccess;
+    const int threads = 64;
+    k_decompress<C><<<(unsigned)((n + threads - 1) / threads), threads, 0, ctx.stream>>>(
+        reinterpret_cast<const uint4 *>(d_in), n, d_out, d_valid, d_bad);
     HS_LAUNCH_CHECK(ctx);
     return cudaSuccess;
 }
@@ -1108,8 +1175,8 @@ cudaError_t join(Context &ctx, const uint32_t *d_a, const uint32_t *d_b, uint32_
 template <class C>
 CurveOps make_ops()
 {
-    return CurveOps{&msm_tail<C>,     &to_affine<C>, &to_affine_scratch, &format_out<C>, &map_to_curve<C>,
-                    &to_jac24<C>,     &field_op<C>,  &fixed_table<C>,    &join<C>};
+    return CurveOps{&msm_tail<C>, &to_affine<C>, &to_affine_scratch, &format_out<C>, &map_to_curve<C>,
+                    &to_jac24<C>, &field_op<C>,  &fixed_table<C>,    &join<C>,       &decompress<C>};
 }
 
 }  // namespace hs

@@ -748,6 +748,19 @@ static void identity_out(int curve, int out_fmt, void *out)
 
 static bool valid_curve(int c) { return c == HS_HELIOS || c == HS_SELENE; }
 static bool valid_in_fmt(int f) { return f == HS_FMT_JACOBIAN51 || f == HS_FMT_AFFINE51 || f == HS_FMT_AFFINE; }
+// point inputs of the MSM forms: also the 32-byte encoding, decoded on the device
+static bool valid_pt_fmt(int f) { return valid_in_fmt(f) || f == HS_FMT_COMPRESSED; }
+
+// after a stream synchronise: the invalid-encoding count that to_affine left in
+// the first word of its scratch
+static int check_decoded(Context &ctx, const void *d_scratch)
+{
+    uint32_t bad = 0;
+    HS_CU(cudaMemcpy(&bad, d_scratch, sizeof(bad), cudaMemcpyDeviceToHost), "decode check");
+    if (bad)
+        return fail_msg(ctx, HS_EINVAL, "invalid point encoding");
+    return HS_OK;
+}
 static bool valid_out_fmt(int f) { return f >= HS_FMT_JACOBIAN51 && f <= HS_FMT_COMPRESSED; }
 
 // Reserve the arena for one batch plus extra_bytes of call-specific staging
@@ -1226,13 +1239,15 @@ static int msm_host(Context &ctx, int curve, const uint8_t *lead_scalar, const v
         return rc;
     HS_CU(cudaMemcpyAsync(out, d_out, fmt_bytes(out_fmt), cudaMemcpyDeviceToHost, st), "D2H result");
     HS_CU(cudaStreamSynchronize(st), "MSM");
+    if (point_fmt == HS_FMT_COMPRESSED)
+        return check_decoded(ctx, d_scratch);
     return HS_OK;
 }
 
 int hs_msm(hs_context *h, int curve, const uint8_t *scalars, const void *points, int point_fmt, size_t n, void *out,
            int out_fmt)
 {
-    if (!h || !valid_curve(curve) || !valid_in_fmt(point_fmt) || !valid_out_fmt(out_fmt) || !out ||
+    if (!h || !valid_curve(curve) || !valid_pt_fmt(point_fmt) || !valid_out_fmt(out_fmt) || !out ||
         (n && (!scalars || !points)))
         return HS_EINVAL;
     Context &ctx = h->c;
@@ -1243,7 +1258,7 @@ int hs_msm(hs_context *h, int curve, const uint8_t *scalars, const void *points,
 int hs_pedersen(hs_context *h, int curve, const uint8_t blinding[32], const void *H, const uint8_t *values,
                 const void *generators, int point_fmt, size_t n, void *out, int out_fmt)
 {
-    if (!h || !valid_curve(curve) || !valid_in_fmt(point_fmt) || !valid_out_fmt(out_fmt) || !out || !blinding ||
+    if (!h || !valid_curve(curve) || !valid_pt_fmt(point_fmt) || !valid_out_fmt(out_fmt) || !out || !blinding ||
         !H || (n && (!values || !generators)))
         return HS_EINVAL;
     Context &ctx = h->c;
@@ -1306,6 +1321,69 @@ int hs_compress(hs_context *h, int curve, const void *in, int in_fmt, size_t n, 
     HS_CU(ops.format_out(ctx, d_j, n, HS_FMT_COMPRESSED, d_o), "compress");
     HS_CU(cudaMemcpyAsync(out, d_o, n * 32, cudaMemcpyDeviceToHost, st), "D2H");
     HS_CU(cudaStreamSynchronize(st), "compress");
+    return HS_OK;
+}
+
+int hs_decompress(hs_context *h, int curve, const uint8_t *in, size_t n, void *out, int out_fmt, uint8_t *valid)
+{
+    if (!h || !valid_curve(curve) || (n && (!in || !out)) ||
+        (out_fmt != HS_FMT_AFFINE && out_fmt != HS_FMT_AFFINE51 && out_fmt != HS_FMT_JACOBIAN51))
+        return HS_EINVAL;
+    if (n == 0)
+        return HS_OK;
+    Context &ctx = h->c;
+    std::lock_guard<std::mutex> lk(ctx.mu);
+    DeviceGuard g(ctx.device);
+    const CurveOps &ops = curve_ops(curve);
+    const size_t ob = fmt_bytes(out_fmt);
+    HS_CU(ctx.arena.reserve(align256(n * 32) + align256(n * 64) + align256(n * 96) + align256(n * ob) + align256(n) +
+                            2048),
+          "workspace allocation");
+    uint8_t *d_in = (uint8_t *)ctx.arena.take(n * 32);
+    uint4 *d_aff = (uint4 *)ctx.arena.take(n * 64);
+    uint32_t *d_j = (uint32_t *)ctx.arena.take(n * 96);
+    uint8_t *d_o = (uint8_t *)ctx.arena.take(n * ob);
+    uint8_t *d_valid = (uint8_t *)ctx.arena.take(n);
+    uint32_t *d_bad = (uint32_t *)ctx.arena.take(256);
+    if (!d_in || !d_aff || !d_j || !d_o || !d_valid || !d_bad)
+        return fail_msg(ctx, HS_ENOMEM, "workspace carve");
+    cudaStream_t st = ctx.stream;
+    HS_CU(cudaMemcpyAsync(d_in, in, n * 32, cudaMemcpyHostToDevice, st), "H2D");
+    HS_CU(cudaMemsetAsync(d_bad, 0, sizeof(uint32_t), st), "memset");
+    HS_CU(ops.decompress(ctx, d_in, n, d_aff, d_valid, d_bad), "decompress");
+    const void *src = d_aff;
+    if (out_fmt != HS_FMT_AFFINE) {
+        // canonical Jacobian with Z = 1 (identity for invalid entries), then the radix-2^51 record
+        HS_CU(ops.to_jac24(ctx, d_aff, HS_FMT_AFFINE, n, d_j), "decompress");
+        HS_CU(ops.format_out(ctx, d_j, n, out_fmt, d_o), "decompress");
+        src = d_o;
+    }
+    HS_CU(cudaMemcpyAsync(out, src, n * ob, cudaMemcpyDeviceToHost, st), "D2H");
+    if (valid)
+        HS_CU(cudaMemcpyAsync(valid, d_valid, n, cudaMemcpyDeviceToHost, st), "D2H");
+    uint32_t bad = 0;
+    HS_CU(cudaMemcpyAsync(&bad, d_bad, sizeof(bad), cudaMemcpyDeviceToHost, st), "D2H");
+    HS_CU(cudaStreamSynchronize(st), "decompress");
+    if (bad)
+        return fail_msg(ctx, HS_EINVAL, "invalid point encoding");
+    return HS_OK;
+}
+
+int hs_decompress_device(hs_context *h, int curve, const void *d_in, size_t n, void *d_out, uint8_t *d_valid)
+{
+    if (!h || !valid_curve(curve) || (n && (!d_in || !d_out || !d_valid)))
+        return HS_EINVAL;
+    if (n == 0)
+        return HS_OK;
+    Context &ctx = h->c;
+    std::lock_guard<std::mutex> lk(ctx.mu);
+    DeviceGuard g(ctx.device);
+    HS_CU(ctx.arena.reserve(1024), "workspace allocation");
+    uint32_t *d_bad = (uint32_t *)ctx.arena.take(256);
+    if (!d_bad)
+        return fail_msg(ctx, HS_ENOMEM, "workspace carve");
+    HS_CU(cudaMemsetAsync(d_bad, 0, sizeof(uint32_t), ctx.stream), "memset");
+    HS_CU(curve_ops(curve).decompress(ctx, d_in, n, static_cast<uint4 *>(d_out), d_valid, d_bad), "decompress");
     return HS_OK;
 }
 
@@ -1410,7 +1488,7 @@ int hs_msm_batch_device(hs_context *h, int curve, const size_t *sizes, size_t co
 // the Selene group runs on a second stream concurrently with the Helios group.
 int hs_msm_batch(hs_context *h, const hs_msm_desc *descs, size_t count, int point_fmt, int out_fmt)
 {
-    if (!h || (count && !descs) || !valid_in_fmt(point_fmt) || !valid_out_fmt(out_fmt))
+    if (!h || (count && !descs) || !valid_pt_fmt(point_fmt) || !valid_out_fmt(out_fmt))
         return HS_EINVAL;
     for (size_t i = 0; i < count; i++)
         if (!valid_curve(descs[i].curve) || !descs[i].out || (descs[i].n && (!descs[i].scalars || !descs[i].points)))
@@ -1468,6 +1546,7 @@ int hs_msm_batch(hs_context *h, const hs_msm_desc *descs, size_t count, int poin
         }
     } evg{ev_in, ev_done};
     uint8_t *d_out[2] = {nullptr, nullptr};
+    uint8_t *d_scr_k[2] = {nullptr, nullptr};
     // stage inputs (all copies on the first stream)
     for (int k = 0; k < 2; k++) {
         if (idx[k].empty())
@@ -1478,6 +1557,7 @@ int hs_msm_batch(hs_context *h, const hs_msm_desc *descs, size_t count, int poin
         uint8_t *d_raw = point_fmt == HS_FMT_AFFINE ? d_pts : d_pts + align256(t * 64);
         uint8_t *d_scr = point_fmt == HS_FMT_AFFINE ? d_pts + align256(t * 64) : d_raw + align256(t * pb);
         d_out[k] = d_scr + align256(curve_ops(k).to_affine_scratch(t));
+        d_scr_k[k] = d_scr;
         size_t off = 0;
         for (size_t j = 0; j < idx[k].size(); j++) {
             const hs_msm_desc &d = descs[idx[k][j]];
@@ -1515,6 +1595,10 @@ int hs_msm_batch(hs_context *h, const hs_msm_desc *descs, size_t count, int poin
         HS_CU(cudaMemcpyAsync(host_out[k].data(), d_out[k], host_out[k].size(), cudaMemcpyDeviceToHost, s1), "D2H");
     }
     HS_CU(cudaStreamSynchronize(s1), "MSM batch");
+    if (point_fmt == HS_FMT_COMPRESSED)
+        for (int k = 0; k < 2; k++)
+            if (!idx[k].empty() && totals[k] && (rc = check_decoded(ctx, d_scr_k[k])) != HS_OK)
+                return rc;
     for (int k = 0; k < 2; k++)
         for (size_t j = 0; j < idx[k].size(); j++)
             std::memcpy(descs[idx[k][j]].out, host_out[k].data() + j * ob, ob);
@@ -1614,7 +1698,7 @@ static int fixed_window(size_t n)
 int hs_fixed_base_create(hs_context *h, int curve, const void *generators, int point_fmt, size_t n, const void *H,
                          int window, hs_fixed_base **out)
 {
-    if (!h || !out || !valid_curve(curve) || !valid_in_fmt(point_fmt) || (n && !generators) ||
+    if (!h || !out || !valid_curve(curve) || !valid_pt_fmt(point_fmt) || (n && !generators) ||
         (window != 0 && (window < 4 || window > 20)))
         return HS_EINVAL;
     *out = nullptr;
@@ -1675,6 +1759,16 @@ int hs_fixed_base_create(hs_context *h, int curve, const void *generators, int p
         return bail(e, "window table");
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess)
         return bail(e, "window table");
+    if (point_fmt == HS_FMT_COMPRESSED && n_gen) {
+        uint32_t bad = 0;
+        if ((e = cudaMemcpy(&bad, d_scr, sizeof(bad), cudaMemcpyDeviceToHost)) != cudaSuccess)
+            return bail(e, "decode check");
+        if (bad) {
+            cudaFree(fb->d_table);
+            delete fb;
+            return fail_msg(ctx, HS_EINVAL, "invalid point encoding");
+        }
+    }
     *out = fb;
     return HS_OK;
 }

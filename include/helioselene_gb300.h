@@ -131,6 +131,20 @@ int hs_batch_to_affine(hs_context *ctx, int curve, const void *in, size_t n, voi
  * in: n points in in_fmt (JACOBIAN51, AFFINE51 or AFFINE); out: n*32 bytes. */
 int hs_compress(hs_context *ctx, int curve, const void *in, int in_fmt, size_t n, uint8_t *out);
 
+/* ---- decoding of n 32-byte encodings (helios/src/x64/helios_frombytes.cpp:59-109,
+ * selene twin; HeliosPoint::from_bytes, src/api_point.cpp:58-64) ----
+ * out: n points in HS_FMT_AFFINE, HS_FMT_AFFINE51 or HS_FMT_JACOBIAN51; valid:
+ * n bytes (1 = decoded) or NULL.  An encoding the reference rejects (x not
+ * canonical, no square root; this includes the identity's 32 zero bytes) is
+ * written as the identity with valid[i] = 0, and the call returns HS_EINVAL.
+ * The MSM forms (hs_msm, hs_pedersen, hs_msm_batch, hs_fixed_base_create) also
+ * take point_fmt = HS_FMT_COMPRESSED, decode on the device and return HS_EINVAL
+ * when any input point is invalid. */
+int hs_decompress(hs_context *ctx, int curve, const uint8_t *in, size_t n, void *out, int out_fmt, uint8_t *valid);
+/* device form: d_in n*32 bytes -> d_out n*64 bytes (HS_FMT_AFFINE), d_valid n
+ * bytes; on the context stream, does not synchronise */
+int hs_decompress_device(hs_context *ctx, int curve, const void *d_in, size_t n, void *d_out, uint8_t *d_valid);
+
 /* ---- simplified SWU map of n field elements (helios/src/x64/helios_map_to_curve.cpp:98-198,
  * selene twin); u: n*32 bytes (bit 255 ignored); out: n points in out_fmt ----
  * Used to derive bases / generators (HeliosPoint::map_to_curve, api_point.cpp:146-151). */
