@@ -429,6 +429,58 @@ def run_fixed(hs, torch, device: str, local: int, count: int = 64) -> dict:
     return out
 
 
+IMAD_PER_MODSQR = {0: 88, 1: 176}  # F_p, F_q squaring: 36 products + the same reduction
+# per decoded point: x^3 - 3x + b, one 4-bit-window exponentiation (256 S + 78 M), the root check
+DECODE_SQR, DECODE_MUL = 258, 80
+
+
+def run_decompress(hs, torch, ctxs, data, n: int, flush, imad_peak: float) -> dict:
+    """Point decoding on the device (hs_decompress_device) over the bench bases'
+    32-byte encodings, and one MSM fed with encodings through hs_msm
+    (HS_FMT_COMPRESSED, host buffers, decoding inside the timed call)."""
+    out = {}
+    for curve, name in ((hs.HELIOS, "helios"), (hs.SELENE, "selene")):
+        c = ctxs[curve]
+        s = torch.cuda.ExternalStream(c.stream, device=data[curve]["d_pts"].device)
+        enc = c.compress(curve, data[curve]["d_pts"].cpu().numpy(), hs.FMT_AFFINE)
+        data[curve]["enc"] = enc
+        d_in = torch.from_numpy(enc.copy()).to(data[curve]["d_pts"].device)
+        d_out = torch.empty(n * 64, dtype=torch.uint8, device=d_in.device)
+        d_valid = torch.empty(n, dtype=torch.uint8, device=d_in.device)
+        torch.cuda.synchronize()
+        ts = []
+        for i in range(4):
+            with torch.cuda.stream(s):
+                flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(s)
+            c.decompress_device(curve, d_in.data_ptr(), n, d_out.data_ptr(), d_valid.data_ptr())
+            b.record(s)
+            torch.cuda.synchronize()
+            if i:
+                ts.append(a.elapsed_time(b))
+        ok = bool(torch.equal(d_out, data[curve]["d_pts"]))
+        ms = min(ts)
+        work = n * (DECODE_SQR * IMAD_PER_MODSQR[curve] + DECODE_MUL * IMAD_PER_MODMUL[curve])
+        h_sc = data[curve]["h_sc"].numpy()
+        h_enc = torch.empty(n * 32, dtype=torch.uint8, pin_memory=True)
+        h_enc.numpy()[:] = enc
+        c.msm(curve, h_sc, h_enc.numpy(), hs.FMT_COMPRESSED, hs.FMT_JACOBIAN51)
+        t0 = time.perf_counter()
+        for _ in range(3):
+            c.msm(curve, h_sc, h_enc.numpy(), hs.FMT_COMPRESSED, hs.FMT_JACOBIAN51)
+        e2e = (time.perf_counter() - t0) / 3
+        out[name] = {"points": n, "ms": ms, "points_per_s": n / (ms * 1e-3), "round_trip_exact": ok,
+                     "roofline": {"bound": "imad", "achieved": work / (ms * 1e-3) / 1e12, "peak": imad_peak / 1e12,
+                                  "unit": "T IMAD/s", "frac": work / (ms * 1e-3) / imad_peak if imad_peak else None,
+                                  "work": f"{DECODE_SQR} squarings + {DECODE_MUL} products per point, "
+                                          "IMAD-eq as for the MSM"},
+                     "msm_from_encodings_e2e": {"ms": e2e * 1e3, "points_per_s": n / e2e,
+                                                "api": "hs_msm(point_fmt=HS_FMT_COMPRESSED), pinned host buffers, "
+                                                       "32 B scalar + 32 B encoding per point"}}
+    return out
+
+
 def cpu_baseline_leg(data, n: int, gpu_results: dict) -> dict:
     """The oracle port on all host cores, on the same workload; also checks the GPU results."""
     sys.path.insert(0, str(ROOT / "oracle"))
@@ -441,7 +493,17 @@ def cpu_baseline_leg(data, n: int, gpu_results: dict) -> dict:
         r = oracle.msm_mt(curve, d["w"].scalars, pts, threads)
         match = match and (r == gpu_results.get(curve))
     dt = time.perf_counter() - t0
+    dec = {}
+    for curve, d in data.items():
+        if "enc" not in d:
+            continue
+        k = min(n, 1 << 14)
+        t1 = time.perf_counter()
+        pts, bad = oracle.decompress(curve, d["enc"][:32 * k])
+        dec[curve] = {"points_per_s": k / (time.perf_counter() - t1), "cores": 1, "sample": f"{k} encodings",
+                      "matches_gpu_bases": bool(bad == 0 and pts.tobytes() == d["d_pts"][:64 * k].cpu().numpy().tobytes())}
     return {"value": 2 * n / dt, "unit": "points/s", "cores": threads, "kind": "port",
+            "decompress": dec,
             "sample": f"the full timed workload (Helios + Selene MSM, n=2^{n.bit_length() - 1} each), split into "
                       f"{threads} per-thread sub-MSMs summed with the group law, one pass",
             "seconds": dt, "bit_exact_vs_gpu": bool(match)}
@@ -590,6 +652,9 @@ def run_ours(args) -> None:
     fixed = None
     if not args.no_fixed:
         fixed = run_fixed(hs, torch, device, local)
+    decode = None
+    if not args.no_decompress:
+        decode = run_decompress(hs, torch, ctxs, data, n, flush, imad_peak)
     m_n, c_star = modmul_count(n)
     whole = m_n * (IMAD_PER_MODMUL[0] + IMAD_PER_MODMUL[1]) / (ms_per_step * 1e-3)
 
@@ -616,7 +681,8 @@ def run_ours(args) -> None:
                          "kernel": "k_accumulate",
                          "work": "point-window entries x 6 modmul (batch-affine bucket add) x IMAD-eq per modmul "
                                  "(F_p 144, F_q 232), summed over one Helios and one Selene launch",
-                         "peak_source": "measured in this run by hs_measure_imad_peak (mad.lo/mad.hi chains)",
+                         "peak_source": "measured in this run by hs_measure_imad_peak (the faster of mad.lo/mad.hi "
+                                        "and mad.wide.u32 chains on every SM)",
                          "accumulate_ms_per_launch": acc_ms,
                          "whole_msm_frac": whole / imad_peak if imad_peak else None},
         }
@@ -626,6 +692,8 @@ def run_ours(args) -> None:
             line["serving"] = serving
         if not args.no_fixed:
             line["fixed_base"] = fixed
+        if not args.no_decompress:
+            line["decompress"] = decode
         if ws == 1 and not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline_leg(data, n, results)
         print(json.dumps(line), flush=True)
@@ -683,6 +751,7 @@ def main() -> None:
     ap.add_argument("--no-batched", action="store_true", help="skip the batched (1024 uneven MSMs) section")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving (Poisson arrivals) section")
     ap.add_argument("--no-fixed", action="store_true", help="skip the fixed-base commitment section")
+    ap.add_argument("--no-decompress", action="store_true", help="skip the point-decoding section")
     ap.add_argument("--split", type=int, default=None,
                     help="window-split threshold in points for single MSMs (0: off; default: the library's)")
     args = ap.parse_args()

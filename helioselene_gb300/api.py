@@ -90,6 +90,10 @@ class Context:
     def set_graphs(self, on: bool) -> None:
         self._check(self._lib.hs_context_set_graphs(self._h, int(on)), "set_graphs")
 
+    def set_priority(self, high: bool) -> None:
+        """new context stream of the greatest (or default) priority; stream handle changes"""
+        self._check(self._lib.hs_context_set_priority(self._h, int(bool(high))), "set_priority")
+
     def set_split(self, min_points: int) -> None:
         """single MSMs of >= min_points run as two window halves on two streams (0: off)"""
         self._check(self._lib.hs_context_set_split(self._h, int(min_points)), "set_split")

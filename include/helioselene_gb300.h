@@ -96,6 +96,12 @@ int hs_context_set_graphs(hs_context *ctx, int on);
  * the accumulation of the lower half (default 2^18; 0 turns the split off, for
  * callers that already overlap several MSMs on the device) */
 int hs_context_set_split(hs_context *ctx, size_t min_points);
+/* replace the context stream by one of the greatest (high != 0) or the default
+ * (high == 0) priority: when several contexts share a device, the blocks of a
+ * high-priority context are scheduled first, so its MSMs finish first and the
+ * others fill the SMs its latency-bound tail leaves idle.  The stream handle
+ * (hs_context_stream) changes. */
+int hs_context_set_priority(hs_context *ctx, int high);
 
 /* ---- MSM: sum of scalars[i] * points[i] ----
  * Replaces helios_msm_vartime / selene_msm_vartime
@@ -282,9 +288,10 @@ void hs_selene_batch_to_affine(hs_affine51 *out, const hs_jacobian51 *points, si
 int hs_profile_enable(hs_context *ctx, int on);
 int hs_profile_read(hs_context *ctx, double *accumulate_ms, uint64_t *accumulate_launches, uint64_t *entries,
                     int reset);
-/* Integer multiply-add throughput of this device: a kernel of independent
- * mad.lo/mad.hi chains on every SM, timed with CUDA events.  Returns
- * multiply-add instructions per second (one 32x32 half-product each). */
+/* Integer multiply throughput of this device: kernels of independent
+ * mad.lo/mad.hi chains and of independent mad.wide.u32 chains on every SM,
+ * timed with CUDA events.  Returns the faster, in IMAD-equivalents per second
+ * (a 32x32->64 product counts as 2, in either form). */
 int hs_measure_imad_peak(hs_context *ctx, double *imad_per_s);
 
 /* Field arithmetic on the device, for validation of the field layer:
