@@ -45,6 +45,7 @@ IMAD_PER_MODMUL = {0: 144, 1: 232}  # F_p, F_q: 2 IMAD per 32x32->64 product
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_accumulate launch at
 # n = 2^20, mean of the Helios and Selene launches of one ncu capture
 ACC_TRAFFIC_BYTES = (477.2e6 + 497.5e6) / 2
+SPLIT_DEFAULT = 1 << 18  # the library's window-split threshold for single MSMs
 
 
 def modmul_count(n: int) -> tuple:
@@ -523,9 +524,14 @@ def run_ours(args) -> None:
     device = f"cuda:{local}"
     ctx = hs.Context(local)
     ctx2 = hs.Context(local)  # the Selene MSM of a step runs on its own stream, overlapping the Helios one
-    if args.split is not None:
-        ctx.set_split(args.split)
-        ctx2.set_split(args.split)
+    # the two curves already overlap on two streams, so the window split is off for
+    # the throughput step; the Selene context (the longer MSM) gets the
+    # high-priority stream so its blocks are scheduled first and the Helios MSM
+    # fills the SMs its tail leaves idle
+    head_split = 0 if args.split is None else args.split
+    ctx.set_split(head_split)
+    ctx2.set_split(head_split)
+    ctx2.set_priority(True)
     ctxs = {hs.HELIOS: ctx, hs.SELENE: ctx2}
     n = args.n
     data = make_inputs(hs, ctx, torch, n, device)
@@ -535,49 +541,56 @@ def run_ours(args) -> None:
     d_out = torch.empty(2 * 128, dtype=torch.uint8, device=device)
     torch.cuda.synchronize()
 
-    def step(ev_pair=None):
-        # steps do not overlap: L2 flush, then a synchronize, then the timed events
-        start = torch.cuda.Event(enable_timing=True)
-        with torch.cuda.stream(stream):
-            flush.zero_()
-        torch.cuda.synchronize()
-        start.record(stream)
-        streams[hs.SELENE].wait_event(start)
-        ends = []
+    def launch_pair():
         for curve in (hs.HELIOS, hs.SELENE):
             ctxs[curve].msm_device(curve, data[curve]["d_sc"].data_ptr(), data[curve]["d_pts"].data_ptr(), n,
                                    d_out.data_ptr() + 128 * curve, hs.FMT_JACOBIAN51)
-            e = torch.cuda.Event(enable_timing=True)
-            e.record(streams[curve])
-            ends.append(e)
-        return start, ends
 
-    for _ in range(args.warmup):
-        step()
+    def run_steps(k):
+        """k steps issued back to back on the two context streams; events bracket all of them"""
+        start, end, end_s = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        start.record(stream)
+        streams[hs.SELENE].wait_event(start)
+        for _ in range(k):
+            launch_pair()
+        end_s.record(streams[hs.SELENE])
+        stream.wait_event(end_s)
+        end.record(stream)
+        return start, end
+
+    def isolated_step():
+        """one step alone: L2 flushed and the device synchronised before its events"""
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        torch.cuda.synchronize()
+        start, end = run_steps(1)
+        torch.cuda.synchronize()
+        return start.elapsed_time(end)
+
+    run_steps(args.warmup)
     torch.cuda.synchronize()
     # results as the reference returns them (Jacobian records), serialized for the bit-exact check
     out_host = d_out.cpu().numpy()
     results = {c: ctx.compress(c, out_host[128 * c:128 * c + 120], hs.FMT_JACOBIAN51).tobytes()
                for c in (hs.HELIOS, hs.SELENE)}
 
-    # ---- timed region: device-resident inputs, both curves per step ----
+    # ---- timed region: device-resident inputs, K steps of both curves ----
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
     launches0 = ctx.launches + ctx2.launches
-    marks = []
     with ClockSampler(local) as clocks:
-        for i in range(args.steps):
-            marks.append(step())
+        t_start, t_end = run_steps(args.steps)
         torch.cuda.synchronize()
     launches = ctx.launches + ctx2.launches - launches0
-    ms = sum(max(s.elapsed_time(e) for e in ends) for s, ends in marks)
+    ms = t_start.elapsed_time(t_end)
     if dist:
         t = torch.tensor([ms], dtype=torch.float64, device=device)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     ms_per_step = ms / args.steps
     value = ws * 2 * n / (ms_per_step * 1e-3)
+    isolated_ms = sorted(isolated_step() for _ in range(5))[2]
 
     # per-curve latency, one MSM at a time; then the roofline pass: the unsplit
     # batch path of the same MSM with its accumulation launch timed by events on
@@ -603,7 +616,9 @@ def run_ours(args) -> None:
                 ts.append(a.elapsed_time(b))
             return min(ts)
 
+        c.set_split(SPLIT_DEFAULT if args.split is None else args.split)  # a lone MSM: the library default
         t_split = timed(lambda: c.msm_device(curve, *args_dev, n, d_out.data_ptr(), hs.FMT_JACOBIAN51))
+        c.set_split(head_split)
         c.profile(True)
         c.profile_read(reset=True)
         t_plain = timed(lambda: c.msm_batch_device(curve, [n], *args_dev, d_out.data_ptr(), hs.FMT_JACOBIAN51))
@@ -664,8 +679,12 @@ def run_ours(args) -> None:
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "n": n, "curves": ["helios", "selene"], "parallelism": f"replicas{ws}",
-                       "window_split_min_points": args.split if args.split is not None else "library default (2^18)",
-                       "l2": "flushed before every step (256 MiB memset, outside the timed events)",
+                       "window_split_min_points": head_split,
+                       "streams": "Helios and Selene MSMs on two context streams, Selene's of high priority",
+                       "l2": "inputs of one step (2 x 96 MiB scalars + bases, plus the bucket workspaces) exceed "
+                             "L2 (129 MB); steps are issued back to back and the events bracket all K of them",
+                       "isolated_ms_per_step": isolated_ms,
+                       "isolated_note": "median of 5 single steps, each after a 256 MiB L2 flush and a synchronise",
                        "inputs": "device-resident scalars + canonical affine bases"},
             "per_curve": per_curve,
             "clocks": clocks.summary(),

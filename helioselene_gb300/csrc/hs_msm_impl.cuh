@@ -199,38 +199,75 @@ __global__ void __launch_bounds__(128, 4) k_reduce_groups(const uint32_t *__rest
 // and the window sum is S = sum_b C_b + m0 RED_CHUNK sum_b b R_b.  Each step
 // is a short running sum, a log-depth scan or tree, and log2 of a power of two
 // doublings: no scalar multiples by group index.
+// Shared-memory points are stored word-group-major (uint4 c of thread i at
+// c * N + i), so a warp's 16-byte accesses to one uint4 of consecutive threads
+// fall in distinct banks.
+__device__ __forceinline__ void st_fe_soa(uint4 *sh, uint32_t c, uint32_t i, uint32_t N, const Fe &f)
+{
+    sh[(2 * c) * N + i] = make_uint4(f.w[0], f.w[1], f.w[2], f.w[3]);
+    sh[(2 * c + 1) * N + i] = make_uint4(f.w[4], f.w[5], f.w[6], f.w[7]);
+}
+
+__device__ __forceinline__ Fe ld_fe_soa(const uint4 *sh, uint32_t c, uint32_t i, uint32_t N)
+{
+    const uint4 a = sh[(2 * c) * N + i], b = sh[(2 * c + 1) * N + i];
+    Fe f;
+    f.w[0] = a.x; f.w[1] = a.y; f.w[2] = a.z; f.w[3] = a.w;
+    f.w[4] = b.x; f.w[5] = b.y; f.w[6] = b.z; f.w[7] = b.w;
+    return f;
+}
+
+__device__ __forceinline__ void st_soa(uint4 *sh, uint32_t i, uint32_t N, const Xyzz &p)
+{
+    st_fe_soa(sh, 0, i, N, p.X);
+    st_fe_soa(sh, 1, i, N, p.Y);
+    st_fe_soa(sh, 2, i, N, p.ZZ);
+    st_fe_soa(sh, 3, i, N, p.ZZZ);
+}
+
+__device__ __forceinline__ Xyzz ld_soa(const uint4 *sh, uint32_t i, uint32_t N)
+{
+    Xyzz p;
+    p.X = ld_fe_soa(sh, 0, i, N);
+    p.Y = ld_fe_soa(sh, 1, i, N);
+    p.ZZ = ld_fe_soa(sh, 2, i, N);
+    p.ZZZ = ld_fe_soa(sh, 3, i, N);
+    return p;
+}
+
+// inclusive suffix scan of r over the first nt threads (sh holds N points)
 template <class C>
-__device__ __forceinline__ Xyzz block_suffix_scan(uint4 *sh, Xyzz r, uint32_t i, uint32_t nt)
+__device__ __forceinline__ Xyzz block_suffix_scan(uint4 *sh, uint32_t N, Xyzz r, uint32_t i, uint32_t nt)
 {
     using G = Group<C>;
-    store_xyzz(sh + 8 * i, r);
+    st_soa(sh, i, N, r);
     __syncthreads();
     for (uint32_t dl = 1; dl < nt; dl <<= 1) {
         Xyzz o = G::inf();
         const bool take = i + dl < nt;
         if (take)
-            o = load_xyzz(sh + 8 * (i + dl));
+            o = ld_soa(sh, i + dl, N);
         __syncthreads();
         if (take) {
             r = G::add(r, o);
-            store_xyzz(sh + 8 * i, r);
+            st_soa(sh, i, N, r);
         }
         __syncthreads();
     }
     return r;
 }
 
-// sum of v over the first nt (a power of two) threads, result in sh[0]
+// sum of v over the first nt (a power of two) threads, result at index 0
 template <class C>
-__device__ __forceinline__ void block_tree_sum(uint4 *sh, const Xyzz &v, uint32_t i, uint32_t nt)
+__device__ __forceinline__ void block_tree_sum(uint4 *sh, uint32_t N, const Xyzz &v, uint32_t i, uint32_t nt)
 {
     using G = Group<C>;
     __syncthreads();
-    store_xyzz(sh + 8 * i, v);
+    st_soa(sh, i, N, v);
     __syncthreads();
     for (uint32_t stride = nt / 2; stride > 0; stride >>= 1) {
         if (i < stride)
-            store_xyzz(sh + 8 * i, G::add(load_xyzz(sh + 8 * i), load_xyzz(sh + 8 * (i + stride))));
+            st_soa(sh, i, N, G::add(ld_soa(sh, i, N), ld_soa(sh, i + stride, N)));
         __syncthreads();
     }
 }
@@ -273,7 +310,7 @@ __global__ void __launch_bounds__(RED_CHUNK_THREADS) k_window_chunks(const uint4
                 w = G::add(w, r);
         }
     }
-    r = block_suffix_scan<C>(sh, r, i, P);
+    r = block_suffix_scan<C>(sh, RED_CHUNK_THREADS, r, i, P);
     Xyzz v = (i >= 1 && i < P) ? r : G::inf();
     for (uint32_t m = q; m > 1; m >>= 1)
         v = G::dbl(v);
@@ -281,12 +318,12 @@ __global__ void __launch_bounds__(RED_CHUNK_THREADS) k_window_chunks(const uint4
     for (uint32_t m = d.m0; m > 1; m >>= 1)
         v = G::dbl(v);
     v = G::add(v, a);
-    block_tree_sum<C>(sh, v, i, P);
+    block_tree_sum<C>(sh, RED_CHUNK_THREADS, v, i, P);
     if (i == 0) {
         if (DIRECT) {
-            store_xyzz(outC + 8 * (size_t)ch, load_xyzz(sh));
+            store_xyzz(outC + 8 * (size_t)ch, ld_soa(sh, 0, RED_CHUNK_THREADS));
         } else {
-            store_xyzz(outC + 16 * (size_t)ch, load_xyzz(sh));
+            store_xyzz(outC + 16 * (size_t)ch, ld_soa(sh, 0, RED_CHUNK_THREADS));
             store_xyzz(outC + 16 * (size_t)ch + 8, r);  // thread 0's suffix sum is the chunk's run total
         }
     }
@@ -309,14 +346,14 @@ __global__ void __launch_bounds__(RED_CHUNK) k_window_sum(const uint4 *__restric
         cb = load_xyzz(inC + 16 * c);
         r = load_xyzz(inC + 16 * c + 8);
     }
-    r = block_suffix_scan<C>(sh, r, i, nbk);
+    r = block_suffix_scan<C>(sh, RED_CHUNK, r, i, nbk);
     Xyzz v = (i >= 1 && i < nbk) ? r : G::inf();
     for (uint32_t m = d.m0 * RED_CHUNK; m > 1 && nbk > 1; m >>= 1)
         v = G::dbl(v);
     v = G::add(v, cb);
-    block_tree_sum<C>(sh, v, i, nbk);
+    block_tree_sum<C>(sh, RED_CHUNK, v, i, nbk);
     if (i == 0)
-        store_xyzz(S + 8 * (size_t)s, load_xyzz(sh));
+        store_xyzz(S + 8 * (size_t)s, ld_soa(sh, 0, RED_CHUNK));
 }
 
 // ---------------------------------------------------------------------------
