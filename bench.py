@@ -597,7 +597,7 @@ def run_ours(args) -> None:
     # the context stream (a split MSM runs two accumulations concurrently, which
     # per-launch events cannot separate)
     per_curve = {}
-    prof_total = {"ms": 0.0, "work": 0.0, "launches": 0}
+    prof_total = {"ms": 0.0, "work": 0.0, "executed": 0.0, "launches": 0}
     for curve, name in ((hs.HELIOS, "helios"), (hs.SELENE, "selene")):
         c = ctxs[curve]
         s = streams[curve]
@@ -629,6 +629,7 @@ def run_ours(args) -> None:
         prof_total["ms"] += pr["accumulate_ms"]
         prof_total["launches"] += pr["accumulate_launches"]
         prof_total["work"] += pr["entries"] * 6 * IMAD_PER_MODMUL[curve]
+        prof_total["executed"] += pr["entries"] * (8 * IMAD_PER_MODMUL[curve] + 2 * IMAD_PER_MODSQR[curve])
 
     # ---- e2e: reference-facing call with host buffers ----
     e2e_steps = max(3, min(args.steps, 10))
@@ -703,6 +704,10 @@ def run_ours(args) -> None:
                          "peak_source": "measured in this run by hs_measure_imad_peak (the faster of mad.lo/mad.hi "
                                         "and mad.wide.u32 chains on every SM)",
                          "accumulate_ms_per_launch": acc_ms,
+                         "executed_frac": (prof_total["executed"] / (prof_total["ms"] * 1e-3) / imad_peak
+                                           if imad_peak and prof_total["ms"] > 0 else None),
+                         "executed_note": "the same launches counted with the products the kernel executes: "
+                                          "XYZZ mixed addition, 8 products + 2 squares per entry",
                          "whole_msm_frac": whole / imad_peak if imad_peak else None},
         }
         if not args.no_batched:

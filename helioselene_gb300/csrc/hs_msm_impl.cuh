@@ -569,13 +569,15 @@ template <class C>
 cudaError_t msm_tail(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
 {
     cudaStream_t st = ctx.stream;
-    // 2. accumulate: one thread per segment, the grid sized by the host bound on
-    //    the segment count (threads past the device-side count exit at once).
-    //    Blocks are short, so kernels of other streams (the tail of the other
-    //    window half or of another MSM) get SM slots while this one runs.
+    // 2. accumulate: a grid of short blocks (up to 32 per SM, several waves), each
+    //    thread taking segments at a stride of the grid.  Segments come longest
+    //    first, so every block gets a like mix of long and short ones; blocks end
+    //    wave by wave, so kernels of other streams (another MSM's tail) get SM
+    //    slots while this one runs.  Threads past the device-side count exit.
     {
         const int threads = 128;
-        const int blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>((p.max_segs + threads - 1) / threads, 1u << 30));
+        const uint64_t want = (p.max_segs + threads - 1) / threads;
+        const int blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)ctx.sm_count * 32));
         cudaEvent_t ev0 = nullptr;
         prof_begin(ctx, &ev0);
         k_accumulate<C><<<blocks, threads, 0, st>>>(b.segs, b.seg_off + p.NB, b.sorted, b.points, b.seg_sum);
