@@ -359,12 +359,14 @@ def run_serving(hs, torch, device: str, local: int, requests_per_rate: int = 100
     return out
 
 
-def run_fixed(hs, torch, device: str, local: int, count: int = 64) -> dict:
+def run_fixed(hs, torch, device: str, local: int, count: int = 4096, chunk: int = 256) -> dict:
     """Config 5: Pedersen-style commitments r*H + sum v_i G_i over n = 2^20 resident
-    generators per curve with device window tables; scalars uniform mod order
-    (< 2^255, bit 255 cleared) with 10% of the commitments sparse (one 16-bit value
-    per scalar, <= 16 set bits); all outputs normalised to affine with one shared
-    inversion per 16 commitments.  Against the plain per-call MSM of n + 1 terms."""
+    generators per curve with device window tables; 4096 commitments per curve,
+    submitted 256 at a time from two device scalar buffers used alternately;
+    scalars uniform mod order (< 2^255, bit 255 cleared) with 10% of each chunk's
+    commitments sparse (one 16-bit value per scalar, <= 16 set bits); all outputs
+    normalised to affine with one shared inversion per 16 commitments.  Against
+    the plain per-call MSM of n + 1 terms."""
     from helioselene_gb300.workload import random_field_bytes
     n = 1 << 20
     rng = np.random.default_rng(SEED + 5)
@@ -372,7 +374,20 @@ def run_fixed(hs, torch, device: str, local: int, count: int = 64) -> dict:
     gen.manual_seed(SEED + 5)
     ctx = hs.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream, device=device)
-    out = {"generators": n, "commitments": count, "sparse_fraction": 0.1}
+    nsparse = max(1, chunk // 10)
+    out = {"generators": n, "commitments": count, "chunk": chunk, "sparse_fraction": nsparse / chunk}
+
+    def make_scalars():
+        sc = torch.randint(0, 256, (chunk, n + 1, 32), dtype=torch.uint8, device=device, generator=gen)
+        sc[:, :, 31] &= 0x7F
+        sp = sc[:nsparse]
+        sp.zero_()
+        v16 = torch.randint(0, 65536, (nsparse, n + 1), device=device, generator=gen)
+        off = torch.randint(0, 30, (nsparse, n + 1), device=device, generator=gen)
+        sp.scatter_(2, off.unsqueeze(2), (v16 & 0xFF).to(torch.uint8).unsqueeze(2))
+        sp.scatter_(2, (off + 1).unsqueeze(2), (v16 >> 8).to(torch.uint8).unsqueeze(2))
+        return sc
+
     for curve, name in ((hs.HELIOS, "helios"), (hs.SELENE, "selene")):
         d_u = torch.from_numpy(random_field_bytes(rng, n + 1).reshape(-1)).to(device)
         d_pts = torch.empty((n + 1) * 64, dtype=torch.uint8, device=device)
@@ -383,39 +398,33 @@ def run_fixed(hs, torch, device: str, local: int, count: int = 64) -> dict:
         t0 = time.perf_counter()
         fb = hs.FixedBase(ctx, curve, gens[:n], H=gens[n])
         table_s = time.perf_counter() - t0
-        sc = torch.randint(0, 256, (count, n + 1, 32), dtype=torch.uint8, device=device, generator=gen)
-        sc[:, :, 31] &= 0x7F
-        nsparse = max(1, count // 10)
-        sp = sc[:nsparse]
-        sp.zero_()
-        v16 = torch.randint(0, 65536, (nsparse, n + 1), device=device, generator=gen)
-        off = torch.randint(0, 30, (nsparse, n + 1), device=device, generator=gen)
-        lo = (v16 & 0xFF).to(torch.uint8)
-        hi = (v16 >> 8).to(torch.uint8)
-        sp.scatter_(2, off.unsqueeze(2), lo.unsqueeze(2))
-        sp.scatter_(2, (off + 1).unsqueeze(2), hi.unsqueeze(2))
+        bufs = [make_scalars(), make_scalars()]
         d_out = torch.empty(count * 64, dtype=torch.uint8, device=device)
         torch.cuda.synchronize()
-        fb.commit_device(sc.data_ptr(), count, d_out.data_ptr(), hs.FMT_AFFINE)  # warm-up / graph capture
+        fb.commit_device(bufs[0].data_ptr(), chunk, d_out.data_ptr(), hs.FMT_AFFINE)  # warm-up / graph capture
+        fb.commit_device(bufs[1].data_ptr(), chunk, d_out.data_ptr(), hs.FMT_AFFINE)
         stream.synchronize()
         a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
-        fb.commit_device(sc.data_ptr(), count, d_out.data_ptr(), hs.FMT_AFFINE)
+        for j in range(count // chunk):
+            fb.commit_device(bufs[j & 1].data_ptr(), chunk, d_out.data_ptr() + 64 * chunk * j, hs.FMT_AFFINE)
         e.record(stream)
         stream.synchronize()
         fixed_ms = a.elapsed_time(e)
         # plain path: one MSM of n + 1 terms per commitment, on the same device data
         k = 3
         d_plain = torch.empty(k * 120, dtype=torch.uint8, device=device)
-        ctx.msm_device(curve, sc[nsparse].data_ptr(), d_pts.data_ptr(), n + 1, d_plain.data_ptr())
+        ctx.msm_device(curve, bufs[0][nsparse].data_ptr(), d_pts.data_ptr(), n + 1, d_plain.data_ptr())
         stream.synchronize()
         a.record(stream)
         for j in range(k):
-            ctx.msm_device(curve, sc[nsparse + j].data_ptr(), d_pts.data_ptr(), n + 1, d_plain.data_ptr() + 120 * j)
+            ctx.msm_device(curve, bufs[0][nsparse + j].data_ptr(), d_pts.data_ptr(), n + 1,
+                           d_plain.data_ptr() + 120 * j)
         e.record(stream)
         stream.synchronize()
         plain_ms = a.elapsed_time(e) / k
         aff = d_out.cpu().numpy().reshape(count, 64)
+        # the last chunk used buffer (count // chunk - 1) & 1; compare chunk 0 (buffer 0) with the plain path
         got = ctx.compress(curve, aff[nsparse:nsparse + k], hs.FMT_AFFINE)
         want = ctx.compress(curve, d_plain.cpu().numpy(), hs.FMT_JACOBIAN51)
         out[name] = {"window": fb.window, "table_bytes": fb.table_bytes, "table_build_s": table_s,
@@ -424,9 +433,49 @@ def run_fixed(hs, torch, device: str, local: int, count: int = 64) -> dict:
                      "speedup_vs_plain": plain_ms * count / fixed_ms,
                      "bit_exact_vs_plain": bool((got == want).all())}
         fb.close()
-        del sc, d_out, d_pts, d_u
+        del bufs, d_out, d_pts, d_u
         torch.cuda.empty_cache()
     ctx.close()
+    return out
+
+
+def run_sweep(hs, torch, device: str, local: int, flush) -> dict:
+    """Config 2: single MSMs at n = 2^10, 2^12, ..., 2^22 on both curves, uniform
+    scalars mod order, SWU bases, 1% edge slices (zero, order-1, repeated base,
+    top-window-only); one MSM at a time, L2 flushed before each, median of 3."""
+    from helioselene_gb300.workload import make_workload
+    ctx = hs.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=device)
+    out = {}
+    for curve, name in ((hs.HELIOS, "helios"), (hs.SELENE, "selene")):
+        rows = []
+        for lg in range(10, 23, 2):
+            n = 1 << lg
+            w = make_workload(curve, n, SEED + 2 + lg, edge_fraction=0.01)
+            d_u = torch.from_numpy(w.u.reshape(-1).copy()).to(device)
+            d_sc = torch.from_numpy(w.scalars.reshape(-1).copy()).to(device)
+            d_pts = torch.empty(n * 64, dtype=torch.uint8, device=device)
+            d_out = torch.empty(128, dtype=torch.uint8, device=device)
+            torch.cuda.synchronize()
+            ctx.map_to_curve_device(curve, d_u.data_ptr(), n, d_pts.data_ptr())
+            ctx.msm_device(curve, d_sc.data_ptr(), d_pts.data_ptr(), n, d_out.data_ptr())
+            torch.cuda.synchronize()
+            ts = []
+            for _ in range(3):
+                with torch.cuda.stream(stream):
+                    flush.zero_()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                ctx.msm_device(curve, d_sc.data_ptr(), d_pts.data_ptr(), n, d_out.data_ptr())
+                b.record(stream)
+                torch.cuda.synchronize()
+                ts.append(a.elapsed_time(b))
+            ms = sorted(ts)[1]
+            rows.append({"n": n, "ms": ms, "points_per_s": n / (ms * 1e-3)})
+            del d_u, d_sc, d_pts
+        out[name] = rows
+    ctx.close()
+    torch.cuda.empty_cache()
     return out
 
 
@@ -668,6 +717,9 @@ def run_ours(args) -> None:
     fixed = None
     if not args.no_fixed:
         fixed = run_fixed(hs, torch, device, local)
+    sweep = None
+    if not args.no_sweep:
+        sweep = run_sweep(hs, torch, device, local, flush)
     decode = None
     if not args.no_decompress:
         decode = run_decompress(hs, torch, ctxs, data, n, flush, imad_peak)
@@ -718,6 +770,8 @@ def run_ours(args) -> None:
             line["fixed_base"] = fixed
         if not args.no_decompress:
             line["decompress"] = decode
+        if not args.no_sweep:
+            line["sweep"] = sweep
         if ws == 1 and not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline_leg(data, n, results)
         print(json.dumps(line), flush=True)
@@ -776,6 +830,7 @@ def main() -> None:
     ap.add_argument("--no-serving", action="store_true", help="skip the serving (Poisson arrivals) section")
     ap.add_argument("--no-fixed", action="store_true", help="skip the fixed-base commitment section")
     ap.add_argument("--no-decompress", action="store_true", help="skip the point-decoding section")
+    ap.add_argument("--no-sweep", action="store_true", help="skip the n = 2^10 .. 2^22 single-MSM sweep")
     ap.add_argument("--split", type=int, default=None,
                     help="window-split threshold in points for single MSMs (0: off; default: the library's)")
     args = ap.parse_args()

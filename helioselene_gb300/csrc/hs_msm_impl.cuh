@@ -97,6 +97,22 @@ __global__ void __launch_bounds__(128) k_accumulate(const uint4 *__restrict__ se
     }
 }
 
+// Out-of-line point operations for the latency-bound level-2 reduction kernels
+// (k_window_chunks, k_window_sum): with about one warp per scheduler their
+// inlined copies overflow the instruction cache, while one shared body stays
+// resident (a call costs a few dozen instructions next to the ~2000 of an
+// addition).
+template <class C>
+__device__ __noinline__ Xyzz l2_add(const Xyzz a, const Xyzz b)
+{
+    return Group<C>::add(a, b);
+}
+template <class C>
+__device__ __noinline__ Xyzz l2_dbl(const Xyzz a)
+{
+    return Group<C>::dbl(a);
+}
+
 // ---------------------------------------------------------------------------
 // 3. folding buckets that were cut into several segments
 // ---------------------------------------------------------------------------
@@ -249,7 +265,7 @@ __device__ __forceinline__ Xyzz block_suffix_scan(uint4 *sh, uint32_t N, Xyzz r,
             o = ld_soa(sh, i + dl, N);
         __syncthreads();
         if (take) {
-            r = G::add(r, o);
+            r = l2_add<C>(r, o);
             st_soa(sh, i, N, r);
         }
         __syncthreads();
@@ -267,7 +283,7 @@ __device__ __forceinline__ void block_tree_sum(uint4 *sh, uint32_t N, const Xyzz
     __syncthreads();
     for (uint32_t stride = nt / 2; stride > 0; stride >>= 1) {
         if (i < stride)
-            st_soa(sh, i, N, G::add(ld_soa(sh, i, N), ld_soa(sh, i + stride, N)));
+            st_soa(sh, i, N, l2_add<C>(ld_soa(sh, i, N), ld_soa(sh, i + stride, N)));
         __syncthreads();
     }
 }
@@ -304,20 +320,20 @@ __global__ void __launch_bounds__(RED_CHUNK_THREADS) k_window_chunks(const uint4
     if (i < P) {
         const size_t lo = (size_t)d.group_base + (size_t)k * d.T + (size_t)b * RED_CHUNK + (size_t)i * q;
         for (int u = (int)q - 1; u >= 0; u--) {
-            a = G::add(a, load_xyzz(in + 16 * (lo + u)));
-            r = G::add(r, load_xyzz(in + 16 * (lo + u) + 8));
+            a = l2_add<C>(a, load_xyzz(in + 16 * (lo + u)));
+            r = l2_add<C>(r, load_xyzz(in + 16 * (lo + u) + 8));
             if (u > 0)
-                w = G::add(w, r);
+                w = l2_add<C>(w, r);
         }
     }
     r = block_suffix_scan<C>(sh, RED_CHUNK_THREADS, r, i, P);
     Xyzz v = (i >= 1 && i < P) ? r : G::inf();
     for (uint32_t m = q; m > 1; m >>= 1)
-        v = G::dbl(v);
-    v = G::add(v, w);
+        v = l2_dbl<C>(v);
+    v = l2_add<C>(v, w);
     for (uint32_t m = d.m0; m > 1; m >>= 1)
-        v = G::dbl(v);
-    v = G::add(v, a);
+        v = l2_dbl<C>(v);
+    v = l2_add<C>(v, a);
     block_tree_sum<C>(sh, RED_CHUNK_THREADS, v, i, P);
     if (i == 0) {
         if (DIRECT) {
@@ -349,8 +365,8 @@ __global__ void __launch_bounds__(RED_CHUNK) k_window_sum(const uint4 *__restric
     r = block_suffix_scan<C>(sh, RED_CHUNK, r, i, nbk);
     Xyzz v = (i >= 1 && i < nbk) ? r : G::inf();
     for (uint32_t m = d.m0 * RED_CHUNK; m > 1 && nbk > 1; m >>= 1)
-        v = G::dbl(v);
-    v = G::add(v, cb);
+        v = l2_dbl<C>(v);
+    v = l2_add<C>(v, cb);
     block_tree_sum<C>(sh, RED_CHUNK, v, i, nbk);
     if (i == 0)
         store_xyzz(S + 8 * (size_t)s, ld_soa(sh, 0, RED_CHUNK));

@@ -235,10 +235,12 @@ def test_msm_large_vs_threaded_oracle(ctx, curve):
 
 
 @pytest.mark.parametrize("curve", [0, 1])
-def test_linearity_at_full_size(ctx, curve):
-    """size-independent property at n = 2^20: MSM(a) + MSM(b) == MSM(a + b mod order)"""
+@pytest.mark.parametrize("lg", [20, 22])
+def test_linearity_at_full_size(ctx, curve, lg):
+    """size-independent property at n = 2^20 and 2^22 (the largest size of the
+    sweep): MSM(a) + MSM(b) == MSM(a + b mod order)"""
     from helioselene_gb300.workload import ORDER, make_workload, random_scalars
-    n = 1 << 20
+    n = 1 << lg
     w = make_workload(curve, n, seed=31337 + curve, edge_fraction=0.01)
     pts = ctx.map_to_curve(curve, w.u, HS_AFF)
     a = w.scalars
