@@ -479,6 +479,60 @@ def run_sweep(hs, torch, device: str, local: int, flush) -> dict:
     return out
 
 
+def run_tree(hs, torch, device: str, local: int, nodes: int = 8192) -> dict:
+    """FCMP++ tree-hash layers (src/benchmark_fcmpp.cpp:137-198): a node hash is an
+    MSM over the layer's fixed generators followed by to_affine.  A layer of
+    `nodes` hashes runs as fixed-base commitments over resident tables with
+    affine outputs, against the per-call path (hs_msm_device + affine output) on a
+    sample of the same nodes."""
+    from helioselene_gb300.workload import ORDER, random_field_bytes, random_scalars
+    rng = np.random.default_rng(SEED + 7)
+    ctx = hs.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=device)
+    out = {"nodes_per_layer": nodes}
+    for curve, n, name in ((hs.SELENE, 228, "selene_tree_hash(228)"), (hs.SELENE, 38, "selene_tree_hash(38)"),
+                           (hs.HELIOS, 18, "helios_tree_hash(18)")):
+        d_u = torch.from_numpy(random_field_bytes(rng, n).reshape(-1)).to(device)
+        d_g = torch.empty(n * 64, dtype=torch.uint8, device=device)
+        torch.cuda.synchronize()
+        ctx.map_to_curve_device(curve, d_u.data_ptr(), n, d_g.data_ptr())
+        torch.cuda.synchronize()
+        fb = hs.FixedBase(ctx, curve, d_g.cpu().numpy())
+        sc = torch.from_numpy(random_scalars(rng, nodes * n, ORDER[curve]).reshape(-1)).to(device)
+        d_out = torch.empty(nodes * 64, dtype=torch.uint8, device=device)
+        torch.cuda.synchronize()
+        fb.commit_device(sc.data_ptr(), nodes, d_out.data_ptr(), hs.FMT_AFFINE)
+        stream.synchronize()
+        ts = []
+        for _ in range(3):
+            a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fb.commit_device(sc.data_ptr(), nodes, d_out.data_ptr(), hs.FMT_AFFINE)
+            e.record(stream)
+            stream.synchronize()
+            ts.append(a.elapsed_time(e))
+        ms = sorted(ts)[1]
+        k = 64
+        d_plain = torch.empty(k * 64, dtype=torch.uint8, device=device)
+        ctx.msm_device(curve, sc.data_ptr(), d_g.data_ptr(), n, d_plain.data_ptr(), hs.FMT_AFFINE)
+        stream.synchronize()
+        a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for j in range(k):
+            ctx.msm_device(curve, sc.data_ptr() + 32 * n * j, d_g.data_ptr(), n, d_plain.data_ptr() + 64 * j,
+                           hs.FMT_AFFINE)
+        e.record(stream)
+        stream.synchronize()
+        plain_ms = a.elapsed_time(e) / k
+        exact = bool(torch.equal(d_out[:k * 64], d_plain))
+        out[name] = {"generators": n, "layer_ms": ms, "hashes_per_s": nodes / (ms * 1e-3),
+                     "per_call_ms": plain_ms, "speedup_vs_per_call": plain_ms * nodes / ms,
+                     "bit_exact_vs_per_call": exact, "window": fb.window}
+        fb.close()
+    ctx.close()
+    return out
+
+
 IMAD_PER_MODSQR = {0: 88, 1: 176}  # F_p, F_q squaring: 36 products + the same reduction
 # per decoded point: x^3 - 3x + b, one 4-bit-window exponentiation (256 S + 78 M), the root check
 DECODE_SQR, DECODE_MUL = 258, 80
@@ -717,6 +771,9 @@ def run_ours(args) -> None:
     fixed = None
     if not args.no_fixed:
         fixed = run_fixed(hs, torch, device, local)
+    tree = None
+    if not args.no_tree:
+        tree = run_tree(hs, torch, device, local)
     sweep = None
     if not args.no_sweep:
         sweep = run_sweep(hs, torch, device, local, flush)
@@ -772,6 +829,8 @@ def run_ours(args) -> None:
             line["decompress"] = decode
         if not args.no_sweep:
             line["sweep"] = sweep
+        if not args.no_tree:
+            line["tree_hash"] = tree
         if ws == 1 and not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline_leg(data, n, results)
         print(json.dumps(line), flush=True)
@@ -831,6 +890,7 @@ def main() -> None:
     ap.add_argument("--no-fixed", action="store_true", help="skip the fixed-base commitment section")
     ap.add_argument("--no-decompress", action="store_true", help="skip the point-decoding section")
     ap.add_argument("--no-sweep", action="store_true", help="skip the n = 2^10 .. 2^22 single-MSM sweep")
+    ap.add_argument("--no-tree", action="store_true", help="skip the FCMP++ tree-hash layer section")
     ap.add_argument("--split", type=int, default=None,
                     help="window-split threshold in points for single MSMs (0: off; default: the library's)")
     args = ap.parse_args()

@@ -81,3 +81,23 @@ def test_fixed_base_refuses_blinding_without_H(ctx):
             fb.commit(np.zeros((1, 10, 32), np.uint8), np.zeros((1, 32), np.uint8))
     finally:
         fb.close()
+
+
+@pytest.mark.parametrize("curve,n", [(1, 228), (1, 38), (0, 18)])
+def test_tree_hash_layer_shapes(ctx, curve, n):
+    """the FCMP++ tree-hash node shapes (src/benchmark_fcmpp.cpp:137-198): one
+    layer = many MSMs over the same generators, each output taken to affine"""
+    import helioselene_gb300 as hs
+    from helioselene_gb300.workload import ORDER, random_scalars
+    count = 40
+    _, G, _ = oracle_inputs(curve, n, seed=300 + n)
+    rng = np.random.default_rng(n)
+    vals = random_scalars(rng, count * n, ORDER[curve]).reshape(count, n, 32)
+    fb = hs.FixedBase(ctx, curve, G)
+    try:
+        aff = fb.commit(vals, out_fmt=hs.FMT_AFFINE)
+        want = [oracle.msm(curve, vals[j], G) for j in range(count)]
+        assert [oracle.compress(curve, a).tobytes() for a in aff] == want
+        assert fb.commit(vals) == want
+    finally:
+        fb.close()
