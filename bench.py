@@ -533,6 +533,33 @@ def run_tree(hs, torch, device: str, local: int, nodes: int = 8192) -> dict:
     return out
 
 
+def run_scalar_mul(hs, torch, ctxs, data, n: int, flush) -> dict:
+    """Independent variable-time scalar multiplications s_i P_i (the n = 1 MSM of
+    the serving path, helios_scalarmult_vartime) over the bench's scalars and
+    bases, device-resident, one thread per pair."""
+    out = {}
+    for curve, name in ((hs.HELIOS, "helios"), (hs.SELENE, "selene")):
+        c = ctxs[curve]
+        s = torch.cuda.ExternalStream(c.stream, device=data[curve]["d_pts"].device)
+        d_out = torch.empty(n * 96, dtype=torch.uint8, device=data[curve]["d_pts"].device)
+        args = (data[curve]["d_sc"].data_ptr(), data[curve]["d_pts"].data_ptr(), n, d_out.data_ptr())
+        c.scalar_mul_device(curve, *args, hs.FMT_AFFINE)
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(3):
+            with torch.cuda.stream(s):
+                flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(s)
+            c.scalar_mul_device(curve, *args, hs.FMT_AFFINE)
+            b.record(s)
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        ms = sorted(ts)[1]
+        out[name] = {"pairs": n, "ms": ms, "scalar_mults_per_s": n / (ms * 1e-3), "out_fmt": "affine"}
+    return out
+
+
 IMAD_PER_MODSQR = {0: 88, 1: 176}  # F_p, F_q squaring: 36 products + the same reduction
 # per decoded point: x^3 - 3x + b, one 4-bit-window exponentiation (256 S + 78 M), the root check
 DECODE_SQR, DECODE_MUL = 258, 80
@@ -771,6 +798,9 @@ def run_ours(args) -> None:
     fixed = None
     if not args.no_fixed:
         fixed = run_fixed(hs, torch, device, local)
+    smul = None
+    if not args.no_scalar_mul:
+        smul = run_scalar_mul(hs, torch, ctxs, data, n, flush)
     tree = None
     if not args.no_tree:
         tree = run_tree(hs, torch, device, local)
@@ -831,6 +861,8 @@ def run_ours(args) -> None:
             line["sweep"] = sweep
         if not args.no_tree:
             line["tree_hash"] = tree
+        if not args.no_scalar_mul:
+            line["scalar_mul"] = smul
         if ws == 1 and not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline_leg(data, n, results)
         print(json.dumps(line), flush=True)
@@ -891,6 +923,7 @@ def main() -> None:
     ap.add_argument("--no-decompress", action="store_true", help="skip the point-decoding section")
     ap.add_argument("--no-sweep", action="store_true", help="skip the n = 2^10 .. 2^22 single-MSM sweep")
     ap.add_argument("--no-tree", action="store_true", help="skip the FCMP++ tree-hash layer section")
+    ap.add_argument("--no-scalar-mul", action="store_true", help="skip the independent scalar-multiplication section")
     ap.add_argument("--split", type=int, default=None,
                     help="window-split threshold in points for single MSMs (0: off; default: the library's)")
     args = ap.parse_args()

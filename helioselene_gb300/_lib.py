@@ -66,6 +66,8 @@ SIGNATURES = {
     "hs_batch_to_affine": (_int, [_vp, _int, _vp, _sz, _vp, _int]),
     "hs_compress": (_int, [_vp, _int, _vp, _int, _sz, _vp]),
     "hs_decompress": (_int, [_vp, _int, _vp, _sz, _vp, _int, _vp]),
+    "hs_scalar_mul": (_int, [_vp, _int, _vp, _vp, _int, _sz, _vp, _int]),
+    "hs_scalar_mul_device": (_int, [_vp, _int, _vp, _vp, _sz, _vp, _int]),
     "hs_decompress_device": (_int, [_vp, _int, _vp, _sz, _vp, _vp]),
     "hs_map_to_curve": (_int, [_vp, _int, _vp, _sz, _vp, _int]),
     "hs_map_to_curve_device": (_int, [_vp, _int, _vp, _sz, _vp]),
@@ -91,6 +93,8 @@ SIGNATURES = {
     "hs_msm_noalloc_scratch_bytes": (_sz, []),
     "hs_helios_msm_vartime": (None, [_vp, _vp, _vp, _sz]),
     "hs_selene_msm_vartime": (None, [_vp, _vp, _vp, _sz]),
+    "hs_helios_scalarmult_vartime": (None, [_vp, _vp, _vp]),
+    "hs_selene_scalarmult_vartime": (None, [_vp, _vp, _vp]),
     "hs_helios_pedersen_commit": (None, [_vp, _vp, _vp, _vp, _vp, _sz]),
     "hs_selene_pedersen_commit": (None, [_vp, _vp, _vp, _vp, _vp, _sz]),
     "hs_helios_batch_to_affine": (None, [_vp, _vp, _sz]),

@@ -186,6 +186,22 @@ class Context:
         self._check(self._lib.hs_compress(self._h, curve, _ptr(p), in_fmt, n, _ptr(out)), "hs_compress")
         return out
 
+    def scalar_mul(self, curve: int, scalars, points, point_fmt: int = L.FMT_AFFINE,
+                   out_fmt: int = L.FMT_COMPRESSED) -> np.ndarray:
+        """out[i] = scalars[i] * points[i], variable time (hs_scalar_mul); n records of out_fmt"""
+        s, p = _u8(scalars), _u8(points)
+        n = s.size // 32
+        out = np.zeros(n * L.FMT_BYTES[out_fmt], np.uint8)
+        self._check(self._lib.hs_scalar_mul(self._h, curve, _ptr(s), _ptr(p), point_fmt, n, _ptr(out), out_fmt),
+                    "hs_scalar_mul")
+        return out
+
+    def scalar_mul_device(self, curve: int, d_scalars: int, d_points: int, n: int, d_out: int,
+                          out_fmt: int = L.FMT_JACOBIAN51) -> None:
+        self._check(self._lib.hs_scalar_mul_device(self._h, curve, ctypes.c_void_p(d_scalars),
+                                                   ctypes.c_void_p(d_points), n, ctypes.c_void_p(d_out), out_fmt),
+                    "hs_scalar_mul_device")
+
     def decompress(self, curve: int, encodings, out_fmt: int = L.FMT_AFFINE, check: bool = True):
         """32-byte encodings -> points in out_fmt and a validity mask (hs_decompress).
         With check=False invalid encodings come back as the identity instead of raising."""
@@ -439,6 +455,13 @@ class _PointBase:
         v = b"".join(bytes(x) for x in values)
         g = b"".join(pt.jac51 for pt in generators)
         return cls(ctx.pedersen(cls.CURVE, bytes(blinding), H.jac51, v, g, L.FMT_JACOBIAN51, L.FMT_JACOBIAN51))
+
+    def scalar_mul_vartime(self, scalar: bytes, ctx: Context = None):
+        """scalar * self, variable time, for public scalars (helios_scalarmult_vartime,
+        helios/include/helios_scalarmult_vartime.h:39-57)"""
+        ctx = ctx or default_context()
+        return type(self)(ctx.scalar_mul(self.CURVE, bytes(scalar), self.jac51, L.FMT_JACOBIAN51,
+                                         L.FMT_JACOBIAN51).tobytes())
 
     @classmethod
     def map_to_curve(cls, u: bytes, ctx: Context = None):

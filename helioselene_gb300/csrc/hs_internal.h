@@ -193,6 +193,8 @@ struct CurveOps {
     // (d_valid may be null) and a count in *d_bad (not cleared here)
     cudaError_t (*decompress)(Context &ctx, const void *d_in, size_t n, uint4 *d_out, uint8_t *d_valid,
                               uint32_t *d_bad);
+    // out[i] = s_i P_i as canonical Jacobians (24 words), points canonical affine
+    cudaError_t (*scalar_mul)(Context &ctx, const void *d_scalars, const uint4 *d_points, size_t n, uint32_t *d_out);
 };
 extern const CurveOps helios_ops;
 extern const CurveOps selene_ops;

@@ -1227,11 +1227,78 @@ cudaError_t join(Context &ctx, const uint32_t *d_a, const uint32_t *d_b, uint32_
     return cudaSuccess;
 }
 
+// ---------------------------------------------------------------------------
+// independent variable-time scalar multiplications s_i * P_i
+// (helios/include/helios_scalarmult_vartime.h:39-57, the n = 1 case of the MSM)
+// ---------------------------------------------------------------------------
+// One thread per pair: signed 4-bit digits d_0..d_64 in [-8, 8] (the recode of
+// the MSM with c = 4, carry kept), a table of P..8P in XYZZ, then from the top
+// digit four doublings and one addition of +-|d| P per digit.
+template <class C>
+__global__ void __launch_bounds__(128) k_scalar_mul(const uint4 *__restrict__ scalars, const uint4 *__restrict__ pts,
+                                                   size_t n, uint32_t *__restrict__ out)
+{
+    using G = Group<C>;
+    using F = typename C::F;
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    Fe x, y;
+    load_affine(pts, (uint32_t)i, x, y);
+    Xyzz Q = G::inf();
+    if (!(F::is_exact_zero(x) && F::is_exact_zero(y))) {
+        const uint4 sa = __ldg(scalars + 2 * i), sb = __ldg(scalars + 2 * i + 1);
+        const uint32_t s[8] = {sa.x, sa.y, sa.z, sa.w, sb.x, sb.y, sb.z, sb.w};
+        int8_t d[65];
+        uint32_t carry = 0;
+#pragma unroll
+        for (int k = 0; k < 65; k++) {
+            const uint32_t v = (k < 64 ? (s[k >> 3] >> (4 * (k & 7))) & 15u : 0u) + carry;
+            if (k < 64 && v >= 8u) {
+                d[k] = (int8_t)((int)v - 16);
+                carry = 1;
+            } else {
+                d[k] = (int8_t)v;
+                carry = 0;
+            }
+        }
+        Xyzz T[8];
+        T[0] = G::from_affine(x, y);
+        T[1] = G::dbl(T[0]);
+        for (int j = 2; j < 8; j++) {
+            T[j] = T[j - 1];
+            G::add_affine(T[j], x, y);
+        }
+        for (int k = 64; k >= 0; k--) {
+            if (k < 64)
+                for (int b = 0; b < 4; b++)
+                    Q = G::dbl(Q);
+            const int dk = d[k];
+            if (dk != 0)
+                Q = G::add(Q, dk > 0 ? T[dk - 1] : G::neg(T[-dk - 1]));
+        }
+    }
+    store_jacobian_canon<C>(out + 24 * i, Q);
+}
+
+template <class C>
+cudaError_t scalar_mul(Context &ctx, const void *d_scalars, const uint4 *d_points, size_t n, uint32_t *d_out)
+{
+    if (n == 0)
+        return cudaSuccess;
+    const int threads = 128;
+    k_scalar_mul<C><<<(unsigned)((n + threads - 1) / threads), threads, 0, ctx.stream>>>(
+        static_cast<const uint4 *>(d_scalars), d_points, n, d_out);
+    HS_LAUNCH_CHECK(ctx);
+    return cudaSuccess;
+}
+
 template <class C>
 CurveOps make_ops()
 {
     return CurveOps{&msm_tail<C>, &to_affine<C>, &to_affine_scratch, &format_out<C>, &map_to_curve<C>,
-                    &to_jac24<C>, &field_op<C>,  &fixed_table<C>,    &join<C>,       &decompress<C>};
+                    &to_jac24<C>, &field_op<C>,  &fixed_table<C>,    &join<C>,       &decompress<C>,
+                    &scalar_mul<C>};
 }
 
 }  // namespace hs

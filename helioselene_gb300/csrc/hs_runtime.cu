@@ -1472,6 +1472,66 @@ int hs_map_to_curve(hs_context *h, int curve, const uint8_t *u, size_t n, void *
     return HS_OK;
 }
 
+int hs_scalar_mul_device(hs_context *h, int curve, const void *d_scalars, const void *d_points, size_t n, void *d_out,
+                         int out_fmt)
+{
+    if (!h || !valid_curve(curve) || !valid_out_fmt(out_fmt) || (n && (!d_scalars || !d_points || !d_out)))
+        return HS_EINVAL;
+    if (n == 0)
+        return HS_OK;
+    Context &ctx = h->c;
+    std::lock_guard<std::mutex> lk(ctx.mu);
+    DeviceGuard g(ctx.device);
+    const CurveOps &ops = curve_ops(curve);
+    HS_CU(ctx.arena.reserve(align256(n * 96) + 1024), "workspace allocation");
+    uint32_t *d_j = (uint32_t *)ctx.arena.take(n * 96);
+    if (!d_j)
+        return fail_msg(ctx, HS_ENOMEM, "workspace carve");
+    HS_CU(ops.scalar_mul(ctx, d_scalars, static_cast<const uint4 *>(d_points), n, d_j), "scalar multiplication");
+    HS_CU(ops.format_out(ctx, d_j, n, out_fmt, d_out), "format");
+    return HS_OK;
+}
+
+int hs_scalar_mul(hs_context *h, int curve, const uint8_t *scalars, const void *points, int point_fmt, size_t n,
+                  void *out, int out_fmt)
+{
+    if (!h || !valid_curve(curve) || !valid_pt_fmt(point_fmt) || !valid_out_fmt(out_fmt) ||
+        (n && (!scalars || !points || !out)))
+        return HS_EINVAL;
+    if (n == 0)
+        return HS_OK;
+    Context &ctx = h->c;
+    std::lock_guard<std::mutex> lk(ctx.mu);
+    DeviceGuard g(ctx.device);
+    const CurveOps &ops = curve_ops(curve);
+    const size_t pb = fmt_bytes(point_fmt), ob = fmt_bytes(out_fmt);
+    HS_CU(ctx.arena.reserve(align256(n * 32) + align256(n * pb) + align256(n * 64) +
+                            align256(ops.to_affine_scratch(n)) + align256(n * 96) + align256(n * ob) + 2048),
+          "workspace allocation");
+    uint8_t *d_sc = (uint8_t *)ctx.arena.take(n * 32);
+    uint8_t *d_raw = (uint8_t *)ctx.arena.take(n * pb);
+    uint4 *d_aff = (uint4 *)ctx.arena.take(n * 64);
+    void *d_scr = ctx.arena.take(ops.to_affine_scratch(n));
+    uint32_t *d_j = (uint32_t *)ctx.arena.take(n * 96);
+    void *d_o = ctx.arena.take(n * ob);
+    if (!d_sc || !d_raw || !d_aff || !d_scr || !d_j || !d_o)
+        return fail_msg(ctx, HS_ENOMEM, "workspace carve");
+    cudaStream_t st = ctx.stream;
+    HS_CU(cudaMemcpyAsync(d_sc, scalars, n * 32, cudaMemcpyHostToDevice, st), "H2D scalars");
+    HS_CU(cudaMemcpyAsync(d_raw, points, n * pb, cudaMemcpyHostToDevice, st), "H2D points");
+    if (point_fmt == HS_FMT_AFFINE)
+        HS_CU(cudaMemcpyAsync(d_aff, d_raw, n * 64, cudaMemcpyDeviceToDevice, st), "copy");
+    else
+        HS_CU(ops.to_affine(ctx, d_raw, point_fmt, n, d_aff, d_scr), "input conversion");
+    HS_CU(ops.scalar_mul(ctx, d_sc, d_aff, n, d_j), "scalar multiplication");
+    HS_CU(ops.format_out(ctx, d_j, n, out_fmt, d_o), "format");
+    HS_CU(cudaMemcpyAsync(out, d_o, n * ob, cudaMemcpyDeviceToHost, st), "D2H");
+    HS_CU(cudaStreamSynchronize(st), "scalar multiplication");
+    if (point_fmt == HS_FMT_COMPRESSED)
+        return check_decoded(ctx, d_scr);
+    return HS_OK;
+}
+
 int hs_field_op(hs_context *h, int field, int op, const uint8_t *a, const uint8_t *b, size_t n, uint8_t *out)
 {
     const bool binary = op == 0 || op == 2 || op == 3;
@@ -2013,6 +2073,18 @@ void hs_selene_msm_vartime(hs_jacobian51 *result, const unsigned char *scalars, 
     }
     must(hs_msm(global_ctx(), HS_SELENE, scalars, points, HS_FMT_JACOBIAN51, n, result, HS_FMT_JACOBIAN51),
          "selene MSM");
+}
+
+void hs_helios_scalarmult_vartime(hs_jacobian51 *result, const unsigned char scalar[32], const hs_jacobian51 *p)
+{
+    must(hs_scalar_mul(global_ctx(), HS_HELIOS, scalar, p, HS_FMT_JACOBIAN51, 1, result, HS_FMT_JACOBIAN51),
+         "helios scalar multiplication");
+}
+
+void hs_selene_scalarmult_vartime(hs_jacobian51 *result, const unsigned char scalar[32], const hs_jacobian51 *p)
+{
+    must(hs_scalar_mul(global_ctx(), HS_SELENE, scalar, p, HS_FMT_JACOBIAN51, 1, result, HS_FMT_JACOBIAN51),
+         "selene scalar multiplication");
 }
 
 void hs_helios_pedersen_commit(hs_jacobian51 *result, const unsigned char *blinding, const hs_jacobian51 *H,

@@ -137,6 +137,18 @@ int hs_batch_to_affine(hs_context *ctx, int curve, const void *in, size_t n, voi
  * in: n points in in_fmt (JACOBIAN51, AFFINE51 or AFFINE); out: n*32 bytes. */
 int hs_compress(hs_context *ctx, int curve, const void *in, int in_fmt, size_t n, uint8_t *out);
 
+/* ---- independent variable-time scalar multiplications: out[i] = scalars[i] * points[i] ----
+ * Replaces helios_scalarmult_vartime / selene_scalarmult_vartime
+ * (helios/include/helios_scalarmult_vartime.h:39-57), batched: one thread per
+ * pair, any 32-byte scalar.  points in point_fmt (any input form); out n
+ * records of out_fmt. */
+int hs_scalar_mul(hs_context *ctx, int curve, const uint8_t *scalars, const void *points, int point_fmt, size_t n,
+                  void *out, int out_fmt);
+/* device form: d_scalars n*32 bytes, d_points n*64 bytes (HS_FMT_AFFINE), d_out n
+ * records of out_fmt; on the context stream, does not synchronise */
+int hs_scalar_mul_device(hs_context *ctx, int curve, const void *d_scalars, const void *d_points, size_t n, void *d_out,
+                         int out_fmt);
+
 /* ---- decoding of n 32-byte encodings (helios/src/x64/helios_frombytes.cpp:59-109,
  * selene twin; HeliosPoint::from_bytes, src/api_point.cpp:58-64) ----
  * out: n points in HS_FMT_AFFINE, HS_FMT_AFFINE51 or HS_FMT_JACOBIAN51; valid:
@@ -273,6 +285,10 @@ void hs_helios_msm_vartime(hs_jacobian51 *result, const unsigned char *scalars, 
                            size_t n);
 void hs_selene_msm_vartime(hs_jacobian51 *result, const unsigned char *scalars, const hs_jacobian51 *points,
                            size_t n);
+/* exact signature of helios_scalarmult_vartime / selene_scalarmult_vartime
+ * (helios/include/helios_scalarmult_vartime.h:39-57); aborts on a device failure */
+void hs_helios_scalarmult_vartime(hs_jacobian51 *result, const unsigned char scalar[32], const hs_jacobian51 *p);
+void hs_selene_scalarmult_vartime(hs_jacobian51 *result, const unsigned char scalar[32], const hs_jacobian51 *p);
 void hs_helios_pedersen_commit(hs_jacobian51 *result, const unsigned char *blinding, const hs_jacobian51 *H,
                                const unsigned char *values, const hs_jacobian51 *generators, size_t n);
 void hs_selene_pedersen_commit(hs_jacobian51 *result, const unsigned char *blinding, const hs_jacobian51 *H,
