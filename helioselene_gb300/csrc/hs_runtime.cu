@@ -146,23 +146,39 @@ static void plan_chunks(BatchPlan &p)
     p.CH = (uint32_t)ch;
 }
 
+// Buckets per level-1 group for a plan of nb buckets: 8 while the groups are
+// few (their threads are the parallelism of level 1), more once there are
+// millions of buckets, so that level 2 -- latency-bound, a scan per window --
+// has fewer groups to combine.
+static uint32_t group_size(uint64_t nb)
+{
+    return nb < (1ull << 21) ? RED_GROUP : nb < (1ull << 22) ? 2 * RED_GROUP : 4 * RED_GROUP;
+}
+
 BatchPlan make_batch_plan(const Context &ctx, int curve, const size_t *sizes, uint32_t M)
 {
     BatchPlan p;
     p.curve = curve;
     p.M = M;
     p.msms.resize(M);
+    uint64_t nb_all = 0;
+    std::vector<int> cs(M);
+    for (uint32_t i = 0; i < M; i++) {
+        cs[i] = choose_window(ctx, curve, sizes[i] ? sizes[i] : 1);
+        nb_all += (uint64_t)((257 + cs[i] - 1) / cs[i]) << (cs[i] - 1);
+    }
+    const uint32_t gsz = group_size(nb_all);
     uint64_t pt = 0, nb = 0, g = 0, ws = 0, ent = 0;
     for (uint32_t i = 0; i < M; i++) {
         MsmDesc &d = p.msms[i];
         const size_t n = sizes[i];
-        const int c = choose_window(ctx, curve, n ? n : 1);
+        const int c = cs[i];
         d.pt_off = (uint32_t)pt;
         d.n = (uint32_t)n;
         d.c = (uint32_t)c;
         d.W = (uint32_t)((257 + c - 1) / c);
         d.B = 1u << (c - 1);
-        d.m0 = std::min<uint32_t>(RED_GROUP, d.B);
+        d.m0 = std::min<uint32_t>(gsz, d.B);
         d.log2m0 = 0;
         while ((1u << d.log2m0) < d.m0)
             d.log2m0++;
@@ -202,7 +218,7 @@ BatchPlan make_fixed_plan(int curve, size_t n, int c, uint32_t count)
     p.M = count;
     p.msms.resize(count);
     const uint32_t W = (uint32_t)((257 + c - 1) / c), B = 1u << (c - 1);
-    const uint32_t m0 = std::min<uint32_t>(RED_GROUP, B);
+    const uint32_t m0 = std::min<uint32_t>(group_size((uint64_t)count * B), B);
     uint32_t log2m0 = 0;
     while ((1u << log2m0) < m0)
         log2m0++;
