@@ -91,7 +91,15 @@ struct MsmDesc {
     uint32_t w_cnt;   // windows emitted: [w_lo, w_lo + w_cnt)
     uint32_t shift;   // doublings applied after the Horner step (c * w_lo for an upper half)
     uint32_t chunk_base;  // first level-2 reduction chunk (Wr * max(1, T / RED_CHUNK) per MSM)
+    uint32_t slices;      // counting sort: point slices per emitted window (one block each)
+    uint32_t sblk_base;   // first counting-sort block of this MSM (w_cnt * slices blocks)
+    uint32_t cnt_base;    // first per-block bucket count of this MSM
+    uint32_t dig_base;    // first signed digit of this MSM (w_cnt x n, window-major)
 };
+
+// counting sort in shared memory: buckets per window it handles, threads per block
+constexpr uint32_t SORT_SMEM_MAX_B = 32768;
+constexpr int SORT_THREADS = 1024;
 
 // A run of MSMs sharing one window width (one templated recode launch).
 struct WindowClass {
@@ -113,6 +121,11 @@ struct BatchPlan {
     uint32_t CH = 0;            // level-2 reduction chunks
     uint32_t max_T = 1;         // largest groups-per-window of the batch
     uint32_t max_nbk = 1;       // largest chunks-per-window of the batch
+    uint32_t max_B = 1;         // largest buckets-per-window of the batch
+    uint32_t sort_blocks = 0;   // counting-sort blocks (shared-memory path)
+    uint64_t cnt_len = 0;       // per-block bucket counts (shared-memory path)
+    bool global_sort = false;   // keep the global-atomic sort (no digit and count buffers)
+    bool smem_sort() const { return !global_sort && max_B <= SORT_SMEM_MAX_B; }
     uint32_t L = 0;             // max entries per accumulation segment
     uint32_t max_entries = 0;
     uint32_t max_segs = 0;
@@ -138,6 +151,8 @@ struct BatchBuffers {
     uint32_t *heavy_n = nullptr;        // 1 counter
     uint4 *redA = nullptr;              // G group (acc, run) pairs
     uint4 *redC = nullptr;              // CH chunk (sum, run) pairs
+    uint32_t *sort_cnt = nullptr;       // cnt_len per-block bucket counts, then offsets
+    uint32_t *digits = nullptr;         // max_entries signed digits (|d| | sign << 31, 0 = none)
     uint4 *redS = nullptr;              // WS window sums
     uint32_t *out_jac = nullptr;        // M x 24 words: canonical Jacobian X, Y, Z
 };
@@ -223,6 +238,7 @@ struct DeviceGuard {
 int reserve_batch(Context &ctx, const BatchPlan &p, size_t extra_bytes, BatchBuffers &b, void **extra);
 int execute_batch(Context &ctx, const BatchPlan &p, const BatchBuffers &b, void *d_out, int out_fmt);
 // recode, sort, accumulate, reduce, combine and format one batch with direct launches
+cudaError_t sort_smem_attrs(int device);
 cudaError_t launch_batch(Context &ctx, const BatchPlan &p, const BatchBuffers &b, void *d_out, int out_fmt);
 void drop_graphs(Context &ctx);
 int fail(Context &ctx, cudaError_t e, const char *what);

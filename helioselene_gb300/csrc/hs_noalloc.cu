@@ -72,12 +72,14 @@ int hs_msm_device_noalloc(int curve, const void *d_scalars, const void *d_points
     ctx.device = device;
     ctx.stream = static_cast<cudaStream_t>(stream);
     ctx.use_graphs = false;
-    if (cudaDeviceGetAttribute(&ctx.sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
+    if (cudaDeviceGetAttribute(&ctx.sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+        sort_smem_attrs(device) != cudaSuccess) {
         cudaGetLastError();
         return HS_ECUDA;
     }
     const size_t sizes[1] = {n};
-    const BatchPlan p = make_batch_plan(ctx, curve, sizes, 1);
+    BatchPlan p = make_batch_plan(ctx, curve, sizes, 1);
+    p.global_sort = true;  // the smaller workspace: the fixed scratch array bounds it
     if (batch_bytes(p) > NOALLOC_SCRATCH_BYTES)
         return HS_ERANGE;
     ctx.arena.base = static_cast<char *>(scratch);

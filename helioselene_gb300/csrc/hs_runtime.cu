@@ -130,6 +130,31 @@ int choose_window(const Context &ctx, int curve, size_t n)
     return c;
 }
 
+// Shared-memory counting sort: MSM m's emitted windows are each cut into
+// `slices` point ranges, one block per (window, slice).  A block counts its
+// bucket keys in shared memory and writes one row of counts; a bucket's rows
+// are Q = slices (or w_cnt * slices for a fixed-base MSM, whose windows share
+// its B buckets) and its columns the MSM's buckets, so cnt_base + q * Bm + col.
+static void plan_sort(BatchPlan &p)
+{
+    uint64_t blk = 0, cnt = 0, dig = 0;
+    p.max_B = 1;
+    for (MsmDesc &d : p.msms) {
+        d.dig_base = (uint32_t)dig;
+        dig += (uint64_t)d.w_cnt * d.n;
+        d.slices = (uint32_t)std::min<uint64_t>(64, std::max<uint64_t>(1, ((uint64_t)d.n + 131071) / 131072));
+        d.sblk_base = (uint32_t)blk;
+        d.cnt_base = (uint32_t)cnt;
+        blk += (uint64_t)d.w_cnt * d.slices;
+        const uint64_t Bm = d.fixed ? d.B : (uint64_t)d.w_cnt * d.B;
+        const uint64_t Q = d.fixed ? (uint64_t)d.w_cnt * d.slices : d.slices;
+        cnt += Bm * Q;
+        p.max_B = std::max(p.max_B, d.B);
+    }
+    p.sort_blocks = (uint32_t)blk;
+    p.cnt_len = cnt;
+}
+
 // level-2 reduction chunks: chunk_base per MSM and the plan totals
 static void plan_chunks(BatchPlan &p)
 {
@@ -208,6 +233,7 @@ BatchPlan make_batch_plan(const Context &ctx, int curve, const size_t *sizes, ui
     p.max_segs = (uint32_t)(std::min<uint64_t>(ent, nb) + ent / p.L + 1);
     p.hist_blocks = (p.NB + SEG_HIST_THREADS - 1) / SEG_HIST_THREADS;
     plan_chunks(p);
+    plan_sort(p);
     return p;
 }
 
@@ -253,6 +279,7 @@ BatchPlan make_fixed_plan(int curve, size_t n, int c, uint32_t count)
     p.max_segs = (uint32_t)(std::min<uint64_t>(ent, p.NB) + ent / p.L + 1);
     p.hist_blocks = (p.NB + SEG_HIST_THREADS - 1) / SEG_HIST_THREADS;
     plan_chunks(p);
+    plan_sort(p);
     return p;
 }
 
@@ -293,6 +320,7 @@ BatchPlan make_window_plan(int curve, size_t n, int c, uint32_t w_lo, uint32_t w
     p.max_segs = (uint32_t)(std::min<uint64_t>(ent, p.NB) + ent / p.L + 1);
     p.hist_blocks = (p.NB + SEG_HIST_THREADS - 1) / SEG_HIST_THREADS;
     plan_chunks(p);
+    plan_sort(p);
     return p;
 }
 
@@ -318,6 +346,8 @@ size_t batch_bytes(const BatchPlan &p)
     b += align256((size_t)p.NB * 4) + 256;                                                 // heavy list + counter
     b += align256((size_t)std::max<uint32_t>(1, p.G) * 256);                               // group (acc, run) pairs
     b += align256((size_t)std::max<uint32_t>(1, p.CH) * 256);                              // chunk (sum, run) pairs
+    b += p.smem_sort() ? align256((size_t)std::max<uint64_t>(1, p.cnt_len) * 4) : 0;         // per-block counts
+    b += p.smem_sort() ? align256((size_t)p.max_entries * 4) : 0;                            // signed digits
     b += align256((size_t)std::max<uint32_t>(1, p.WS) * 128);                              // window sums
     b += align256((size_t)std::max<uint32_t>(1, p.M) * 96);                                // results
     return b + 16 * 256;
@@ -340,10 +370,13 @@ bool carve(DeviceArena &a, const BatchPlan &p, BatchBuffers &b)
     b.heavy_n = (uint32_t *)a.take(4);
     b.redA = (uint4 *)a.take((size_t)std::max<uint32_t>(1, p.G) * 256);
     b.redC = (uint4 *)a.take((size_t)std::max<uint32_t>(1, p.CH) * 256);
+    b.sort_cnt = p.smem_sort() ? (uint32_t *)a.take((size_t)std::max<uint64_t>(1, p.cnt_len) * 4) : nullptr;
+    b.digits = p.smem_sort() ? (uint32_t *)a.take((size_t)p.max_entries * 4) : nullptr;
     b.redS = (uint4 *)a.take((size_t)std::max<uint32_t>(1, p.WS) * 128);
     b.out_jac = (uint32_t *)a.take((size_t)std::max<uint32_t>(1, p.M) * 96);
     return b.desc && b.counts && b.offsets && b.seg_off && b.scan_tmp && b.len_hist && b.len_scan && b.sorted &&
-           b.segs && b.seg_sum && b.heavy && b.heavy_n && b.redA && b.redC && b.redS && b.out_jac;
+           b.segs && b.seg_sum && b.heavy && b.heavy_n && b.redA && b.redC && b.redS && b.out_jac &&
+           ((b.sort_cnt && b.digits) || !p.smem_sort());
 }
 
 // ---------------------------------------------------------------------------
@@ -444,6 +477,215 @@ __global__ void k_recode(const uint4 *__restrict__ scalars, uint32_t n_total, co
 #undef HS_CASE
     default:
         break;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// counting sort in shared memory (window widths up to 16): one block per
+// (emitted window, point slice).  Bucket keys of one window fit a block's
+// shared memory, so the per-entry atomics are shared-memory atomics; only one
+// row of counts per block goes to global memory.
+//   k_digits       every scalar's signed digits, window-major, in one pass
+//   k_sort_count   count the block's keys, write its row of counts
+//   k_sort_totals  per bucket: the sum of its rows -> counts (then the scan)
+//   k_sort_offsets per bucket: each row's first slot, offsets + earlier rows
+//   k_sort_scatter place "index | sign" at the row's slot + running fill
+// ---------------------------------------------------------------------------
+struct SortBlock {
+    uint32_t m, k_abs, q, col, lo, hi;  // MSM, window, count row, first column, point range
+};
+
+__device__ __forceinline__ SortBlock sort_block(const MsmDesc *__restrict__ desc, uint32_t M, uint32_t blk)
+{
+    SortBlock sb;
+    sb.m = find_msm(M, blk, [&](uint32_t k) { return desc[k].sblk_base; });
+    const MsmDesc &d = desc[sb.m];
+    const uint32_t local = blk - d.sblk_base;
+    const uint32_t k = local / d.slices, s = local % d.slices;
+    sb.k_abs = d.w_lo + k;
+    sb.q = d.fixed ? k * d.slices + s : s;
+    sb.col = d.fixed ? 0u : k * d.B;
+    const uint32_t per = (d.n + d.slices - 1) / d.slices;
+    sb.lo = d.pt_off + min(d.n, s * per);
+    sb.hi = d.pt_off + min(d.n, (s + 1) * per);
+    return sb;
+}
+
+__device__ __forceinline__ void load_scalar(const uint4 *__restrict__ scalars, uint32_t i, uint32_t s[8])
+{
+    const uint4 a = __ldg(scalars + 2 * (size_t)i), b = __ldg(scalars + 2 * (size_t)i + 1);
+    s[0] = a.x; s[1] = a.y; s[2] = a.z; s[3] = a.w;
+    s[4] = b.x; s[5] = b.y; s[6] = b.z; s[7] = b.w;
+}
+
+// all emitted signed digits of one scalar, window-major per MSM (the rule of
+// recode_one: the carry runs up from window 0, the top window keeps it)
+template <int CB>
+__device__ __forceinline__ void digits_one(const uint32_t s[8], uint32_t w_lo, uint32_t w_cnt, uint32_t *__restrict__ out,
+                                           uint32_t stride)
+{
+    constexpr int W = (257 + CB - 1) / CB;
+    constexpr uint32_t B = 1u << (CB - 1);
+    uint32_t carry = 0;
+#pragma unroll
+    for (int k = 0; k < W; k++) {
+        const uint32_t v = window_bits<CB>(s, k) + carry;
+        uint32_t mag, neg = 0;
+        if (k < W - 1 && v >= B) {
+            mag = (1u << CB) - v;
+            neg = mag != 0 ? 1u : 0u;
+            carry = 1;
+        } else {
+            mag = v;
+            carry = 0;
+        }
+        if ((uint32_t)k - w_lo < w_cnt)
+            out[(size_t)((uint32_t)k - w_lo) * stride] = mag | (neg << 31);
+    }
+}
+
+__global__ void k_digits(const uint4 *__restrict__ scalars, uint32_t n_total, const MsmDesc *__restrict__ desc,
+                         uint32_t M, uint32_t *__restrict__ digits)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_total)
+        return;
+    const uint32_t m = find_msm(M, i, [&](uint32_t k) { return desc[k].pt_off; });
+    const MsmDesc &d = desc[m];
+    uint32_t s[8];
+    load_scalar(scalars, i, s);
+    uint32_t *out = digits + d.dig_base + (i - d.pt_off);
+    switch (d.c) {
+#define HS_CASE(v)                                            \
+    case v:                                                   \
+        digits_one<v>(s, d.w_lo, d.w_cnt, out, d.n);          \
+        break;
+        HS_CASE(4)
+        HS_CASE(5)
+        HS_CASE(6)
+        HS_CASE(7)
+        HS_CASE(8)
+        HS_CASE(9)
+        HS_CASE(10)
+        HS_CASE(11)
+        HS_CASE(12)
+        HS_CASE(13)
+        HS_CASE(14)
+        HS_CASE(15)
+        HS_CASE(16)
+#undef HS_CASE
+    default:
+        break;
+    }
+}
+
+__global__ void __launch_bounds__(SORT_THREADS) k_sort_count(const uint32_t *__restrict__ digits,
+                                                           const MsmDesc *__restrict__ desc, uint32_t M,
+                                                           uint32_t *__restrict__ cnt)
+{
+    extern __shared__ uint32_t hist[];
+    const SortBlock sb = sort_block(desc, M, blockIdx.x);
+    const MsmDesc &d = desc[sb.m];
+    for (uint32_t j = threadIdx.x; j < d.B; j += blockDim.x)
+        hist[j] = 0;
+    __syncthreads();
+    const uint32_t *dg = digits + d.dig_base + (size_t)(sb.k_abs - d.w_lo) * d.n;
+    // four independent loads in flight per thread, then their atomics
+    const uint32_t step = blockDim.x;
+    uint32_t i = sb.lo + threadIdx.x;
+    for (; i + 3 * step < sb.hi; i += 4 * step) {
+        uint32_t v[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            v[u] = __ldg(dg + (i + u * step - d.pt_off)) & 0x7fffffffu;
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            if (v[u])
+                atomicAdd(hist + v[u] - 1, 1u);
+    }
+    for (; i < sb.hi; i += step) {
+        const uint32_t mag = __ldg(dg + (i - d.pt_off)) & 0x7fffffffu;
+        if (mag)
+            atomicAdd(hist + mag - 1, 1u);
+    }
+    __syncthreads();
+    const uint64_t Bm = d.fixed ? d.B : (uint64_t)d.w_cnt * d.B;
+    uint32_t *row = cnt + d.cnt_base + (uint64_t)sb.q * Bm + sb.col;
+    for (uint32_t j = threadIdx.x; j < d.B; j += blockDim.x)
+        row[j] = hist[j];
+}
+
+// one thread per bucket of the batch: total over its rows (mode 0), or turn the
+// rows into first slots from offsets (mode 1)
+template <int MODE>
+__global__ void k_sort_rows(const MsmDesc *__restrict__ desc, uint32_t M, uint32_t NB, uint32_t *__restrict__ cnt,
+                            uint32_t *__restrict__ counts, const uint32_t *__restrict__ offsets)
+{
+    const uint32_t kb = blockIdx.x * blockDim.x + threadIdx.x;
+    if (kb >= NB)
+        return;
+    const uint32_t m = find_msm(M, kb, [&](uint32_t k) { return desc[k].bucket_base; });
+    const MsmDesc &d = desc[m];
+    const uint32_t lb = kb - d.bucket_base;
+    const uint64_t Bm = d.fixed ? d.B : (uint64_t)d.w_cnt * d.B;
+    const uint32_t Q = d.fixed ? d.w_cnt * d.slices : d.slices;
+    uint32_t *col = cnt + d.cnt_base + lb;
+    uint32_t run = MODE == 0 ? 0u : offsets[kb];
+    for (uint32_t q0 = 0; q0 < Q; q0 += 8) {  // eight loads in flight, then their sums
+        uint32_t v[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+            v[u] = q0 + u < Q ? col[(uint64_t)(q0 + u) * Bm] : 0u;
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            if (MODE == 1 && q0 + u < Q)
+                col[(uint64_t)(q0 + u) * Bm] = run;
+            run += v[u];
+        }
+    }
+    if (MODE == 0)
+        counts[kb] = run;
+}
+
+__global__ void __launch_bounds__(SORT_THREADS) k_sort_scatter(const uint32_t *__restrict__ digits,
+                                                             const MsmDesc *__restrict__ desc, uint32_t M,
+                                                             const uint32_t *__restrict__ cnt,
+                                                             uint32_t *__restrict__ sorted)
+{
+    extern __shared__ uint32_t slot[];
+    const SortBlock sb = sort_block(desc, M, blockIdx.x);
+    const MsmDesc &d = desc[sb.m];
+    const uint64_t Bm = d.fixed ? d.B : (uint64_t)d.w_cnt * d.B;
+    const uint32_t *row = cnt + d.cnt_base + (uint64_t)sb.q * Bm + sb.col;
+    for (uint32_t j = threadIdx.x; j < d.B; j += blockDim.x)
+        slot[j] = row[j];
+    __syncthreads();
+    const uint32_t *dg = digits + d.dig_base + (size_t)(sb.k_abs - d.w_lo) * d.n;
+    const uint32_t step = blockDim.x;
+    uint32_t i = sb.lo + threadIdx.x;
+    for (; i + 3 * step < sb.hi; i += 4 * step) {
+        uint32_t dv[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            dv[u] = __ldg(dg + (i + u * step - d.pt_off));
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const uint32_t mag = dv[u] & 0x7fffffffu;
+            if (mag) {
+                const uint32_t ii = i + u * step;
+                const uint32_t pos = atomicAdd(slot + mag - 1, 1u);
+                const uint32_t v = d.fixed ? (ii - d.pt_off) * d.W + sb.k_abs : ii;
+                sorted[pos] = v | (dv[u] & 0x80000000u);
+            }
+        }
+    }
+    for (; i < sb.hi; i += step) {
+        const uint32_t dv = __ldg(dg + (i - d.pt_off)), mag = dv & 0x7fffffffu;
+        if (mag) {
+            const uint32_t pos = atomicAdd(slot + mag - 1, 1u);
+            const uint32_t v = d.fixed ? (i - d.pt_off) * d.W + sb.k_abs : i;
+            sorted[pos] = v | (dv & 0x80000000u);
+        }
     }
 }
 
@@ -644,6 +886,28 @@ static cudaError_t launch_scan(Context &ctx, const uint32_t *in, uint32_t n, uin
 }
 
 // recode + counting sort + segments of a whole batch (descriptors already on the device)
+// the sort kernels' shared-memory opt-in, once per device (outside any capture:
+// contexts set it when they are created)
+cudaError_t sort_smem_attrs(int device)
+{
+    static std::once_flag once[64];
+    static cudaError_t err[64];
+    if (device < 0 || device >= 64)
+        return cudaErrorInvalidDevice;
+    std::call_once(once[device], [device] {
+        int prev = 0;
+        cudaGetDevice(&prev);
+        cudaSetDevice(device);
+        cudaError_t a = cudaFuncSetAttribute(k_sort_count, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)(SORT_SMEM_MAX_B * 4));
+        cudaError_t b = cudaFuncSetAttribute(k_sort_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)(SORT_SMEM_MAX_B * 4));
+        cudaSetDevice(prev);
+        err[device] = a != cudaSuccess ? a : b;
+    });
+    return err[device];
+}
+
 cudaError_t launch_sort(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
 {
     cudaStream_t st = ctx.stream;
@@ -651,18 +915,39 @@ cudaError_t launch_sort(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
     if ((e = cudaMemsetAsync(b.counts, 0, (size_t)(p.NB + 1) * 4, st)) != cudaSuccess)
         return e;
     const uint4 *sc = reinterpret_cast<const uint4 *>(b.scalars);
-    const unsigned rblocks = (p.n_total + 255) / 256;
-    if (p.n_total) {
-        k_recode<false><<<rblocks, 256, 0, st>>>(sc, p.n_total, b.desc, p.M, b.counts, b.offsets, b.sorted);
+    if (p.smem_sort()) {
+        if ((e = sort_smem_attrs(ctx.device)) != cudaSuccess)
+            return e;
+        const size_t smem = (size_t)p.max_B * 4;
+        const unsigned tb = (p.NB + 255) / 256;
+        if (p.n_total) {
+            k_digits<<<(p.n_total + 255) / 256, 256, 0, st>>>(sc, p.n_total, b.desc, p.M, b.digits);
+            HS_LAUNCH_CHECK(ctx);
+        }
+        k_sort_count<<<p.sort_blocks, SORT_THREADS, smem, st>>>(b.digits, b.desc, p.M, b.sort_cnt);
         HS_LAUNCH_CHECK(ctx);
-    }
-    if ((e = launch_scan(ctx, b.counts, p.NB, p.L, b.offsets, b.seg_off, b.scan_tmp)) != cudaSuccess)
-        return e;
-    if ((e = cudaMemsetAsync(b.counts, 0, (size_t)(p.NB + 1) * 4, st)) != cudaSuccess)
-        return e;
-    if (p.n_total) {
-        k_recode<true><<<rblocks, 256, 0, st>>>(sc, p.n_total, b.desc, p.M, b.counts, b.offsets, b.sorted);
+        k_sort_rows<0><<<tb, 256, 0, st>>>(b.desc, p.M, p.NB, b.sort_cnt, b.counts, nullptr);
         HS_LAUNCH_CHECK(ctx);
+        if ((e = launch_scan(ctx, b.counts, p.NB, p.L, b.offsets, b.seg_off, b.scan_tmp)) != cudaSuccess)
+            return e;
+        k_sort_rows<1><<<tb, 256, 0, st>>>(b.desc, p.M, p.NB, b.sort_cnt, nullptr, b.offsets);
+        HS_LAUNCH_CHECK(ctx);
+        k_sort_scatter<<<p.sort_blocks, SORT_THREADS, smem, st>>>(b.digits, b.desc, p.M, b.sort_cnt, b.sorted);
+        HS_LAUNCH_CHECK(ctx);
+    } else {
+        const unsigned rblocks = (p.n_total + 255) / 256;
+        if (p.n_total) {
+            k_recode<false><<<rblocks, 256, 0, st>>>(sc, p.n_total, b.desc, p.M, b.counts, b.offsets, b.sorted);
+            HS_LAUNCH_CHECK(ctx);
+        }
+        if ((e = launch_scan(ctx, b.counts, p.NB, p.L, b.offsets, b.seg_off, b.scan_tmp)) != cudaSuccess)
+            return e;
+        if ((e = cudaMemsetAsync(b.counts, 0, (size_t)(p.NB + 1) * 4, st)) != cudaSuccess)
+            return e;
+        if (p.n_total) {
+            k_recode<true><<<rblocks, 256, 0, st>>>(sc, p.n_total, b.desc, p.M, b.counts, b.offsets, b.sorted);
+            HS_LAUNCH_CHECK(ctx);
+        }
     }
     // segments, longest first
     const uint32_t nh = (uint32_t)hist_len(p);
@@ -1113,6 +1398,8 @@ int hs_context_create(hs_context **out, int device)
     e = cudaStreamCreateWithFlags(&ctx.stream, cudaStreamNonBlocking);
     if (e == cudaSuccess)
         e = cudaDeviceGetAttribute(&ctx.sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess)
+        e = sort_smem_attrs(device);
     if (e != cudaSuccess) {
         g_tls_error = std::string("context creation: ") + cudaGetErrorString(e);
         cudaGetLastError();

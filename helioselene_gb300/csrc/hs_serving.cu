@@ -347,6 +347,10 @@ int hs_server_create(hs_server **out, const hs_server_config *cfg)
     }
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, S.cfg.device);
+    if (sort_smem_attrs(S.cfg.device) != cudaSuccess) {
+        cudaGetLastError();
+        return HS_ECUDA;
+    }
     for (int i = 0; i < S.cfg.slots; i++) {
         auto sl = std::make_unique<Slot>();
         sl->ctx.device = S.cfg.device;
