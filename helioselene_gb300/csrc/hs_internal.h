@@ -100,6 +100,7 @@ struct MsmDesc {
 // counting sort in shared memory: buckets per window it handles, threads per block
 constexpr uint32_t SORT_SMEM_MAX_B = 32768;
 constexpr int SORT_THREADS = 1024;
+constexpr uint32_t SORT_MIN_POINTS_PER_BLOCK = 8192;  // below this average per block: the global-atomic sort
 
 // A run of MSMs sharing one window width (one templated recode launch).
 struct WindowClass {

@@ -153,6 +153,10 @@ static void plan_sort(BatchPlan &p)
     }
     p.sort_blocks = (uint32_t)blk;
     p.cnt_len = cnt;
+    // a block clears and writes a whole row of B counts: worth it only when its
+    // slice holds thousands of points (many small MSMs keep the global atomics)
+    if (dig < (uint64_t)SORT_MIN_POINTS_PER_BLOCK * std::max<uint64_t>(1, blk))
+        p.global_sort = true;
 }
 
 // level-2 reduction chunks: chunk_base per MSM and the plan totals
