@@ -46,6 +46,7 @@ struct Context {
     cudaStream_t stream = nullptr;   // the stream every launch goes to
     cudaStream_t stream2 = nullptr;  // second curve group of a mixed batch, lower window half of a split MSM
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;  // fork/join of the two streams (created with stream2)
+    cudaEvent_t ev_aux = nullptr;                      // host-input path: bases ready on the second stream
     bool use_graphs = true;
     size_t split_min = size_t(1) << 18;  // single MSMs this large run as two window halves (0: never)
     std::vector<GraphEntry> graphs;

@@ -1219,6 +1219,8 @@ static cudaError_t ensure_stream2(Context &ctx)
         return e;
     if (!ctx.ev_join && (e = cudaEventCreateWithFlags(&ctx.ev_join, cudaEventDisableTiming)) != cudaSuccess)
         return e;
+    if (!ctx.ev_aux && (e = cudaEventCreateWithFlags(&ctx.ev_aux, cudaEventDisableTiming)) != cudaSuccess)
+        return e;
     return e;
 }
 
@@ -1430,6 +1432,8 @@ void hs_context_destroy(hs_context *h)
             cudaEventDestroy(h->c.ev_fork);
         if (h->c.ev_join)
             cudaEventDestroy(h->c.ev_join);
+        if (h->c.ev_aux)
+            cudaEventDestroy(h->c.ev_aux);
     }
     delete h;
 }
@@ -1562,27 +1566,64 @@ static int msm_host(Context &ctx, int curve, const uint8_t *lead_scalar, const v
     uint8_t *d_raw = point_fmt == HS_FMT_AFFINE ? d_pts : d_pts + align256(total * 64);
     uint8_t *d_scratch = (point_fmt == HS_FMT_AFFINE ? d_pts + align256(total * 64) : d_raw + align256(total * pb));
     uint8_t *d_out = d_scratch + align256(ops.to_affine_scratch(total));
-    cudaStream_t st = ctx.stream;
-    if (lead) {
+    // Scalars go first on the context stream, the bases (copy and conversion) on
+    // the second stream: the counting sort needs only the scalars, so it runs
+    // while the bases are still arriving; the accumulation waits for them.
+    HS_CU(ensure_stream2(ctx), "stream creation");
+    cudaStream_t st = ctx.stream, s2 = ctx.stream2;
+    HS_CU(cudaEventRecord(ctx.ev_fork, st), "event");  // the second stream follows earlier work on the buffers
+    HS_CU(cudaStreamWaitEvent(s2, ctx.ev_fork, 0), "stream wait");
+    if (lead)
         HS_CU(cudaMemcpyAsync(d_sc, lead_scalar, 32, cudaMemcpyHostToDevice, st), "H2D scalars");
-        HS_CU(cudaMemcpyAsync(d_raw, lead_point, pb, cudaMemcpyHostToDevice, st), "H2D points");
-    }
-    if (n) {
+    if (n)
         HS_CU(cudaMemcpyAsync(d_sc + 32 * lead, scalars, n * 32, cudaMemcpyHostToDevice, st), "H2D scalars");
-        HS_CU(cudaMemcpyAsync(d_raw + pb * lead, points, n * pb, cudaMemcpyHostToDevice, st), "H2D points");
+    if (lead)
+        HS_CU(cudaMemcpyAsync(d_raw, lead_point, pb, cudaMemcpyHostToDevice, s2), "H2D points");
+    if (n)
+        HS_CU(cudaMemcpyAsync(d_raw + pb * lead, points, n * pb, cudaMemcpyHostToDevice, s2), "H2D points");
+    if (point_fmt != HS_FMT_AFFINE) {
+        ctx.stream = s2;
+        const cudaError_t ce = ops.to_affine(ctx, d_raw, point_fmt, total, (uint4 *)d_pts, d_scratch);
+        ctx.stream = st;
+        HS_CU(ce, "input conversion");
     }
-    if (point_fmt != HS_FMT_AFFINE)
-        HS_CU(ops.to_affine(ctx, d_raw, point_fmt, total, (uint4 *)d_pts, d_scratch), "input conversion");
-    int rc;
+    HS_CU(cudaEventRecord(ctx.ev_aux, s2), "event");
+    int rc = HS_OK;
     if (split) {
-        rc = execute_split(ctx, s, d_sc, d_pts, d_out, out_fmt);
+        BatchBuffers bh, bl;
+        uint32_t *d_final = nullptr;
+        if (!carve(ctx.arena, s.hi, bh) || !carve(ctx.arena, s.lo, bl) || !(d_final = (uint32_t *)ctx.arena.take(96)))
+            return fail_msg(ctx, HS_ENOMEM, "workspace carve");
+        bh.scalars = bl.scalars = (const uint32_t *)d_sc;
+        bh.points = bl.points = (const uint4 *)d_pts;
+        HS_CU(cudaMemcpyAsync(bh.desc, s.hi.msms.data(), sizeof(MsmDesc), cudaMemcpyHostToDevice, st), "descriptors");
+        HS_CU(cudaMemcpyAsync(bl.desc, s.lo.msms.data(), sizeof(MsmDesc), cudaMemcpyHostToDevice, st), "descriptors");
+        HS_CU(launch_sort(ctx, s.hi, bh), "sort");
+        HS_CU(launch_sort(ctx, s.lo, bl), "sort");
+        // upper half on the second stream once both sorts are in: its bases are there already
+        HS_CU(cudaEventRecord(ctx.ev_fork, st), "event");
+        HS_CU(cudaStreamWaitEvent(s2, ctx.ev_fork, 0), "stream wait");
+        ctx.stream = s2;
+        const cudaError_t te = ops.msm_tail(ctx, s.hi, bh);
+        ctx.stream = st;
+        HS_CU(te, "MSM tail");
+        HS_CU(cudaEventRecord(ctx.ev_join, s2), "event");
+        HS_CU(cudaStreamWaitEvent(st, ctx.ev_aux, 0), "stream wait");
+        HS_CU(ops.msm_tail(ctx, s.lo, bl), "MSM tail");
+        HS_CU(cudaStreamWaitEvent(st, ctx.ev_join, 0), "stream wait");
+        HS_CU(ops.join(ctx, bh.out_jac, bl.out_jac, d_final), "join");
+        HS_CU(ops.format_out(ctx, d_final, 1, out_fmt, d_out), "format");
     } else {
         BatchBuffers b;
         if (!carve(ctx.arena, p, b))
             return fail_msg(ctx, HS_ENOMEM, "workspace carve");
         b.scalars = (const uint32_t *)d_sc;
         b.points = (const uint4 *)d_pts;
-        rc = execute_batch(ctx, p, b, d_out, out_fmt);
+        HS_CU(cudaMemcpyAsync(b.desc, p.msms.data(), sizeof(MsmDesc), cudaMemcpyHostToDevice, st), "descriptors");
+        HS_CU(launch_sort(ctx, p, b), "sort");
+        HS_CU(cudaStreamWaitEvent(st, ctx.ev_aux, 0), "stream wait");
+        HS_CU(ops.msm_tail(ctx, p, b), "MSM tail");
+        HS_CU(ops.format_out(ctx, b.out_jac, 1, out_fmt, d_out), "format");
     }
     if (rc != HS_OK)
         return rc;
