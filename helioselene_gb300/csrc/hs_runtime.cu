@@ -1497,6 +1497,13 @@ int hs_context_set_split(hs_context *h, size_t min_points)
     return HS_OK;
 }
 
+// one launch sequence indexes its (point, window) entries with 31 bits
+static bool entries_fit(const Context &ctx, int curve, size_t n)
+{
+    const int c = choose_window(ctx, curve, n);
+    return (uint64_t)n * (uint64_t)((257 + c - 1) / c) < 0x80000000ull;
+}
+
 int hs_msm_device(hs_context *h, int curve, const void *d_scalars, const void *d_points, size_t n, void *d_out,
                   int out_fmt)
 {
@@ -1506,6 +1513,8 @@ int hs_msm_device(hs_context *h, int curve, const void *d_scalars, const void *d
         return HS_ERANGE;
     Context &ctx = h->c;
     std::lock_guard<std::mutex> lk(ctx.mu);
+    if (!entries_fit(ctx, curve, n))
+        return fail_msg(ctx, HS_ERANGE, "n x windows exceeds one launch sequence: sum partial MSMs of smaller slices");
     DeviceGuard g(ctx.device);
     if (n == 0) {
         unsigned char idb[128];
@@ -1541,8 +1550,8 @@ static int msm_host(Context &ctx, int curve, const uint8_t *lead_scalar, const v
         identity_out(curve, out_fmt, out);
         return HS_OK;
     }
-    if (total >= 0x80000000ull)
-        return fail_msg(ctx, HS_ERANGE, "n too large");
+    if (total >= 0x80000000ull || !entries_fit(ctx, curve, total))
+        return fail_msg(ctx, HS_ERANGE, "n x windows exceeds one launch sequence: sum partial MSMs of smaller slices");
     DeviceGuard g(ctx.device);
     const size_t pb = fmt_bytes(point_fmt);
     const CurveOps &ops = curve_ops(curve);

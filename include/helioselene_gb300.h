@@ -109,7 +109,10 @@ int hs_context_set_priority(hs_context *ctx, int high);
  * and HeliosPoint/SelenePoint::multi_scalar_mul (include/helioselene_point.h:166-167,
  * src/api_point.cpp:98-116, 202-220).
  * Host buffers.  out: one point in out_fmt (JACOBIAN51 or COMPRESSED or AFFINE).
- * n == 0 gives the identity, as in the reference (helios_msm_vartime.cpp:402-406). */
+ * n == 0 gives the identity, as in the reference (helios_msm_vartime.cpp:402-406).
+ * One call handles n x W(c) < 2^31 (point, window) entries, about 126M points
+ * at c = 16; beyond that it returns HS_ERANGE and the caller sums the results
+ * of slices (they add as points). */
 int hs_msm(hs_context *ctx, int curve, const uint8_t *scalars, const void *points, int point_fmt, size_t n,
            void *out, int out_fmt);
 
