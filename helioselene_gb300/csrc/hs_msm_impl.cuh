@@ -706,16 +706,19 @@ __global__ void k_jac_to_affine(const uint64_t *__restrict__ in, int fmt, size_t
                                 uint4 *__restrict__ scratch)
 {
     using F = typename C::F;
+    // thread t takes points t, t + T, t + 2T, ... (T threads in the grid, at most
+    // AFF_CHUNK points each): a warp reads consecutive records
     const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    const size_t lo = t * AFF_CHUNK;
-    if (lo >= n)
+    const size_t T = (size_t)gridDim.x * blockDim.x;
+    if (t >= n)
         return;
-    const size_t hi = lo + AFF_CHUNK < n ? lo + AFF_CHUNK : n;
+    const size_t cnt = (n - t + T - 1) / T;
     const size_t stride = (fmt == HS_FMT_JACOBIAN51) ? 15 : (fmt == HS_FMT_AFFINE51 ? 10 : 8);
     // pass 1: prefix products of the Z values that need inverting
     Fe run = F::one();
     bool any = false;
-    for (size_t i = lo; i < hi; i++) {
+    for (size_t j = 0; j < cnt; j++) {
+        const size_t i = t + j * T;
         Fe z;
         if (fmt == HS_FMT_JACOBIAN51) {
             z = fe_from_51<C>(in + stride * i + 10);
@@ -735,7 +738,8 @@ __global__ void k_jac_to_affine(const uint64_t *__restrict__ in, int fmt, size_t
     }
     Fe inv = any ? F::inv(run) : F::one();
     // pass 2: walk back
-    for (size_t i = hi; i-- > lo;) {
+    for (size_t j = cnt; j-- > 0;) {
+        const size_t i = t + j * T;
         Fe x, y;
         if (fmt == HS_FMT_JACOBIAN51) {
             x = fe_from_51<C>(in + stride * i);
@@ -761,7 +765,7 @@ __global__ void k_jac_to_affine(const uint64_t *__restrict__ in, int fmt, size_t
             if (is0) {
                 ident = true;
             } else if (!is1) {
-                Fe prev = (i > lo) ? load_fe(scratch + 2 * (i - 1)) : F::one();
+                Fe prev = (j > 0) ? load_fe(scratch + 2 * (i - T)) : F::one();
                 Fe zi = F::mul(inv, prev);  // 1/z
                 inv = F::mul(inv, z);
                 Fe zi2 = F::sqr(zi);
