@@ -762,6 +762,13 @@ def run_ours(args) -> None:
         prof_total["executed"] += pr["entries"] * (8 * IMAD_PER_MODMUL[curve] + 2 * IMAD_PER_MODSQR[curve])
 
     # ---- e2e: reference-facing call with host buffers ----
+    # Each e2e step is one isolated pair of calls (nothing of the next step
+    # overlaps its tail), so the contexts use the library's default window split,
+    # which shortens a lone MSM's tail.  The heavier Selene call is started first:
+    # the device's shared copy stream then delivers its inputs first.
+    e2e_split = SPLIT_DEFAULT if args.split is None else args.split
+    for c in ctxs.values():
+        c.set_split(e2e_split)
     e2e_steps = max(3, min(args.steps, 10))
     for _ in range(2):
         for curve in (hs.HELIOS, hs.SELENE):
@@ -774,12 +781,21 @@ def run_ours(args) -> None:
         # the two curves from two host threads (one context each), as a caller would overlap them
         ths = [threading.Thread(target=ctxs[c].msm, args=(c, data[c]["h_sc"].numpy(), data[c]["h_jac"].numpy(),
                                                          hs.FMT_JACOBIAN51, hs.FMT_JACOBIAN51))
-               for c in (hs.HELIOS, hs.SELENE)]
+               for c in (hs.SELENE, hs.HELIOS)]
         for t in ths:
             t.start()
         for t in ths:
             t.join()
     e2e_s = (time.perf_counter() - t0) / e2e_steps
+    for c in ctxs.values():
+        c.set_split(head_split)
+    # the same pair as one hs_msm_batch call (both curves, one context)
+    pair = [(c, data[c]["h_sc"].numpy(), data[c]["h_jac"].numpy()) for c in (hs.SELENE, hs.HELIOS)]
+    ctx.msm_batch(pair, hs.FMT_JACOBIAN51, hs.FMT_JACOBIAN51)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        ctx.msm_batch(pair, hs.FMT_JACOBIAN51, hs.FMT_JACOBIAN51)
+    e2e_batch_s = (time.perf_counter() - t0) / e2e_steps
     if dist:
         t = torch.tensor([e2e_s], dtype=torch.float64, device=device)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -831,7 +847,10 @@ def run_ours(args) -> None:
             "gpu_launches": launches,
             "e2e": {"value": ws * 2 * n / e2e_s, "unit": "points/s",
                     "h2d_bytes_per_step": 2 * n * (32 + 120), "d2h_bytes_per_step": 2 * 120,
-                    "api": "hs_msm(point_fmt=HS_FMT_JACOBIAN51, out_fmt=HS_FMT_JACOBIAN51), pinned host buffers"},
+                    "api": "hs_msm(point_fmt=HS_FMT_JACOBIAN51, out_fmt=HS_FMT_JACOBIAN51), pinned host buffers",
+                    "calls": "one per curve from two host threads, Selene first", "window_split_min": e2e_split,
+                    "one_batch_call": {"value": ws * 2 * n / e2e_batch_s, "unit": "points/s",
+                                       "api": "hs_msm_batch with both MSMs (HS_FMT_JACOBIAN51 in and out)"}},
             "roofline": {"bound": "imad", "achieved": achieved / 1e12, "peak": imad_peak / 1e12,
                          "unit": "T IMAD/s", "frac": achieved / imad_peak if imad_peak else None,
                          "traffic": ACC_TRAFFIC_BYTES, "traffic_unit": "bytes per launch (DRAM read + write)",

@@ -46,7 +46,12 @@ struct Context {
     cudaStream_t stream = nullptr;   // the stream every launch goes to
     cudaStream_t stream2 = nullptr;  // second curve group of a mixed batch, lower window half of a split MSM
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;  // fork/join of the two streams (created with stream2)
-    cudaEvent_t ev_aux = nullptr;                      // host-input path: bases ready on the second stream
+    // host-input path (created with stream2): inputs arrive on the device's link
+    // stream, the bases are converted on stream3
+    cudaStream_t stream3 = nullptr;
+    cudaEvent_t ev_sc = nullptr;   // scalars on the device
+    cudaEvent_t ev_rec = nullptr;  // input records on the device
+    cudaEvent_t ev_pts = nullptr;  // affine bases ready
     bool use_graphs = true;
     size_t split_min = size_t(1) << 18;  // single MSMs this large run as two window halves (0: never)
     std::vector<GraphEntry> graphs;
@@ -157,6 +162,7 @@ struct BatchBuffers {
     uint32_t *digits = nullptr;         // max_entries signed digits (|d| | sign << 31, 0 = none)
     uint4 *redS = nullptr;              // WS window sums
     uint32_t *out_jac = nullptr;        // M x 24 words: canonical Jacobian X, Y, Z
+    cudaEvent_t bases_ready = nullptr;  // host inputs: the accumulation waits for it (null: bases resident)
 };
 
 // index of the MSM owning element x of a batch: the largest m with key(m) <= x

@@ -594,6 +594,11 @@ cudaError_t msm_tail(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
         const int threads = 128;
         const uint64_t want = (p.max_segs + threads - 1) / threads;
         const int blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)ctx.sm_count * 32));
+        if (b.bases_ready) {  // host inputs: the bases arrive on another stream
+            const cudaError_t e = cudaStreamWaitEvent(st, b.bases_ready, 0);
+            if (e != cudaSuccess)
+                return e;
+        }
         cudaEvent_t ev0 = nullptr;
         prof_begin(ctx, &ev0);
         k_accumulate<C><<<blocks, threads, 0, st>>>(b.segs, b.seg_off + p.NB, b.sorted, b.points, b.seg_sum);

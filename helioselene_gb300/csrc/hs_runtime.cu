@@ -1219,9 +1219,52 @@ static cudaError_t ensure_stream2(Context &ctx)
         return e;
     if (!ctx.ev_join && (e = cudaEventCreateWithFlags(&ctx.ev_join, cudaEventDisableTiming)) != cudaSuccess)
         return e;
-    if (!ctx.ev_aux && (e = cudaEventCreateWithFlags(&ctx.ev_aux, cudaEventDisableTiming)) != cudaSuccess)
-        return e;
+    if (!ctx.stream3) {
+        int least = 0, greatest = 0;
+        if ((e = cudaDeviceGetStreamPriorityRange(&least, &greatest)) != cudaSuccess)
+            return e;
+        if ((e = cudaStreamCreateWithPriority(&ctx.stream3, cudaStreamNonBlocking, greatest)) != cudaSuccess)
+            return e;
+    }
+    for (cudaEvent_t *ev : {&ctx.ev_sc, &ctx.ev_rec, &ctx.ev_pts})
+        if (!*ev && (e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming)) != cudaSuccess)
+            return e;
     return e;
+}
+
+// The host-to-device input copies of every context on a device go to one
+// stream, in the order the calls issue them (one call's copies back to back
+// under the mutex).  Calls from several host threads then receive their inputs
+// one after another at the link's full rate, so the first can start computing
+// while the next is still arriving, instead of all of them sharing the link and
+// all starting late.  The streams live as long as the process.
+struct LinkStream {
+    std::mutex mu;
+    cudaStream_t s = nullptr;
+};
+
+static cudaError_t link_stream(int device, LinkStream **out)
+{
+    static std::mutex reg_mu;
+    static std::vector<LinkStream *> reg;
+    std::lock_guard<std::mutex> lk(reg_mu);
+    if (device < 0)
+        return cudaErrorInvalidDevice;
+    if (reg.size() <= (size_t)device)
+        reg.resize((size_t)device + 1, nullptr);
+    if (!reg[device]) {
+        LinkStream *ls = new (std::nothrow) LinkStream();
+        if (!ls)
+            return cudaErrorMemoryAllocation;
+        const cudaError_t e = cudaStreamCreateWithFlags(&ls->s, cudaStreamNonBlocking);
+        if (e != cudaSuccess) {
+            delete ls;
+            return e;
+        }
+        reg[device] = ls;
+    }
+    *out = reg[device];
+    return cudaSuccess;
 }
 
 struct SplitPlan {
@@ -1432,8 +1475,11 @@ void hs_context_destroy(hs_context *h)
             cudaEventDestroy(h->c.ev_fork);
         if (h->c.ev_join)
             cudaEventDestroy(h->c.ev_join);
-        if (h->c.ev_aux)
-            cudaEventDestroy(h->c.ev_aux);
+        if (h->c.stream3)
+            cudaStreamDestroy(h->c.stream3);
+        for (cudaEvent_t ev : {h->c.ev_sc, h->c.ev_rec, h->c.ev_pts})
+            if (ev)
+                cudaEventDestroy(ev);
     }
     delete h;
 }
@@ -1575,28 +1621,39 @@ static int msm_host(Context &ctx, int curve, const uint8_t *lead_scalar, const v
     uint8_t *d_raw = point_fmt == HS_FMT_AFFINE ? d_pts : d_pts + align256(total * 64);
     uint8_t *d_scratch = (point_fmt == HS_FMT_AFFINE ? d_pts + align256(total * 64) : d_raw + align256(total * pb));
     uint8_t *d_out = d_scratch + align256(ops.to_affine_scratch(total));
-    // Scalars go first on the context stream, the bases (copy and conversion) on
-    // the second stream: the counting sort needs only the scalars, so it runs
-    // while the bases are still arriving; the accumulation waits for them.
+    // Inputs go to the device's link stream, the scalars first: the counting
+    // sort needs only them, so it runs while the bases arrive; the bases are
+    // converted on the third stream and the accumulation waits for them.
     HS_CU(ensure_stream2(ctx), "stream creation");
-    cudaStream_t st = ctx.stream, s2 = ctx.stream2;
-    HS_CU(cudaEventRecord(ctx.ev_fork, st), "event");  // the second stream follows earlier work on the buffers
-    HS_CU(cudaStreamWaitEvent(s2, ctx.ev_fork, 0), "stream wait");
-    if (lead)
-        HS_CU(cudaMemcpyAsync(d_sc, lead_scalar, 32, cudaMemcpyHostToDevice, st), "H2D scalars");
-    if (n)
-        HS_CU(cudaMemcpyAsync(d_sc + 32 * lead, scalars, n * 32, cudaMemcpyHostToDevice, st), "H2D scalars");
-    if (lead)
-        HS_CU(cudaMemcpyAsync(d_raw, lead_point, pb, cudaMemcpyHostToDevice, s2), "H2D points");
-    if (n)
-        HS_CU(cudaMemcpyAsync(d_raw + pb * lead, points, n * pb, cudaMemcpyHostToDevice, s2), "H2D points");
+    LinkStream *link = nullptr;
+    HS_CU(link_stream(ctx.device, &link), "stream creation");
+    cudaStream_t st = ctx.stream, s2 = ctx.stream2, s3 = ctx.stream3;
+    HS_CU(cudaEventRecord(ctx.ev_fork, st), "event");  // earlier work on the buffers comes first
+    {
+        std::lock_guard<std::mutex> lk(link->mu);
+        cudaStream_t cs = link->s;
+        HS_CU(cudaStreamWaitEvent(cs, ctx.ev_fork, 0), "stream wait");
+        if (lead)
+            HS_CU(cudaMemcpyAsync(d_sc, lead_scalar, 32, cudaMemcpyHostToDevice, cs), "H2D scalars");
+        if (n)
+            HS_CU(cudaMemcpyAsync(d_sc + 32 * lead, scalars, n * 32, cudaMemcpyHostToDevice, cs), "H2D scalars");
+        HS_CU(cudaEventRecord(ctx.ev_sc, cs), "event");
+        if (lead)
+            HS_CU(cudaMemcpyAsync(d_raw, lead_point, pb, cudaMemcpyHostToDevice, cs), "H2D points");
+        if (n)
+            HS_CU(cudaMemcpyAsync(d_raw + pb * lead, points, n * pb, cudaMemcpyHostToDevice, cs), "H2D points");
+        HS_CU(cudaEventRecord(ctx.ev_rec, cs), "event");
+    }
+    cudaEvent_t bases_ready = ctx.ev_rec;
     if (point_fmt != HS_FMT_AFFINE) {
-        ctx.stream = s2;
+        HS_CU(cudaStreamWaitEvent(s3, ctx.ev_rec, 0), "stream wait");
+        ctx.stream = s3;
         const cudaError_t ce = ops.to_affine(ctx, d_raw, point_fmt, total, (uint4 *)d_pts, d_scratch);
         ctx.stream = st;
         HS_CU(ce, "input conversion");
+        HS_CU(cudaEventRecord(ctx.ev_pts, s3), "event");
+        bases_ready = ctx.ev_pts;
     }
-    HS_CU(cudaEventRecord(ctx.ev_aux, s2), "event");
     int rc = HS_OK;
     if (split) {
         BatchBuffers bh, bl;
@@ -1605,11 +1662,14 @@ static int msm_host(Context &ctx, int curve, const uint8_t *lead_scalar, const v
             return fail_msg(ctx, HS_ENOMEM, "workspace carve");
         bh.scalars = bl.scalars = (const uint32_t *)d_sc;
         bh.points = bl.points = (const uint4 *)d_pts;
+        bh.bases_ready = bl.bases_ready = bases_ready;
         HS_CU(cudaMemcpyAsync(bh.desc, s.hi.msms.data(), sizeof(MsmDesc), cudaMemcpyHostToDevice, st), "descriptors");
         HS_CU(cudaMemcpyAsync(bl.desc, s.lo.msms.data(), sizeof(MsmDesc), cudaMemcpyHostToDevice, st), "descriptors");
+        HS_CU(cudaStreamWaitEvent(st, ctx.ev_sc, 0), "stream wait");
         HS_CU(launch_sort(ctx, s.hi, bh), "sort");
         HS_CU(launch_sort(ctx, s.lo, bl), "sort");
-        // upper half on the second stream once both sorts are in: its bases are there already
+        // upper half on the second stream once both sorts are in (the accumulations
+        // wait for the bases)
         HS_CU(cudaEventRecord(ctx.ev_fork, st), "event");
         HS_CU(cudaStreamWaitEvent(s2, ctx.ev_fork, 0), "stream wait");
         ctx.stream = s2;
@@ -1617,7 +1677,6 @@ static int msm_host(Context &ctx, int curve, const uint8_t *lead_scalar, const v
         ctx.stream = st;
         HS_CU(te, "MSM tail");
         HS_CU(cudaEventRecord(ctx.ev_join, s2), "event");
-        HS_CU(cudaStreamWaitEvent(st, ctx.ev_aux, 0), "stream wait");
         HS_CU(ops.msm_tail(ctx, s.lo, bl), "MSM tail");
         HS_CU(cudaStreamWaitEvent(st, ctx.ev_join, 0), "stream wait");
         HS_CU(ops.join(ctx, bh.out_jac, bl.out_jac, d_final), "join");
@@ -1628,9 +1687,10 @@ static int msm_host(Context &ctx, int curve, const uint8_t *lead_scalar, const v
             return fail_msg(ctx, HS_ENOMEM, "workspace carve");
         b.scalars = (const uint32_t *)d_sc;
         b.points = (const uint4 *)d_pts;
+        b.bases_ready = bases_ready;
         HS_CU(cudaMemcpyAsync(b.desc, p.msms.data(), sizeof(MsmDesc), cudaMemcpyHostToDevice, st), "descriptors");
+        HS_CU(cudaStreamWaitEvent(st, ctx.ev_sc, 0), "stream wait");
         HS_CU(launch_sort(ctx, p, b), "sort");
-        HS_CU(cudaStreamWaitEvent(st, ctx.ev_aux, 0), "stream wait");
         HS_CU(ops.msm_tail(ctx, p, b), "MSM tail");
         HS_CU(ops.format_out(ctx, b.out_jac, 1, out_fmt, d_out), "format");
     }
@@ -1992,52 +2052,86 @@ int hs_msm_batch(hs_context *h, const hs_msm_desc *descs, size_t count, int poin
             return fail_msg(ctx, HS_ENOMEM, "workspace carve");
     }
     HS_CU(ensure_stream2(ctx), "stream creation");
-    cudaStream_t s1 = ctx.stream;
-    cudaEvent_t ev_in = nullptr, ev_done = nullptr;
-    HS_CU(cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming), "event");
-    HS_CU(cudaEventCreateWithFlags(&ev_done, cudaEventDisableTiming), "event");
+    LinkStream *link = nullptr;
+    HS_CU(link_stream(ctx.device, &link), "stream creation");
+    cudaStream_t s1 = ctx.stream, s3 = ctx.stream3;
+    // per curve group: inputs on the device, bases converted; and the join
+    cudaEvent_t ev_rec[2] = {}, ev_pts[2] = {}, ev_done = nullptr;
     struct EvGuard {
-        cudaEvent_t a, b;
+        cudaEvent_t *e[5];
         ~EvGuard()
         {
-            cudaEventDestroy(a);
-            cudaEventDestroy(b);
+            for (cudaEvent_t *p : e)
+                if (*p)
+                    cudaEventDestroy(*p);
         }
-    } evg{ev_in, ev_done};
+    } evg{{&ev_rec[0], &ev_rec[1], &ev_pts[0], &ev_pts[1], &ev_done}};
+    for (cudaEvent_t *p : evg.e)
+        HS_CU(cudaEventCreateWithFlags(p, cudaEventDisableTiming), "event");
+    // The group with more work (a Selene point costs about 1.6 Helios points)
+    // is staged first on the device's link stream: its computation starts while
+    // the other group's inputs are still arriving.
+    const int first = totals[1] * 8 >= totals[0] * 5 ? 1 : 0;
+    const int order[2] = {first, 1 - first};
     uint8_t *d_out[2] = {nullptr, nullptr};
+    uint8_t *d_raw_k[2] = {nullptr, nullptr};
     uint8_t *d_scr_k[2] = {nullptr, nullptr};
-    // stage inputs (all copies on the first stream)
     for (int k = 0; k < 2; k++) {
         if (idx[k].empty())
             continue;
         const size_t t = std::max<size_t>(1, totals[k]);
         uint8_t *d_sc = st_base[k];
         uint8_t *d_pts = d_sc + align256(t * 32);
-        uint8_t *d_raw = point_fmt == HS_FMT_AFFINE ? d_pts : d_pts + align256(t * 64);
-        uint8_t *d_scr = point_fmt == HS_FMT_AFFINE ? d_pts + align256(t * 64) : d_raw + align256(t * pb);
-        d_out[k] = d_scr + align256(curve_ops(k).to_affine_scratch(t));
-        d_scr_k[k] = d_scr;
-        size_t off = 0;
-        for (size_t j = 0; j < idx[k].size(); j++) {
-            const hs_msm_desc &d = descs[idx[k][j]];
-            if (d.n) {
-                HS_CU(cudaMemcpyAsync(d_sc + 32 * off, d.scalars, d.n * 32, cudaMemcpyHostToDevice, s1), "H2D");
-                HS_CU(cudaMemcpyAsync(d_raw + pb * off, d.points, d.n * pb, cudaMemcpyHostToDevice, s1), "H2D");
-            }
-            off += d.n;
-        }
-        if (point_fmt != HS_FMT_AFFINE && totals[k])
-            HS_CU(curve_ops(k).to_affine(ctx, d_raw, point_fmt, totals[k], (uint4 *)d_pts, d_scr), "conversion");
+        d_raw_k[k] = point_fmt == HS_FMT_AFFINE ? d_pts : d_pts + align256(t * 64);
+        d_scr_k[k] = point_fmt == HS_FMT_AFFINE ? d_pts + align256(t * 64) : d_raw_k[k] + align256(t * pb);
+        d_out[k] = d_scr_k[k] + align256(curve_ops(k).to_affine_scratch(t));
         bufs[k].scalars = (const uint32_t *)d_sc;
         bufs[k].points = (const uint4 *)d_pts;
     }
-    HS_CU(cudaEventRecord(ev_in, s1), "event");
-    // Helios group on the first stream, Selene group on the second
+    HS_CU(cudaEventRecord(ctx.ev_fork, s1), "event");  // earlier work on the buffers comes first
+    {
+        std::lock_guard<std::mutex> lk(link->mu);
+        cudaStream_t cs = link->s;
+        HS_CU(cudaStreamWaitEvent(cs, ctx.ev_fork, 0), "stream wait");
+        for (int k : order) {
+            if (idx[k].empty())
+                continue;
+            size_t off = 0;
+            for (size_t j = 0; j < idx[k].size(); j++) {
+                const hs_msm_desc &d = descs[idx[k][j]];
+                if (d.n) {
+                    HS_CU(cudaMemcpyAsync((uint8_t *)bufs[k].scalars + 32 * off, d.scalars, d.n * 32,
+                                          cudaMemcpyHostToDevice, cs),
+                          "H2D");
+                    HS_CU(cudaMemcpyAsync(d_raw_k[k] + pb * off, d.points, d.n * pb, cudaMemcpyHostToDevice, cs),
+                          "H2D");
+                }
+                off += d.n;
+            }
+            HS_CU(cudaEventRecord(ev_rec[k], cs), "event");
+        }
+    }
+    for (int k : order) {
+        if (idx[k].empty())
+            continue;
+        HS_CU(cudaStreamWaitEvent(s3, ev_rec[k], 0), "stream wait");
+        if (point_fmt != HS_FMT_AFFINE && totals[k]) {
+            ctx.stream = s3;
+            const cudaError_t ce = curve_ops(k).to_affine(ctx, d_raw_k[k], point_fmt, totals[k],
+                                                          (uint4 *)bufs[k].points, d_scr_k[k]);
+            ctx.stream = s1;
+            HS_CU(ce, "conversion");
+        }
+        HS_CU(cudaEventRecord(ev_pts[k], s3), "event");
+    }
+    // Helios group on the first stream, Selene group on the second, each after its inputs
     int rc = HS_OK;
-    if (!idx[0].empty())
+    if (!idx[0].empty()) {
+        HS_CU(cudaStreamWaitEvent(s1, ev_pts[0], 0), "stream wait");
         rc = execute_batch(ctx, plans[0], bufs[0], d_out[0], out_fmt);
+    }
     if (rc == HS_OK && !idx[1].empty()) {
-        HS_CU(cudaStreamWaitEvent(ctx.stream2, ev_in, 0), "stream wait");
+        HS_CU(cudaStreamWaitEvent(ctx.stream2, ev_pts[1], 0), "stream wait");
         ctx.stream = ctx.stream2;
         rc = execute_batch(ctx, plans[1], bufs[1], d_out[1], out_fmt);
         ctx.stream = s1;

@@ -300,3 +300,62 @@ def test_window_split_matches_unsplit(ctx, curve):
     finally:
         ctx.set_window(curve, 0, 0, 0)
     assert ctx.msm(curve, zero, pts) == bytes(32)
+
+
+def _to_fe51_rows(v32: np.ndarray) -> np.ndarray:
+    """(n, 32) little-endian field elements -> (n, 5) radix-2^51 limbs"""
+    w = np.ascontiguousarray(v32).view(np.uint64).reshape(-1, 4)
+    m = np.uint64((1 << 51) - 1)
+    out = np.empty((w.shape[0], 5), np.uint64)
+    out[:, 0] = w[:, 0] & m
+    out[:, 1] = ((w[:, 0] >> np.uint64(51)) | (w[:, 1] << np.uint64(13))) & m
+    out[:, 2] = ((w[:, 1] >> np.uint64(38)) | (w[:, 2] << np.uint64(26))) & m
+    out[:, 3] = ((w[:, 2] >> np.uint64(25)) | (w[:, 3] << np.uint64(39))) & m
+    out[:, 4] = w[:, 3] >> np.uint64(12)
+    return out
+
+
+@pytest.mark.parametrize("curve", [0, 1])
+def test_host_inputs_every_format(ctx, curve):
+    """hs_msm / hs_pedersen with host buffers at n = 3 * 2^17 + 1: the inputs
+    come over the device's shared copy stream, the scalars first (the sort
+    starts on them), the bases converted on a third stream.  Every input
+    format, window split on and off, and a Pedersen lead term, against the
+    batched path (which stages its inputs whole)."""
+    import helioselene_gb300 as hs
+    from helioselene_gb300.workload import make_workload
+    n = 3 * (1 << 17) + 1
+    w = make_workload(curve, n, seed=4242 + curve, edge_fraction=0.01)
+    pts = ctx.map_to_curve(curve, w.u, HS_AFF).reshape(n, 64)
+    sc = w.scalars
+    want = ctx.msm_batch([(curve, sc, pts)])[0]
+    # reference records: Z = 1 for most points, random Z for a sample, Z = 0
+    # (the identity) for a few, across every part
+    F = pyref.CURVES["helios" if curve == 0 else "selene"].F
+    x51, y51 = _to_fe51_rows(pts[:, :32]), _to_fe51_rows(pts[:, 32:])
+    jac = np.zeros((n, 15), np.uint64)
+    jac[:, 0:5], jac[:, 5:10], jac[:, 10] = x51, y51, 1
+    rng = random.Random(9)
+    for i in range(0, n, 977):
+        x = int.from_bytes(pts[i, :32].tobytes(), "little")
+        y = int.from_bytes(pts[i, 32:].tobytes(), "little")
+        z = rng.randrange(2, F)
+        jac[i] = hs.int_to_fe51(x * z * z % F) + hs.int_to_fe51(y * z * z * z % F) + hs.int_to_fe51(z)
+    ident = np.arange(5, n, 65537)
+    jac[ident] = 0
+    jac[ident, 0] = jac[ident, 5] = 1
+    pts_id = pts.copy()
+    pts_id[ident] = 0
+    want_id = ctx.msm_batch([(curve, sc, pts_id)])[0]
+    aff51 = np.concatenate([x51, y51], axis=1)
+    try:
+        for split in (1 << 18, 0):
+            ctx.set_split(split)
+            assert ctx.msm(curve, sc, pts) == want, f"affine, split {split}"
+            assert ctx.msm(curve, sc, aff51.view(np.uint8), HS_AFF51) == want, f"affine51, split {split}"
+            assert ctx.msm(curve, sc, jac.view(np.uint8), HS_JAC51) == want_id, f"jacobian51, split {split}"
+            assert ctx.pedersen(curve, sc[0], pts[0], sc[1:], pts[1:]) == want, f"pedersen, split {split}"
+            assert ctx.pedersen(curve, sc[0], jac[0].view(np.uint8), sc[1:], jac[1:].view(np.uint8),
+                                HS_JAC51) == want_id, f"pedersen jacobian51, split {split}"
+    finally:
+        ctx.set_split(1 << 18)
