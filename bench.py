@@ -533,6 +533,100 @@ def run_tree(hs, torch, device: str, local: int, nodes: int = 8192) -> dict:
     return out
 
 
+def run_verify(hs, torch, device: str, local: int, with_cpu: bool, batch_count: int = 256) -> dict:
+    """FCMP++ verification (src/benchmark_fcmpp.cpp:350-439): a batch of proofs
+    verifies with one Selene MSM of 522 + 80*batch terms and one Helios MSM of
+    265 + 80*batch terms.  Per batch size:
+      - the pair of calls from host buffers of reference records (hs_msm, the
+        helios_msm_vartime / selene_msm_vartime signature), one after the other
+        as the reference benchmark calls them, results read back;
+      - the pair on the device, the two MSMs overlapping on two contexts;
+      - `batch_count` independent verifications as one batched launch sequence
+        per curve (hs_msm_batch_device);
+      - the oracle on one host core for one pair (the reference's algorithm)."""
+    from helioselene_gb300.workload import ORDER, random_field_bytes, random_scalars
+    rng = np.random.default_rng(SEED + 11)
+    H, S = hs.HELIOS, hs.SELENE
+    ctxs = {H: hs.Context(local), S: hs.Context(local)}
+    ctxs[S].set_priority(True)
+    streams = {c: torch.cuda.ExternalStream(x.stream, device=device) for c, x in ctxs.items()}
+    V = batch_count
+    out = {"batched_verifications": V}
+    if with_cpu:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import oracle
+
+    def pair_timed(launch):
+        start = torch.cuda.Event(enable_timing=True)
+        ends = {c: torch.cuda.Event(enable_timing=True) for c in streams}
+        start.record(streams[H])
+        streams[S].wait_event(start)
+        for c in (S, H):
+            launch(c)
+            ends[c].record(streams[c])
+        for st in streams.values():
+            st.synchronize()
+        return max(start.elapsed_time(e) for e in ends.values())
+
+    for batch in (1, 2, 4, 10):
+        sizes = {S: 522 + 80 * batch, H: 265 + 80 * batch}
+        g = {}
+        for c, n in sizes.items():
+            d_u = torch.from_numpy(random_field_bytes(rng, n * V).reshape(-1)).to(device)
+            d_pts = torch.empty(n * V * 64, dtype=torch.uint8, device=device)
+            torch.cuda.synchronize()
+            ctxs[c].map_to_curve_device(c, d_u.data_ptr(), n * V, d_pts.data_ptr())
+            d_sc = torch.from_numpy(random_scalars(rng, n * V, ORDER[c]).reshape(-1)).to(device)
+            torch.cuda.synchronize()
+            aff = d_pts[:n * 64].cpu().numpy()
+            g[c] = {"n": n, "d_sc": d_sc, "d_pts": d_pts, "h_sc": d_sc[:n * 32].cpu().numpy(), "aff": aff,
+                    "h_jac": affine_to_jac51_fast(aff, n),
+                    "d_out": torch.empty(V * 120, dtype=torch.uint8, device=device)}
+
+        def host_pair():
+            return [ctxs[c].msm(c, g[c]["h_sc"], g[c]["h_jac"], hs.FMT_JACOBIAN51, hs.FMT_JACOBIAN51) for c in (S, H)]
+
+        for _ in range(3):
+            got = host_pair()
+        ts = []
+        for _ in range(20):
+            t0 = time.perf_counter()
+            host_pair()
+            ts.append(time.perf_counter() - t0)
+        host_ms = statistics.median(ts) * 1e3
+
+        def dev(c):
+            ctxs[c].msm_device(c, g[c]["d_sc"].data_ptr(), g[c]["d_pts"].data_ptr(), g[c]["n"],
+                               g[c]["d_out"].data_ptr(), hs.FMT_JACOBIAN51)
+
+        for _ in range(3):
+            pair_timed(dev)
+        dev_ms = statistics.median([pair_timed(dev) for _ in range(20)])
+
+        def bat(c):
+            ctxs[c].msm_batch_device(c, [g[c]["n"]] * V, g[c]["d_sc"].data_ptr(), g[c]["d_pts"].data_ptr(),
+                                     g[c]["d_out"].data_ptr(), hs.FMT_JACOBIAN51)
+
+        pair_timed(bat)  # capture the graphs
+        bat_ms = statistics.median([pair_timed(bat) for _ in range(5)])
+        # the batched results' first verification against the per-call pair
+        exact = all((ctxs[c].compress(c, g[c]["d_out"][:120].cpu().numpy(), hs.FMT_JACOBIAN51) ==
+                     ctxs[c].compress(c, np.frombuffer(got[k], np.uint8), hs.FMT_JACOBIAN51)).all()
+                    for k, c in enumerate((S, H)))
+        row = {"selene_n": sizes[S], "helios_n": sizes[H], "host_pair_ms": host_ms, "device_pair_ms": dev_ms,
+               "batched_ms": bat_ms, "verifications_per_s": V / (bat_ms * 1e-3), "bit_exact_batched_vs_call": exact}
+        if with_cpu:
+            t0 = time.perf_counter()
+            want = [oracle.msm(c, g[c]["h_sc"].reshape(-1, 32), g[c]["aff"].reshape(-1, 64)) for c in (S, H)]
+            row["cpu_port_pair_ms_1core"] = (time.perf_counter() - t0) * 1e3
+            row["bit_exact_vs_oracle"] = all(ctxs[c].msm(c, g[c]["h_sc"], g[c]["aff"]) == want[k]
+                                             for k, c in enumerate((S, H)))
+        out[f"batch={batch}"] = row
+    for c in ctxs.values():
+        c.close()
+    return out
+
+
 def run_scalar_mul(hs, torch, ctxs, data, n: int, flush) -> dict:
     """Independent variable-time scalar multiplications s_i P_i (the n = 1 MSM of
     the serving path, helios_scalarmult_vartime) over the bench's scalars and
@@ -820,6 +914,9 @@ def run_ours(args) -> None:
     tree = None
     if not args.no_tree:
         tree = run_tree(hs, torch, device, local)
+    verify = None
+    if not args.no_verify:
+        verify = run_verify(hs, torch, device, local, with_cpu=(ws == 1 and not args.no_cpu))
     sweep = None
     if not args.no_sweep:
         sweep = run_sweep(hs, torch, device, local, flush)
@@ -880,6 +977,8 @@ def run_ours(args) -> None:
             line["sweep"] = sweep
         if not args.no_tree:
             line["tree_hash"] = tree
+        if not args.no_verify:
+            line["fcmpp_verify"] = verify
         if not args.no_scalar_mul:
             line["scalar_mul"] = smul
         if ws == 1 and not args.no_cpu:
@@ -942,6 +1041,7 @@ def main() -> None:
     ap.add_argument("--no-decompress", action="store_true", help="skip the point-decoding section")
     ap.add_argument("--no-sweep", action="store_true", help="skip the n = 2^10 .. 2^22 single-MSM sweep")
     ap.add_argument("--no-tree", action="store_true", help="skip the FCMP++ tree-hash layer section")
+    ap.add_argument("--no-verify", action="store_true", help="skip the FCMP++ verification-batch section")
     ap.add_argument("--no-scalar-mul", action="store_true", help="skip the independent scalar-multiplication section")
     ap.add_argument("--split", type=int, default=None,
                     help="window-split threshold in points for single MSMs (0: off; default: the library's)")

@@ -35,6 +35,21 @@ def test_host_batch_mixed_curves(ctx):
     assert not bad, f"mismatching MSMs: {bad[:10]}"
 
 
+@pytest.mark.parametrize("batch", [1, 4, 10])
+def test_fcmpp_verification_shapes(ctx, batch):
+    """FCMP++ verification of `batch` proofs (src/benchmark_fcmpp.cpp:350-439):
+    one Selene MSM of 522 + 80*batch terms and one Helios MSM of 265 + 80*batch,
+    as two single calls from reference records and as one mixed-curve batch of
+    three verifications; batch = 10 puts both sizes in the reference's w = 8
+    band, where the GPU gives the exact sum."""
+    import helioselene_gb300 as hs
+    sizes = [522 + 80 * batch, 265 + 80 * batch] * 3
+    items, want = _batch(4000 + batch, sizes, [1, 0] * 3)
+    for (c, sc, pts), w in list(zip(items, want))[:2]:
+        assert ctx.msm(c, sc, hs.affine64_to_jac51(pts), HS_JAC51, HS_COMPRESSED) == w
+    assert ctx.msm_batch(items, HS_AFF, HS_COMPRESSED) == want
+
+
 def test_host_batch_reference_records(ctx):
     import helioselene_gb300 as hs
     sizes = [5, 300, 2000]
