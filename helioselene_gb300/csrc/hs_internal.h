@@ -20,6 +20,10 @@ struct DeviceArena {
     char *base = nullptr;
     size_t cap = 0;
     size_t off = 0;
+    // When set, the arena is allocated and freed in the order of this stream
+    // (stream-ordered allocator), so growing it does not synchronise the device
+    // and stall the work of other streams.
+    cudaStream_t ordered = nullptr;
     cudaError_t reserve(size_t bytes);
     void *take(size_t bytes);
     void reset() { off = 0; }

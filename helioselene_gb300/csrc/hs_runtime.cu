@@ -40,14 +40,15 @@ cudaError_t DeviceArena::reserve(size_t bytes)
     if (bytes <= cap)
         return cudaSuccess;
     if (base) {
-        cudaError_t e = cudaFree(base);
+        cudaError_t e = ordered ? cudaFreeAsync(base, ordered) : cudaFree(base);
         base = nullptr;
         cap = 0;
         if (e != cudaSuccess)
             return e;
     }
     size_t want = bytes + bytes / 8;
-    cudaError_t e = cudaMalloc(reinterpret_cast<void **>(&base), want);
+    cudaError_t e = ordered ? cudaMallocAsync(reinterpret_cast<void **>(&base), want, ordered)
+                            : cudaMalloc(reinterpret_cast<void **>(&base), want);
     if (e != cudaSuccess) {
         cudaGetLastError();
         base = nullptr;
@@ -68,8 +69,14 @@ void *DeviceArena::take(size_t bytes)
 
 void DeviceArena::release()
 {
-    if (base)
-        cudaFree(base);
+    if (base) {
+        if (ordered) {
+            cudaFreeAsync(base, ordered);
+            cudaStreamSynchronize(ordered);
+        } else {
+            cudaFree(base);
+        }
+    }
     base = nullptr;
     cap = off = 0;
 }

@@ -351,6 +351,8 @@ int hs_server_create(hs_server **out, const hs_server_config *cfg)
         cudaGetLastError();
         return HS_ECUDA;
     }
+    int pools = 0;
+    cudaDeviceGetAttribute(&pools, cudaDevAttrMemoryPoolsSupported, S.cfg.device);
     for (int i = 0; i < S.cfg.slots; i++) {
         auto sl = std::make_unique<Slot>();
         sl->ctx.device = S.cfg.device;
@@ -361,6 +363,10 @@ int hs_server_create(hs_server **out, const hs_server_config *cfg)
             cudaGetLastError();
             return HS_ECUDA;
         }
+        // a slot's workspace grows in its own stream's order: a larger batch on
+        // one slot does not stall the batches in flight on the others
+        if (pools)
+            sl->ctx.arena.ordered = sl->ctx.stream;
         S.slots.push_back(std::move(sl));
     }
     S.thr = std::thread(scheduler, &S);
