@@ -266,7 +266,8 @@ def run_serving(hs, torch, device: str, local: int, requests_per_rate: int = 100
     """Config 4: Poisson arrivals of MSM requests, sizes from the mixture 70%
     log-uniform [256, 4096], 25% [4096, 65536], 5% 2^18, curves alternating;
     75% of each request's bases come from a 2^18-point resident pool per curve,
-    25% are fresh points sent with the request.  Continuous batching (4 slots)
+    25% are fresh points sent with the request.  Continuous batching (8 slots,
+    batches of up to 2^23 points)
     against the plain path: the same requests one MSM per launch sequence, one
     at a time (a server with one slot and one request per batch)."""
     from helioselene_gb300.workload import ORDER, random_field_bytes, random_scalars
@@ -336,7 +337,7 @@ def run_serving(hs, torch, device: str, local: int, requests_per_rate: int = 100
     out = {"requests_per_rate": requests_per_rate, "pool_points_per_curve": pool_n,
            "mix": "70% [256,4096], 25% [4096,65536], 5% 2^18 log-uniform; 75% pool bases, 25% fresh",
            "plain": "same requests, one MSM per launch sequence, one at a time", "rates": []}
-    srv = hs.Server(local, slots=4, max_batch_points=1 << 22, max_batch_msms=1024)
+    srv = hs.Server(local, slots=8, max_batch_points=1 << 23, max_batch_msms=1024)
     plain = hs.Server(local, slots=1, max_batch_msms=1)
     for s in (srv, plain):
         for c in (hs.HELIOS, hs.SELENE):

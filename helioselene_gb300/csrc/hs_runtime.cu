@@ -1472,7 +1472,12 @@ void hs_context_destroy(hs_context *h)
         return;
     {
         DeviceGuard g(h->c.device);
+        // every stream that may still use the workspace finishes first
         cudaStreamSynchronize(h->c.stream);
+        if (h->c.stream2)
+            cudaStreamSynchronize(h->c.stream2);
+        if (h->c.stream3)
+            cudaStreamSynchronize(h->c.stream3);
         drop_graphs(h->c);
         h->c.arena.release();
         cudaStreamDestroy(h->c.stream);
