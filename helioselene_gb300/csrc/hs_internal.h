@@ -54,8 +54,8 @@ struct Context {
     // stream, the bases are converted on stream3
     cudaStream_t stream3 = nullptr;
     cudaEvent_t ev_sc = nullptr;   // scalars on the device
-    cudaEvent_t ev_rec = nullptr;  // input records on the device
-    cudaEvent_t ev_pts = nullptr;  // affine bases ready
+    cudaEvent_t ev_rec[2] = {};    // input records on the device (per part)
+    cudaEvent_t ev_pts[2] = {};    // affine bases ready (per part)
     bool use_graphs = true;
     size_t split_min = size_t(1) << 18;  // single MSMs this large run as two window halves (0: never)
     std::vector<GraphEntry> graphs;
@@ -141,6 +141,11 @@ struct BatchPlan {
     uint32_t max_entries = 0;
     uint32_t max_segs = 0;
     uint32_t hist_blocks = 0;   // blocks of the segment-length histogram
+    // > 0: host inputs arrive in two parts, points below and above counting-sort
+    // slice part_slice (one MSM, shared-memory sort).  Every bucket then has
+    // its own segments per part, in two longest-first lists; a bucket's first
+    // part-1 segment continues the sum of its first part-0 segment.
+    uint32_t part_slice = 0;
     uint64_t entries_bound = 0; // sum n_i * W_i
 };
 
@@ -166,7 +171,9 @@ struct BatchBuffers {
     uint32_t *digits = nullptr;         // max_entries signed digits (|d| | sign << 31, 0 = none)
     uint4 *redS = nullptr;              // WS window sums
     uint32_t *out_jac = nullptr;        // M x 24 words: canonical Jacobian X, Y, Z
-    cudaEvent_t bases_ready = nullptr;  // host inputs: the accumulation waits for it (null: bases resident)
+    uint32_t *counts0 = nullptr;        // NB part-0 entry counts (plans with part_slice)
+    // host inputs: the accumulation of part j waits for ready[j] (null: bases resident)
+    cudaEvent_t ready[2] = {nullptr, nullptr};
 };
 
 // index of the MSM owning element x of a batch: the largest m with key(m) <= x

@@ -70,19 +70,23 @@ __device__ __forceinline__ Xyzz load_xyzz(const uint4 *o)
 
 // ---------------------------------------------------------------------------
 // 2. bucket accumulation: one thread per segment of <= L entries (segments come
-//    longest first, so the lanes of a warp do equal work)
+//    longest first, so the lanes of a warp do equal work).  The launch takes the
+//    descriptors [*seg_lo, *seg_hi) (device values: one list, or one part of
+//    host inputs in two parts); with RESUME, a descriptor with d.w set
+//    continues the sum stored in its slot by the earlier part.
 // ---------------------------------------------------------------------------
-template <class C>
-__global__ void __launch_bounds__(128) k_accumulate(const uint4 *__restrict__ segs, const uint32_t *__restrict__ seg_total,
+template <class C, bool RESUME>
+__global__ void __launch_bounds__(128) k_accumulate(const uint4 *__restrict__ segs, const uint32_t *__restrict__ seg_lo,
+                                                   const uint32_t *__restrict__ seg_hi,
                                                    const uint32_t *__restrict__ sorted, const uint4 *__restrict__ pts,
                                                    uint4 *__restrict__ seg_sum)
 {
     using G = Group<C>;
     using F = typename C::F;
-    const uint32_t S = *seg_total;
-    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < S; s += gridDim.x * blockDim.x) {
-        const uint4 d = segs[s];  // start, length, destination slot
-        Xyzz acc = G::inf();
+    const uint32_t S0 = *seg_lo, S = *seg_hi;
+    for (uint32_t s = S0 + blockIdx.x * blockDim.x + threadIdx.x; s < S; s += gridDim.x * blockDim.x) {
+        const uint4 d = segs[s];  // start, length, destination slot, continue
+        Xyzz acc = (RESUME && d.w) ? load_xyzz(seg_sum + 8 * (size_t)d.z) : G::inf();
         for (uint32_t i = 0; i < d.y; i++) {
             const uint32_t e = __ldg(sorted + d.x + i);
             Fe x, y;
@@ -594,16 +598,28 @@ cudaError_t msm_tail(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
         const int threads = 128;
         const uint64_t want = (p.max_segs + threads - 1) / threads;
         const int blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)ctx.sm_count * 32));
-        if (b.bases_ready) {  // host inputs: the bases arrive on another stream
-            const cudaError_t e = cudaStreamWaitEvent(st, b.bases_ready, 0);
-            if (e != cudaSuccess)
-                return e;
+        // the segment lists: [0, total), or per part [0, P1) and [P1, total) with P1
+        // the scan position where the part-1 histogram starts
+        const size_t nh = (size_t)(p.L + 1) * p.hist_blocks * (p.part_slice ? 2 : 1);
+        const int parts = p.part_slice ? 2 : 1;
+        const uint32_t *bound[3] = {b.len_scan, b.len_scan + (p.part_slice ? nh / 2 : nh), b.len_scan + nh};
+        for (int j = 0; j < parts; j++) {
+            if (b.ready[j]) {  // host inputs: this part of the bases arrives on another stream
+                const cudaError_t e = cudaStreamWaitEvent(st, b.ready[j], 0);
+                if (e != cudaSuccess)
+                    return e;
+            }
+            cudaEvent_t ev0 = nullptr;
+            prof_begin(ctx, &ev0);
+            if (j == 0)
+                k_accumulate<C, false><<<blocks, threads, 0, st>>>(b.segs, bound[0], bound[1], b.sorted, b.points,
+                                                                   b.seg_sum);
+            else
+                k_accumulate<C, true><<<blocks, threads, 0, st>>>(b.segs, bound[1], bound[2], b.sorted, b.points,
+                                                                  b.seg_sum);
+            HS_LAUNCH_CHECK(ctx);
+            prof_end(ctx, ev0, j == 0 ? p.entries_bound : 0);
         }
-        cudaEvent_t ev0 = nullptr;
-        prof_begin(ctx, &ev0);
-        k_accumulate<C><<<blocks, threads, 0, st>>>(b.segs, b.seg_off + p.NB, b.sorted, b.points, b.seg_sum);
-        HS_LAUNCH_CHECK(ctx);
-        prof_end(ctx, ev0, p.entries_bound);
     }
     // 3. merge multi-segment buckets
     {

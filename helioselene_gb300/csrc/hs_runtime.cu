@@ -341,7 +341,7 @@ static constexpr uint32_t SCAN_BLOCK = SCAN_THREADS * SCAN_ITEMS;
 
 static uint32_t scan_blocks(uint32_t NB) { return (NB + SCAN_BLOCK - 1) / SCAN_BLOCK; }
 
-static size_t hist_len(const BatchPlan &p) { return (size_t)(p.L + 1) * p.hist_blocks; }
+static size_t hist_len(const BatchPlan &p) { return (size_t)(p.L + 1) * p.hist_blocks * (p.part_slice ? 2 : 1); }
 
 size_t batch_bytes(const BatchPlan &p)
 {
@@ -361,6 +361,7 @@ size_t batch_bytes(const BatchPlan &p)
     b += p.smem_sort() ? align256((size_t)p.max_entries * 4) : 0;                            // signed digits
     b += align256((size_t)std::max<uint32_t>(1, p.WS) * 128);                              // window sums
     b += align256((size_t)std::max<uint32_t>(1, p.M) * 96);                                // results
+    b += p.part_slice ? align256((size_t)(p.NB + 1) * 4) : 0;                                // part-0 counts
     return b + 16 * 256;
 }
 
@@ -385,9 +386,10 @@ bool carve(DeviceArena &a, const BatchPlan &p, BatchBuffers &b)
     b.digits = p.smem_sort() ? (uint32_t *)a.take((size_t)p.max_entries * 4) : nullptr;
     b.redS = (uint4 *)a.take((size_t)std::max<uint32_t>(1, p.WS) * 128);
     b.out_jac = (uint32_t *)a.take((size_t)std::max<uint32_t>(1, p.M) * 96);
+    b.counts0 = p.part_slice ? (uint32_t *)a.take((size_t)(p.NB + 1) * 4) : nullptr;
     return b.desc && b.counts && b.offsets && b.seg_off && b.scan_tmp && b.len_hist && b.len_scan && b.sorted &&
            b.segs && b.seg_sum && b.heavy && b.heavy_n && b.redA && b.redC && b.redS && b.out_jac &&
-           ((b.sort_cnt && b.digits) || !p.smem_sort());
+           ((b.sort_cnt && b.digits) || !p.smem_sort()) && (b.counts0 || !p.part_slice);
 }
 
 // ---------------------------------------------------------------------------
@@ -630,7 +632,8 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_count(const uint32_t *__r
 // rows into first slots from offsets (mode 1)
 template <int MODE>
 __global__ void k_sort_rows(const MsmDesc *__restrict__ desc, uint32_t M, uint32_t NB, uint32_t *__restrict__ cnt,
-                            uint32_t *__restrict__ counts, const uint32_t *__restrict__ offsets)
+                            uint32_t *__restrict__ counts, const uint32_t *__restrict__ offsets, uint32_t qsplit,
+                            uint32_t *__restrict__ counts0)
 {
     const uint32_t kb = blockIdx.x * blockDim.x + threadIdx.x;
     if (kb >= NB)
@@ -642,6 +645,7 @@ __global__ void k_sort_rows(const MsmDesc *__restrict__ desc, uint32_t M, uint32
     const uint32_t Q = d.fixed ? d.w_cnt * d.slices : d.slices;
     uint32_t *col = cnt + d.cnt_base + lb;
     uint32_t run = MODE == 0 ? 0u : offsets[kb];
+    uint32_t c0 = 0;  // entries of the rows below qsplit (host inputs in two parts)
     for (uint32_t q0 = 0; q0 < Q; q0 += 8) {  // eight loads in flight, then their sums
         uint32_t v[8];
 #pragma unroll
@@ -651,11 +655,16 @@ __global__ void k_sort_rows(const MsmDesc *__restrict__ desc, uint32_t M, uint32
         for (int u = 0; u < 8; u++) {
             if (MODE == 1 && q0 + u < Q)
                 col[(uint64_t)(q0 + u) * Bm] = run;
+            if (MODE == 0 && q0 + u == qsplit)
+                c0 = run;
             run += v[u];
         }
     }
-    if (MODE == 0)
+    if (MODE == 0) {
         counts[kb] = run;
+        if (counts0)
+            counts0[kb] = qsplit < Q ? c0 : run;
+    }
 }
 
 __global__ void __launch_bounds__(SORT_THREADS) k_sort_scatter(const uint32_t *__restrict__ digits,
@@ -738,9 +747,18 @@ __device__ __forceinline__ uint2 block_excl_scan(uint2 v, uint2 *total)
     return make_uint2(wp.x + inc.x - v.x, wp.y + inc.y - v.y);
 }
 
+// destination slots of a bucket of c entries, c0 of them in part 0 of host
+// inputs in two parts: its segments per part, less one when both parts have
+// some (the first part-1 segment continues the first part-0 segment's sum)
+__device__ __forceinline__ uint32_t part_slots(uint32_t c, uint32_t c0, uint32_t L)
+{
+    const uint32_t c1 = c - c0;
+    return (c0 + L - 1) / L + (c1 + L - 1) / L - ((c0 && c1) ? 1u : 0u);
+}
+
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_a(const uint32_t *__restrict__ counts, uint32_t NB, uint32_t L,
                                                         uint32_t *__restrict__ offsets, uint32_t *__restrict__ seg_off,
-                                                        uint32_t *__restrict__ tmp)
+                                                        uint32_t *__restrict__ tmp, const uint32_t *__restrict__ counts0)
 {
     __shared__ uint2 tot;
     const uint32_t base = blockIdx.x * SCAN_BLOCK + threadIdx.x * SCAN_ITEMS;
@@ -750,7 +768,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_a(const uint32_t *__restr
     for (int j = 0; j < SCAN_ITEMS; j++) {
         const uint32_t idx = base + j;
         c[j] = idx < NB ? counts[idx] : 0u;
-        s[j] = (c[j] + L - 1) / L;
+        s[j] = counts0 ? (idx < NB ? part_slots(c[j], counts0[idx], L) : 0u) : (c[j] + L - 1) / L;
         v.x += c[j];
         v.y += s[j];
     }
@@ -834,58 +852,88 @@ __global__ void k_scan_c(uint32_t *__restrict__ offsets, uint32_t *__restrict__ 
 // through block-local cursors.  Each descriptor carries its destination slot
 // seg_off[bucket] + j, so a bucket's partial sums stay contiguous.
 __global__ void __launch_bounds__(SEG_HIST_THREADS) k_seg_hist(const uint32_t *__restrict__ offsets, uint32_t NB,
-                                                              uint32_t L, uint32_t nblk, uint32_t *__restrict__ hist)
+                                                              uint32_t L, uint32_t nblk, uint32_t *__restrict__ hist,
+                                                              const uint32_t *__restrict__ counts0)
 {
     extern __shared__ uint32_t h[];
-    for (uint32_t i = threadIdx.x; i <= L; i += blockDim.x)
+    const uint32_t parts = counts0 ? 2u : 1u;
+    for (uint32_t i = threadIdx.x; i < parts * (L + 1); i += blockDim.x)
         h[i] = 0;
     __syncthreads();
     const uint32_t kb = blockIdx.x * blockDim.x + threadIdx.x;
     if (kb < NB) {
         const uint32_t cnt = offsets[kb + 1] - offsets[kb];
-        const uint32_t nfull = cnt / L, rem = cnt % L;
-        if (nfull)
-            atomicAdd(&h[L], nfull);
-        if (rem)
-            atomicAdd(&h[rem], 1u);
+        const uint32_t c0 = counts0 ? counts0[kb] : cnt;
+        for (uint32_t part = 0; part < parts; part++) {
+            const uint32_t c = part ? cnt - c0 : c0;
+            const uint32_t nfull = c / L, rem = c % L;
+            if (nfull)
+                atomicAdd(&h[part * (L + 1) + L], nfull);
+            if (rem)
+                atomicAdd(&h[part * (L + 1) + rem], 1u);
+        }
     }
     __syncthreads();
-    for (uint32_t len = threadIdx.x; len <= L; len += blockDim.x)
-        hist[(size_t)(L - len) * nblk + blockIdx.x] = h[len];
+    for (uint32_t i = threadIdx.x; i < parts * (L + 1); i += blockDim.x) {
+        const uint32_t part = i / (L + 1), len = i % (L + 1);
+        hist[(size_t)(part * (L + 1) + L - len) * nblk + blockIdx.x] = h[i];
+    }
+}
+
+// one part's segments of a bucket: entries [start, start + cnt) cut into
+// pieces of L (then the remainder); piece j goes to slot first (j = 0) or
+// rest + j - 1, the first one continuing the stored sum when resume is set
+__device__ __forceinline__ void emit_segments(uint32_t *cur, uint32_t L, uint32_t start, uint32_t cnt, uint32_t first,
+                                              uint32_t rest, uint32_t resume, uint4 *__restrict__ segs)
+{
+    const uint32_t nfull = cnt / L, rem = cnt % L;
+    if (nfull) {
+        const uint32_t p = atomicAdd(&cur[L], nfull);
+        for (uint32_t j = 0; j < nfull; j++)
+            segs[p + j] = make_uint4(start + j * L, L, j ? rest + j - 1 : first, j ? 0u : resume);
+    }
+    if (rem) {
+        const uint32_t p = atomicAdd(&cur[rem], 1u);
+        segs[p] = make_uint4(start + nfull * L, rem, nfull ? rest + nfull - 1 : first, nfull ? 0u : resume);
+    }
 }
 
 __global__ void __launch_bounds__(SEG_HIST_THREADS) k_seg_scatter(const uint32_t *__restrict__ offsets,
                                                                  const uint32_t *__restrict__ seg_off, uint32_t NB,
                                                                  uint32_t L, uint32_t nblk,
                                                                  const uint32_t *__restrict__ hist_scan,
-                                                                 uint4 *__restrict__ segs)
+                                                                 uint4 *__restrict__ segs,
+                                                                 const uint32_t *__restrict__ counts0)
 {
     extern __shared__ uint32_t cur[];
-    for (uint32_t len = threadIdx.x; len <= L; len += blockDim.x)
-        cur[len] = hist_scan[(size_t)(L - len) * nblk + blockIdx.x];
+    const uint32_t parts = counts0 ? 2u : 1u;
+    for (uint32_t i = threadIdx.x; i < parts * (L + 1); i += blockDim.x) {
+        const uint32_t part = i / (L + 1), len = i % (L + 1);
+        cur[i] = hist_scan[(size_t)(part * (L + 1) + L - len) * nblk + blockIdx.x];
+    }
     __syncthreads();
     const uint32_t kb = blockIdx.x * blockDim.x + threadIdx.x;
     if (kb >= NB)
         return;
-    const uint32_t start = offsets[kb], cnt = offsets[kb + 1] - start;
-    const uint32_t nfull = cnt / L, rem = cnt % L, dest = seg_off[kb];
-    if (nfull) {
-        const uint32_t p = atomicAdd(&cur[L], nfull);
-        for (uint32_t j = 0; j < nfull; j++)
-            segs[p + j] = make_uint4(start + j * L, L, dest + j, 0u);
+    const uint32_t start = offsets[kb], cnt = offsets[kb + 1] - start, dest = seg_off[kb];
+    if (!counts0) {
+        emit_segments(cur, L, start, cnt, dest, dest + 1, 0u, segs);
+        return;
     }
-    if (rem) {
-        const uint32_t p = atomicAdd(&cur[rem], 1u);
-        segs[p] = make_uint4(start + nfull * L, rem, dest + nfull, 0u);
-    }
+    const uint32_t c0 = counts0[kb], s0 = (c0 + L - 1) / L;
+    emit_segments(cur, L, start, c0, dest, dest + 1, 0u, segs);
+    if (s0)
+        emit_segments(cur + (L + 1), L, start + c0, cnt - c0, dest, dest + s0, 1u, segs);
+    else
+        emit_segments(cur + (L + 1), L, start + c0, cnt - c0, dest, dest + 1, 0u, segs);
 }
 
 static cudaError_t launch_scan(Context &ctx, const uint32_t *in, uint32_t n, uint32_t L, uint32_t *out,
-                               uint32_t *out2, uint32_t *tmp)
+                               uint32_t *out2, uint32_t *tmp, const uint32_t *counts0 = nullptr)
 {
     cudaStream_t st = ctx.stream;
     const uint32_t nblk = std::max<uint32_t>(1, scan_blocks(n));
-    k_scan_a<<<nblk, SCAN_THREADS, 0, st>>>(in, n, L, out, out2, tmp);
+    k_scan_a<<<nblk, SCAN_THREADS, 0, st>>>(in, n, L, out, out2, tmp, counts0);
     HS_LAUNCH_CHECK(ctx);
     k_scan_b<<<1, SCAN_THREADS, 0, st>>>(tmp, nblk, out + n, out2 ? out2 + n : nullptr);
     HS_LAUNCH_CHECK(ctx);
@@ -937,11 +985,13 @@ cudaError_t launch_sort(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
         }
         k_sort_count<<<p.sort_blocks, SORT_THREADS, smem, st>>>(b.digits, b.desc, p.M, b.sort_cnt);
         HS_LAUNCH_CHECK(ctx);
-        k_sort_rows<0><<<tb, 256, 0, st>>>(b.desc, p.M, p.NB, b.sort_cnt, b.counts, nullptr);
+        const uint32_t *c0 = p.part_slice ? b.counts0 : nullptr;
+        k_sort_rows<0><<<tb, 256, 0, st>>>(b.desc, p.M, p.NB, b.sort_cnt, b.counts, nullptr, p.part_slice,
+                                           p.part_slice ? b.counts0 : nullptr);
         HS_LAUNCH_CHECK(ctx);
-        if ((e = launch_scan(ctx, b.counts, p.NB, p.L, b.offsets, b.seg_off, b.scan_tmp)) != cudaSuccess)
+        if ((e = launch_scan(ctx, b.counts, p.NB, p.L, b.offsets, b.seg_off, b.scan_tmp, c0)) != cudaSuccess)
             return e;
-        k_sort_rows<1><<<tb, 256, 0, st>>>(b.desc, p.M, p.NB, b.sort_cnt, nullptr, b.offsets);
+        k_sort_rows<1><<<tb, 256, 0, st>>>(b.desc, p.M, p.NB, b.sort_cnt, nullptr, b.offsets, 0u, nullptr);
         HS_LAUNCH_CHECK(ctx);
         k_sort_scatter<<<p.sort_blocks, SORT_THREADS, smem, st>>>(b.digits, b.desc, p.M, b.sort_cnt, b.sorted);
         HS_LAUNCH_CHECK(ctx);
@@ -962,13 +1012,14 @@ cudaError_t launch_sort(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
     }
     // segments, longest first
     const uint32_t nh = (uint32_t)hist_len(p);
-    const size_t hsm = (size_t)(p.L + 1) * 4;
-    k_seg_hist<<<p.hist_blocks, SEG_HIST_THREADS, hsm, st>>>(b.offsets, p.NB, p.L, p.hist_blocks, b.len_hist);
+    const uint32_t *c0 = (p.part_slice && p.smem_sort()) ? b.counts0 : nullptr;
+    const size_t hsm = (size_t)(p.L + 1) * 4 * (c0 ? 2 : 1);
+    k_seg_hist<<<p.hist_blocks, SEG_HIST_THREADS, hsm, st>>>(b.offsets, p.NB, p.L, p.hist_blocks, b.len_hist, c0);
     HS_LAUNCH_CHECK(ctx);
     if ((e = launch_scan(ctx, b.len_hist, nh, 1u, b.len_scan, nullptr, b.scan_tmp)) != cudaSuccess)
         return e;
     k_seg_scatter<<<p.hist_blocks, SEG_HIST_THREADS, hsm, st>>>(b.offsets, b.seg_off, p.NB, p.L, p.hist_blocks,
-                                                                 b.len_scan, b.segs);
+                                                                 b.len_scan, b.segs, c0);
     HS_LAUNCH_CHECK(ctx);
     return cudaSuccess;
 }
@@ -1233,7 +1284,7 @@ static cudaError_t ensure_stream2(Context &ctx)
         if ((e = cudaStreamCreateWithPriority(&ctx.stream3, cudaStreamNonBlocking, greatest)) != cudaSuccess)
             return e;
     }
-    for (cudaEvent_t *ev : {&ctx.ev_sc, &ctx.ev_rec, &ctx.ev_pts})
+    for (cudaEvent_t *ev : {&ctx.ev_sc, &ctx.ev_rec[0], &ctx.ev_rec[1], &ctx.ev_pts[0], &ctx.ev_pts[1]})
         if (!*ev && (e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming)) != cudaSuccess)
             return e;
     return e;
@@ -1489,7 +1540,7 @@ void hs_context_destroy(hs_context *h)
             cudaEventDestroy(h->c.ev_join);
         if (h->c.stream3)
             cudaStreamDestroy(h->c.stream3);
-        for (cudaEvent_t ev : {h->c.ev_sc, h->c.ev_rec, h->c.ev_pts})
+        for (cudaEvent_t ev : {h->c.ev_sc, h->c.ev_rec[0], h->c.ev_rec[1], h->c.ev_pts[0], h->c.ev_pts[1]})
             if (ev)
                 cudaEventDestroy(ev);
     }
@@ -1597,6 +1648,15 @@ int hs_msm_device(hs_context *h, int curve, const void *d_scalars, const void *d
     return execute_batch(ctx, p, b, d_out, out_fmt);
 }
 
+// Host inputs in two parts split at counting-sort slice `slice`: each bucket
+// may get one more segment descriptor (its part-1 entries).
+static void plan_parts(BatchPlan &p, uint32_t slice)
+{
+    p.part_slice = slice;
+    const uint64_t more = std::min<uint64_t>(p.entries_bound, p.NB);
+    p.max_segs = (uint32_t)std::min<uint64_t>(0xffffffffull, (uint64_t)p.max_segs + more);
+}
+
 // Stage host inputs (scalars and points in any format) and run one MSM of
 // n_total terms whose first `lead` terms come from (lead_scalar, lead_point).
 static int msm_host(Context &ctx, int curve, const uint8_t *lead_scalar, const void *lead_point, const uint8_t *scalars,
@@ -1622,6 +1682,25 @@ static int msm_host(Context &ctx, int curve, const uint8_t *lead_scalar, const v
         const size_t sizes[1] = {total};
         p = make_batch_plan(ctx, curve, sizes, 1);
     }
+    // Bases spanning several counting-sort slices arrive in two parts, split at a
+    // slice boundary: the entries of a bucket come in slice order, so each part's
+    // entries of a bucket are contiguous and get their own segments, and the
+    // accumulation of part 0 runs while part 1 is still on the link.
+    const MsmDesc &d0 = split ? s.lo.msms[0] : p.msms[0];
+    const bool two = point_fmt != HS_FMT_COMPRESSED && d0.slices >= 2 &&
+                     (split ? (s.hi.smem_sort() && s.lo.smem_sort()) : p.smem_sort());
+    size_t bound[3] = {0, total, total};
+    if (two) {
+        const uint32_t cut = d0.slices / 2;
+        if (split) {
+            plan_parts(s.hi, cut);
+            plan_parts(s.lo, cut);
+        } else {
+            plan_parts(p, cut);
+        }
+        bound[1] = std::min<size_t>(total, (size_t)((total + d0.slices - 1) / d0.slices) * cut);
+    }
+    const int nparts = two ? 2 : 1;
     const size_t need_in = align256(total * 32) + align256(total * 64) +
                            (point_fmt == HS_FMT_AFFINE ? 0 : align256(total * pb)) +
                            align256(ops.to_affine_scratch(total)) + 256;
@@ -1634,8 +1713,9 @@ static int msm_host(Context &ctx, int curve, const uint8_t *lead_scalar, const v
     uint8_t *d_scratch = (point_fmt == HS_FMT_AFFINE ? d_pts + align256(total * 64) : d_raw + align256(total * pb));
     uint8_t *d_out = d_scratch + align256(ops.to_affine_scratch(total));
     // Inputs go to the device's link stream, the scalars first: the counting
-    // sort needs only them, so it runs while the bases arrive; the bases are
-    // converted on the third stream and the accumulation waits for them.
+    // sort needs only them, so it runs while the bases arrive; each part of the
+    // bases is converted on the third stream as soon as it is in, and each
+    // accumulation launch waits for its part.
     HS_CU(ensure_stream2(ctx), "stream creation");
     LinkStream *link = nullptr;
     HS_CU(link_stream(ctx.device, &link), "stream creation");
@@ -1650,21 +1730,33 @@ static int msm_host(Context &ctx, int curve, const uint8_t *lead_scalar, const v
         if (n)
             HS_CU(cudaMemcpyAsync(d_sc + 32 * lead, scalars, n * 32, cudaMemcpyHostToDevice, cs), "H2D scalars");
         HS_CU(cudaEventRecord(ctx.ev_sc, cs), "event");
-        if (lead)
-            HS_CU(cudaMemcpyAsync(d_raw, lead_point, pb, cudaMemcpyHostToDevice, cs), "H2D points");
-        if (n)
-            HS_CU(cudaMemcpyAsync(d_raw + pb * lead, points, n * pb, cudaMemcpyHostToDevice, cs), "H2D points");
-        HS_CU(cudaEventRecord(ctx.ev_rec, cs), "event");
+        for (int j = 0; j < nparts; j++) {
+            // point g of the MSM: the lead term at 0, then points[g - lead]
+            size_t g = bound[j];
+            if (lead && g == 0 && bound[j + 1] > 0) {
+                HS_CU(cudaMemcpyAsync(d_raw, lead_point, pb, cudaMemcpyHostToDevice, cs), "H2D points");
+                g = 1;
+            }
+            if (bound[j + 1] > g)
+                HS_CU(cudaMemcpyAsync(d_raw + pb * g, static_cast<const uint8_t *>(points) + pb * (g - lead),
+                                      pb * (bound[j + 1] - g), cudaMemcpyHostToDevice, cs),
+                      "H2D points");
+            HS_CU(cudaEventRecord(ctx.ev_rec[j], cs), "event");
+        }
     }
-    cudaEvent_t bases_ready = ctx.ev_rec;
-    if (point_fmt != HS_FMT_AFFINE) {
-        HS_CU(cudaStreamWaitEvent(s3, ctx.ev_rec, 0), "stream wait");
+    cudaEvent_t ready[2] = {nullptr, nullptr};
+    for (int j = 0; j < nparts; j++) {
+        ready[j] = ctx.ev_rec[j];
+        if (point_fmt == HS_FMT_AFFINE)  // copied in place, nothing to convert
+            continue;
+        HS_CU(cudaStreamWaitEvent(s3, ctx.ev_rec[j], 0), "stream wait");
         ctx.stream = s3;
-        const cudaError_t ce = ops.to_affine(ctx, d_raw, point_fmt, total, (uint4 *)d_pts, d_scratch);
+        const cudaError_t ce = ops.to_affine(ctx, d_raw + pb * bound[j], point_fmt, bound[j + 1] - bound[j],
+                                             (uint4 *)d_pts + 4 * bound[j], d_scratch);
         ctx.stream = st;
         HS_CU(ce, "input conversion");
-        HS_CU(cudaEventRecord(ctx.ev_pts, s3), "event");
-        bases_ready = ctx.ev_pts;
+        HS_CU(cudaEventRecord(ctx.ev_pts[j], s3), "event");
+        ready[j] = ctx.ev_pts[j];
     }
     int rc = HS_OK;
     if (split) {
@@ -1674,7 +1766,8 @@ static int msm_host(Context &ctx, int curve, const uint8_t *lead_scalar, const v
             return fail_msg(ctx, HS_ENOMEM, "workspace carve");
         bh.scalars = bl.scalars = (const uint32_t *)d_sc;
         bh.points = bl.points = (const uint4 *)d_pts;
-        bh.bases_ready = bl.bases_ready = bases_ready;
+        for (int j = 0; j < 2; j++)
+            bh.ready[j] = bl.ready[j] = ready[j];
         HS_CU(cudaMemcpyAsync(bh.desc, s.hi.msms.data(), sizeof(MsmDesc), cudaMemcpyHostToDevice, st), "descriptors");
         HS_CU(cudaMemcpyAsync(bl.desc, s.lo.msms.data(), sizeof(MsmDesc), cudaMemcpyHostToDevice, st), "descriptors");
         HS_CU(cudaStreamWaitEvent(st, ctx.ev_sc, 0), "stream wait");
@@ -1699,7 +1792,8 @@ static int msm_host(Context &ctx, int curve, const uint8_t *lead_scalar, const v
             return fail_msg(ctx, HS_ENOMEM, "workspace carve");
         b.scalars = (const uint32_t *)d_sc;
         b.points = (const uint4 *)d_pts;
-        b.bases_ready = bases_ready;
+        b.ready[0] = ready[0];
+        b.ready[1] = ready[1];
         HS_CU(cudaMemcpyAsync(b.desc, p.msms.data(), sizeof(MsmDesc), cudaMemcpyHostToDevice, st), "descriptors");
         HS_CU(cudaStreamWaitEvent(st, ctx.ev_sc, 0), "stream wait");
         HS_CU(launch_sort(ctx, p, b), "sort");
