@@ -877,8 +877,9 @@ def run_ours(args) -> None:
     args_of = {c: (c, data[c]["h_sc"].numpy(), data[c]["h_jac"].numpy(), hs.FMT_JACOBIAN51, hs.FMT_JACOBIAN51)
                for c in (hs.SELENE, hs.HELIOS)}
     with ThreadPoolExecutor(max_workers=2) as pool:
-        for f in [pool.submit(ctxs[c].msm, *args_of[c]) for c in (hs.SELENE, hs.HELIOS)]:
-            f.result()
+        for _ in range(3):
+            for f in [pool.submit(ctxs[c].msm, *args_of[c]) for c in (hs.SELENE, hs.HELIOS)]:
+                f.result()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
             for f in [pool.submit(ctxs[c].msm, *args_of[c]) for c in (hs.SELENE, hs.HELIOS)]:
