@@ -112,7 +112,11 @@ int hs_context_set_priority(hs_context *ctx, int high);
  * n == 0 gives the identity, as in the reference (helios_msm_vartime.cpp:402-406).
  * One call handles n x W(c) < 2^31 (point, window) entries, about 126M points
  * at c = 16; beyond that it returns HS_ERANGE and the caller sums the results
- * of slices (they add as points). */
+ * of slices (they add as points).
+ * The host-to-device copies of every context on a device go through one copy
+ * stream in call order (pinned host memory keeps them asynchronous); the
+ * scalars go first, and bases of more than 2^17 points go in two parts whose
+ * first is accumulated while the second is in transit. */
 int hs_msm(hs_context *ctx, int curve, const uint8_t *scalars, const void *points, int point_fmt, size_t n,
            void *out, int out_fmt);
 
