@@ -301,6 +301,12 @@ class Server:
         if rc != L.HS_OK:
             raise L.HsError(rc, "hs_server_set_pool")
 
+    def set_window(self, curve: int, n_min: int, n_max: int, window: int) -> None:
+        """window rule for every slot's batches (hs_server_set_window; window 0 clears)"""
+        rc = self._lib.hs_server_set_window(self._h, curve, int(n_min), int(n_max), int(window))
+        if rc != L.HS_OK:
+            raise L.HsError(rc, "hs_server_set_window")
+
     def submit(self, curve: int, scalars, pool_idx=None, fresh_points=None) -> int:
         s = _u8(scalars)
         idx = np.ascontiguousarray(pool_idx, dtype=np.uint32) if pool_idx is not None else None

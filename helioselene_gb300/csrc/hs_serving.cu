@@ -404,6 +404,23 @@ int hs_server_set_pool(hs_server *h, int curve, const void *pts, size_t n)
     return HS_OK;
 }
 
+int hs_server_set_window(hs_server *h, int curve, size_t n_min, size_t n_max, int window)
+{
+    if (!h || (curve != HS_HELIOS && curve != HS_SELENE) || n_min > n_max ||
+        (window != 0 && (window < 4 || window > 20)))
+        return HS_EINVAL;
+    Server &S = h->s;
+    std::lock_guard<std::mutex> lk(S.mu);  // batches are planned under this lock
+    for (auto &sp : S.slots) {
+        auto &rules = sp->ctx.rules[curve == HS_SELENE ? 1 : 0];
+        if (window == 0)
+            rules.clear();
+        else
+            rules.push_back(WindowRule{n_min, n_max, window});
+    }
+    return HS_OK;
+}
+
 int hs_server_submit(hs_server *h, const hs_request *req, uint64_t *ticket)
 {
     if (!h || !req || !ticket || (req->curve != HS_HELIOS && req->curve != HS_SELENE) || !req->out)

@@ -271,6 +271,9 @@ typedef struct hs_server_stats {
 int hs_server_create(hs_server **srv, const hs_server_config *cfg);
 /* upload (replace) the resident base pool of one curve: n HS_FMT_AFFINE points */
 int hs_server_set_pool(hs_server *srv, int curve, const void *affine_points, size_t n);
+/* window rule for the batches of every slot, as hs_context_set_window (window 0
+ * clears the curve's rules); applies to batches planned after the call */
+int hs_server_set_window(hs_server *srv, int curve, size_t n_min, size_t n_max, int window);
 /* queue a request; HS_ERANGE if it alone exceeds the batch caps or the budget */
 int hs_server_submit(hs_server *srv, const hs_request *req, uint64_t *ticket);
 /* wait up to timeout_ms for a request: HS_OK (result written, latency from

@@ -69,6 +69,28 @@ def test_same_alone_and_in_the_mix(pools):
     assert alone == [r["want"] for r in reqs]
 
 
+def test_window_rules_apply_to_every_slot(pools):
+    """hs_server_set_window: every window width the slots may be given yields the
+    same results; bad rules are refused"""
+    import helioselene_gb300 as hs
+    from helioselene_gb300._lib import HsError
+    rng = np.random.default_rng(3)
+    reqs = make_requests(rng, pools, 16, 4096)
+    with hs.Server(0, slots=2) as srv:
+        for c in (0, 1):
+            srv.set_pool(c, pools[c])
+        for w in (5, 9, 13):
+            for c in (0, 1):
+                srv.set_window(c, 0, 0, 0)
+                srv.set_window(c, 1, 1 << 20, w)
+            tickets = [srv.submit(r["curve"], r["scalars"], r["idx"], r["fresh"]) for r in reqs]
+            got = [srv.wait(t)[0] for t in tickets]
+            assert got == [r["want"] for r in reqs], f"window {w}"
+        for bad in ((2, 0, 10, 8), (0, 10, 5, 8), (0, 0, 10, 3), (0, 0, 10, 21)):
+            with pytest.raises(HsError):
+                srv.set_window(*bad)
+
+
 def test_budget_defers_but_completes(pools):
     import helioselene_gb300 as hs
     rng = np.random.default_rng(3)
