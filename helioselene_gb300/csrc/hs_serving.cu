@@ -27,15 +27,19 @@
 
 namespace hs {
 
-// out[dst[p]] = pool[src[p]] (64-byte affine points)
+// Pooled bases of a batch: request r's pool indices are src[seg[r].y, seg[r].y +
+// seg[r].z) and its bases go to out[seg[r].x ...].  Entry p belongs to the last
+// request whose first index is <= p (requests without pooled bases share the
+// next one's start and lose the search).
 __global__ void k_gather_pool(const uint4 *__restrict__ pool, const uint32_t *__restrict__ src,
-                              const uint32_t *__restrict__ dst, uint32_t count, uint4 *__restrict__ out)
+                              const uint4 *__restrict__ seg, uint32_t nseg, uint32_t count, uint4 *__restrict__ out)
 {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= count)
         return;
+    const uint32_t r = find_msm(nseg, p, [&](uint32_t k) { return seg[k].y; });
     const uint4 *s = pool + 4 * (size_t)src[p];
-    uint4 *d = out + 4 * (size_t)dst[p];
+    uint4 *d = out + 4 * ((size_t)seg[r].x + (p - seg[r].y));
     d[0] = s[0];
     d[1] = s[1];
     d[2] = s[2];
@@ -61,12 +65,13 @@ struct Slot {
     std::vector<uint64_t> tickets;
     uint8_t *pinned_out = nullptr;
     size_t pinned_cap = 0;
-    std::vector<uint32_t> h_src, h_dst;  // staging of the pool gather (kept alive until retire)
+    std::vector<uint4> h_seg;  // per request: (first point, first pool index, pool count); kept until retire
 };
 
 struct Pool {
     uint4 *d = nullptr;
     size_t n = 0;
+    uint64_t gen = 0;  // bumped by every replacement
 };
 
 struct Server {
@@ -88,7 +93,8 @@ struct Server {
 static size_t batch_stage_bytes(size_t total, size_t total_pool, size_t msms, size_t ob)
 {
     return align256(std::max<size_t>(1, total) * 32) + align256(std::max<size_t>(1, total) * 64) +
-           2 * align256(std::max<size_t>(1, total_pool) * 4) + align256(std::max<size_t>(1, msms) * ob);
+           align256(std::max<size_t>(1, total_pool) * 4) + align256(std::max<size_t>(1, msms) * 16) +
+           align256(std::max<size_t>(1, msms) * ob);
 }
 
 // launch one batch on slot s; called with the server lock held; false = deferred (budget)
@@ -128,8 +134,8 @@ static bool launch(Server &S, Slot &s, std::vector<uint64_t> &batch, int curve)
     uint8_t *d_sc = (uint8_t *)ext;
     uint8_t *d_pts = d_sc + align256(std::max<size_t>(1, total) * 32);
     uint32_t *d_src = (uint32_t *)(d_pts + align256(std::max<size_t>(1, total) * 64));
-    uint32_t *d_dst = d_src + align256(std::max<size_t>(1, total_pool) * 4) / 4;
-    uint8_t *d_out = (uint8_t *)(d_dst) + align256(std::max<size_t>(1, total_pool) * 4);
+    uint4 *d_seg = (uint4 *)((uint8_t *)d_src + align256(std::max<size_t>(1, total_pool) * 4));
+    uint8_t *d_out = (uint8_t *)d_seg + align256(std::max<size_t>(1, batch.size()) * 16);
     if (s.pinned_cap < batch.size() * ob) {
         if (s.pinned_out)
             cudaFreeHost(s.pinned_out);
@@ -142,9 +148,11 @@ static bool launch(Server &S, Slot &s, std::vector<uint64_t> &batch, int curve)
         }
     }
     cudaStream_t st = ctx.stream;
-    s.h_src.clear();
-    s.h_dst.clear();
-    size_t off = 0;
+    // per request: its scalars, fresh bases and pool indices copied straight from
+    // the caller's buffers, plus one table row; the pooled bases are gathered on
+    // the device
+    s.h_seg.clear();
+    size_t off = 0, poff = 0;
     cudaError_t e = cudaSuccess;
     for (uint64_t t : batch) {
         const hs_request &q = S.reqs[t].req;
@@ -154,19 +162,17 @@ static bool launch(Server &S, Slot &s, std::vector<uint64_t> &batch, int curve)
         if (q.n_fresh && e == cudaSuccess)
             e = cudaMemcpyAsync(d_pts + 64 * (off + q.n_pool), q.fresh_points, 64 * q.n_fresh,
                                 cudaMemcpyHostToDevice, st);
-        for (size_t j = 0; j < q.n_pool; j++) {
-            s.h_src.push_back(q.pool_idx[j]);
-            s.h_dst.push_back((uint32_t)(off + j));
-        }
+        if (q.n_pool && e == cudaSuccess)
+            e = cudaMemcpyAsync(d_src + poff, q.pool_idx, 4 * q.n_pool, cudaMemcpyHostToDevice, st);
+        s.h_seg.push_back(make_uint4((uint32_t)off, (uint32_t)poff, (uint32_t)q.n_pool, 0u));
         off += n;
+        poff += q.n_pool;
     }
     if (total_pool && e == cudaSuccess) {
-        e = cudaMemcpyAsync(d_src, s.h_src.data(), 4 * total_pool, cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(d_dst, s.h_dst.data(), 4 * total_pool, cudaMemcpyHostToDevice, st);
+        e = cudaMemcpyAsync(d_seg, s.h_seg.data(), 16 * s.h_seg.size(), cudaMemcpyHostToDevice, st);
         if (e == cudaSuccess) {
-            k_gather_pool<<<(unsigned)((total_pool + 255) / 256), 256, 0, st>>>(S.pools[curve].d, d_src, d_dst,
-                                                                              (uint32_t)total_pool, (uint4 *)d_pts);
+            k_gather_pool<<<(unsigned)((total_pool + 255) / 256), 256, 0, st>>>(
+                S.pools[curve].d, d_src, d_seg, (uint32_t)s.h_seg.size(), (uint32_t)total_pool, (uint4 *)d_pts);
             ctx.launches++;
             e = cudaGetLastError();
         }
@@ -389,6 +395,7 @@ int hs_server_set_pool(hs_server *h, int curve, const void *pts, size_t n)
         cudaFree(p.d);
     p.d = nullptr;
     p.n = 0;
+    p.gen++;
     if (!n)
         return HS_OK;
     if (cudaMalloc((void **)&p.d, n * 64) != cudaSuccess) {
@@ -431,14 +438,24 @@ int hs_server_submit(hs_server *h, const hs_request *req, uint64_t *ticket)
     Server &S = h->s;
     if (n > S.cfg.max_batch_points)
         return HS_ERANGE;
-    std::lock_guard<std::mutex> lk(S.mu);
+    // the indices are checked without the lock (the scheduler keeps running),
+    // against the pool size of a generation that is still current when queued
+    std::unique_lock<std::mutex> lk(S.mu);
     if (S.stop)
         return HS_EBUSY;
-    if (req->n_pool) {
+    while (req->n_pool) {
         const Pool &p = S.pools[req->curve];
+        const size_t pool_n = p.n;
+        const uint64_t gen = p.gen;
+        lk.unlock();
         for (size_t j = 0; j < req->n_pool; j++)
-            if (req->pool_idx[j] >= p.n)
+            if (req->pool_idx[j] >= pool_n)
                 return HS_EINVAL;
+        lk.lock();
+        if (S.stop)
+            return HS_EBUSY;
+        if (S.pools[req->curve].gen == gen)
+            break;
     }
     const uint64_t t = S.next_ticket++;
     ReqState &r = S.reqs[t];
