@@ -359,3 +359,39 @@ def test_host_inputs_every_format(ctx, curve):
                                 HS_JAC51) == want_id, f"pedersen jacobian51, split {split}"
     finally:
         ctx.set_split(1 << 18)
+
+
+@pytest.mark.parametrize("curve", [0, 1])
+def test_host_parts_edge_cases(ctx, curve):
+    """host bases in two parts, with the work lopsided between them: every scalar
+    of one part zero, a base repeated across both parts with one scalar (one
+    bucket of thousands of entries, cut into many segments in each part), and
+    identity bases gathered in one part; against the batched path"""
+    from helioselene_gb300.workload import make_workload
+    n = (1 << 18) + 5
+    w = make_workload(curve, n, seed=909 + curve, edge_fraction=0.0)
+    pts = ctx.map_to_curve(curve, w.u, HS_AFF).reshape(n, 64).copy()
+    half = n // 2
+    cases = []
+    sc = w.scalars.copy()
+    sc[half:] = 0
+    cases.append(("second part zero", sc, pts))
+    sc = w.scalars.copy()
+    sc[:half] = 0
+    cases.append(("first part zero", sc, pts))
+    sc = w.scalars.copy()
+    p2 = pts.copy()
+    rep = np.arange(1000, n, 37)
+    p2[rep] = pts[1000]
+    sc[rep] = sc[1000]
+    cases.append(("repeated base across parts", sc, p2))
+    p3 = pts.copy()
+    p3[: half // 2] = 0
+    cases.append(("identity bases in part 0", w.scalars, p3))
+    try:
+        for split in (1 << 18, 0):
+            ctx.set_split(split)
+            for name, s, p in cases:
+                assert ctx.msm(curve, s, p) == ctx.msm_batch([(curve, s, p)])[0], f"{name}, split {split}"
+    finally:
+        ctx.set_split(1 << 18)
