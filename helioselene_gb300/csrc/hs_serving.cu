@@ -48,9 +48,13 @@ __global__ void k_gather_pool(const uint4 *__restrict__ pool, const uint32_t *__
 
 using Clock = std::chrono::steady_clock;
 
+// one launch sequence indexes its (point, window) entries with 31 bits
+constexpr uint64_t BATCH_ENTRIES_MAX = 0x7fffffffull;
+
 struct ReqState {
     hs_request req;
     size_t n = 0;
+    uint64_t entries = 0;  // n x windows under the slots' window rules at submission
     Clock::time_point submitted;
     double latency_ms = 0.0;
     int status = 1;  // 1 = pending, else HS_OK / error
@@ -111,6 +115,14 @@ static bool launch(Server &S, Slot &s, std::vector<uint64_t> &batch, int curve)
     }
     Context &ctx = s.ctx;
     const BatchPlan p = make_batch_plan(ctx, curve, sizes.data(), (uint32_t)sizes.size());
+    if (p.entries_bound > BATCH_ENTRIES_MAX) {  // window rules changed since submission
+        for (uint64_t t : batch) {
+            S.reqs[t].status = HS_ERANGE;
+            S.stats.failed++;
+        }
+        S.cv_done.notify_all();
+        return true;
+    }
     const size_t extra = batch_stage_bytes(total, total_pool, batch.size(), ob);
     const size_t bytes = batch_bytes(p) + extra + 2048;
     if (S.in_flight > 0 && S.in_flight + bytes > S.cfg.hbm_budget) {
@@ -270,15 +282,17 @@ static void scheduler(Server *Sp)
             const int curve = S.reqs[S.queue.front()].req.curve;
             std::vector<uint64_t> batch;
             size_t pts = 0;
+            uint64_t ent = 0;
             std::deque<uint64_t> rest;
             while (!S.queue.empty()) {
                 const uint64_t t = S.queue.front();
                 S.queue.pop_front();
                 const ReqState &r = S.reqs[t];
                 if (r.req.curve == curve && batch.size() < S.cfg.max_batch_msms &&
-                    (batch.empty() || pts + r.n <= S.cfg.max_batch_points)) {
+                    (batch.empty() || (pts + r.n <= S.cfg.max_batch_points && ent + r.entries <= BATCH_ENTRIES_MAX))) {
                     batch.push_back(t);
                     pts += r.n;
+                    ent += r.entries;
                 } else {
                     rest.push_back(t);
                 }
@@ -457,10 +471,15 @@ int hs_server_submit(hs_server *h, const hs_request *req, uint64_t *ticket)
         if (S.pools[req->curve].gen == gen)
             break;
     }
+    const int c = choose_window(S.slots[0]->ctx, req->curve, n);
+    const uint64_t entries = (uint64_t)n * (uint64_t)((257 + c - 1) / c);
+    if (entries > BATCH_ENTRIES_MAX)
+        return HS_ERANGE;
     const uint64_t t = S.next_ticket++;
     ReqState &r = S.reqs[t];
     r.req = *req;
     r.n = n;
+    r.entries = entries;
     r.submitted = Clock::now();
     S.queue.push_back(t);
     S.stats.submitted++;

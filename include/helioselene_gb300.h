@@ -274,7 +274,8 @@ int hs_server_set_pool(hs_server *srv, int curve, const void *affine_points, siz
 /* window rule for the batches of every slot, as hs_context_set_window (window 0
  * clears the curve's rules); applies to batches planned after the call */
 int hs_server_set_window(hs_server *srv, int curve, size_t n_min, size_t n_max, int window);
-/* queue a request; HS_ERANGE if it alone exceeds the batch caps or the budget */
+/* queue a request; HS_ERANGE if it alone exceeds the batch caps or the budget,
+ * or its n x windows reaches 2^31 (batches are also formed below that bound) */
 int hs_server_submit(hs_server *srv, const hs_request *req, uint64_t *ticket);
 /* wait up to timeout_ms for a request: HS_OK (result written, latency from
  * submit to completion in *latency_ms), HS_ETIMEDOUT, or the failure status */
