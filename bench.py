@@ -871,6 +871,18 @@ def run_ours(args) -> None:
                             hs.FMT_JACOBIAN51)
     if dist:
         dist.barrier()
+    # the host link's rate right now, for reading the e2e number: one copy of the
+    # Selene records (pinned) to the device
+    h2d_probe = torch.empty(data[hs.SELENE]["h_jac"].numel(), dtype=torch.uint8, device=device)
+    h2d_gbps = []
+    for _ in range(3):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        h2d_probe.copy_(data[hs.SELENE]["h_jac"], non_blocking=True)
+        b.record()
+        torch.cuda.synchronize()
+        h2d_gbps.append(h2d_probe.numel() / (a.elapsed_time(b) * 1e6))
+    del h2d_probe
     # the two curves from two host threads of a pool (one context each), as a
     # caller would overlap them
     from concurrent.futures import ThreadPoolExecutor
@@ -880,10 +892,13 @@ def run_ours(args) -> None:
         for _ in range(3):
             for f in [pool.submit(ctxs[c].msm, *args_of[c]) for c in (hs.SELENE, hs.HELIOS)]:
                 f.result()
+        e2e_step_ms = []
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
+            ts = time.perf_counter()
             for f in [pool.submit(ctxs[c].msm, *args_of[c]) for c in (hs.SELENE, hs.HELIOS)]:
                 f.result()
+            e2e_step_ms.append((time.perf_counter() - ts) * 1e3)
         e2e_s = (time.perf_counter() - t0) / e2e_steps
     for c in ctxs.values():
         c.set_split(head_split)
@@ -950,6 +965,9 @@ def run_ours(args) -> None:
                     "h2d_bytes_per_step": 2 * n * (32 + 120), "d2h_bytes_per_step": 2 * 120,
                     "api": "hs_msm(point_fmt=HS_FMT_JACOBIAN51, out_fmt=HS_FMT_JACOBIAN51), pinned host buffers",
                     "calls": "one per curve from a pool of two host threads, Selene first", "window_split_min": e2e_split,
+                    "step_ms": {"median": statistics.median(e2e_step_ms), "min": min(e2e_step_ms),
+                                "max": max(e2e_step_ms)},
+                    "h2d_GBps_before": round(statistics.median(h2d_gbps), 1),
                     "one_batch_call": {"value": ws * 2 * n / e2e_batch_s, "unit": "points/s",
                                        "api": "hs_msm_batch with both MSMs (HS_FMT_JACOBIAN51 in and out)"}},
             "roofline": {"bound": "imad", "achieved": achieved / 1e12, "peak": imad_peak / 1e12,
