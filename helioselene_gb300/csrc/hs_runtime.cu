@@ -182,13 +182,32 @@ static void plan_chunks(BatchPlan &p)
     p.CH = (uint32_t)ch;
 }
 
-// Buckets per level-1 group for a plan of nb buckets: 8 while the groups are
-// few (their threads are the parallelism of level 1), more once there are
-// millions of buckets, so that level 2 -- latency-bound, a scan per window --
-// has fewer groups to combine.
+// Buckets per level-1 group for a plan of nb buckets.  A group is one thread's
+// chain of 2 m0 additions and the groups are level 1's parallelism: 8 for one
+// large MSM, fewer for small plans (latency-bound, so shorter chains on more
+// threads win), more once there are millions of buckets, so that level 2 --
+// latency-bound, a scan per window -- has fewer groups to combine.
 static uint32_t group_size(uint64_t nb)
 {
-    return nb < (1ull << 21) ? RED_GROUP : nb < (1ull << 22) ? 2 * RED_GROUP : 4 * RED_GROUP;
+    if (nb >= (1ull << 22))
+        return 4 * RED_GROUP;
+    if (nb >= (1ull << 21))
+        return 2 * RED_GROUP;
+    if (nb >= (1ull << 18))
+        return RED_GROUP;
+    return nb >= (1ull << 16) ? RED_GROUP / 2 : RED_GROUP / 4;
+}
+
+// Entries per accumulation segment at most.  A large plan keeps about two
+// buckets' worth (one segment per bucket, few merges: the accumulation is
+// throughput-bound).  A plan too small to fill the device is latency-bound --
+// its longest segment sets the time -- so the cap shrinks with the entry count
+// (about 65536 segments' worth), down to 4, at the price of more, short merges.
+static uint32_t seg_cap(uint64_t ent, uint64_t nb)
+{
+    const uint64_t avg = nb ? (ent + nb - 1) / nb : 1;
+    const uint64_t big = std::max<uint64_t>(16, std::min<uint64_t>(128, 2 * avg));
+    return (uint32_t)std::max<uint64_t>(4, std::min<uint64_t>(big, ent / 65536));
 }
 
 BatchPlan make_batch_plan(const Context &ctx, int curve, const size_t *sizes, uint32_t M)
@@ -239,8 +258,7 @@ BatchPlan make_batch_plan(const Context &ctx, int curve, const size_t *sizes, ui
     p.WS = (uint32_t)ws;
     p.entries_bound = ent;
     p.max_entries = (uint32_t)std::max<uint64_t>(1, ent);
-    const uint64_t avg = nb ? (ent + nb - 1) / nb : 1;
-    p.L = (uint32_t)std::max<uint64_t>(16, std::min<uint64_t>(128, 2 * avg));
+    p.L = seg_cap(ent, nb);
     p.max_segs = (uint32_t)(std::min<uint64_t>(ent, nb) + ent / p.L + 1);
     p.hist_blocks = (p.NB + SEG_HIST_THREADS - 1) / SEG_HIST_THREADS;
     plan_chunks(p);
@@ -285,8 +303,7 @@ BatchPlan make_fixed_plan(int curve, size_t n, int c, uint32_t count)
     p.WS = count;
     p.entries_bound = ent;
     p.max_entries = (uint32_t)std::max<uint64_t>(1, ent);
-    const uint64_t avg = (ent + p.NB - 1) / p.NB;
-    p.L = (uint32_t)std::max<uint64_t>(16, std::min<uint64_t>(128, 2 * avg));
+    p.L = seg_cap(ent, p.NB);
     p.max_segs = (uint32_t)(std::min<uint64_t>(ent, p.NB) + ent / p.L + 1);
     p.hist_blocks = (p.NB + SEG_HIST_THREADS - 1) / SEG_HIST_THREADS;
     plan_chunks(p);
@@ -306,7 +323,7 @@ BatchPlan make_window_plan(int curve, size_t n, int c, uint32_t w_lo, uint32_t w
     d.c = (uint32_t)c;
     d.W = (uint32_t)((257 + c - 1) / c);
     d.B = 1u << (c - 1);
-    d.m0 = std::min<uint32_t>(RED_GROUP, d.B);
+    d.m0 = std::min<uint32_t>(group_size((uint64_t)w_cnt * d.B), d.B);
     d.log2m0 = 0;
     while ((1u << d.log2m0) < d.m0)
         d.log2m0++;
@@ -326,8 +343,7 @@ BatchPlan make_window_plan(int curve, size_t n, int c, uint32_t w_lo, uint32_t w
     p.WS = w_cnt;
     p.entries_bound = ent;
     p.max_entries = (uint32_t)std::max<uint64_t>(1, ent);
-    const uint64_t avg = (ent + p.NB - 1) / p.NB;
-    p.L = (uint32_t)std::max<uint64_t>(16, std::min<uint64_t>(128, 2 * avg));
+    p.L = seg_cap(ent, p.NB);
     p.max_segs = (uint32_t)(std::min<uint64_t>(ent, p.NB) + ent / p.L + 1);
     p.hist_blocks = (p.NB + SEG_HIST_THREADS - 1) / SEG_HIST_THREADS;
     plan_chunks(p);
