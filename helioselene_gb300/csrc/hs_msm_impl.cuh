@@ -160,7 +160,11 @@ __global__ void __launch_bounds__(HEAVY_THREADS) k_merge_heavy(const uint32_t *_
             acc = G::add(acc, load_xyzz(seg_sum + 8 * (size_t)(s0 + j)));
         store_xyzz(sh + 8 * threadIdx.x, acc);
         __syncthreads();
-        for (uint32_t stride = HEAVY_THREADS / 2; stride > 0; stride >>= 1) {
+        // the tree spans only the threads that hold a segment (a power of two)
+        uint32_t width = 1;
+        while (width < ns && width < HEAVY_THREADS)
+            width <<= 1;
+        for (uint32_t stride = width / 2; stride > 0; stride >>= 1) {
             if (threadIdx.x < stride) {
                 Xyzz a = load_xyzz(sh + 8 * threadIdx.x);
                 Xyzz b = load_xyzz(sh + 8 * (threadIdx.x + stride));
@@ -293,12 +297,13 @@ __device__ __forceinline__ void block_tree_sum(uint4 *sh, uint32_t N, const Xyzz
 }
 
 // k_window_chunks: thread i of a chunk first runs a top-down running sum over
-// its q = 4 consecutive groups (lo = t0 + i q):
+// its q consecutive groups (lo = t0 + i q):
 //     r_i = sum run_t,  w_i = sum (t - lo) run_t,  a_i = sum acc_t,
 // then the block scans r (X_i = sum_{j >= i} r_j) and thread i contributes
 //     a_i + m0 (w_i + q X_i [i >= 1]),
-// which sums to C_b; X_0 is R_b.  Four groups per thread keep both the
-// sequential part and the scan's extra work small.
+// which sums to C_b; X_0 is R_b.  A full chunk of 256 groups takes q = 4 per
+// thread (the sequential part and the scan's extra work both small); a window
+// of at most 64 groups takes one per thread, so that only the scan is serial.
 constexpr uint32_t RED_CHUNK_Q = 4;
 constexpr uint32_t RED_CHUNK_THREADS = RED_CHUNK / RED_CHUNK_Q;
 
@@ -316,7 +321,9 @@ __global__ void __launch_bounds__(RED_CHUNK_THREADS) k_window_chunks(const uint4
     const MsmDesc d = desc[mi];
     const uint32_t nbk = d.T > RED_CHUNK ? d.T / RED_CHUNK : 1;
     const uint32_t nt = d.T < RED_CHUNK ? d.T : RED_CHUNK;
-    const uint32_t q = nt < RED_CHUNK_Q ? nt : RED_CHUNK_Q;
+    // groups per thread: 4 for a full chunk, fewer when a window has fewer
+    // groups than threads (a shorter running sum, the scan takes the rest)
+    const uint32_t q = nt > RED_CHUNK_THREADS ? nt / RED_CHUNK_THREADS : 1;
     const uint32_t P = nt / q;
     const uint32_t local = ch - d.chunk_base;
     const uint32_t k = local / nbk, b = local % nbk;
@@ -639,7 +646,8 @@ cudaError_t msm_tail(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
         k_reduce_groups<C><<<(p.G + threads - 1) / threads, threads, 0, st>>>(b.seg_off, b.seg_sum, b.desc, p.M,
                                                                             p.G, b.redA);
         HS_LAUNCH_CHECK(ctx);
-        const uint32_t t2 = std::max<uint32_t>(32, std::min<uint32_t>(RED_CHUNK_THREADS, p.max_T / RED_CHUNK_Q));
+        // one thread per group up to RED_CHUNK_THREADS groups, then q groups each
+        const uint32_t t2 = std::max<uint32_t>(32, std::min<uint32_t>(RED_CHUNK_THREADS, p.max_T));
         if (p.max_nbk == 1) {  // one chunk per window: chunk index == window slot
             k_window_chunks<C, true><<<p.CH, t2, 0, st>>>(b.redA, b.desc, p.M, b.redS);
             HS_LAUNCH_CHECK(ctx);

@@ -202,12 +202,13 @@ static uint32_t group_size(uint64_t nb)
 // buckets' worth (one segment per bucket, few merges: the accumulation is
 // throughput-bound).  A plan too small to fill the device is latency-bound --
 // its longest segment sets the time -- so the cap shrinks with the entry count
-// (about 65536 segments' worth), down to 4, at the price of more, short merges.
+// (about 65536 segments' worth), down to 8, at the price of more, short merges
+// (below 8 the merges of the largest buckets would outlast the accumulation).
 static uint32_t seg_cap(uint64_t ent, uint64_t nb)
 {
     const uint64_t avg = nb ? (ent + nb - 1) / nb : 1;
     const uint64_t big = std::max<uint64_t>(16, std::min<uint64_t>(128, 2 * avg));
-    return (uint32_t)std::max<uint64_t>(4, std::min<uint64_t>(big, ent / 65536));
+    return (uint32_t)std::max<uint64_t>(8, std::min<uint64_t>(big, ent / 65536));
 }
 
 BatchPlan make_batch_plan(const Context &ctx, int curve, const size_t *sizes, uint32_t M)
