@@ -113,9 +113,12 @@ static int model_window(size_t n)
     // size class on the device and installs rules that override it.  On GB300 at
     // n = 2^20 the measured optimum agrees (c = 16: 16 full windows plus a
     // carry window that is almost empty).
+    // Below c = 8 the model's work saving does not pay on the GPU: small MSMs are
+    // latency-bound, and c = 8 (32 full windows, the top one with 7 used bits)
+    // measured fastest from 512 to 4096 points on both curves.
     int best = 8;
     double best_cost = 1e300;
-    for (int c = 4; c <= 20; c++) {
+    for (int c = 8; c <= 20; c++) {
         const double W = (257 + c - 1) / c;
         const double cost = W * (10.0 * (double)n + 28.0 * (double)(1u << (c - 1)));
         if (cost < best_cost) {
@@ -202,13 +205,15 @@ static uint32_t group_size(uint64_t nb)
 // buckets' worth (one segment per bucket, few merges: the accumulation is
 // throughput-bound).  A plan too small to fill the device is latency-bound --
 // its longest segment sets the time -- so the cap shrinks with the entry count
-// (about 65536 segments' worth), down to 8, at the price of more, short merges
-// (below 8 the merges of the largest buckets would outlast the accumulation).
+// (about 65536 segments' worth), down to 8 and to a quarter of the mean bucket,
+// at the price of more, short merges (shorter segments made the merges of the
+// largest buckets outlast the accumulation).
 static uint32_t seg_cap(uint64_t ent, uint64_t nb)
 {
     const uint64_t avg = nb ? (ent + nb - 1) / nb : 1;
     const uint64_t big = std::max<uint64_t>(16, std::min<uint64_t>(128, 2 * avg));
-    return (uint32_t)std::max<uint64_t>(8, std::min<uint64_t>(big, ent / 65536));
+    const uint64_t floor = std::max<uint64_t>(8, avg / 4);  // at most ~4 segments per typical bucket
+    return (uint32_t)std::min<uint64_t>(big, std::max<uint64_t>(floor, ent / 65536));
 }
 
 BatchPlan make_batch_plan(const Context &ctx, int curve, const size_t *sizes, uint32_t M)
