@@ -301,9 +301,10 @@ __device__ __forceinline__ void block_tree_sum(uint4 *sh, uint32_t N, const Xyzz
 //     r_i = sum run_t,  w_i = sum (t - lo) run_t,  a_i = sum acc_t,
 // then the block scans r (X_i = sum_{j >= i} r_j) and thread i contributes
 //     a_i + m0 (w_i + q X_i [i >= 1]),
-// which sums to C_b; X_0 is R_b.  A full chunk of 256 groups takes q = 4 per
-// thread (the sequential part and the scan's extra work both small); a window
-// of at most 64 groups takes one per thread, so that only the scan is serial.
+// which sums to C_b; X_0 is R_b.  q = 4 groups per thread keeps both the
+// sequential part and the scans' extra work small; in a plan of few windows
+// (latency-bound) a window of at most 64 groups takes one per thread, so that
+// only the scan is serial.
 constexpr uint32_t RED_CHUNK_Q = 4;
 constexpr uint32_t RED_CHUNK_THREADS = RED_CHUNK / RED_CHUNK_Q;
 
@@ -312,7 +313,7 @@ constexpr uint32_t RED_CHUNK_THREADS = RED_CHUNK / RED_CHUNK_Q;
 template <class C, bool DIRECT>
 __global__ void __launch_bounds__(RED_CHUNK_THREADS) k_window_chunks(const uint4 *__restrict__ in,
                                                                     const MsmDesc *__restrict__ desc, uint32_t M,
-                                                                    uint4 *__restrict__ outC)
+                                                                    uint4 *__restrict__ outC, int wide)
 {
     using G = Group<C>;
     __shared__ uint4 sh[RED_CHUNK_THREADS * 8];
@@ -321,9 +322,10 @@ __global__ void __launch_bounds__(RED_CHUNK_THREADS) k_window_chunks(const uint4
     const MsmDesc d = desc[mi];
     const uint32_t nbk = d.T > RED_CHUNK ? d.T / RED_CHUNK : 1;
     const uint32_t nt = d.T < RED_CHUNK ? d.T : RED_CHUNK;
-    // groups per thread: 4 for a full chunk, fewer when a window has fewer
-    // groups than threads (a shorter running sum, the scan takes the rest)
-    const uint32_t q = nt > RED_CHUNK_THREADS ? nt / RED_CHUNK_THREADS : 1;
+    // groups per thread: RED_CHUNK_Q, or (wide: a plan of few windows, so
+    // latency-bound) as few as fill the block, the scan taking the rest
+    const uint32_t q = wide ? (nt > RED_CHUNK_THREADS ? nt / RED_CHUNK_THREADS : 1)
+                            : (nt < RED_CHUNK_Q ? nt : RED_CHUNK_Q);
     const uint32_t P = nt / q;
     const uint32_t local = ch - d.chunk_base;
     const uint32_t k = local / nbk, b = local % nbk;
@@ -646,13 +648,21 @@ cudaError_t msm_tail(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
         k_reduce_groups<C><<<(p.G + threads - 1) / threads, threads, 0, st>>>(b.seg_off, b.seg_sum, b.desc, p.M,
                                                                             p.G, b.redA);
         HS_LAUNCH_CHECK(ctx);
-        // one thread per group up to RED_CHUNK_THREADS groups, then q groups each
-        const uint32_t t2 = std::max<uint32_t>(32, std::min<uint32_t>(RED_CHUNK_THREADS, p.max_T));
+        // A plan of few chunks (one or a few MSMs) is latency-bound, and so are
+        // windows of at most 16 groups: one thread per group up to
+        // RED_CHUNK_THREADS groups.  Many chunks of more groups (a batch of larger
+        // MSMs) fill the device, and RED_CHUNK_Q groups per thread keep the scans'
+        // extra work small.  (Measured: 256 FCMP++ verifications, 16 groups per
+        // window, 51k -> 65k per second one group per thread; 1024 MSMs of
+        // 64..65536 points 1.5% faster with four.)
+        const int wide = p.CH <= 4u * (uint32_t)ctx.sm_count || p.max_T <= 16;
+        const uint32_t t2 =
+            std::max<uint32_t>(32, std::min<uint32_t>(RED_CHUNK_THREADS, wide ? p.max_T : p.max_T / RED_CHUNK_Q));
         if (p.max_nbk == 1) {  // one chunk per window: chunk index == window slot
-            k_window_chunks<C, true><<<p.CH, t2, 0, st>>>(b.redA, b.desc, p.M, b.redS);
+            k_window_chunks<C, true><<<p.CH, t2, 0, st>>>(b.redA, b.desc, p.M, b.redS, wide);
             HS_LAUNCH_CHECK(ctx);
         } else {
-            k_window_chunks<C, false><<<p.CH, t2, 0, st>>>(b.redA, b.desc, p.M, b.redC);
+            k_window_chunks<C, false><<<p.CH, t2, 0, st>>>(b.redA, b.desc, p.M, b.redC, wide);
             HS_LAUNCH_CHECK(ctx);
             const uint32_t t3 = std::max<uint32_t>(32, std::min<uint32_t>(RED_CHUNK, p.max_nbk));
             k_window_sum<C><<<p.WS, t3, 0, st>>>(b.redC, b.desc, p.M, b.redS);
