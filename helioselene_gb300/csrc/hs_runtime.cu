@@ -212,8 +212,8 @@ static uint32_t seg_cap(uint64_t ent, uint64_t nb)
 {
     const uint64_t avg = nb ? (ent + nb - 1) / nb : 1;
     const uint64_t big = std::max<uint64_t>(16, std::min<uint64_t>(128, 2 * avg));
-    const uint64_t floor = std::max<uint64_t>(8, avg / 4);  // at most ~4 segments per typical bucket
-    return (uint32_t)std::min<uint64_t>(big, std::max<uint64_t>(floor, ent / 65536));
+    const uint64_t least = std::max<uint64_t>(8, avg / 4);  // at most ~4 segments per typical bucket
+    return (uint32_t)std::min<uint64_t>(big, std::max<uint64_t>(least, ent / 65536));
 }
 
 BatchPlan make_batch_plan(const Context &ctx, int curve, const size_t *sizes, uint32_t M)
