@@ -91,7 +91,13 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.time(), line.strip()))
+
+    def wait_ready(self, timeout: float = 10.0) -> None:
+        """block until nvidia-smi has printed its first sample (it takes a while to start)"""
+        t0 = time.time()
+        while self.proc and not self.lines and time.time() - t0 < timeout:
+            time.sleep(0.01)
 
     def __exit__(self, *exc):
         if self.proc:
@@ -101,10 +107,22 @@ class ClockSampler:
             except subprocess.TimeoutExpired:
                 self.proc.kill()
 
-    def summary(self) -> dict:
+    def summary(self, t0: float = None, t1: float = None) -> dict:
+        """samples read within [t0, t1 + one interval] (the timed region), or the
+        first sample after t0 when the region is shorter than the interval"""
+        lines = self.lines
+        note = "samples within the timed region"
+        if t0 is not None:
+            inside = [ln for ts, ln in lines if t0 <= ts <= t1 + 0.05]
+            if not inside:
+                inside = [ln for ts, ln in lines if ts >= t0][:1]
+                note = "the first sample after the timed region began (region shorter than the 50 ms interval)"
+            lines = inside
+        else:
+            lines = [ln for _, ln in lines]
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for ln in lines:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 9:
                 continue
@@ -117,9 +135,9 @@ class ClockSampler:
                 if val.lower() == "active":
                     reasons.add(name)
         if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0, "note": note}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "note": note}
 
 
 def make_inputs(hs, ctx, torch, n: int, device: str):
@@ -805,8 +823,11 @@ def run_ours(args) -> None:
     torch.cuda.synchronize()
     launches0 = ctx.launches + ctx2.launches
     with ClockSampler(local) as clocks:
+        clocks.wait_ready()
+        w0 = time.time()
         t_start, t_end = run_steps(args.steps)
         torch.cuda.synchronize()
+        w1 = time.time()
     launches = ctx.launches + ctx2.launches - launches0
     ms = t_start.elapsed_time(t_end)
     if dist:
@@ -959,7 +980,7 @@ def run_ours(args) -> None:
                        "isolated_note": "median of 5 single steps, each after a 256 MiB L2 flush and a synchronise",
                        "inputs": "device-resident scalars + canonical affine bases"},
             "per_curve": per_curve,
-            "clocks": clocks.summary(),
+            "clocks": clocks.summary(w0, w1),
             "gpu_launches": launches,
             "e2e": {"value": ws * 2 * n / e2e_s, "unit": "points/s",
                     "h2d_bytes_per_step": 2 * n * (32 + 120), "d2h_bytes_per_step": 2 * 120,
