@@ -4,8 +4,11 @@
 
 One step = one Helios MSM and one Selene MSM of n = 2^20 points each (uniform
 scalars mod the group order, SWU bases, 1% edge slices), on inputs already
-resident in device memory; L2 is flushed (256 MiB memset) before every step,
-outside the timed events.  `value` = 2n points / step time, max over ranks.
+resident in device memory.  The K timed steps are issued back to back with no
+L2 flush between them: one step's inputs and workspaces (2 x 96 MiB of
+scalars and bases alone) exceed the 129 MB L2.  `value` = 2n points / step
+time, max over ranks.  The isolated-step latency beside it flushes L2 (256 MiB
+memset) before each of its steps.
 `e2e` = the same metric through the reference-facing call with host buffers:
 hs_msm with the reference's helios_jacobian records (pinned host memory),
 host-to-device copies, the device MSM, and the result read back, every step.
@@ -40,7 +43,7 @@ sys.path.insert(0, str(ROOT))
 METRIC = "MSM points/sec at n=2^20 (both curves, bit-exact); batched-serving MSMs/sec + p50/p99 vs plain"
 WORKLOAD = ("Helios + Selene vartime Pippenger MSM, n=2^20 each; scalars uniform mod order; "
             "SWU-derived affine bases; 1% edge slices (zero, order-1, repeated base, top-window-only)")
-SEED = 0x48454C494F53
+from helioselene_gb300.workload import BENCH_SEED as SEED  # noqa: E402
 IMAD_PER_MODMUL = {0: 144, 1: 232}  # F_p, F_q: 2 IMAD per 32x32->64 product
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_accumulate launch at
 # n = 2^20, mean of the Helios and Selene launches of one ncu capture
@@ -186,16 +189,15 @@ def affine_to_jac51_fast(aff: np.ndarray, n: int) -> np.ndarray:
     return out.view(np.uint8).reshape(-1)
 
 
-def run_batched(hs, torch, device: str, local: int, steps: int) -> dict:
+def run_batched(hs, torch, device: str, local: int, steps: int, with_oracle: bool = True) -> dict:
     """Config 3: 1024 independent MSMs, sizes log-uniform in [64, 65536], curve
     Bernoulli(0.5), as one batched launch sequence per curve (two contexts, so the
     two curve groups overlap) against the plain per-call path on the same MSMs."""
     from helioselene_gb300 import autotune
-    from helioselene_gb300.workload import ORDER, random_field_bytes, random_scalars
-    rng = np.random.default_rng(SEED + 3)
+    from helioselene_gb300.workload import batched_stream
+    bs = batched_stream(SEED + 3)
     count = 1024
-    sizes = np.exp(rng.uniform(np.log(64), np.log(65536), count)).astype(np.int64)
-    curves = rng.integers(0, 2, count)
+    sizes, curves = bs["sizes"], bs["curves"]
     ctxs = [hs.Context(local), hs.Context(local)]
     t0 = time.time()
     tuned = autotune.load_or_tune(ctxs[0], cache=Path.home() / ".cache" / "helioselene_gb300_autotune.json",
@@ -205,20 +207,20 @@ def run_batched(hs, torch, device: str, local: int, steps: int) -> dict:
     tune_s = time.time() - t0
     groups = {}
     for curve in (hs.HELIOS, hs.SELENE):
-        idx = np.nonzero(curves == curve)[0]
-        sz = [int(sizes[i]) for i in idx]
+        g0 = bs[curve]
+        sz = g0["sizes"]
         total = sum(sz)
-        d_u = torch.from_numpy(random_field_bytes(rng, total).reshape(-1)).to(device)
+        d_u = torch.from_numpy(g0["u"].reshape(-1)).to(device)
         d_pts = torch.empty(total * 64, dtype=torch.uint8, device=device)
-        d_sc = torch.from_numpy(random_scalars(rng, total, ORDER[curve]).reshape(-1)).to(device)
+        d_sc = torch.from_numpy(g0["scalars"].reshape(-1)).to(device)
         d_out = torch.empty(len(sz) * 120, dtype=torch.uint8, device=device)
         d_out_plain = torch.empty(len(sz) * 120, dtype=torch.uint8, device=device)
         torch.cuda.synchronize()
         ctxs[0].map_to_curve_device(curve, d_u.data_ptr(), total, d_pts.data_ptr())
         torch.cuda.synchronize()
         offs = np.concatenate([[0], np.cumsum(sz)])
-        groups[curve] = {"idx": idx, "sizes": sz, "offs": offs, "d_sc": d_sc, "d_pts": d_pts, "d_out": d_out,
-                         "d_out_plain": d_out_plain}
+        groups[curve] = {"idx": g0["idx"], "sizes": sz, "offs": offs, "d_sc": d_sc, "d_pts": d_pts, "d_out": d_out,
+                         "d_out_plain": d_out_plain, "scalars": g0["scalars"]}
     streams = [torch.cuda.ExternalStream(c.stream, device=device) for c in ctxs]
 
     def batched_once():
@@ -267,20 +269,35 @@ def run_batched(hs, torch, device: str, local: int, steps: int) -> dict:
         a = plain_ctx.compress(c, groups[c]["d_out"].cpu().numpy(), hs.FMT_JACOBIAN51)
         p = plain_ctx.compress(c, groups[c]["d_out_plain"].cpu().numpy(), hs.FMT_JACOBIAN51)
         same = same and bool((a == p).all())
+    # every batched result against the oracle (one MSM per host thread)
+    oracle_ok, oracle_s = None, None
+    if with_oracle:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import oracle
+        t1 = time.perf_counter()
+        oracle_ok = True
+        for c in (0, 1):
+            g = groups[c]
+            got = plain_ctx.compress(c, g["d_out"].cpu().numpy(), hs.FMT_JACOBIAN51).reshape(-1, 32)
+            want = oracle.msm_many(c, g["scalars"], g["d_pts"].cpu().numpy(), g["sizes"])
+            oracle_ok = oracle_ok and all(got[i].tobytes() == want[i] for i in range(len(want)))
+        oracle_s = time.perf_counter() - t1
     total_pts = int(sizes.sum())
     res = {"msms": count, "points": total_pts, "sizes": "log-uniform [64, 65536], seed-fixed",
            "curves": {"helios": int((curves == 0).sum()), "selene": int((curves == 1).sum())},
            "msms_per_s": count / (batched_ms * 1e-3), "ms": batched_ms,
            "plain_msms_per_s": count / (plain_ms * 1e-3), "plain_ms": plain_ms,
            "speedup_vs_plain": plain_ms / batched_ms, "points_per_s": total_pts / (batched_ms * 1e-3),
-           "bit_exact_vs_plain": bool(same), "autotune": {"seconds": round(tune_s, 2), **tuned},
+           "bit_exact_vs_plain": bool(same), "bit_exact_vs_oracle": oracle_ok,
+           "oracle_check": "all 1024 MSMs, one per host thread" if with_oracle else None, "oracle_s": oracle_s,
+           "autotune": {"seconds": round(tune_s, 2), **tuned},
            "graph": "one captured launch sequence per curve group, replayed"}
     for c in ctxs:
         c.close()
     return res
 
 
-def run_serving(hs, torch, device: str, local: int, requests_per_rate: int = 1000) -> dict:
+def run_serving(hs, torch, device: str, local: int, requests_per_rate: int = 1000, with_oracle: bool = True) -> dict:
     """Config 4: Poisson arrivals of MSM requests, sizes from the mixture 70%
     log-uniform [256, 4096], 25% [4096, 65536], 5% 2^18, curves alternating;
     75% of each request's bases come from a 2^18-point resident pool per curve,
@@ -288,7 +305,7 @@ def run_serving(hs, torch, device: str, local: int, requests_per_rate: int = 100
     batches of up to 2^23 points)
     against the plain path: the same requests one MSM per launch sequence, one
     at a time (a server with one slot and one request per batch)."""
-    from helioselene_gb300.workload import ORDER, random_field_bytes, random_scalars
+    from helioselene_gb300.workload import ORDER, random_field_bytes, random_scalars, serving_sizes
     rng = np.random.default_rng(SEED + 4)
     pool_n = 1 << 18
     res_n = 1 << 19
@@ -313,10 +330,7 @@ def run_serving(hs, torch, device: str, local: int, requests_per_rate: int = 100
     perm.numpy().view(np.uint32)[:] = rng.integers(0, pool_n, 2 * res_n).astype(np.uint32)
 
     def draw(count):
-        u = rng.random(count)
-        n = np.where(u < 0.70, np.exp(rng.uniform(np.log(256), np.log(4096), count)),
-                     np.where(u < 0.95, np.exp(rng.uniform(np.log(4096), np.log(65536), count)), 2.0**18))
-        n = n.astype(np.int64)
+        n = serving_sizes(rng, count)
         reqs = []
         for i in range(count):
             curve = i % 2
@@ -336,8 +350,10 @@ def run_serving(hs, torch, device: str, local: int, requests_per_rate: int = 100
         fr = fresh[curve].numpy()[64 * fo:64 * (fo + nfresh)]
         return curve, sc, idx, fr
 
-    def run(srv, reqs, rate):
-        arrivals = np.cumsum(rng.exponential(1.0 / rate, len(reqs))) if rate else np.zeros(len(reqs))
+    def run(srv, reqs, rate, arrivals=None, results=None):
+        """submit reqs at the given arrival times (Poisson at `rate`, or all at once)"""
+        if arrivals is None:
+            arrivals = np.cumsum(rng.exponential(1.0 / rate, len(reqs))) if rate else np.zeros(len(reqs))
         tickets = []
         t0 = time.perf_counter()
         for r, at in zip(reqs, arrivals):
@@ -346,15 +362,19 @@ def run_serving(hs, torch, device: str, local: int, requests_per_rate: int = 100
                 time.sleep(delay)
             curve, sc, idx, fr = views(r)
             tickets.append(srv.submit(curve, sc, idx, fr))
-        lat = [srv.wait(t, 600000)[1] for t in tickets]
+        done = [srv.wait(t, 600000) for t in tickets]
+        lat = [d[1] for d in done]
         wall = time.perf_counter() - t0
+        if results is not None:
+            results.extend(d[0] for d in done)
         return {"rate_offered": rate or "all-at-once", "requests": len(reqs), "msms_per_s": len(reqs) / wall,
                 "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
                 "mean_points": float(np.mean([r[2] for r in reqs]))}
 
     out = {"requests_per_rate": requests_per_rate, "pool_points_per_curve": pool_n,
            "mix": "70% [256,4096], 25% [4096,65536], 5% 2^18 log-uniform; 75% pool bases, 25% fresh",
-           "plain": "same requests, one MSM per launch sequence, one at a time", "rates": []}
+           "plain": "the same requests at the same arrival times, one MSM per launch sequence, one at a time",
+           "rates": []}
     srv = hs.Server(local, slots=8, max_batch_points=1 << 23, max_batch_msms=1024)
     plain = hs.Server(local, slots=1, max_batch_msms=1)
     for s in (srv, plain):
@@ -363,11 +383,35 @@ def run_serving(hs, torch, device: str, local: int, requests_per_rate: int = 100
     warm = draw(64)
     run(srv, warm, 0)
     run(plain, warm[:16], 0)
+    checked = None
     for rate in (1000, 3000, 9000, 0):
         reqs = draw(requests_per_rate)
-        a = run(srv, reqs, rate)
-        bsec = run(plain, reqs[: max(100, requests_per_rate // 5)], rate)
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, len(reqs))) if rate else np.zeros(len(reqs))
+        res_srv, res_plain = [], []
+        a = run(srv, reqs, rate, arrivals, res_srv)
+        bsec = run(plain, reqs, rate, arrivals, res_plain)
+        a["same_as_plain"] = res_srv == res_plain
         out["rates"].append({"serving": a, "plain": bsec})
+        if rate == 0:
+            checked = (reqs, res_srv)
+    # a sample of the all-at-once requests against the oracle (pooled + fresh bases)
+    if with_oracle and checked:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import oracle
+        reqs, res = checked
+        sample = list(range(0, len(reqs), max(1, len(reqs) // 64)))
+        ok = True
+        t1 = time.perf_counter()
+        for curve in (hs.HELIOS, hs.SELENE):
+            sel = [i for i in sample if reqs[i][0] == curve]
+            sc = np.concatenate([views(reqs[i])[1].reshape(-1, 32) for i in sel])
+            pts = np.concatenate([np.concatenate([pools[curve][views(reqs[i])[2]], views(reqs[i])[3].reshape(-1, 64)])
+                                  for i in sel])
+            want = oracle.msm_many(curve, sc, pts, [reqs[i][2] for i in sel])
+            ok = ok and all(res[i] == want[j] for j, i in enumerate(sel))
+        out["bit_exact_vs_oracle"] = ok
+        out["oracle_check"] = f"{len(sample)} of the {len(reqs)} all-at-once requests, every curve"
+        out["oracle_s"] = time.perf_counter() - t1
     out["server_stats"] = srv.stats()
     peak = out["rates"][-1]
     out["msms_per_s"] = peak["serving"]["msms_per_s"]
@@ -378,7 +422,8 @@ def run_serving(hs, torch, device: str, local: int, requests_per_rate: int = 100
     return out
 
 
-def run_fixed(hs, torch, device: str, local: int, count: int = 4096, chunk: int = 256) -> dict:
+def run_fixed(hs, torch, device: str, local: int, count: int = 4096, chunk: int = 256,
+              with_oracle: bool = True) -> dict:
     """Config 5: Pedersen-style commitments r*H + sum v_i G_i over n = 2^20 resident
     generators per curve with device window tables; 4096 commitments per curve,
     submitted 256 at a time from two device scalar buffers used alternately;
@@ -446,7 +491,18 @@ def run_fixed(hs, torch, device: str, local: int, count: int = 4096, chunk: int 
         # the last chunk used buffer (count // chunk - 1) & 1; compare chunk 0 (buffer 0) with the plain path
         got = ctx.compress(curve, aff[nsparse:nsparse + k], hs.FMT_AFFINE)
         want = ctx.compress(curve, d_plain.cpu().numpy(), hs.FMT_JACOBIAN51)
+        # a sparse and a dense commitment of chunk 0 against the oracle (blinding
+        # last in each commitment's scalars, H appended as generator n)
+        oracle_ok = None
+        if with_oracle:
+            sys.path.insert(0, str(ROOT / "oracle"))
+            import oracle
+            all_aff = ctx.compress(curve, aff[:chunk], hs.FMT_AFFINE).reshape(chunk, 32)
+            oracle_ok = all(oracle.msm_mt(curve, bufs[0][j].cpu().numpy(), gens, oracle.default_threads()) ==
+                            all_aff[j].tobytes() for j in (0, nsparse))
         out[name] = {"window": fb.window, "table_bytes": fb.table_bytes, "table_build_s": table_s,
+                     "bit_exact_vs_oracle": oracle_ok, "oracle_check": "commitments 0 (sparse) and "
+                                                                        f"{nsparse} (dense) of the first chunk",
                      "commitments_per_s": count / (fixed_ms * 1e-3), "ms": fixed_ms,
                      "plain_ms_per_commitment": plain_ms,
                      "speedup_vs_plain": plain_ms * count / fixed_ms,
@@ -458,11 +514,14 @@ def run_fixed(hs, torch, device: str, local: int, count: int = 4096, chunk: int 
     return out
 
 
-def run_sweep(hs, torch, device: str, local: int, flush) -> dict:
+def run_sweep(hs, torch, device: str, local: int, flush, with_oracle: bool = True) -> dict:
     """Config 2: single MSMs at n = 2^10, 2^12, ..., 2^22 on both curves, uniform
     scalars mod order, SWU bases, 1% edge slices (zero, order-1, repeated base,
     top-window-only); one MSM at a time, L2 flushed before each, median of 3."""
     from helioselene_gb300.workload import make_workload
+    if with_oracle:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import oracle
     ctx = hs.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream, device=device)
     out = {}
@@ -490,7 +549,12 @@ def run_sweep(hs, torch, device: str, local: int, flush) -> dict:
                 torch.cuda.synchronize()
                 ts.append(a.elapsed_time(b))
             ms = sorted(ts)[1]
-            rows.append({"n": n, "ms": ms, "points_per_s": n / (ms * 1e-3)})
+            row = {"n": n, "ms": ms, "points_per_s": n / (ms * 1e-3)}
+            if with_oracle:
+                got = ctx.compress(curve, d_out[:120].cpu().numpy(), hs.FMT_JACOBIAN51).tobytes()
+                row["bit_exact_vs_oracle"] = got == oracle.msm_mt(curve, w.scalars, d_pts.cpu().numpy(),
+                                                                  oracle.default_threads())
+            rows.append(row)
             del d_u, d_sc, d_pts
         out[name] = rows
     ctx.close()
@@ -725,6 +789,19 @@ def run_decompress(hs, torch, ctxs, data, n: int, flush, imad_peak: float) -> di
     return out
 
 
+def probe_rates(rates: dict, torch, local: int, clk: dict) -> dict:
+    """the IMAD probe's instruction rates, per SM per clock at the SM clock seen
+    in the timed region (the denominator of every roofline fraction here)"""
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    mhz = clk.get("sm_mhz") or clk.get("sm_max_mhz")
+    out = {"sm_count": sms, "sm_mhz": mhz, "unit": "instructions per SM per clock",
+           "note": "mad_lo_hi: alternating mad.lo/mad.hi (1 IMAD-eq each); mad_wide: mad.wide.u32 (one 32x32->64 "
+                   "product, 2 IMAD-eq); peak = max(mad_lo_hi, 2 x mad_wide) x SMs x clock"}
+    for k, v in rates.items():
+        out[k] = round(v / (sms * mhz * 1e6), 2) if mhz else None
+    return out
+
+
 def cpu_baseline_leg(data, n: int, gpu_results: dict) -> dict:
     """The oracle port on all host cores, on the same workload; also checks the GPU results."""
     sys.path.insert(0, str(ROOT / "oracle"))
@@ -937,17 +1014,18 @@ def run_ours(args) -> None:
 
     # ---- roofline of the dominant kernel (bucket accumulation) ----
     imad_peak = ctx.measure_imad_peak()
+    imad_rates = ctx.measure_imad_rates()
     achieved = prof_total["work"] / (prof_total["ms"] * 1e-3) if prof_total["ms"] > 0 else 0.0
     acc_ms = prof_total["ms"] / max(1, prof_total["launches"])
     batched = None
     if not args.no_batched:
-        batched = run_batched(hs, torch, device, local, args.steps)
+        batched = run_batched(hs, torch, device, local, args.steps, with_oracle=not args.no_cpu)
     serving = None
     if not args.no_serving:
-        serving = run_serving(hs, torch, device, local)
+        serving = run_serving(hs, torch, device, local, with_oracle=not args.no_cpu)
     fixed = None
     if not args.no_fixed:
-        fixed = run_fixed(hs, torch, device, local)
+        fixed = run_fixed(hs, torch, device, local, with_oracle=not args.no_cpu)
     smul = None
     if not args.no_scalar_mul:
         smul = run_scalar_mul(hs, torch, ctxs, data, n, flush)
@@ -959,7 +1037,7 @@ def run_ours(args) -> None:
         verify = run_verify(hs, torch, device, local, with_cpu=(ws == 1 and not args.no_cpu))
     sweep = None
     if not args.no_sweep:
-        sweep = run_sweep(hs, torch, device, local, flush)
+        sweep = run_sweep(hs, torch, device, local, flush, with_oracle=not args.no_cpu)
     decode = None
     if not args.no_decompress:
         decode = run_decompress(hs, torch, ctxs, data, n, flush, imad_peak)
@@ -994,8 +1072,7 @@ def run_ours(args) -> None:
             "roofline": {"bound": "imad", "achieved": achieved / 1e12, "peak": imad_peak / 1e12,
                          "unit": "T IMAD/s", "frac": achieved / imad_peak if imad_peak else None,
                          "traffic": ACC_TRAFFIC_BYTES, "traffic_unit": "bytes per launch (DRAM read + write)",
-                         "traffic_source": "ncu capture of k_accumulate at n=2^20 (Helios 477.2 MB, Selene 497.5 MB), "
-                                           "profiles/k_accumulate_msm_n2p20.md",
+                         "traffic_source": "ncu capture of k_accumulate at n=2^20 (Helios 477.2 MB, Selene 497.5 MB)",
                          "kernel": "k_accumulate",
                          "work": "point-window entries x 6 modmul (batch-affine bucket add) x IMAD-eq per modmul "
                                  "(F_p 144, F_q 232), summed over one Helios and one Selene launch",
@@ -1006,7 +1083,10 @@ def run_ours(args) -> None:
                                            if imad_peak and prof_total["ms"] > 0 else None),
                          "executed_note": "the same launches counted with the products the kernel executes: "
                                           "XYZZ mixed addition, 8 products + 2 squares per entry",
-                         "whole_msm_frac": whole / imad_peak if imad_peak else None},
+                         "whole_msm_frac": whole / imad_peak if imad_peak else None,
+                         "pinned_entries": "n x ceil(256/c) per MSM (c = 16 at n = 2^20: 16 windows), "
+                                           "6 modmul each",
+                         "probe_rates": probe_rates(imad_rates, torch, local, clocks.summary(w0, w1))},
         }
         if not args.no_batched:
             line["batched"] = batched

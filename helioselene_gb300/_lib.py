@@ -77,6 +77,7 @@ SIGNATURES = {
     "hs_profile_read": (_int, [_vp, _c.POINTER(_c.c_double), _c.POINTER(_c.c_uint64), _c.POINTER(_c.c_uint64),
                                _int]),
     "hs_measure_imad_peak": (_int, [_vp, _c.POINTER(_c.c_double)]),
+    "hs_measure_imad_rates": (_int, [_vp, _c.POINTER(_c.c_double)]),
     "hs_field_op": (_int, [_vp, _int, _int, _vp, _vp, _sz, _vp]),
     "hs_fixed_base_create": (_int, [_vp, _int, _vp, _int, _sz, _vp, _int, _c.POINTER(_vp)]),
     "hs_fixed_base_commit": (_int, [_vp, _vp, _vp, _vp, _sz, _vp, _int]),

@@ -113,6 +113,12 @@ class Context:
         self._check(self._lib.hs_measure_imad_peak(self._h, ctypes.byref(v)), "hs_measure_imad_peak")
         return v.value
 
+    def measure_imad_rates(self) -> dict:
+        """the probes behind measure_imad_peak, instructions per second over the device"""
+        r = (ctypes.c_double * 4)()
+        self._check(self._lib.hs_measure_imad_rates(self._h, r), "hs_measure_imad_rates")
+        return {"mad_lo_hi": r[0], "mad_wide": r[1], "mad_lo": r[2], "mad_hi": r[3]}
+
     def field_op(self, field: int, op: int, a, b=None) -> np.ndarray:
         """Element-wise device field arithmetic (0 mul, 1 sqr, 2 add, 3 sub, 4 canon, 5 inv, 6 neg)."""
         x = _u8(a)

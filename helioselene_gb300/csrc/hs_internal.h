@@ -147,6 +147,10 @@ struct BatchPlan {
     // part-1 segment continues the sum of its first part-0 segment.
     uint32_t part_slice = 0;
     uint64_t entries_bound = 0; // sum n_i * W_i
+    // the algorithmic count of (point, window) entries: n_i * ceil(256/c_i) per
+    // MSM (the full windows of a 256-bit scalar, not the carry window), the
+    // unit of the pinned work figure that instrumentation reports
+    uint64_t entries_pinned = 0;
 };
 
 // Device buffers of one batch (carved from the arena).
@@ -261,6 +265,8 @@ cudaError_t sort_smem_attrs(int device);
 cudaError_t launch_batch(Context &ctx, const BatchPlan &p, const BatchBuffers &b, void *d_out, int out_fmt);
 void drop_graphs(Context &ctx);
 int fail(Context &ctx, cudaError_t e, const char *what);
+// the calling thread's error text, read by hs_last_error(NULL)
+void set_thread_error(const std::string &what);
 int fail_msg(Context &ctx, int code, const char *what);
 
 #define HS_LAUNCH_CHECK(ctx)                                 \

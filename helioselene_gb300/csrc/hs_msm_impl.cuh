@@ -105,16 +105,21 @@ __global__ void __launch_bounds__(128) k_accumulate(const uint4 *__restrict__ se
 // (k_window_chunks, k_window_sum): with about one warp per scheduler their
 // inlined copies overflow the instruction cache, while one shared body stays
 // resident (a call costs a few dozen instructions next to the ~2000 of an
-// addition).
+// addition).  Operands and result travel by address (the caller's local
+// memory): no 128-byte point is passed or returned by value across the call,
+// and the result is stored only after both operands have been read, so it may
+// alias either.
 template <class C>
-__device__ __noinline__ Xyzz l2_add(const Xyzz a, const Xyzz b)
+__device__ __noinline__ void l2_add(Xyzz *r, const Xyzz *a, const Xyzz *b)
 {
-    return Group<C>::add(a, b);
+    const Xyzz t = Group<C>::add(*a, *b);
+    *r = t;
 }
 template <class C>
-__device__ __noinline__ Xyzz l2_dbl(const Xyzz a)
+__device__ __noinline__ void l2_dbl(Xyzz *r, const Xyzz *a)
 {
-    return Group<C>::dbl(a);
+    const Xyzz t = Group<C>::dbl(*a);
+    *r = t;
 }
 
 // ---------------------------------------------------------------------------
@@ -273,7 +278,7 @@ __device__ __forceinline__ Xyzz block_suffix_scan(uint4 *sh, uint32_t N, Xyzz r,
             o = ld_soa(sh, i + dl, N);
         __syncthreads();
         if (take) {
-            r = l2_add<C>(r, o);
+            l2_add<C>(&r, &r, &o);
             st_soa(sh, i, N, r);
         }
         __syncthreads();
@@ -290,8 +295,11 @@ __device__ __forceinline__ void block_tree_sum(uint4 *sh, uint32_t N, const Xyzz
     st_soa(sh, i, N, v);
     __syncthreads();
     for (uint32_t stride = nt / 2; stride > 0; stride >>= 1) {
-        if (i < stride)
-            st_soa(sh, i, N, l2_add<C>(ld_soa(sh, i, N), ld_soa(sh, i + stride, N)));
+        if (i < stride) {
+            Xyzz x = ld_soa(sh, i, N), y = ld_soa(sh, i + stride, N);
+            l2_add<C>(&x, &x, &y);
+            st_soa(sh, i, N, x);
+        }
         __syncthreads();
     }
 }
@@ -333,20 +341,22 @@ __global__ void __launch_bounds__(RED_CHUNK_THREADS) k_window_chunks(const uint4
     if (i < P) {
         const size_t lo = (size_t)d.group_base + (size_t)k * d.T + (size_t)b * RED_CHUNK + (size_t)i * q;
         for (int u = (int)q - 1; u >= 0; u--) {
-            a = l2_add<C>(a, load_xyzz(in + 16 * (lo + u)));
-            r = l2_add<C>(r, load_xyzz(in + 16 * (lo + u) + 8));
+            Xyzz t = load_xyzz(in + 16 * (lo + u));
+            l2_add<C>(&a, &a, &t);
+            t = load_xyzz(in + 16 * (lo + u) + 8);
+            l2_add<C>(&r, &r, &t);
             if (u > 0)
-                w = l2_add<C>(w, r);
+                l2_add<C>(&w, &w, &r);
         }
     }
     r = block_suffix_scan<C>(sh, RED_CHUNK_THREADS, r, i, P);
     Xyzz v = (i >= 1 && i < P) ? r : G::inf();
     for (uint32_t m = q; m > 1; m >>= 1)
-        v = l2_dbl<C>(v);
-    v = l2_add<C>(v, w);
+        l2_dbl<C>(&v, &v);
+    l2_add<C>(&v, &v, &w);
     for (uint32_t m = d.m0; m > 1; m >>= 1)
-        v = l2_dbl<C>(v);
-    v = l2_add<C>(v, a);
+        l2_dbl<C>(&v, &v);
+    l2_add<C>(&v, &v, &a);
     block_tree_sum<C>(sh, RED_CHUNK_THREADS, v, i, P);
     if (i == 0) {
         if (DIRECT) {
@@ -378,8 +388,8 @@ __global__ void __launch_bounds__(RED_CHUNK) k_window_sum(const uint4 *__restric
     r = block_suffix_scan<C>(sh, RED_CHUNK, r, i, nbk);
     Xyzz v = (i >= 1 && i < nbk) ? r : G::inf();
     for (uint32_t m = d.m0 * RED_CHUNK; m > 1 && nbk > 1; m >>= 1)
-        v = l2_dbl<C>(v);
-    v = l2_add<C>(v, cb);
+        l2_dbl<C>(&v, &v);
+    l2_add<C>(&v, &v, &cb);
     block_tree_sum<C>(sh, RED_CHUNK, v, i, nbk);
     if (i == 0)
         store_xyzz(S + 8 * (size_t)s, ld_soa(sh, 0, RED_CHUNK));
@@ -627,7 +637,7 @@ cudaError_t msm_tail(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
                 k_accumulate<C, true><<<blocks, threads, 0, st>>>(b.segs, bound[1], bound[2], b.sorted, b.points,
                                                                   b.seg_sum);
             HS_LAUNCH_CHECK(ctx);
-            prof_end(ctx, ev0, j == 0 ? p.entries_bound : 0);
+            prof_end(ctx, ev0, j == 0 ? p.entries_pinned : 0);
         }
     }
     // 3. merge multi-segment buckets

@@ -257,6 +257,7 @@ BatchPlan make_batch_plan(const Context &ctx, int curve, const size_t *sizes, ui
         g += (uint64_t)d.W * d.T;
         ws += d.W;
         ent += (uint64_t)n * d.W;
+        p.entries_pinned += (uint64_t)n * (uint64_t)((256 + c - 1) / c);
     }
     p.n_total = (uint32_t)pt;
     p.NB = (uint32_t)nb;
@@ -303,6 +304,7 @@ BatchPlan make_fixed_plan(int curve, size_t n, int c, uint32_t count)
         d.shift = 0;
     }
     const uint64_t ent = (uint64_t)count * n * W;
+    p.entries_pinned = (uint64_t)count * n * (uint64_t)((256 + c - 1) / c);
     p.n_total = (uint32_t)(count * n);
     p.NB = count * B;
     p.G = count * (B / m0);
@@ -343,6 +345,11 @@ BatchPlan make_window_plan(int curve, size_t n, int c, uint32_t w_lo, uint32_t w
     d.w_cnt = w_cnt;
     d.shift = (uint32_t)c * w_lo;
     const uint64_t ent = (uint64_t)n * w_cnt;
+    {
+        const uint32_t full = (uint32_t)((256 + c - 1) / c);  // windows below the carry window
+        const uint32_t hi = std::min(full, w_lo + w_cnt);
+        p.entries_pinned = hi > w_lo ? (uint64_t)n * (hi - w_lo) : 0;
+    }
     p.n_total = (uint32_t)n;
     p.NB = w_cnt * d.B;
     p.G = w_cnt * d.T;
@@ -1074,10 +1081,12 @@ void prof_end(Context &ctx, cudaEvent_t ev0, uint64_t entries)
     ctx.prof_launches++;
 }
 
-// Two probes of the integer-multiply pipe, each counting one 32x32->64 product
-// as 2 IMAD-equivalents: (a) independent mad.lo / mad.hi chains, 8 per thread;
-// (b) independent mad.wide.u32 chains (the whole product in one instruction),
-// 8 per thread.  The ceiling is the faster of the two.
+// Probes of the integer-multiply pipe, 8 independent chains per thread:
+// MODE 0 alternates mad.lo / mad.hi (one 32x32->64 product = 2 IMAD-equivalents
+// per pair), MODE 1 is mad.lo alone, MODE 2 mad.hi alone; k_imad_wide_peak runs
+// mad.wide.u32 chains (the whole product in one instruction).  The ceiling is
+// the faster of the two product forms.
+template <int MODE>
 __global__ void k_imad_peak(uint32_t seed, int iters, uint32_t *out)
 {
     uint32_t a[8], b = seed ^ (threadIdx.x * 0x9e3779b9u) ^ blockIdx.x;
@@ -1087,8 +1096,10 @@ __global__ void k_imad_peak(uint32_t seed, int iters, uint32_t *out)
     for (int i = 0; i < iters; i++) {
 #pragma unroll
         for (int k = 0; k < 8; k++) {
-            asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(a[k]) : "r"(b), "r"((uint32_t)k));
-            asm volatile("mad.hi.u32 %0, %0, %1, %0;" : "+r"(a[k]) : "r"(b));
+            if (MODE != 2)
+                asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(a[k]) : "r"(b), "r"((uint32_t)k));
+            if (MODE != 1)
+                asm volatile("mad.hi.u32 %0, %0, %1, %0;" : "+r"(a[k]) : "r"(b));
         }
     }
     uint32_t r = 0;
@@ -1478,9 +1489,12 @@ using namespace hs;
 // ===========================================================================
 // C ABI
 // ===========================================================================
-extern "C" {
-
+namespace hs {
 static thread_local std::string g_tls_error;
+void set_thread_error(const std::string &what) { g_tls_error = what; }
+}  // namespace hs
+
+extern "C" {
 
 int hs_abi_version(void) { return 1; }
 
@@ -2325,13 +2339,10 @@ int hs_profile_read(hs_context *h, double *ms, uint64_t *launches, uint64_t *ent
     return HS_OK;
 }
 
-int hs_measure_imad_peak(hs_context *h, double *imad_per_s)
+// instructions per second of probe `probe`: 0 mad.lo/mad.hi pairs, 1 mad.wide.u32,
+// 2 mad.lo alone, 3 mad.hi alone (8 chains x iters per thread)
+static int imad_probe(Context &ctx, int probe, double *instr_per_s)
 {
-    if (!h || !imad_per_s)
-        return HS_EINVAL;
-    Context &ctx = h->c;
-    std::lock_guard<std::mutex> lk(ctx.mu);
-    DeviceGuard g(ctx.device);
     const int threads = 256, blocks = ctx.sm_count * 8, iters = 4096;
     const size_t out_bytes = (size_t)blocks * threads * sizeof(uint32_t);
     HS_CU(ctx.arena.reserve(out_bytes + 256), "workspace allocation");
@@ -2341,34 +2352,69 @@ int hs_measure_imad_peak(hs_context *h, double *imad_per_s)
     cudaEvent_t e0, e1;
     HS_CU(cudaEventCreate(&e0), "event");
     HS_CU(cudaEventCreate(&e1), "event");
-    double best_rate = 0.0;
-    for (int probe = 0; probe < 2; probe++) {
-        auto launch = [&](uint32_t seed, int it) {
-            if (probe == 0)
-                k_imad_peak<<<blocks, threads, 0, ctx.stream>>>(seed, it, d);
-            else
-                k_imad_wide_peak<<<blocks, threads, 0, ctx.stream>>>(seed, it, d);
-            ctx.launches++;
-        };
-        launch(1u, 64);  // warm-up
-        float best = 1e30f;
-        for (int rep = 0; rep < 5; rep++) {
-            cudaEventRecord(e0, ctx.stream);
-            launch((uint32_t)rep, iters);
-            cudaEventRecord(e1, ctx.stream);
-            HS_CU(cudaEventSynchronize(e1), "imad peak");
-            float t = 0.f;
-            cudaEventElapsedTime(&t, e0, e1);
-            best = std::min(best, t);
+    auto launch = [&](uint32_t seed, int it) {
+        switch (probe) {
+        case 0: k_imad_peak<0><<<blocks, threads, 0, ctx.stream>>>(seed, it, d); break;
+        case 1: k_imad_wide_peak<<<blocks, threads, 0, ctx.stream>>>(seed, it, d); break;
+        case 2: k_imad_peak<1><<<blocks, threads, 0, ctx.stream>>>(seed, it, d); break;
+        default: k_imad_peak<2><<<blocks, threads, 0, ctx.stream>>>(seed, it, d); break;
         }
-        // both probes: 8 products per iteration per thread, 2 IMAD-eq each
-        const double ops = (double)blocks * threads * iters * 8.0 * 2.0;
-        best_rate = std::max(best_rate, ops / (best * 1e-3));
+        ctx.launches++;
+    };
+    launch(1u, 64);  // warm-up
+    float best = 1e30f;
+    for (int rep = 0; rep < 5; rep++) {
+        cudaEventRecord(e0, ctx.stream);
+        launch((uint32_t)rep, iters);
+        cudaEventRecord(e1, ctx.stream);
+        const cudaError_t se = cudaEventSynchronize(e1);
+        if (se != cudaSuccess) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return fail(ctx, se, "imad probe");
+        }
+        float t = 0.f;
+        cudaEventElapsedTime(&t, e0, e1);
+        best = std::min(best, t);
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    HS_CU(cudaGetLastError(), "imad peak");
-    *imad_per_s = best_rate;
+    HS_CU(cudaGetLastError(), "imad probe");
+    const double per_iter = probe == 0 ? 16.0 : 8.0;  // instructions per chain step of the 8 chains
+    *instr_per_s = (double)blocks * threads * iters * per_iter / (best * 1e-3);
+    return HS_OK;
+}
+
+int hs_measure_imad_peak(hs_context *h, double *imad_per_s)
+{
+    if (!h || !imad_per_s)
+        return HS_EINVAL;
+    Context &ctx = h->c;
+    std::lock_guard<std::mutex> lk(ctx.mu);
+    DeviceGuard g(ctx.device);
+    double pair = 0.0, wide = 0.0;
+    int rc = imad_probe(ctx, 0, &pair);
+    if (rc == HS_OK)
+        rc = imad_probe(ctx, 1, &wide);
+    if (rc != HS_OK)
+        return rc;
+    // a lo/hi pair is one product (2 IMAD-eq); a wide instruction is one product
+    *imad_per_s = std::max(pair, 2.0 * wide);
+    return HS_OK;
+}
+
+int hs_measure_imad_rates(hs_context *h, double rates[4])
+{
+    if (!h || !rates)
+        return HS_EINVAL;
+    Context &ctx = h->c;
+    std::lock_guard<std::mutex> lk(ctx.mu);
+    DeviceGuard g(ctx.device);
+    for (int probe = 0; probe < 4; probe++) {
+        const int rc = imad_probe(ctx, probe, &rates[probe]);
+        if (rc != HS_OK)
+            return rc;
+    }
     return HS_OK;
 }
 

@@ -10,6 +10,10 @@
   one base repeated with one equal scalar (every window then hits the bucket
   doubling case), and scalars with only the top window nonzero.
 
+The batched stream (1024 MSMs of log-uniform sizes, either curve) and the
+serving mixture are generated here too, so that the parity tests check the
+exact inputs the benchmark times.
+
 There is no public dataset for this path; these seeded inputs stand in for it.
 """
 
@@ -20,6 +24,9 @@ from dataclasses import dataclass
 import numpy as np
 
 from ._lib import HELIOS, SELENE
+
+# seed of the benchmark's workloads (each configuration adds its own offset)
+BENCH_SEED = 0x48454C494F53
 
 P = 2**255 - 19
 Q = 2**255 - 85737960593035654572250192257530476641
@@ -99,3 +106,32 @@ def make_workload(curve: int, n: int, seed: int, edge_fraction: float = 0.0) -> 
         scalars[topw] = top.view(np.uint8).reshape(k, 32)
         edge = {"zero": zero, "order_minus_1": top1, "repeated": rep, "top_window": topw}
     return Workload(curve, n, scalars, u, edge)
+
+
+def batched_stream(seed: int = BENCH_SEED + 3, count: int = 1024) -> dict:
+    """The batched configuration: `count` independent MSMs, sizes log-uniform in
+    [64, 65536], curve Helios or Selene with probability 1/2, uniform scalars and
+    SWU bases.  Returns {"sizes", "curves", HELIOS: group, SELENE: group}, a
+    group being {"idx": MSM indices, "sizes": list, "u": (total, 32) SWU inputs,
+    "scalars": (total, 32)}, the MSMs of a group back to back."""
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(64), np.log(65536), count)).astype(np.int64)
+    curves = rng.integers(0, 2, count)
+    out = {"sizes": sizes, "curves": curves}
+    for curve in (HELIOS, SELENE):
+        idx = np.nonzero(curves == curve)[0]
+        sz = [int(sizes[i]) for i in idx]
+        total = sum(sz)
+        u = random_field_bytes(rng, total)
+        sc = random_scalars(rng, total, ORDER[curve])
+        out[curve] = {"idx": idx, "sizes": sz, "u": u, "scalars": sc}
+    return out
+
+
+def serving_sizes(rng: np.random.Generator, count: int) -> np.ndarray:
+    """Request sizes of the serving mixture: 70% log-uniform [256, 4096], 25%
+    log-uniform [4096, 65536], 5% exactly 2^18."""
+    u = rng.random(count)
+    n = np.where(u < 0.70, np.exp(rng.uniform(np.log(256), np.log(4096), count)),
+                 np.where(u < 0.95, np.exp(rng.uniform(np.log(4096), np.log(65536), count)), 2.0**18))
+    return n.astype(np.int64)

@@ -78,7 +78,7 @@ typedef struct hs_context hs_context;
  * internal lock; use one context per host thread for concurrency. */
 int hs_context_create(hs_context **ctx, int device);
 void hs_context_destroy(hs_context *ctx);
-/* last error text of this context (or of the process when ctx is NULL) */
+/* last error text of this context (or of the calling thread when ctx is NULL) */
 const char *hs_last_error(const hs_context *ctx);
 const char *hs_strerror(int status);
 /* kernels launched on this context since creation (instrumentation) */
@@ -311,7 +311,9 @@ void hs_selene_batch_to_affine(hs_affine51 *out, const hs_jacobian51 *points, si
  * With profiling on, the context records CUDA events around its bucket
  * accumulation launches (the dominant kernel).  hs_profile_read synchronises
  * the context stream and returns the summed device time and launch count
- * since the last reset, plus the entries (point-window pairs) accumulated. */
+ * since the last reset, plus the algorithmic (point, window) entry count of the
+ * profiled MSMs: n x ceil(256/c) per MSM (the full windows of a 256-bit
+ * scalar), the unit of the pinned work figure. */
 int hs_profile_enable(hs_context *ctx, int on);
 int hs_profile_read(hs_context *ctx, double *accumulate_ms, uint64_t *accumulate_launches, uint64_t *entries,
                     int reset);
@@ -320,6 +322,12 @@ int hs_profile_read(hs_context *ctx, double *accumulate_ms, uint64_t *accumulate
  * timed with CUDA events.  Returns the faster, in IMAD-equivalents per second
  * (a 32x32->64 product counts as 2, in either form). */
 int hs_measure_imad_peak(hs_context *ctx, double *imad_per_s);
+/* The probes behind hs_measure_imad_peak, in instructions per second over the
+ * whole device: rates[0] mad.lo/mad.hi alternating (each instruction is one
+ * IMAD-equivalent), rates[1] mad.wide.u32 (each is one 32x32->64 product, two
+ * IMAD-equivalents), rates[2] mad.lo alone, rates[3] mad.hi alone.  Divide by
+ * the SM count and clock for rates per SM per cycle. */
+int hs_measure_imad_rates(hs_context *ctx, double rates[4]);
 
 /* Field arithmetic on the device, for validation of the field layer:
  * field HS_HELIOS selects F_p (2^255-19), HS_SELENE selects F_q (2^255-gamma).
@@ -331,16 +339,23 @@ int hs_field_op(hs_context *ctx, int field, int op, const uint8_t *a, const uint
 /* ---- MSM without device allocation ----
  * For callers that cannot allocate device memory while they run: code under
  * an allocator or memory pool that must not be bypassed, processes whose
- * device memory is reserved up front, and latency-critical or graph-driven
- * callers that must not reach cudaMalloc / cudaFree (both can synchronise the
- * device).  This entry point has no counterpart in the reference.
+ * device memory is reserved up front, and latency-critical callers that must
+ * not reach cudaMalloc / cudaFree (both can synchronise the device).  This
+ * entry point has no counterpart in the reference.
  * Same computation and arguments as hs_msm_device, but every scratch buffer
  * comes from one fixed array of hs_msm_noalloc_scratch_bytes() (64 MiB) in
- * device memory, which each device that loads this library holds until the
- * process exits.  It needs no context: it runs on the current device and on
- * `stream` (a cudaStream_t, NULL for the default stream) and does not
- * synchronise.  n must be 1 .. HS_NOALLOC_MAX_POINTS; larger sizes, and any
- * size whose workspace would not fit the array, return HS_ERANGE.
+ * device memory.  Under CUDA's default lazy module loading a device's array
+ * is reserved by the first call on that device (at library load under
+ * CUDA_MODULE_LOADING=EAGER) and held until the process exits: a caller that
+ * reserves its device memory up front should make one call first.
+ * It needs no context: it runs on the current device and on `stream` (a
+ * cudaStream_t, NULL for the default stream), and writes its descriptor with a
+ * kernel on that stream, so it does not synchronise.  n must be
+ * 1 .. HS_NOALLOC_MAX_POINTS; larger sizes, and any size whose workspace would
+ * not fit the array, return HS_ERANGE.
+ * Errors: a CUDA error already pending on the calling thread is left in place
+ * and the call returns HS_ECUDA; a failure of the call itself is cleared and
+ * described by hs_last_error(NULL).
  * All calls on a device share the one array and find the previous call's
  * contents in it (each call clears what it needs cleared): calls whose work
  * overlaps on the GPU -- on different streams, or from different threads --

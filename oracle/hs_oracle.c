@@ -346,6 +346,76 @@ int hso_msm_mt(int curve, uint8_t out32[32], const uint8_t *scalars, const uint8
     return 0;
 }
 
+/* Many independent MSMs on a pool of threads (each MSM exact-mode hso_msm on
+ * one thread; the threads take MSMs in index order from a shared counter).
+ * MSM i reads sizes[i] scalars / affine points from where MSM i-1 ended. */
+typedef struct
+{
+    int curve;
+    uint8_t *out32s;
+    const uint8_t *scalars, *pts64;
+    const uint64_t *sizes, *offs;
+    size_t count;
+    size_t *next;
+    int rc;
+} many_task;
+
+static void *many_worker(void *arg)
+{
+    many_task *t = (many_task *)arg;
+    for (;;)
+    {
+        size_t i = __atomic_fetch_add(t->next, 1, __ATOMIC_RELAXED);
+        if (i >= t->count)
+            break;
+        const uint64_t o = t->offs[i];
+        if (hso_msm(t->curve, t->out32s + 32 * i, t->scalars + 32 * o, t->pts64 + 64 * o, (size_t)t->sizes[i], 1))
+            t->rc = -1;
+    }
+    return NULL;
+}
+
+int hso_msm_many(int curve, uint8_t *out32s, const uint8_t *scalars, const uint8_t *pts64, const uint64_t *sizes,
+                 size_t count, int nthreads)
+{
+    pthread_once(&g_once, init_consts);
+    if (nthreads < 1)
+        nthreads = 1;
+    uint64_t *offs = (uint64_t *)malloc((count ? count : 1) * sizeof(uint64_t));
+    many_task *tasks = (many_task *)calloc((size_t)nthreads, sizeof(many_task));
+    pthread_t *tids = (pthread_t *)calloc((size_t)nthreads, sizeof(pthread_t));
+    if (!offs || !tasks || !tids)
+    {
+        free(offs);
+        free(tasks);
+        free(tids);
+        return -2;
+    }
+    uint64_t o = 0;
+    for (size_t i = 0; i < count; i++)
+    {
+        offs[i] = o;
+        o += sizes[i];
+    }
+    size_t next = 0;
+    for (int t = 0; t < nthreads; t++)
+    {
+        tasks[t] = (many_task){curve, out32s, scalars, pts64, sizes, offs, count, &next, 0};
+        pthread_create(&tids[t], NULL, many_worker, &tasks[t]);
+    }
+    int rc = 0;
+    for (int t = 0; t < nthreads; t++)
+    {
+        pthread_join(tids[t], NULL);
+        if (tasks[t].rc)
+            rc = tasks[t].rc;
+    }
+    free(offs);
+    free(tasks);
+    free(tids);
+    return rc;
+}
+
 #define BODY_PED(C)                                                          \
     {                                                                        \
         size_t m = n + 1;                                                    \

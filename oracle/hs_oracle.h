@@ -28,6 +28,8 @@ int hso_pippenger_w(int curve, uint8_t out32[32], const uint8_t *scalars, const 
                     int keep_carry);
 int hso_msm_naive(int curve, uint8_t out32[32], const uint8_t *scalars, const uint8_t *pts64, size_t n);
 int hso_msm_mt(int curve, uint8_t out32[32], const uint8_t *scalars, const uint8_t *pts64, size_t n, int nthreads);
+int hso_msm_many(int curve, uint8_t *out32s, const uint8_t *scalars, const uint8_t *pts64, const uint64_t *sizes,
+                 size_t count, int nthreads);
 int hso_pedersen(int curve, uint8_t out32[32], const uint8_t blinding[32], const uint8_t H64[64],
                  const uint8_t *values, const uint8_t *gens64, size_t n, int keep_carry);
 int hso_map_to_curve(int curve, uint8_t *out64, const uint8_t *u32s, size_t n);

@@ -44,6 +44,7 @@ def lib():
             "hso_pippenger_w": [c.c_int, u8p, u8p, u8p, sz, c.c_int, c.c_int],
             "hso_msm_naive": [c.c_int, u8p, u8p, u8p, sz],
             "hso_msm_mt": [c.c_int, u8p, u8p, u8p, sz, c.c_int],
+            "hso_msm_many": [c.c_int, u8p, u8p, u8p, u8p, sz, c.c_int],
             "hso_pedersen": [c.c_int, u8p, u8p, u8p, u8p, u8p, sz, c.c_int],
             "hso_map_to_curve": [c.c_int, u8p, u8p, sz],
             "hso_map_to_curve_mt": [c.c_int, u8p, u8p, sz, c.c_int],
@@ -124,6 +125,19 @@ def msm_mt(curve, scalars, points64, nthreads) -> bytes:
     out = np.zeros(32, np.uint8)
     assert lib().hso_msm_mt(_cid(curve), _p(out), _p(s), _p(p), s.size // 32, int(nthreads)) == 0
     return out.tobytes()
+
+
+def msm_many(curve, scalars, points64, sizes, nthreads=None) -> list:
+    """Independent exact-mode MSMs back to back (MSM i takes sizes[i] scalars and
+    points after those of MSM i-1), on a pool of host threads; 32-byte results."""
+    s, p = _buf(scalars), _buf(points64)
+    sz = np.ascontiguousarray(np.asarray(sizes, dtype=np.uint64))
+    assert s.size // 32 == int(sz.sum()) and p.size // 64 == int(sz.sum())
+    out = np.zeros(32 * sz.size, np.uint8)
+    rc = lib().hso_msm_many(_cid(curve), _p(out), _p(s), _p(p), _p(sz), sz.size,
+                            int(nthreads or default_threads()))
+    assert rc == 0
+    return [out[32 * i:32 * (i + 1)].tobytes() for i in range(sz.size)]
 
 
 def pedersen(curve, blinding, H64, values, gens64, keep_carry=True) -> bytes:

@@ -1,8 +1,9 @@
 """Extract the reference's golden vectors for the MSM path into vectors.json.
 
-Run in a checkout that has the helioselene sources next to it:
+Run where the helioselene sources are checked out, naming their root in
+HELIOSELENE_REF (or passing the fixture's path):
 
-    python tests/golden/make_golden.py /root/reference/test_vectors/helioselene_test_vectors.json
+    HELIOSELENE_REF=<helioselene checkout> python tests/golden/make_golden.py
 
 The source file is the reference's own fixture (generated by its
 tools/gen_test_vectors.cpp:1107-1159 and checked by src/tests.cpp:6036-6142).
@@ -13,6 +14,7 @@ reference tree at run time.
 """
 
 import json
+import os
 import sys
 from pathlib import Path
 
@@ -34,5 +36,5 @@ def main(src: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1
-         else "/root/reference/test_vectors/helioselene_test_vectors.json")
+    ref = os.environ.get("HELIOSELENE_REF", "/root/reference")
+    main(sys.argv[1] if len(sys.argv) > 1 else str(Path(ref) / "test_vectors" / "helioselene_test_vectors.json"))
