@@ -98,6 +98,12 @@ class Context:
         """single MSMs of >= min_points run as two window halves on two streams (0: off)"""
         self._check(self._lib.hs_context_set_split(self._h, int(min_points)), "set_split")
 
+    def set_batch_affine(self, rounds: int, min_entries: int = 1 << 21) -> None:
+        """bucket accumulation by `rounds` rounds of batch-affine additions for plans of at
+        least min_entries entries (0: XYZZ mixed additions throughout)"""
+        self._check(self._lib.hs_context_set_batch_affine(self._h, int(rounds), int(min_entries)),
+                    "set_batch_affine")
+
     # -- instrumentation --
     def profile(self, on: bool = True) -> None:
         self._check(self._lib.hs_profile_enable(self._h, int(on)), "hs_profile_enable")

@@ -58,6 +58,9 @@ struct Context {
     cudaEvent_t ev_pts[2] = {};    // affine bases ready (per part)
     bool use_graphs = true;
     size_t split_min = size_t(1) << 18;  // single MSMs this large run as two window halves (0: never)
+    // batch-affine accumulation: rounds (0: off) for plans of at least ba_min_entries entries
+    uint32_t ba_rounds = 0;
+    uint64_t ba_min_entries = uint64_t(1) << 21;
     std::vector<GraphEntry> graphs;
     DeviceArena arena;
     std::mutex mu;
@@ -151,7 +154,19 @@ struct BatchPlan {
     // MSM (the full windows of a 256-bit scalar, not the carry window), the
     // unit of the pinned work figure that instrumentation reports
     uint64_t entries_pinned = 0;
+    // Batch-affine accumulation (ba_rounds > 0): rounds of pairwise affine
+    // additions halve every bucket's list before the XYZZ fold, whose segments
+    // (L, max_segs, hist_blocks above) then cut the last round's lists.
+    uint32_t ba_rounds = 0;      // 0: the XYZZ accumulation of the entries
+    uint64_t ba_items[3] = {};   // bound on the outputs of round r (index r-1)
+    uint32_t ba_blocks[3] = {};  // blocks of round r's kernels (BA_K * BA_BT outputs each)
 };
+
+// batch-affine rounds: outputs per thread and threads per block of a round (one
+// shared inversion per block), and the rounds at most
+constexpr uint32_t BA_PLAN_K = 16;
+constexpr uint32_t BA_PLAN_BT = 128;
+constexpr uint32_t BA_MAX_ROUNDS = 3;
 
 // Device buffers of one batch (carved from the arena).
 struct BatchBuffers {
@@ -176,6 +191,14 @@ struct BatchBuffers {
     uint4 *redS = nullptr;              // WS window sums
     uint32_t *out_jac = nullptr;        // M x 24 words: canonical Jacobian X, Y, Z
     uint32_t *counts0 = nullptr;        // NB part-0 entry counts (plans with part_slice)
+    // batch-affine rounds (plans with ba_rounds)
+    uint32_t *ba_off[BA_MAX_ROUNDS] = {};  // NB + 1 each: round r's output offsets per bucket
+    uint32_t *ba_tmp = nullptr;         // block partials of their scan
+    uint4 *ba_lvl[2] = {};              // round outputs, affine (4 uint4 each): odd rounds [0], even [1]
+    uint4 *ba_pre = nullptr;            // round-1 bound of outputs: exclusive prefix products (2 uint4 each)
+    uint4 *ba_co = nullptr;             // per thread: product of the other threads' totals of its block
+    uint4 *ba_tot = nullptr;            // per block: product of its denominators
+    uint4 *ba_inv = nullptr;            // per block: its inverse
     // host inputs: the accumulation of part j waits for ready[j] (null: bases resident)
     cudaEvent_t ready[2] = {nullptr, nullptr};
 };
@@ -201,6 +224,9 @@ BatchPlan make_batch_plan(const Context &ctx, int curve, const size_t *sizes, ui
 BatchPlan make_fixed_plan(int curve, size_t n, int c, uint32_t count);
 // one MSM of n points restricted to windows [w_lo, w_lo + w_cnt) of width c
 BatchPlan make_window_plan(int curve, size_t n, int c, uint32_t w_lo, uint32_t w_cnt);
+// switch a plan to batch-affine accumulation with `rounds` rounds (0 or a plan
+// below min_entries: left as it is)
+void plan_batch_affine(BatchPlan &p, uint32_t rounds, uint64_t min_entries);
 size_t batch_bytes(const BatchPlan &p);
 bool carve(DeviceArena &a, const BatchPlan &p, BatchBuffers &b);
 

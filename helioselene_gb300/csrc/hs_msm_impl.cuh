@@ -101,6 +101,280 @@ __global__ void __launch_bounds__(128) k_accumulate(const uint4 *__restrict__ se
     }
 }
 
+// ---------------------------------------------------------------------------
+// 2'. batch-affine bucket accumulation (plans with ba_rounds = R > 0)
+// ---------------------------------------------------------------------------
+// Round r halves every bucket's list: its items (round 1: the sorted entries,
+// later: the previous round's affine sums) are added in pairs (2j, 2j+1) with
+// the affine formula
+//     lambda = (y_b - y_a) / (x_b - x_a)   (doubling: (3 x_a^2 - 3) / (2 y_a)),
+//     x = lambda^2 - x_a - x_b,  y = lambda (x_a - x) - y_a,
+// and an odd last item is carried over.  The round's output j of bucket k sits
+// at off_r[k] + j, off_r being the scan of ceil(count_k / 2^r).  The divisions
+// of a round share inversions by Montgomery's trick (fp/include/fp_batch_invert.h:61-114
+// applied across a wave of additions):
+//   k_ba_pairs   thread t takes the BA_K outputs [t K, t K + K): denominators,
+//                their running product (the exclusive prefix of each output is
+//                stored), then a product tree over the block's BA_BT threads;
+//                the block total goes out, and each thread keeps its co-product
+//                (the product of the other threads' totals);
+//   k_ba_invert  one inversion per block total (2048 additions);
+//   k_ba_finish  1/T_t = inv(block) * co-product, then each output walks back:
+//                1/d = (1/prefix through d) * (prefix before d), and the sum.
+// Pairs with equal x double (d = 2 y_a) or cancel (the identity, d = 1); an
+// identity operand (affine (0,0)) or a carried item takes d = 1.  The sums of
+// the last round are folded into XYZZ bucket sums by k_accumulate_level.
+constexpr int BA_K = (int)BA_PLAN_K;    // outputs per thread
+constexpr int BA_BT = (int)BA_PLAN_BT;  // threads per block: one shared inversion per BA_K * BA_BT outputs
+
+enum BaKind : int { BA_ADD, BA_DBL, BA_COPY_A, BA_COPY_B, BA_ZERO };
+
+// largest bucket k in [0, NB) with off[k] <= o (o below off[NB])
+__device__ __forceinline__ uint32_t ba_bucket(const uint32_t *__restrict__ off, uint32_t NB, uint32_t o)
+{
+    uint32_t lo = 0, hi = NB - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (__ldg(off + mid) <= o)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+// one input item of a round: round 1 reads an entry (point index | sign << 31)
+// and its base, later rounds the previous round's affine sum.  ba_load_x reads
+// the x coordinate alone; ba_load_y the y coordinate (negated for a negative
+// round-1 digit, the identity (0,0) left alone).
+template <bool FIRST>
+__device__ __forceinline__ const uint4 *ba_src(const uint32_t *__restrict__ sorted, const uint4 *__restrict__ pts,
+                                              const uint4 *__restrict__ lvl, uint32_t i, bool &neg)
+{
+    if (FIRST) {
+        const uint32_t e = __ldg(sorted + i);
+        neg = (e >> 31) != 0;
+        return pts + 4 * (size_t)(e & 0x7fffffffu);
+    }
+    neg = false;
+    return lvl + 4 * (size_t)i;
+}
+
+__device__ __forceinline__ Fe ba_ld(const uint4 *p)
+{
+    const uint4 a = __ldg(p), b = __ldg(p + 1);
+    Fe f;
+    f.w[0] = a.x; f.w[1] = a.y; f.w[2] = a.z; f.w[3] = a.w;
+    f.w[4] = b.x; f.w[5] = b.y; f.w[6] = b.z; f.w[7] = b.w;
+    return f;
+}
+
+template <class C>
+__device__ __forceinline__ Fe ba_load_y(const uint4 *src, bool neg, const Fe &x)
+{
+    using F = typename C::F;
+    const Fe y = ba_ld(src + 2);
+    return (neg && !(F::is_exact_zero(x) && F::is_exact_zero(y))) ? F::neg(y) : y;
+}
+
+// Kind and denominator of output j of a bucket whose round input holds m items
+// from `base`.  With FULL every coordinate is loaded (for the sum); without, a
+// y coordinate only when the case needs it (identity check, equal x).
+template <class C, bool FIRST, bool FULL>
+__device__ __forceinline__ int ba_item(const uint32_t *__restrict__ sorted, const uint4 *__restrict__ pts,
+                                       const uint4 *__restrict__ lvl, uint32_t base, uint32_t m, uint32_t j, Fe &xa,
+                                       Fe &ya, Fe &xb, Fe &yb, Fe &d)
+{
+    using F = typename C::F;
+    const uint32_t i0 = base + 2 * j;
+    bool na, nb;
+    const uint4 *sa = ba_src<FIRST>(sorted, pts, lvl, i0, na);
+    xa = ba_ld(sa);
+    d = F::one();
+    const bool single = 2 * j + 1 >= m;
+    if (FULL || single || F::is_exact_zero(xa))
+        ya = ba_load_y<C>(sa, na, xa);
+    if (single)
+        return BA_COPY_A;  // carried over to the next round
+    const uint4 *sb = ba_src<FIRST>(sorted, pts, lvl, i0 + 1, nb);
+    xb = ba_ld(sb);
+    const bool xb0 = F::is_exact_zero(xb);
+    if (FULL || xb0)
+        yb = ba_load_y<C>(sb, nb, xb);
+    if (xb0 && F::is_exact_zero(yb))
+        return BA_COPY_A;  // b is the identity
+    if (F::is_exact_zero(xa) && F::is_exact_zero(ya))
+        return BA_COPY_B;  // a is the identity
+    const Fe dx = F::sub(xb, xa);
+    if (F::is_zero(dx)) {
+        if (!FULL) {
+            ya = ba_load_y<C>(sa, na, xa);
+            yb = ba_load_y<C>(sb, nb, xb);
+        }
+        if (!F::is_zero(F::sub(yb, ya)) || F::is_zero(ya))
+            return BA_ZERO;  // b = -a (or a point of order 2, which doubles to the identity)
+        d = F::dbl(ya);  // b = a: double
+        return BA_DBL;
+    }
+    d = dx;
+    return BA_ADD;
+}
+
+template <class C, bool FIRST>
+__global__ void __launch_bounds__(BA_BT) k_ba_pairs(const uint32_t *__restrict__ in_off,
+                                                   const uint32_t *__restrict__ out_off, uint32_t NB,
+                                                   const uint32_t *__restrict__ sorted, const uint4 *__restrict__ pts,
+                                                   const uint4 *__restrict__ lvl, uint4 *__restrict__ pre,
+                                                   uint4 *__restrict__ co, uint4 *__restrict__ tot)
+{
+    using F = typename C::F;
+    __shared__ Fe tree[2 * BA_BT];
+    __shared__ Fe cop[2 * BA_BT];
+    const uint32_t E = __ldg(out_off + NB);
+    const uint32_t t = threadIdx.x;
+    const uint64_t first = ((uint64_t)blockIdx.x * BA_BT + t) * BA_K;
+    if ((uint64_t)blockIdx.x * BA_BT * BA_K >= E)
+        return;  // the whole block is past the round's outputs
+    Fe run = F::one();
+    bool any = false;
+    if (first < E) {
+        uint32_t o = (uint32_t)first;
+        uint32_t k = ba_bucket(out_off, NB, o);
+        const uint32_t end = (uint32_t)(first + BA_K < E ? first + BA_K : E);
+        for (; o < end; o++) {
+            while (__ldg(out_off + k + 1) <= o)
+                k++;
+            const uint32_t base = __ldg(in_off + k), m = __ldg(in_off + k + 1) - base;
+            Fe xa, ya, xb, yb, d;
+            const int kind = ba_item<C, FIRST, false>(sorted, pts, lvl, base, m, o - __ldg(out_off + k), xa, ya, xb, yb, d);
+            if (kind == BA_ADD || kind == BA_DBL) {
+                store_fe(pre + 2 * (size_t)o, run);  // exclusive prefix of this output (1 for the first)
+                run = any ? F::mul(run, d) : d;
+                any = true;
+            }
+        }
+    }
+    // product tree over the block's thread totals (leaf t at BA_BT + t)
+    tree[BA_BT + t] = run;
+    __syncthreads();
+    for (uint32_t s2 = BA_BT / 2; s2 >= 1; s2 >>= 1) {
+        if (t < s2)
+            tree[s2 + t] = F::mul(tree[2 * (s2 + t)], tree[2 * (s2 + t) + 1]);
+        __syncthreads();
+    }
+    // co-products top-down: cop[node] = product of all leaves outside node's subtree
+    if (t == 0)
+        cop[1] = F::one();
+    __syncthreads();
+    for (uint32_t s2 = 1; s2 < BA_BT; s2 <<= 1) {
+        if (t < s2) {
+            const uint32_t nd = s2 + t;
+            const Fe c = cop[nd];
+            cop[2 * nd] = F::mul(c, tree[2 * nd + 1]);
+            cop[2 * nd + 1] = F::mul(c, tree[2 * nd]);
+        }
+        __syncthreads();
+    }
+    store_fe(co + 2 * ((size_t)blockIdx.x * BA_BT + t), cop[BA_BT + t]);
+    if (t == 0)
+        store_fe(tot + 2 * (size_t)blockIdx.x, tree[1]);
+}
+
+// one inversion per block total (a block total is never zero: every factor is)
+template <class C>
+__global__ void k_ba_invert(const uint32_t *__restrict__ out_off, uint32_t NB, const uint4 *__restrict__ tot,
+                            uint4 *__restrict__ inv)
+{
+    using F = typename C::F;
+    const uint32_t E = __ldg(out_off + NB);
+    const uint32_t nblk = (uint32_t)(((uint64_t)E + BA_BT * BA_K - 1) / (BA_BT * BA_K));
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nblk)
+        return;
+    store_fe(inv + 2 * (size_t)i, F::inv(load_fe(tot + 2 * (size_t)i)));
+}
+
+template <class C, bool FIRST>
+__global__ void __launch_bounds__(BA_BT) k_ba_finish(const uint32_t *__restrict__ in_off,
+                                                    const uint32_t *__restrict__ out_off, uint32_t NB,
+                                                    const uint32_t *__restrict__ sorted, const uint4 *__restrict__ pts,
+                                                    const uint4 *__restrict__ lvl, const uint4 *__restrict__ pre,
+                                                    const uint4 *__restrict__ co, const uint4 *__restrict__ inv,
+                                                    uint4 *__restrict__ out)
+{
+    using F = typename C::F;
+    const uint32_t E = __ldg(out_off + NB);
+    const uint64_t gt = (uint64_t)blockIdx.x * BA_BT + threadIdx.x;
+    const uint64_t first = gt * BA_K;
+    if (first >= E)
+        return;
+    Fe inv_run = F::mul(load_fe(inv + 2 * (size_t)blockIdx.x), load_fe(co + 2 * gt));  // 1 / (this thread's total)
+    const uint32_t lo = (uint32_t)first;
+    const uint32_t last = (uint32_t)(first + BA_K < E ? first + BA_K : E) - 1;
+    uint32_t k = ba_bucket(out_off, NB, last);
+    for (uint32_t o = last + 1; o-- > lo;) {
+        while (__ldg(out_off + k) > o)
+            k--;
+        const uint32_t base = __ldg(in_off + k), m = __ldg(in_off + k + 1) - base;
+        Fe xa, ya, xb, yb, d;
+        const int kind = ba_item<C, FIRST, true>(sorted, pts, lvl, base, m, o - __ldg(out_off + k), xa, ya, xb, yb, d);
+        Fe x3, y3;
+        if (kind == BA_ADD || kind == BA_DBL) {
+            const Fe inv_d = F::mul(inv_run, load_fe(pre + 2 * (size_t)o));
+            inv_run = F::mul(inv_run, d);
+            Fe num;
+            if (kind == BA_ADD) {
+                num = F::sub(yb, ya);
+            } else {
+                const Fe t = F::sub(F::sqr(xa), F::one());
+                num = F::add(F::dbl(t), t);  // 3 x^2 + a, a = -3
+                xb = xa;
+            }
+            const Fe lam = F::mul(num, inv_d);
+            x3 = F::sub(F::sub(F::sqr(lam), xa), xb);
+            y3 = F::sub(F::mul(lam, F::sub(xa, x3)), ya);
+        } else if (kind == BA_COPY_A) {
+            x3 = xa;
+            y3 = ya;
+        } else if (kind == BA_COPY_B) {
+            x3 = xb;
+            y3 = yb;
+        } else {
+            x3 = F::zero();
+            y3 = F::zero();
+        }
+        uint4 *dst = out + 4 * (size_t)o;
+        store_fe(dst, x3);
+        store_fe(dst + 2, y3);
+    }
+}
+
+// The batch-affine rounds' last sums, folded per segment into XYZZ bucket sums
+// (segments of a bucket's list in the last level buffer, longest first, as in
+// k_accumulate; the items are affine points, (0,0) the identity).
+template <class C>
+__global__ void __launch_bounds__(128) k_accumulate_level(const uint4 *__restrict__ segs,
+                                                         const uint32_t *__restrict__ seg_lo,
+                                                         const uint32_t *__restrict__ seg_hi,
+                                                         const uint4 *__restrict__ lvl, uint4 *__restrict__ seg_sum)
+{
+    using G = Group<C>;
+    using F = typename C::F;
+    const uint32_t S0 = *seg_lo, S = *seg_hi;
+    for (uint32_t s = S0 + blockIdx.x * blockDim.x + threadIdx.x; s < S; s += gridDim.x * blockDim.x) {
+        const uint4 d = segs[s];  // start, length, destination slot
+        Xyzz acc = G::inf();
+        for (uint32_t i = 0; i < d.y; i++) {
+            Fe x, y;
+            load_affine(lvl, d.x + i, x, y);
+            if (F::is_exact_zero(x) && F::is_exact_zero(y))
+                continue;
+            G::add_affine(acc, x, y);
+        }
+        store_xyzz(seg_sum + 8 * (size_t)d.z, acc);
+    }
+}
+
 // Out-of-line point operations for the latency-bound level-2 reduction kernels
 // (k_window_chunks, k_window_sum): with about one warp per scheduler their
 // inlined copies overflow the instruction cache, while one shared body stays
@@ -613,7 +887,46 @@ cudaError_t msm_tail(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
     //    first, so every block gets a like mix of long and short ones; blocks end
     //    wave by wave, so kernels of other streams (another MSM's tail) get SM
     //    slots while this one runs.  Threads past the device-side count exit.
-    {
+    if (p.ba_rounds) {
+        if (b.ready[0]) {  // host inputs: the bases arrive on another stream (one part: no part split here)
+            const cudaError_t e = cudaStreamWaitEvent(st, b.ready[0], 0);
+            if (e != cudaSuccess)
+                return e;
+        }
+        cudaEvent_t ev0 = nullptr;
+        prof_begin(ctx, &ev0);
+        for (uint32_t r = 1; r <= p.ba_rounds; r++) {
+            const uint32_t *in_off = r == 1 ? b.offsets : b.ba_off[r - 2];
+            const uint32_t *out_off = b.ba_off[r - 1];
+            const uint4 *in_lvl = r == 1 ? nullptr : b.ba_lvl[(r - 2) & 1];
+            uint4 *out_lvl = b.ba_lvl[(r - 1) & 1];
+            const uint32_t blocks = std::max<uint32_t>(1, p.ba_blocks[r - 1]);
+            if (r == 1)
+                k_ba_pairs<C, true><<<blocks, BA_BT, 0, st>>>(in_off, out_off, p.NB, b.sorted, b.points, in_lvl,
+                                                              b.ba_pre, b.ba_co, b.ba_tot);
+            else
+                k_ba_pairs<C, false><<<blocks, BA_BT, 0, st>>>(in_off, out_off, p.NB, b.sorted, b.points, in_lvl,
+                                                               b.ba_pre, b.ba_co, b.ba_tot);
+            HS_LAUNCH_CHECK(ctx);
+            k_ba_invert<C><<<(blocks + 63) / 64, 64, 0, st>>>(out_off, p.NB, b.ba_tot, b.ba_inv);
+            HS_LAUNCH_CHECK(ctx);
+            if (r == 1)
+                k_ba_finish<C, true><<<blocks, BA_BT, 0, st>>>(in_off, out_off, p.NB, b.sorted, b.points, in_lvl,
+                                                               b.ba_pre, b.ba_co, b.ba_inv, out_lvl);
+            else
+                k_ba_finish<C, false><<<blocks, BA_BT, 0, st>>>(in_off, out_off, p.NB, b.sorted, b.points, in_lvl,
+                                                                b.ba_pre, b.ba_co, b.ba_inv, out_lvl);
+            HS_LAUNCH_CHECK(ctx);
+        }
+        const int threads = 128;
+        const uint64_t want = (p.max_segs + threads - 1) / threads;
+        const int blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)ctx.sm_count * 32));
+        const size_t nh = (size_t)(p.L + 1) * p.hist_blocks;
+        k_accumulate_level<C><<<blocks, threads, 0, st>>>(b.segs, b.len_scan, b.len_scan + nh,
+                                                          b.ba_lvl[(p.ba_rounds - 1) & 1], b.seg_sum);
+        HS_LAUNCH_CHECK(ctx);
+        prof_end(ctx, ev0, p.entries_pinned);
+    } else {
         const int threads = 128;
         const uint64_t want = (p.max_segs + threads - 1) / threads;
         const int blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)ctx.sm_count * 32));

@@ -270,6 +270,7 @@ BatchPlan make_batch_plan(const Context &ctx, int curve, const size_t *sizes, ui
     p.hist_blocks = (p.NB + SEG_HIST_THREADS - 1) / SEG_HIST_THREADS;
     plan_chunks(p);
     plan_sort(p);
+    plan_batch_affine(p, ctx.ba_rounds, ctx.ba_min_entries);
     return p;
 }
 
@@ -364,6 +365,25 @@ BatchPlan make_window_plan(int curve, size_t n, int c, uint32_t w_lo, uint32_t w
     return p;
 }
 
+// Batch-affine rounds: round r leaves ceil(count / 2^r) items per bucket, at
+// most entries / 2^r + NB over the plan; the fold's segments cut the last
+// round's lists with the cap of an entry count that size.
+void plan_batch_affine(BatchPlan &p, uint32_t rounds, uint64_t min_entries)
+{
+    rounds = std::min<uint32_t>(rounds, BA_MAX_ROUNDS);
+    if (rounds == 0 || p.entries_bound < min_entries || p.part_slice)
+        return;
+    p.ba_rounds = rounds;
+    const uint64_t per_block = (uint64_t)BA_PLAN_K * BA_PLAN_BT;
+    for (uint32_t r = 1; r <= rounds; r++) {
+        p.ba_items[r - 1] = (p.entries_bound >> r) + p.NB + 1;
+        p.ba_blocks[r - 1] = (uint32_t)((p.ba_items[r - 1] + per_block - 1) / per_block);
+    }
+    const uint64_t ent = p.ba_items[rounds - 1];
+    p.L = seg_cap(ent, p.NB);
+    p.max_segs = (uint32_t)(std::min<uint64_t>(ent, p.NB) + ent / p.L + 1);
+}
+
 static constexpr int SCAN_THREADS = 1024;
 static constexpr int SCAN_ITEMS = 4;
 static constexpr uint32_t SCAN_BLOCK = SCAN_THREADS * SCAN_ITEMS;
@@ -391,6 +411,16 @@ size_t batch_bytes(const BatchPlan &p)
     b += align256((size_t)std::max<uint32_t>(1, p.WS) * 128);                              // window sums
     b += align256((size_t)std::max<uint32_t>(1, p.M) * 96);                                // results
     b += p.part_slice ? align256((size_t)(p.NB + 1) * 4) : 0;                                // part-0 counts
+    if (p.ba_rounds) {
+        b += p.ba_rounds * align256((size_t)(p.NB + 1) * 4);                                  // round offsets
+        b += align256((size_t)4 * 4 * (scan_blocks(p.NB) + 1));                                // their partials
+        b += align256((size_t)p.ba_items[0] * 64);                                            // odd rounds
+        b += p.ba_rounds > 1 ? align256((size_t)p.ba_items[1] * 64) : 0;                      // even rounds
+        b += align256((size_t)p.ba_items[0] * 32);                                            // prefixes
+        b += align256((size_t)p.ba_blocks[0] * BA_PLAN_BT * 32);                              // co-products
+        b += 2 * align256((size_t)p.ba_blocks[0] * 32);                                       // totals, inverses
+        b += 8 * 256;
+    }
     return b + 16 * 256;
 }
 
@@ -416,9 +446,22 @@ bool carve(DeviceArena &a, const BatchPlan &p, BatchBuffers &b)
     b.redS = (uint4 *)a.take((size_t)std::max<uint32_t>(1, p.WS) * 128);
     b.out_jac = (uint32_t *)a.take((size_t)std::max<uint32_t>(1, p.M) * 96);
     b.counts0 = p.part_slice ? (uint32_t *)a.take((size_t)(p.NB + 1) * 4) : nullptr;
+    bool ba_ok = true;
+    if (p.ba_rounds) {
+        for (uint32_t r = 0; r < p.ba_rounds; r++)
+            ba_ok = ba_ok && (b.ba_off[r] = (uint32_t *)a.take((size_t)(p.NB + 1) * 4));
+        ba_ok = ba_ok && (b.ba_tmp = (uint32_t *)a.take((size_t)4 * 4 * (scan_blocks(p.NB) + 1)));
+        ba_ok = ba_ok && (b.ba_lvl[0] = (uint4 *)a.take((size_t)p.ba_items[0] * 64));
+        if (p.ba_rounds > 1)
+            ba_ok = ba_ok && (b.ba_lvl[1] = (uint4 *)a.take((size_t)p.ba_items[1] * 64));
+        ba_ok = ba_ok && (b.ba_pre = (uint4 *)a.take((size_t)p.ba_items[0] * 32));
+        ba_ok = ba_ok && (b.ba_co = (uint4 *)a.take((size_t)p.ba_blocks[0] * BA_PLAN_BT * 32));
+        ba_ok = ba_ok && (b.ba_tot = (uint4 *)a.take((size_t)p.ba_blocks[0] * 32));
+        ba_ok = ba_ok && (b.ba_inv = (uint4 *)a.take((size_t)p.ba_blocks[0] * 32));
+    }
     return b.desc && b.counts && b.offsets && b.seg_off && b.scan_tmp && b.len_hist && b.len_scan && b.sorted &&
            b.segs && b.seg_sum && b.heavy && b.heavy_n && b.redA && b.redC && b.redS && b.out_jac &&
-           ((b.sort_cnt && b.digits) || !p.smem_sort()) && (b.counts0 || !p.part_slice);
+           ((b.sort_cnt && b.digits) || !p.smem_sort()) && (b.counts0 || !p.part_slice) && ba_ok;
 }
 
 // ---------------------------------------------------------------------------
@@ -973,6 +1016,139 @@ static cudaError_t launch_scan(Context &ctx, const uint32_t *in, uint32_t n, uin
     return cudaSuccess;
 }
 
+// Scans of the batch-affine rounds, four at once per bucket of count c:
+// ceil(c/2), ceil(c/4), ceil(c/8) (the round outputs) and the segments of the
+// fold, ceil(ceil(c/2^R)/L); the three phases of k_scan_a/b/c on uint4.
+__device__ __forceinline__ uint4 warp_incl_scan4(uint4 v)
+{
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t x = __shfl_up_sync(0xffffffffu, v.x, d), y = __shfl_up_sync(0xffffffffu, v.y, d);
+        const uint32_t z = __shfl_up_sync(0xffffffffu, v.z, d), w = __shfl_up_sync(0xffffffffu, v.w, d);
+        if (lane >= d) {
+            v.x += x;
+            v.y += y;
+            v.z += z;
+            v.w += w;
+        }
+    }
+    return v;
+}
+
+__device__ __forceinline__ uint4 add4(uint4 a, uint4 b) { return make_uint4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+__device__ __forceinline__ uint4 sub4(uint4 a, uint4 b) { return make_uint4(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w); }
+
+__device__ __forceinline__ uint4 block_excl_scan4(uint4 v, uint4 *total)
+{
+    __shared__ uint4 warp_tot[SCAN_THREADS / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint4 inc = warp_incl_scan4(v);
+    __syncthreads();
+    if (lane == 31)
+        warp_tot[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        const uint4 t = (lane < (int)(blockDim.x >> 5)) ? warp_tot[lane] : make_uint4(0, 0, 0, 0);
+        const uint4 ti = warp_incl_scan4(t);
+        warp_tot[lane] = sub4(ti, t);
+        if (lane == 31)
+            *total = ti;
+    }
+    __syncthreads();
+    return add4(warp_tot[warp], sub4(inc, v));
+}
+
+struct BaScanOut {
+    uint32_t *o[4];  // round 1..3 offsets, fold segment offsets (null: not wanted)
+};
+
+__device__ __forceinline__ uint4 ba_values(uint32_t c, uint32_t R, uint32_t L)
+{
+    const uint32_t mR = (c + (1u << R) - 1) >> R;
+    return make_uint4((c + 1) >> 1, (c + 3) >> 2, (c + 7) >> 3, (mR + L - 1) / L);
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_ba_scan_a(const uint32_t *__restrict__ counts, uint32_t NB,
+                                                           uint32_t R, uint32_t L, BaScanOut out,
+                                                           uint4 *__restrict__ tmp)
+{
+    __shared__ uint4 tot;
+    const uint32_t base = blockIdx.x * SCAN_BLOCK + threadIdx.x * SCAN_ITEMS;
+    uint4 it[SCAN_ITEMS];
+    uint4 v = make_uint4(0, 0, 0, 0);
+#pragma unroll
+    for (int j = 0; j < SCAN_ITEMS; j++) {
+        const uint32_t idx = base + j;
+        it[j] = idx < NB ? ba_values(counts[idx], R, L) : make_uint4(0, 0, 0, 0);
+        v = add4(v, it[j]);
+    }
+    uint4 pre = block_excl_scan4(v, &tot);
+#pragma unroll
+    for (int j = 0; j < SCAN_ITEMS; j++) {
+        const uint32_t idx = base + j;
+        if (idx < NB) {
+            const uint32_t pv[4] = {pre.x, pre.y, pre.z, pre.w};
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                if (out.o[q])
+                    out.o[q][idx] = pv[q];
+        }
+        pre = add4(pre, it[j]);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+        tmp[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_ba_scan_b(uint4 *__restrict__ tmp, uint32_t nblocks, uint32_t NB,
+                                                           BaScanOut out)
+{
+    __shared__ uint4 tot;
+    uint4 carry = make_uint4(0, 0, 0, 0);
+    for (uint32_t chunk = 0; chunk < nblocks; chunk += SCAN_BLOCK) {
+        const uint32_t base = chunk + threadIdx.x * SCAN_ITEMS;
+        uint4 it[SCAN_ITEMS];
+        uint4 v = make_uint4(0, 0, 0, 0);
+#pragma unroll
+        for (int j = 0; j < SCAN_ITEMS; j++) {
+            const uint32_t idx = base + j;
+            it[j] = idx < nblocks ? tmp[idx] : make_uint4(0, 0, 0, 0);
+            v = add4(v, it[j]);
+        }
+        uint4 pre = add4(block_excl_scan4(v, &tot), carry);
+#pragma unroll
+        for (int j = 0; j < SCAN_ITEMS; j++) {
+            const uint32_t idx = base + j;
+            if (idx < nblocks)
+                tmp[idx] = pre;
+            pre = add4(pre, it[j]);
+        }
+        __syncthreads();
+        carry = add4(carry, tot);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const uint32_t cv[4] = {carry.x, carry.y, carry.z, carry.w};
+        for (int q = 0; q < 4; q++)
+            if (out.o[q])
+                out.o[q][NB] = cv[q];
+    }
+}
+
+__global__ void k_ba_scan_c(uint32_t NB, const uint4 *__restrict__ tmp, BaScanOut out)
+{
+    const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= NB)
+        return;
+    const uint4 t = tmp[idx / SCAN_BLOCK];
+    const uint32_t tv[4] = {t.x, t.y, t.z, t.w};
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+        if (out.o[q])
+            out.o[q][idx] += tv[q];
+}
+
 // recode + counting sort + segments of a whole batch (descriptors already on the device)
 // the sort kernels' shared-memory opt-in, once per device (outside any capture:
 // contexts set it when they are created)
@@ -1039,15 +1215,32 @@ cudaError_t launch_sort(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
             HS_LAUNCH_CHECK(ctx);
         }
     }
+    // batch-affine rounds: each round's output offsets, and the fold's segment
+    // offsets over the last round's lists (in place of the entries' ones)
+    const uint32_t *seg_src = b.offsets;
+    if (p.ba_rounds) {
+        BaScanOut o;
+        for (int q = 0; q < 3; q++)
+            o.o[q] = (uint32_t)q < p.ba_rounds ? b.ba_off[q] : nullptr;
+        o.o[3] = b.seg_off;
+        const uint32_t nblk = std::max<uint32_t>(1, scan_blocks(p.NB));
+        k_ba_scan_a<<<nblk, SCAN_THREADS, 0, st>>>(b.counts, p.NB, p.ba_rounds, p.L, o, (uint4 *)b.ba_tmp);
+        HS_LAUNCH_CHECK(ctx);
+        k_ba_scan_b<<<1, SCAN_THREADS, 0, st>>>((uint4 *)b.ba_tmp, nblk, p.NB, o);
+        HS_LAUNCH_CHECK(ctx);
+        k_ba_scan_c<<<(p.NB + 255) / 256, 256, 0, st>>>(p.NB, (const uint4 *)b.ba_tmp, o);
+        HS_LAUNCH_CHECK(ctx);
+        seg_src = b.ba_off[p.ba_rounds - 1];
+    }
     // segments, longest first
     const uint32_t nh = (uint32_t)hist_len(p);
     const uint32_t *c0 = (p.part_slice && p.smem_sort()) ? b.counts0 : nullptr;
     const size_t hsm = (size_t)(p.L + 1) * 4 * (c0 ? 2 : 1);
-    k_seg_hist<<<p.hist_blocks, SEG_HIST_THREADS, hsm, st>>>(b.offsets, p.NB, p.L, p.hist_blocks, b.len_hist, c0);
+    k_seg_hist<<<p.hist_blocks, SEG_HIST_THREADS, hsm, st>>>(seg_src, p.NB, p.L, p.hist_blocks, b.len_hist, c0);
     HS_LAUNCH_CHECK(ctx);
     if ((e = launch_scan(ctx, b.len_hist, nh, 1u, b.len_scan, nullptr, b.scan_tmp)) != cudaSuccess)
         return e;
-    k_seg_scatter<<<p.hist_blocks, SEG_HIST_THREADS, hsm, st>>>(b.offsets, b.seg_off, p.NB, p.L, p.hist_blocks,
+    k_seg_scatter<<<p.hist_blocks, SEG_HIST_THREADS, hsm, st>>>(seg_src, b.seg_off, p.NB, p.L, p.hist_blocks,
                                                                  b.len_scan, b.segs, c0);
     HS_LAUNCH_CHECK(ctx);
     return cudaSuccess;
@@ -1233,6 +1426,7 @@ int execute_batch(Context &ctx, const BatchPlan &p, const BatchBuffers &b, void 
     key.push_back((uint64_t)(uintptr_t)d_out);
     key.push_back((uint64_t)(uintptr_t)st);
     key.push_back((uint64_t)(uintptr_t)b.counts);
+    key.push_back((uint64_t)p.ba_rounds);
     for (const MsmDesc &d : p.msms) {
         key.push_back(((uint64_t)d.n << 16) | ((uint64_t)d.fixed << 8) | d.c);
         key.push_back(d.pt_off);
@@ -1367,7 +1561,10 @@ static SplitPlan make_split(const Context &ctx, int curve, size_t n)
     const int c = choose_window(ctx, curve, n);
     const uint32_t W = (uint32_t)((257 + c - 1) / c);
     const uint32_t h = W / 2;
-    return SplitPlan{make_window_plan(curve, n, c, h, W - h), make_window_plan(curve, n, c, 0, h)};
+    SplitPlan sp{make_window_plan(curve, n, c, h, W - h), make_window_plan(curve, n, c, 0, h)};
+    plan_batch_affine(sp.hi, ctx.ba_rounds, ctx.ba_min_entries);
+    plan_batch_affine(sp.lo, ctx.ba_rounds, ctx.ba_min_entries);
+    return sp;
 }
 
 static size_t split_bytes(const SplitPlan &s) { return batch_bytes(s.hi) + batch_bytes(s.lo) + 2048; }
@@ -1419,7 +1616,8 @@ static int execute_split(Context &ctx, const SplitPlan &s, const void *d_scalars
     std::vector<uint64_t> key = {0x5350u, (uint64_t)s.hi.curve, (uint64_t)s.hi.msms[0].n, (uint64_t)s.hi.msms[0].c,
                                  (uint64_t)out_fmt, (uint64_t)(uintptr_t)ctx.arena.base, (uint64_t)ctx.arena.cap,
                                  (uint64_t)(uintptr_t)bh.counts, (uint64_t)(uintptr_t)d_scalars,
-                                 (uint64_t)(uintptr_t)d_points, (uint64_t)(uintptr_t)d_out, (uint64_t)(uintptr_t)st};
+                                 (uint64_t)(uintptr_t)d_points, (uint64_t)(uintptr_t)d_out, (uint64_t)(uintptr_t)st,
+                                 (uint64_t)s.hi.ba_rounds, (uint64_t)s.lo.ba_rounds};
     for (GraphEntry &g : ctx.graphs) {
         if (g.key == key) {
             HS_CU(cudaGraphLaunch(g.exec, st), "graph launch");
@@ -1642,6 +1840,19 @@ int hs_context_set_split(hs_context *h, size_t min_points)
     return HS_OK;
 }
 
+int hs_context_set_batch_affine(hs_context *h, int rounds, size_t min_entries)
+{
+    if (!h || rounds < 0 || rounds > (int)BA_MAX_ROUNDS)
+        return HS_EINVAL;
+    Context &ctx = h->c;
+    std::lock_guard<std::mutex> lk(ctx.mu);
+    DeviceGuard g(ctx.device);
+    drop_graphs(ctx);
+    ctx.ba_rounds = (uint32_t)rounds;
+    ctx.ba_min_entries = min_entries;
+    return HS_OK;
+}
+
 // one launch sequence indexes its (point, window) entries with 31 bits
 static bool entries_fit(const Context &ctx, int curve, size_t n)
 {
@@ -1723,8 +1934,11 @@ static int msm_host(Context &ctx, int curve, const uint8_t *lead_scalar, const v
     // entries of a bucket are contiguous and get their own segments, and the
     // accumulation of part 0 runs while part 1 is still on the link.
     const MsmDesc &d0 = split ? s.lo.msms[0] : p.msms[0];
+    // (a batch-affine plan takes its bases in one part: its rounds pair entries
+    // of both parts)
     const bool two = point_fmt != HS_FMT_COMPRESSED && d0.slices >= 2 &&
-                     (split ? (s.hi.smem_sort() && s.lo.smem_sort()) : p.smem_sort());
+                     (split ? (s.hi.smem_sort() && s.lo.smem_sort() && !s.hi.ba_rounds && !s.lo.ba_rounds)
+                            : (p.smem_sort() && !p.ba_rounds));
     size_t bound[3] = {0, total, total};
     if (two) {
         const uint32_t cut = d0.slices / 2;

@@ -15,7 +15,7 @@ import pytest
 
 import oracle
 import pyref
-from conftest import CURVES, oracle_inputs
+from conftest import BA_DEFAULT, CURVES, oracle_inputs
 
 pytestmark = pytest.mark.gpu
 
@@ -349,16 +349,21 @@ def test_host_inputs_every_format(ctx, curve):
     want_id = ctx.msm_batch([(curve, sc, pts_id)])[0]
     aff51 = np.concatenate([x51, y51], axis=1)
     try:
-        for split in (1 << 18, 0):
-            ctx.set_split(split)
-            assert ctx.msm(curve, sc, pts) == want, f"affine, split {split}"
-            assert ctx.msm(curve, sc, aff51.view(np.uint8), HS_AFF51) == want, f"affine51, split {split}"
-            assert ctx.msm(curve, sc, jac.view(np.uint8), HS_JAC51) == want_id, f"jacobian51, split {split}"
-            assert ctx.pedersen(curve, sc[0], pts[0], sc[1:], pts[1:]) == want, f"pedersen, split {split}"
-            assert ctx.pedersen(curve, sc[0], jac[0].view(np.uint8), sc[1:], jac[1:].view(np.uint8),
-                                HS_JAC51) == want_id, f"pedersen jacobian51, split {split}"
+        # XYZZ accumulation: bases in two parts; batch-affine rounds: one part
+        for rounds in (0, 2):
+            ctx.set_batch_affine(rounds, 1 << 21)
+            for split in (1 << 18, 0):
+                ctx.set_split(split)
+                tag = f"split {split}, rounds {rounds}"
+                assert ctx.msm(curve, sc, pts) == want, f"affine, {tag}"
+                assert ctx.msm(curve, sc, aff51.view(np.uint8), HS_AFF51) == want, f"affine51, {tag}"
+                assert ctx.msm(curve, sc, jac.view(np.uint8), HS_JAC51) == want_id, f"jacobian51, {tag}"
+                assert ctx.pedersen(curve, sc[0], pts[0], sc[1:], pts[1:]) == want, f"pedersen, {tag}"
+                assert ctx.pedersen(curve, sc[0], jac[0].view(np.uint8), sc[1:], jac[1:].view(np.uint8),
+                                    HS_JAC51) == want_id, f"pedersen jacobian51, {tag}"
     finally:
         ctx.set_split(1 << 18)
+        ctx.set_batch_affine(*BA_DEFAULT)
 
 
 @pytest.mark.parametrize("curve", [0, 1])
@@ -389,9 +394,13 @@ def test_host_parts_edge_cases(ctx, curve):
     p3[: half // 2] = 0
     cases.append(("identity bases in part 0", w.scalars, p3))
     try:
-        for split in (1 << 18, 0):
-            ctx.set_split(split)
-            for name, s, p in cases:
-                assert ctx.msm(curve, s, p) == ctx.msm_batch([(curve, s, p)])[0], f"{name}, split {split}"
+        for rounds in (0, 2):
+            ctx.set_batch_affine(rounds, 1 << 21)
+            for split in (1 << 18, 0):
+                ctx.set_split(split)
+                for name, s, p in cases:
+                    assert ctx.msm(curve, s, p) == ctx.msm_batch([(curve, s, p)])[0], \
+                        f"{name}, split {split}, rounds {rounds}"
     finally:
         ctx.set_split(1 << 18)
+        ctx.set_batch_affine(*BA_DEFAULT)
