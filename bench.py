@@ -852,6 +852,9 @@ def run_ours(args) -> None:
     ctx.set_split(head_split)
     ctx2.set_split(head_split)
     ctx2.set_priority(True)
+    if args.ba_rounds is not None:
+        for c in (ctx, ctx2):
+            c.set_batch_affine(args.ba_rounds, 1 << 21)
     ctxs = {hs.HELIOS: ctx, hs.SELENE: ctx2}
     n = args.n
     data = make_inputs(hs, ctx, torch, n, device)
@@ -1224,6 +1227,9 @@ def main() -> None:
     ap.add_argument("--no-tree", action="store_true", help="skip the FCMP++ tree-hash layer section")
     ap.add_argument("--no-verify", action="store_true", help="skip the FCMP++ verification-batch section")
     ap.add_argument("--no-scalar-mul", action="store_true", help="skip the independent scalar-multiplication section")
+    ap.add_argument("--ba-rounds", type=int, default=None,
+                    help="batch-affine accumulation rounds for plans of >= 2^21 entries (0: XYZZ; default: the "
+                         "library's)")
     ap.add_argument("--split", type=int, default=None,
                     help="window-split threshold in points for single MSMs (0: off; default: the library's)")
     args = ap.parse_args()

@@ -379,21 +379,30 @@ __global__ void __launch_bounds__(128) k_accumulate_level(const uint4 *__restric
 // (k_window_chunks, k_window_sum): with about one warp per scheduler their
 // inlined copies overflow the instruction cache, while one shared body stays
 // resident (a call costs a few dozen instructions next to the ~2000 of an
-// addition).  Operands and result travel by address (the caller's local
-// memory): no 128-byte point is passed or returned by value across the call,
-// and the result is stored only after both operands have been read, so it may
-// alias either.
+// addition).  The points cross the call by value.  A form that passed them by
+// address (the caller's local memory, result stored after both operands were
+// read) gave wrong sums on this toolchain for sm_103a, in every MSM, while
+// this form has passed every parity test; the l2_add / l2_dbl wrappers keep
+// the call sites in the by-address shape.
 template <class C>
-__device__ __noinline__ void l2_add(Xyzz *r, const Xyzz *a, const Xyzz *b)
+__device__ __noinline__ Xyzz l2_addv(const Xyzz a, const Xyzz b)
 {
-    const Xyzz t = Group<C>::add(*a, *b);
-    *r = t;
+    return Group<C>::add(a, b);
 }
 template <class C>
-__device__ __noinline__ void l2_dbl(Xyzz *r, const Xyzz *a)
+__device__ __noinline__ Xyzz l2_dblv(const Xyzz a)
 {
-    const Xyzz t = Group<C>::dbl(*a);
-    *r = t;
+    return Group<C>::dbl(a);
+}
+template <class C>
+__device__ __forceinline__ void l2_add(Xyzz *r, const Xyzz *a, const Xyzz *b)
+{
+    *r = l2_addv<C>(*a, *b);
+}
+template <class C>
+__device__ __forceinline__ void l2_dbl(Xyzz *r, const Xyzz *a)
+{
+    *r = l2_dblv<C>(*a);
 }
 
 // ---------------------------------------------------------------------------
