@@ -57,6 +57,9 @@ struct Context {
     cudaEvent_t ev_rec[2] = {};    // input records on the device (per part)
     cudaEvent_t ev_pts[2] = {};    // affine bases ready (per part)
     bool use_graphs = true;
+    // set while a launch sequence of host inputs is being captured: waits on the
+    // input events (recorded outside the capture) become external event waits
+    bool capturing_host = false;
     size_t split_min = size_t(1) << 18;  // single MSMs this large run as two window halves (0: never)
     // batch-affine accumulation: rounds (0: off) for plans of at least ba_min_entries entries
     uint32_t ba_rounds = 0;
@@ -157,7 +160,7 @@ struct BatchPlan {
     // Batch-affine accumulation (ba_rounds > 0): rounds of pairwise affine
     // additions halve every bucket's list before the XYZZ fold, whose segments
     // (L, max_segs, hist_blocks above) then cut the last round's lists.
-    uint32_t ba_rounds = 0;      // 0: the XYZZ accumulation of the entries
+    uint32_t ba_rounds = 0;      // 0: the XYZZ accumulation of the entries (else: entries padded per bucket)
     uint64_t ba_items[3] = {};   // bound on the outputs of round r (index r-1)
     uint32_t ba_blocks[3] = {};  // blocks of round r's kernels (BA_K * BA_BT outputs each)
 };
@@ -191,9 +194,8 @@ struct BatchBuffers {
     uint4 *redS = nullptr;              // WS window sums
     uint32_t *out_jac = nullptr;        // M x 24 words: canonical Jacobian X, Y, Z
     uint32_t *counts0 = nullptr;        // NB part-0 entry counts (plans with part_slice)
-    // batch-affine rounds (plans with ba_rounds)
-    uint32_t *ba_off[BA_MAX_ROUNDS] = {};  // NB + 1 each: round r's output offsets per bucket
-    uint32_t *ba_tmp = nullptr;         // block partials of their scan
+    // batch-affine rounds (plans with ba_rounds): round r's list of bucket k is
+    // [offsets[k] >> r, offsets[k+1] >> r) of its level
     uint4 *ba_lvl[2] = {};              // round outputs, affine (4 uint4 each): odd rounds [0], even [1]
     uint4 *ba_pre = nullptr;            // round-1 bound of outputs: exclusive prefix products (2 uint4 each)
     uint4 *ba_co = nullptr;             // per thread: product of the other threads' totals of its block

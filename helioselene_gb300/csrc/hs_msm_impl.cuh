@@ -104,61 +104,33 @@ __global__ void __launch_bounds__(128) k_accumulate(const uint4 *__restrict__ se
 // ---------------------------------------------------------------------------
 // 2'. batch-affine bucket accumulation (plans with ba_rounds = R > 0)
 // ---------------------------------------------------------------------------
-// Round r halves every bucket's list: its items (round 1: the sorted entries,
-// later: the previous round's affine sums) are added in pairs (2j, 2j+1) with
-// the affine formula
+// Every bucket's entry list is padded to a multiple of 2^R (padding entries are
+// PAD_ENTRY, the identity), so the lists of every round start at even
+// positions.  Round r then adds the items of the previous level in flat pairs:
+// output q = item 2q + item 2q+1 (round 1: entries, later: affine sums), by
 //     lambda = (y_b - y_a) / (x_b - x_a)   (doubling: (3 x_a^2 - 3) / (2 y_a)),
 //     x = lambda^2 - x_a - x_b,  y = lambda (x_a - x) - y_a,
-// and an odd last item is carried over.  The round's output j of bucket k sits
-// at off_r[k] + j, off_r being the scan of ceil(count_k / 2^r).  The divisions
-// of a round share inversions by Montgomery's trick (fp/include/fp_batch_invert.h:61-114
-// applied across a wave of additions):
-//   k_ba_pairs   thread t takes the BA_K outputs [t K, t K + K): denominators,
-//                their running product (the exclusive prefix of each output is
-//                stored), then a product tree over the block's BA_BT threads;
-//                the block total goes out, and each thread keeps its co-product
-//                (the product of the other threads' totals);
-//   k_ba_invert  one inversion per block total (2048 additions);
+// and bucket k's round-r list is [off_k >> r, off_{k+1} >> r) with no scan:
+// a round is a pure stream over the level, every warp reading 32 consecutive
+// pairs.  The divisions of a round share inversions by Montgomery's trick
+// (fp/include/fp_batch_invert.h:61-114 applied across a wave of additions):
+//   k_ba_pairs   lane l of warp tile w takes outputs w*32K + l + 32k (k < K):
+//                denominators, their running product (each output's exclusive
+//                prefix is stored), then a product tree over the block's
+//                threads; the block total goes out and each thread keeps its
+//                co-product (the product of the other threads' totals);
+//   k_ba_invert  one inversion per block total (BA_K * BA_BT additions);
 //   k_ba_finish  1/T_t = inv(block) * co-product, then each output walks back:
 //                1/d = (1/prefix through d) * (prefix before d), and the sum.
 // Pairs with equal x double (d = 2 y_a) or cancel (the identity, d = 1); an
-// identity operand (affine (0,0)) or a carried item takes d = 1.  The sums of
-// the last round are folded into XYZZ bucket sums by k_accumulate_level.
+// identity operand (affine (0,0), or a padding entry) takes d = 1 and the
+// other operand is copied.  The last round's sums are folded into XYZZ bucket
+// sums by k_accumulate_level.
 constexpr int BA_K = (int)BA_PLAN_K;    // outputs per thread
 constexpr int BA_BT = (int)BA_PLAN_BT;  // threads per block: one shared inversion per BA_K * BA_BT outputs
+constexpr uint32_t PAD_ENTRY = 0xffffffffu;
 
 enum BaKind : int { BA_ADD, BA_DBL, BA_COPY_A, BA_COPY_B, BA_ZERO };
-
-// largest bucket k in [0, NB) with off[k] <= o (o below off[NB])
-__device__ __forceinline__ uint32_t ba_bucket(const uint32_t *__restrict__ off, uint32_t NB, uint32_t o)
-{
-    uint32_t lo = 0, hi = NB - 1;
-    while (lo < hi) {
-        const uint32_t mid = (lo + hi + 1) >> 1;
-        if (__ldg(off + mid) <= o)
-            lo = mid;
-        else
-            hi = mid - 1;
-    }
-    return lo;
-}
-
-// one input item of a round: round 1 reads an entry (point index | sign << 31)
-// and its base, later rounds the previous round's affine sum.  ba_load_x reads
-// the x coordinate alone; ba_load_y the y coordinate (negated for a negative
-// round-1 digit, the identity (0,0) left alone).
-template <bool FIRST>
-__device__ __forceinline__ const uint4 *ba_src(const uint32_t *__restrict__ sorted, const uint4 *__restrict__ pts,
-                                              const uint4 *__restrict__ lvl, uint32_t i, bool &neg)
-{
-    if (FIRST) {
-        const uint32_t e = __ldg(sorted + i);
-        neg = (e >> 31) != 0;
-        return pts + 4 * (size_t)(e & 0x7fffffffu);
-    }
-    neg = false;
-    return lvl + 4 * (size_t)i;
-}
 
 __device__ __forceinline__ Fe ba_ld(const uint4 *p)
 {
@@ -169,6 +141,22 @@ __device__ __forceinline__ Fe ba_ld(const uint4 *p)
     return f;
 }
 
+// Where item i of a round's input lives: round 1 reads entry i (point index |
+// sign << 31; PAD_ENTRY is the identity, src null), later rounds the previous
+// level's affine sum i.
+template <bool FIRST>
+__device__ __forceinline__ const uint4 *ba_src(uint32_t e, const uint4 *__restrict__ pts,
+                                              const uint4 *__restrict__ lvl, uint32_t i, bool &neg)
+{
+    if (FIRST) {
+        neg = (e >> 31) != 0;
+        return e == PAD_ENTRY ? nullptr : pts + 4 * (size_t)(e & 0x7fffffffu);
+    }
+    neg = false;
+    return lvl + 4 * (size_t)i;
+}
+
+// y of an item (negated for a negative round-1 digit; the identity left (0,0))
 template <class C>
 __device__ __forceinline__ Fe ba_load_y(const uint4 *src, bool neg, const Fe &x)
 {
@@ -177,33 +165,33 @@ __device__ __forceinline__ Fe ba_load_y(const uint4 *src, bool neg, const Fe &x)
     return (neg && !(F::is_exact_zero(x) && F::is_exact_zero(y))) ? F::neg(y) : y;
 }
 
-// Kind and denominator of output j of a bucket whose round input holds m items
-// from `base`.  With FULL every coordinate is loaded (for the sum); without, a
-// y coordinate only when the case needs it (identity check, equal x).
+// Kind and denominator of output q (items 2q and 2q+1).  With FULL every
+// coordinate is loaded (for the sum); without, a y coordinate only when the
+// case needs it (identity check, equal x).
 template <class C, bool FIRST, bool FULL>
 __device__ __forceinline__ int ba_item(const uint32_t *__restrict__ sorted, const uint4 *__restrict__ pts,
-                                       const uint4 *__restrict__ lvl, uint32_t base, uint32_t m, uint32_t j, Fe &xa,
-                                       Fe &ya, Fe &xb, Fe &yb, Fe &d)
+                                       const uint4 *__restrict__ lvl, uint32_t q, Fe &xa, Fe &ya, Fe &xb, Fe &yb,
+                                       Fe &d)
 {
     using F = typename C::F;
-    const uint32_t i0 = base + 2 * j;
+    uint32_t ea = 0, eb = 0;
+    if (FIRST) {
+        const uint2 e = __ldg(reinterpret_cast<const uint2 *>(sorted) + q);
+        ea = e.x;
+        eb = e.y;
+    }
     bool na, nb;
-    const uint4 *sa = ba_src<FIRST>(sorted, pts, lvl, i0, na);
-    xa = ba_ld(sa);
+    const uint4 *sa = ba_src<FIRST>(ea, pts, lvl, 2 * q, na);
+    const uint4 *sb = ba_src<FIRST>(eb, pts, lvl, 2 * q + 1, nb);
     d = F::one();
-    const bool single = 2 * j + 1 >= m;
-    if (FULL || single || F::is_exact_zero(xa))
-        ya = ba_load_y<C>(sa, na, xa);
-    if (single)
-        return BA_COPY_A;  // carried over to the next round
-    const uint4 *sb = ba_src<FIRST>(sorted, pts, lvl, i0 + 1, nb);
-    xb = ba_ld(sb);
-    const bool xb0 = F::is_exact_zero(xb);
-    if (FULL || xb0)
-        yb = ba_load_y<C>(sb, nb, xb);
+    xa = sa ? ba_ld(sa) : F::zero();
+    xb = sb ? ba_ld(sb) : F::zero();
+    const bool xa0 = F::is_exact_zero(xa), xb0 = F::is_exact_zero(xb);
+    ya = (sa && (FULL || xa0)) ? ba_load_y<C>(sa, na, xa) : F::zero();
+    yb = (sb && (FULL || xb0)) ? ba_load_y<C>(sb, nb, xb) : F::zero();
     if (xb0 && F::is_exact_zero(yb))
         return BA_COPY_A;  // b is the identity
-    if (F::is_exact_zero(xa) && F::is_exact_zero(ya))
+    if (xa0 && F::is_exact_zero(ya))
         return BA_COPY_B;  // a is the identity
     const Fe dx = F::sub(xb, xa);
     if (F::is_zero(dx)) {
@@ -220,9 +208,15 @@ __device__ __forceinline__ int ba_item(const uint32_t *__restrict__ sorted, cons
     return BA_ADD;
 }
 
+// first output of this thread's warp tile, plus its lane (outputs base + 32 k)
+__device__ __forceinline__ uint64_t ba_tile_base()
+{
+    const uint64_t tile = (uint64_t)blockIdx.x * (BA_BT / 32) + (threadIdx.x >> 5);
+    return tile * 32 * BA_K + (threadIdx.x & 31);
+}
+
 template <class C, bool FIRST>
-__global__ void __launch_bounds__(BA_BT) k_ba_pairs(const uint32_t *__restrict__ in_off,
-                                                   const uint32_t *__restrict__ out_off, uint32_t NB,
+__global__ void __launch_bounds__(BA_BT) k_ba_pairs(const uint32_t *__restrict__ offsets, uint32_t NB, uint32_t r,
                                                    const uint32_t *__restrict__ sorted, const uint4 *__restrict__ pts,
                                                    const uint4 *__restrict__ lvl, uint4 *__restrict__ pre,
                                                    uint4 *__restrict__ co, uint4 *__restrict__ tot)
@@ -230,28 +224,24 @@ __global__ void __launch_bounds__(BA_BT) k_ba_pairs(const uint32_t *__restrict__
     using F = typename C::F;
     __shared__ Fe tree[2 * BA_BT];
     __shared__ Fe cop[2 * BA_BT];
-    const uint32_t E = __ldg(out_off + NB);
+    const uint32_t E = __ldg(offsets + NB) >> r;  // outputs of this round
     const uint32_t t = threadIdx.x;
-    const uint64_t first = ((uint64_t)blockIdx.x * BA_BT + t) * BA_K;
     if ((uint64_t)blockIdx.x * BA_BT * BA_K >= E)
         return;  // the whole block is past the round's outputs
+    const uint64_t base = ba_tile_base();
     Fe run = F::one();
     bool any = false;
-    if (first < E) {
-        uint32_t o = (uint32_t)first;
-        uint32_t k = ba_bucket(out_off, NB, o);
-        const uint32_t end = (uint32_t)(first + BA_K < E ? first + BA_K : E);
-        for (; o < end; o++) {
-            while (__ldg(out_off + k + 1) <= o)
-                k++;
-            const uint32_t base = __ldg(in_off + k), m = __ldg(in_off + k + 1) - base;
-            Fe xa, ya, xb, yb, d;
-            const int kind = ba_item<C, FIRST, false>(sorted, pts, lvl, base, m, o - __ldg(out_off + k), xa, ya, xb, yb, d);
-            if (kind == BA_ADD || kind == BA_DBL) {
-                store_fe(pre + 2 * (size_t)o, run);  // exclusive prefix of this output (1 for the first)
-                run = any ? F::mul(run, d) : d;
-                any = true;
-            }
+#pragma unroll 1
+    for (int k = 0; k < BA_K; k++) {
+        const uint64_t q = base + 32 * (uint64_t)k;
+        if (q >= E)
+            break;
+        Fe xa, ya, xb, yb, d;
+        const int kind = ba_item<C, FIRST, false>(sorted, pts, lvl, (uint32_t)q, xa, ya, xb, yb, d);
+        if (kind == BA_ADD || kind == BA_DBL) {
+            store_fe(pre + 2 * q, run);  // exclusive prefix of this output (1 for the first)
+            run = any ? F::mul(run, d) : d;
+            any = true;
         }
     }
     // product tree over the block's thread totals (leaf t at BA_BT + t)
@@ -282,11 +272,11 @@ __global__ void __launch_bounds__(BA_BT) k_ba_pairs(const uint32_t *__restrict__
 
 // one inversion per block total (a block total is never zero: every factor is)
 template <class C>
-__global__ void k_ba_invert(const uint32_t *__restrict__ out_off, uint32_t NB, const uint4 *__restrict__ tot,
-                            uint4 *__restrict__ inv)
+__global__ void k_ba_invert(const uint32_t *__restrict__ offsets, uint32_t NB, uint32_t r,
+                            const uint4 *__restrict__ tot, uint4 *__restrict__ inv)
 {
     using F = typename C::F;
-    const uint32_t E = __ldg(out_off + NB);
+    const uint32_t E = __ldg(offsets + NB) >> r;
     const uint32_t nblk = (uint32_t)(((uint64_t)E + BA_BT * BA_K - 1) / (BA_BT * BA_K));
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nblk)
@@ -295,32 +285,29 @@ __global__ void k_ba_invert(const uint32_t *__restrict__ out_off, uint32_t NB, c
 }
 
 template <class C, bool FIRST>
-__global__ void __launch_bounds__(BA_BT) k_ba_finish(const uint32_t *__restrict__ in_off,
-                                                    const uint32_t *__restrict__ out_off, uint32_t NB,
+__global__ void __launch_bounds__(BA_BT) k_ba_finish(const uint32_t *__restrict__ offsets, uint32_t NB, uint32_t r,
                                                     const uint32_t *__restrict__ sorted, const uint4 *__restrict__ pts,
                                                     const uint4 *__restrict__ lvl, const uint4 *__restrict__ pre,
                                                     const uint4 *__restrict__ co, const uint4 *__restrict__ inv,
                                                     uint4 *__restrict__ out)
 {
     using F = typename C::F;
-    const uint32_t E = __ldg(out_off + NB);
-    const uint64_t gt = (uint64_t)blockIdx.x * BA_BT + threadIdx.x;
-    const uint64_t first = gt * BA_K;
-    if (first >= E)
+    const uint32_t E = __ldg(offsets + NB) >> r;
+    const uint64_t base = ba_tile_base();
+    if (base >= E)
         return;
-    Fe inv_run = F::mul(load_fe(inv + 2 * (size_t)blockIdx.x), load_fe(co + 2 * gt));  // 1 / (this thread's total)
-    const uint32_t lo = (uint32_t)first;
-    const uint32_t last = (uint32_t)(first + BA_K < E ? first + BA_K : E) - 1;
-    uint32_t k = ba_bucket(out_off, NB, last);
-    for (uint32_t o = last + 1; o-- > lo;) {
-        while (__ldg(out_off + k) > o)
-            k--;
-        const uint32_t base = __ldg(in_off + k), m = __ldg(in_off + k + 1) - base;
+    // 1 / (this thread's total)
+    Fe inv_run = F::mul(load_fe(inv + 2 * (size_t)blockIdx.x),
+                        load_fe(co + 2 * ((size_t)blockIdx.x * BA_BT + threadIdx.x)));
+    const int kmax = (int)((E - 1 - base) / 32) < BA_K - 1 ? (int)((E - 1 - base) / 32) : BA_K - 1;
+#pragma unroll 1
+    for (int k = kmax; k >= 0; k--) {
+        const uint64_t q = base + 32 * (uint64_t)k;
         Fe xa, ya, xb, yb, d;
-        const int kind = ba_item<C, FIRST, true>(sorted, pts, lvl, base, m, o - __ldg(out_off + k), xa, ya, xb, yb, d);
+        const int kind = ba_item<C, FIRST, true>(sorted, pts, lvl, (uint32_t)q, xa, ya, xb, yb, d);
         Fe x3, y3;
         if (kind == BA_ADD || kind == BA_DBL) {
-            const Fe inv_d = F::mul(inv_run, load_fe(pre + 2 * (size_t)o));
+            const Fe inv_d = F::mul(inv_run, load_fe(pre + 2 * q));
             inv_run = F::mul(inv_run, d);
             Fe num;
             if (kind == BA_ADD) {
@@ -343,7 +330,7 @@ __global__ void __launch_bounds__(BA_BT) k_ba_finish(const uint32_t *__restrict_
             x3 = F::zero();
             y3 = F::zero();
         }
-        uint4 *dst = out + 4 * (size_t)o;
+        uint4 *dst = out + 4 * q;
         store_fe(dst, x3);
         store_fe(dst + 2, y3);
     }
@@ -898,32 +885,30 @@ cudaError_t msm_tail(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
     //    slots while this one runs.  Threads past the device-side count exit.
     if (p.ba_rounds) {
         if (b.ready[0]) {  // host inputs: the bases arrive on another stream (one part: no part split here)
-            const cudaError_t e = cudaStreamWaitEvent(st, b.ready[0], 0);
+            const cudaError_t e = cudaStreamWaitEvent(st, b.ready[0], ctx.capturing_host ? cudaEventWaitExternal : 0);
             if (e != cudaSuccess)
                 return e;
         }
         cudaEvent_t ev0 = nullptr;
         prof_begin(ctx, &ev0);
         for (uint32_t r = 1; r <= p.ba_rounds; r++) {
-            const uint32_t *in_off = r == 1 ? b.offsets : b.ba_off[r - 2];
-            const uint32_t *out_off = b.ba_off[r - 1];
             const uint4 *in_lvl = r == 1 ? nullptr : b.ba_lvl[(r - 2) & 1];
             uint4 *out_lvl = b.ba_lvl[(r - 1) & 1];
             const uint32_t blocks = std::max<uint32_t>(1, p.ba_blocks[r - 1]);
             if (r == 1)
-                k_ba_pairs<C, true><<<blocks, BA_BT, 0, st>>>(in_off, out_off, p.NB, b.sorted, b.points, in_lvl,
+                k_ba_pairs<C, true><<<blocks, BA_BT, 0, st>>>(b.offsets, p.NB, r, b.sorted, b.points, in_lvl,
                                                               b.ba_pre, b.ba_co, b.ba_tot);
             else
-                k_ba_pairs<C, false><<<blocks, BA_BT, 0, st>>>(in_off, out_off, p.NB, b.sorted, b.points, in_lvl,
+                k_ba_pairs<C, false><<<blocks, BA_BT, 0, st>>>(b.offsets, p.NB, r, b.sorted, b.points, in_lvl,
                                                                b.ba_pre, b.ba_co, b.ba_tot);
             HS_LAUNCH_CHECK(ctx);
-            k_ba_invert<C><<<(blocks + 63) / 64, 64, 0, st>>>(out_off, p.NB, b.ba_tot, b.ba_inv);
+            k_ba_invert<C><<<(blocks + 63) / 64, 64, 0, st>>>(b.offsets, p.NB, r, b.ba_tot, b.ba_inv);
             HS_LAUNCH_CHECK(ctx);
             if (r == 1)
-                k_ba_finish<C, true><<<blocks, BA_BT, 0, st>>>(in_off, out_off, p.NB, b.sorted, b.points, in_lvl,
+                k_ba_finish<C, true><<<blocks, BA_BT, 0, st>>>(b.offsets, p.NB, r, b.sorted, b.points, in_lvl,
                                                                b.ba_pre, b.ba_co, b.ba_inv, out_lvl);
             else
-                k_ba_finish<C, false><<<blocks, BA_BT, 0, st>>>(in_off, out_off, p.NB, b.sorted, b.points, in_lvl,
+                k_ba_finish<C, false><<<blocks, BA_BT, 0, st>>>(b.offsets, p.NB, r, b.sorted, b.points, in_lvl,
                                                                 b.ba_pre, b.ba_co, b.ba_inv, out_lvl);
             HS_LAUNCH_CHECK(ctx);
         }
@@ -946,7 +931,7 @@ cudaError_t msm_tail(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
         const uint32_t *bound[3] = {b.len_scan, b.len_scan + (p.part_slice ? nh / 2 : nh), b.len_scan + nh};
         for (int j = 0; j < parts; j++) {
             if (b.ready[j]) {  // host inputs: this part of the bases arrives on another stream
-                const cudaError_t e = cudaStreamWaitEvent(st, b.ready[j], 0);
+                const cudaError_t e = cudaStreamWaitEvent(st, b.ready[j], ctx.capturing_host ? cudaEventWaitExternal : 0);
                 if (e != cudaSuccess)
                     return e;
             }

@@ -365,18 +365,21 @@ BatchPlan make_window_plan(int curve, size_t n, int c, uint32_t w_lo, uint32_t w
     return p;
 }
 
-// Batch-affine rounds: round r leaves ceil(count / 2^r) items per bucket, at
-// most entries / 2^r + NB over the plan; the fold's segments cut the last
-// round's lists with the cap of an entry count that size.
+// Batch-affine rounds: every bucket's entry list is padded to a multiple of
+// 2^R (at most NB (2^R - 1) padding entries), so round r's lists are the
+// padded offsets shifted right by r and need no scan; the fold's segments cut
+// the last round's lists with the cap of an entry count that size.
 void plan_batch_affine(BatchPlan &p, uint32_t rounds, uint64_t min_entries)
 {
     rounds = std::min<uint32_t>(rounds, BA_MAX_ROUNDS);
-    if (rounds == 0 || p.entries_bound < min_entries || p.part_slice)
+    const uint64_t padded = (uint64_t)p.max_entries + (uint64_t)p.NB * ((1u << rounds) - 1);
+    if (rounds == 0 || p.entries_bound < min_entries || p.part_slice || padded >= 0x80000000ull)
         return;
     p.ba_rounds = rounds;
+    p.max_entries = (uint32_t)padded;
     const uint64_t per_block = (uint64_t)BA_PLAN_K * BA_PLAN_BT;
     for (uint32_t r = 1; r <= rounds; r++) {
-        p.ba_items[r - 1] = (p.entries_bound >> r) + p.NB + 1;
+        p.ba_items[r - 1] = (padded >> r) + 1;
         p.ba_blocks[r - 1] = (uint32_t)((p.ba_items[r - 1] + per_block - 1) / per_block);
     }
     const uint64_t ent = p.ba_items[rounds - 1];
@@ -412,8 +415,6 @@ size_t batch_bytes(const BatchPlan &p)
     b += align256((size_t)std::max<uint32_t>(1, p.M) * 96);                                // results
     b += p.part_slice ? align256((size_t)(p.NB + 1) * 4) : 0;                                // part-0 counts
     if (p.ba_rounds) {
-        b += p.ba_rounds * align256((size_t)(p.NB + 1) * 4);                                  // round offsets
-        b += align256((size_t)4 * 4 * (scan_blocks(p.NB) + 1));                                // their partials
         b += align256((size_t)p.ba_items[0] * 64);                                            // odd rounds
         b += p.ba_rounds > 1 ? align256((size_t)p.ba_items[1] * 64) : 0;                      // even rounds
         b += align256((size_t)p.ba_items[0] * 32);                                            // prefixes
@@ -448,9 +449,6 @@ bool carve(DeviceArena &a, const BatchPlan &p, BatchBuffers &b)
     b.counts0 = p.part_slice ? (uint32_t *)a.take((size_t)(p.NB + 1) * 4) : nullptr;
     bool ba_ok = true;
     if (p.ba_rounds) {
-        for (uint32_t r = 0; r < p.ba_rounds; r++)
-            ba_ok = ba_ok && (b.ba_off[r] = (uint32_t *)a.take((size_t)(p.NB + 1) * 4));
-        ba_ok = ba_ok && (b.ba_tmp = (uint32_t *)a.take((size_t)4 * 4 * (scan_blocks(p.NB) + 1)));
         ba_ok = ba_ok && (b.ba_lvl[0] = (uint4 *)a.take((size_t)p.ba_items[0] * 64));
         if (p.ba_rounds > 1)
             ba_ok = ba_ok && (b.ba_lvl[1] = (uint4 *)a.take((size_t)p.ba_items[1] * 64));
@@ -828,9 +826,11 @@ __device__ __forceinline__ uint32_t part_slots(uint32_t c, uint32_t c0, uint32_t
     return (c0 + L - 1) / L + (c1 + L - 1) / L - ((c0 && c1) ? 1u : 0u);
 }
 
+// pad: counts rounded up to a multiple of pad + 1 (a power of two) first
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_a(const uint32_t *__restrict__ counts, uint32_t NB, uint32_t L,
                                                         uint32_t *__restrict__ offsets, uint32_t *__restrict__ seg_off,
-                                                        uint32_t *__restrict__ tmp, const uint32_t *__restrict__ counts0)
+                                                        uint32_t *__restrict__ tmp, const uint32_t *__restrict__ counts0,
+                                                        uint32_t pad)
 {
     __shared__ uint2 tot;
     const uint32_t base = blockIdx.x * SCAN_BLOCK + threadIdx.x * SCAN_ITEMS;
@@ -839,7 +839,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_a(const uint32_t *__restr
 #pragma unroll
     for (int j = 0; j < SCAN_ITEMS; j++) {
         const uint32_t idx = base + j;
-        c[j] = idx < NB ? counts[idx] : 0u;
+        c[j] = idx < NB ? (counts[idx] + pad) & ~pad : 0u;
         s[j] = counts0 ? (idx < NB ? part_slots(c[j], counts0[idx], L) : 0u) : (c[j] + L - 1) / L;
         v.x += c[j];
         v.y += s[j];
@@ -923,9 +923,11 @@ __global__ void k_scan_c(uint32_t *__restrict__ offsets, uint32_t *__restrict__ 
 // segment lengths, a scan over (length descending, block), and a scatter
 // through block-local cursors.  Each descriptor carries its destination slot
 // seg_off[bucket] + j, so a bucket's partial sums stay contiguous.
+// shift: the lists segmented are the entry lists shifted right by it (the last
+// batch-affine round's, 2^shift times shorter; offsets are multiples of 2^shift)
 __global__ void __launch_bounds__(SEG_HIST_THREADS) k_seg_hist(const uint32_t *__restrict__ offsets, uint32_t NB,
                                                               uint32_t L, uint32_t nblk, uint32_t *__restrict__ hist,
-                                                              const uint32_t *__restrict__ counts0)
+                                                              const uint32_t *__restrict__ counts0, uint32_t shift)
 {
     extern __shared__ uint32_t h[];
     const uint32_t parts = counts0 ? 2u : 1u;
@@ -934,7 +936,7 @@ __global__ void __launch_bounds__(SEG_HIST_THREADS) k_seg_hist(const uint32_t *_
     __syncthreads();
     const uint32_t kb = blockIdx.x * blockDim.x + threadIdx.x;
     if (kb < NB) {
-        const uint32_t cnt = offsets[kb + 1] - offsets[kb];
+        const uint32_t cnt = (offsets[kb + 1] - offsets[kb]) >> shift;
         const uint32_t c0 = counts0 ? counts0[kb] : cnt;
         for (uint32_t part = 0; part < parts; part++) {
             const uint32_t c = part ? cnt - c0 : c0;
@@ -975,7 +977,7 @@ __global__ void __launch_bounds__(SEG_HIST_THREADS) k_seg_scatter(const uint32_t
                                                                  uint32_t L, uint32_t nblk,
                                                                  const uint32_t *__restrict__ hist_scan,
                                                                  uint4 *__restrict__ segs,
-                                                                 const uint32_t *__restrict__ counts0)
+                                                                 const uint32_t *__restrict__ counts0, uint32_t shift)
 {
     extern __shared__ uint32_t cur[];
     const uint32_t parts = counts0 ? 2u : 1u;
@@ -987,7 +989,7 @@ __global__ void __launch_bounds__(SEG_HIST_THREADS) k_seg_scatter(const uint32_t
     const uint32_t kb = blockIdx.x * blockDim.x + threadIdx.x;
     if (kb >= NB)
         return;
-    const uint32_t start = offsets[kb], cnt = offsets[kb + 1] - start, dest = seg_off[kb];
+    const uint32_t start = offsets[kb] >> shift, cnt = (offsets[kb + 1] >> shift) - start, dest = seg_off[kb];
     if (!counts0) {
         emit_segments(cur, L, start, cnt, dest, dest + 1, 0u, segs);
         return;
@@ -1001,11 +1003,11 @@ __global__ void __launch_bounds__(SEG_HIST_THREADS) k_seg_scatter(const uint32_t
 }
 
 static cudaError_t launch_scan(Context &ctx, const uint32_t *in, uint32_t n, uint32_t L, uint32_t *out,
-                               uint32_t *out2, uint32_t *tmp, const uint32_t *counts0 = nullptr)
+                               uint32_t *out2, uint32_t *tmp, const uint32_t *counts0 = nullptr, uint32_t pad = 0)
 {
     cudaStream_t st = ctx.stream;
     const uint32_t nblk = std::max<uint32_t>(1, scan_blocks(n));
-    k_scan_a<<<nblk, SCAN_THREADS, 0, st>>>(in, n, L, out, out2, tmp, counts0);
+    k_scan_a<<<nblk, SCAN_THREADS, 0, st>>>(in, n, L, out, out2, tmp, counts0, pad);
     HS_LAUNCH_CHECK(ctx);
     k_scan_b<<<1, SCAN_THREADS, 0, st>>>(tmp, nblk, out + n, out2 ? out2 + n : nullptr);
     HS_LAUNCH_CHECK(ctx);
@@ -1014,139 +1016,6 @@ static cudaError_t launch_scan(Context &ctx, const uint32_t *in, uint32_t n, uin
         HS_LAUNCH_CHECK(ctx);
     }
     return cudaSuccess;
-}
-
-// Scans of the batch-affine rounds, four at once per bucket of count c:
-// ceil(c/2), ceil(c/4), ceil(c/8) (the round outputs) and the segments of the
-// fold, ceil(ceil(c/2^R)/L); the three phases of k_scan_a/b/c on uint4.
-__device__ __forceinline__ uint4 warp_incl_scan4(uint4 v)
-{
-    const int lane = threadIdx.x & 31;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const uint32_t x = __shfl_up_sync(0xffffffffu, v.x, d), y = __shfl_up_sync(0xffffffffu, v.y, d);
-        const uint32_t z = __shfl_up_sync(0xffffffffu, v.z, d), w = __shfl_up_sync(0xffffffffu, v.w, d);
-        if (lane >= d) {
-            v.x += x;
-            v.y += y;
-            v.z += z;
-            v.w += w;
-        }
-    }
-    return v;
-}
-
-__device__ __forceinline__ uint4 add4(uint4 a, uint4 b) { return make_uint4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
-__device__ __forceinline__ uint4 sub4(uint4 a, uint4 b) { return make_uint4(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w); }
-
-__device__ __forceinline__ uint4 block_excl_scan4(uint4 v, uint4 *total)
-{
-    __shared__ uint4 warp_tot[SCAN_THREADS / 32];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint4 inc = warp_incl_scan4(v);
-    __syncthreads();
-    if (lane == 31)
-        warp_tot[warp] = inc;
-    __syncthreads();
-    if (warp == 0) {
-        const uint4 t = (lane < (int)(blockDim.x >> 5)) ? warp_tot[lane] : make_uint4(0, 0, 0, 0);
-        const uint4 ti = warp_incl_scan4(t);
-        warp_tot[lane] = sub4(ti, t);
-        if (lane == 31)
-            *total = ti;
-    }
-    __syncthreads();
-    return add4(warp_tot[warp], sub4(inc, v));
-}
-
-struct BaScanOut {
-    uint32_t *o[4];  // round 1..3 offsets, fold segment offsets (null: not wanted)
-};
-
-__device__ __forceinline__ uint4 ba_values(uint32_t c, uint32_t R, uint32_t L)
-{
-    const uint32_t mR = (c + (1u << R) - 1) >> R;
-    return make_uint4((c + 1) >> 1, (c + 3) >> 2, (c + 7) >> 3, (mR + L - 1) / L);
-}
-
-__global__ void __launch_bounds__(SCAN_THREADS) k_ba_scan_a(const uint32_t *__restrict__ counts, uint32_t NB,
-                                                           uint32_t R, uint32_t L, BaScanOut out,
-                                                           uint4 *__restrict__ tmp)
-{
-    __shared__ uint4 tot;
-    const uint32_t base = blockIdx.x * SCAN_BLOCK + threadIdx.x * SCAN_ITEMS;
-    uint4 it[SCAN_ITEMS];
-    uint4 v = make_uint4(0, 0, 0, 0);
-#pragma unroll
-    for (int j = 0; j < SCAN_ITEMS; j++) {
-        const uint32_t idx = base + j;
-        it[j] = idx < NB ? ba_values(counts[idx], R, L) : make_uint4(0, 0, 0, 0);
-        v = add4(v, it[j]);
-    }
-    uint4 pre = block_excl_scan4(v, &tot);
-#pragma unroll
-    for (int j = 0; j < SCAN_ITEMS; j++) {
-        const uint32_t idx = base + j;
-        if (idx < NB) {
-            const uint32_t pv[4] = {pre.x, pre.y, pre.z, pre.w};
-#pragma unroll
-            for (int q = 0; q < 4; q++)
-                if (out.o[q])
-                    out.o[q][idx] = pv[q];
-        }
-        pre = add4(pre, it[j]);
-    }
-    __syncthreads();
-    if (threadIdx.x == 0)
-        tmp[blockIdx.x] = tot;
-}
-
-__global__ void __launch_bounds__(SCAN_THREADS) k_ba_scan_b(uint4 *__restrict__ tmp, uint32_t nblocks, uint32_t NB,
-                                                           BaScanOut out)
-{
-    __shared__ uint4 tot;
-    uint4 carry = make_uint4(0, 0, 0, 0);
-    for (uint32_t chunk = 0; chunk < nblocks; chunk += SCAN_BLOCK) {
-        const uint32_t base = chunk + threadIdx.x * SCAN_ITEMS;
-        uint4 it[SCAN_ITEMS];
-        uint4 v = make_uint4(0, 0, 0, 0);
-#pragma unroll
-        for (int j = 0; j < SCAN_ITEMS; j++) {
-            const uint32_t idx = base + j;
-            it[j] = idx < nblocks ? tmp[idx] : make_uint4(0, 0, 0, 0);
-            v = add4(v, it[j]);
-        }
-        uint4 pre = add4(block_excl_scan4(v, &tot), carry);
-#pragma unroll
-        for (int j = 0; j < SCAN_ITEMS; j++) {
-            const uint32_t idx = base + j;
-            if (idx < nblocks)
-                tmp[idx] = pre;
-            pre = add4(pre, it[j]);
-        }
-        __syncthreads();
-        carry = add4(carry, tot);
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        const uint32_t cv[4] = {carry.x, carry.y, carry.z, carry.w};
-        for (int q = 0; q < 4; q++)
-            if (out.o[q])
-                out.o[q][NB] = cv[q];
-    }
-}
-
-__global__ void k_ba_scan_c(uint32_t NB, const uint4 *__restrict__ tmp, BaScanOut out)
-{
-    const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= NB)
-        return;
-    const uint4 t = tmp[idx / SCAN_BLOCK];
-    const uint32_t tv[4] = {t.x, t.y, t.z, t.w};
-#pragma unroll
-    for (int q = 0; q < 4; q++)
-        if (out.o[q])
-            out.o[q][idx] += tv[q];
 }
 
 // recode + counting sort + segments of a whole batch (descriptors already on the device)
@@ -1179,6 +1048,13 @@ cudaError_t launch_sort(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
     if ((e = cudaMemsetAsync(b.counts, 0, (size_t)(p.NB + 1) * 4, st)) != cudaSuccess)
         return e;
     const uint4 *sc = reinterpret_cast<const uint4 *>(b.scalars);
+    // batch-affine plans: every bucket's list padded to a multiple of 2^R with
+    // PAD_ENTRY (the identity), and the fold's segments counted on lists 2^R
+    // times shorter
+    const uint32_t pad = p.ba_rounds ? (1u << p.ba_rounds) - 1 : 0u;
+    const uint32_t seg_L = p.L << p.ba_rounds;
+    if (p.ba_rounds && (e = cudaMemsetAsync(b.sorted, 0xff, (size_t)p.max_entries * 4, st)) != cudaSuccess)
+        return e;
     if (p.smem_sort()) {
         if ((e = sort_smem_attrs(ctx.device)) != cudaSuccess)
             return e;
@@ -1194,7 +1070,7 @@ cudaError_t launch_sort(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
         k_sort_rows<0><<<tb, 256, 0, st>>>(b.desc, p.M, p.NB, b.sort_cnt, b.counts, nullptr, p.part_slice,
                                            p.part_slice ? b.counts0 : nullptr);
         HS_LAUNCH_CHECK(ctx);
-        if ((e = launch_scan(ctx, b.counts, p.NB, p.L, b.offsets, b.seg_off, b.scan_tmp, c0)) != cudaSuccess)
+        if ((e = launch_scan(ctx, b.counts, p.NB, seg_L, b.offsets, b.seg_off, b.scan_tmp, c0, pad)) != cudaSuccess)
             return e;
         k_sort_rows<1><<<tb, 256, 0, st>>>(b.desc, p.M, p.NB, b.sort_cnt, nullptr, b.offsets, 0u, nullptr);
         HS_LAUNCH_CHECK(ctx);
@@ -1206,7 +1082,8 @@ cudaError_t launch_sort(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
             k_recode<false><<<rblocks, 256, 0, st>>>(sc, p.n_total, b.desc, p.M, b.counts, b.offsets, b.sorted);
             HS_LAUNCH_CHECK(ctx);
         }
-        if ((e = launch_scan(ctx, b.counts, p.NB, p.L, b.offsets, b.seg_off, b.scan_tmp)) != cudaSuccess)
+        if ((e = launch_scan(ctx, b.counts, p.NB, seg_L, b.offsets, b.seg_off, b.scan_tmp, nullptr, pad)) !=
+            cudaSuccess)
             return e;
         if ((e = cudaMemsetAsync(b.counts, 0, (size_t)(p.NB + 1) * 4, st)) != cudaSuccess)
             return e;
@@ -1215,33 +1092,17 @@ cudaError_t launch_sort(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
             HS_LAUNCH_CHECK(ctx);
         }
     }
-    // batch-affine rounds: each round's output offsets, and the fold's segment
-    // offsets over the last round's lists (in place of the entries' ones)
-    const uint32_t *seg_src = b.offsets;
-    if (p.ba_rounds) {
-        BaScanOut o;
-        for (int q = 0; q < 3; q++)
-            o.o[q] = (uint32_t)q < p.ba_rounds ? b.ba_off[q] : nullptr;
-        o.o[3] = b.seg_off;
-        const uint32_t nblk = std::max<uint32_t>(1, scan_blocks(p.NB));
-        k_ba_scan_a<<<nblk, SCAN_THREADS, 0, st>>>(b.counts, p.NB, p.ba_rounds, p.L, o, (uint4 *)b.ba_tmp);
-        HS_LAUNCH_CHECK(ctx);
-        k_ba_scan_b<<<1, SCAN_THREADS, 0, st>>>((uint4 *)b.ba_tmp, nblk, p.NB, o);
-        HS_LAUNCH_CHECK(ctx);
-        k_ba_scan_c<<<(p.NB + 255) / 256, 256, 0, st>>>(p.NB, (const uint4 *)b.ba_tmp, o);
-        HS_LAUNCH_CHECK(ctx);
-        seg_src = b.ba_off[p.ba_rounds - 1];
-    }
     // segments, longest first
     const uint32_t nh = (uint32_t)hist_len(p);
     const uint32_t *c0 = (p.part_slice && p.smem_sort()) ? b.counts0 : nullptr;
     const size_t hsm = (size_t)(p.L + 1) * 4 * (c0 ? 2 : 1);
-    k_seg_hist<<<p.hist_blocks, SEG_HIST_THREADS, hsm, st>>>(seg_src, p.NB, p.L, p.hist_blocks, b.len_hist, c0);
+    k_seg_hist<<<p.hist_blocks, SEG_HIST_THREADS, hsm, st>>>(b.offsets, p.NB, p.L, p.hist_blocks, b.len_hist, c0,
+                                                             p.ba_rounds);
     HS_LAUNCH_CHECK(ctx);
     if ((e = launch_scan(ctx, b.len_hist, nh, 1u, b.len_scan, nullptr, b.scan_tmp)) != cudaSuccess)
         return e;
-    k_seg_scatter<<<p.hist_blocks, SEG_HIST_THREADS, hsm, st>>>(seg_src, b.seg_off, p.NB, p.L, p.hist_blocks,
-                                                                 b.len_scan, b.segs, c0);
+    k_seg_scatter<<<p.hist_blocks, SEG_HIST_THREADS, hsm, st>>>(b.offsets, b.seg_off, p.NB, p.L, p.hist_blocks,
+                                                                 b.len_scan, b.segs, c0, p.ba_rounds);
     HS_LAUNCH_CHECK(ctx);
     return cudaSuccess;
 }
@@ -2008,50 +1869,128 @@ static int msm_host(Context &ctx, int curve, const uint8_t *lead_scalar, const v
         HS_CU(cudaEventRecord(ctx.ev_pts[j], s3), "event");
         ready[j] = ctx.ev_pts[j];
     }
-    int rc = HS_OK;
+    // The device work of the call -- sorts, accumulations, reductions, combine,
+    // join and output format -- is one captured launch sequence per call shape,
+    // replayed: a call then costs its copies, the input conversion and one graph
+    // launch instead of dozens of kernel launches.  Its waits on the input events
+    // (recorded above, outside the sequence) are external event waits.
+    BatchBuffers bh, bl, b;
+    uint32_t *d_final = nullptr;
     if (split) {
-        BatchBuffers bh, bl;
-        uint32_t *d_final = nullptr;
         if (!carve(ctx.arena, s.hi, bh) || !carve(ctx.arena, s.lo, bl) || !(d_final = (uint32_t *)ctx.arena.take(96)))
             return fail_msg(ctx, HS_ENOMEM, "workspace carve");
         bh.scalars = bl.scalars = (const uint32_t *)d_sc;
         bh.points = bl.points = (const uint4 *)d_pts;
         for (int j = 0; j < 2; j++)
             bh.ready[j] = bl.ready[j] = ready[j];
-        HS_CU(cudaMemcpyAsync(bh.desc, s.hi.msms.data(), sizeof(MsmDesc), cudaMemcpyHostToDevice, st), "descriptors");
-        HS_CU(cudaMemcpyAsync(bl.desc, s.lo.msms.data(), sizeof(MsmDesc), cudaMemcpyHostToDevice, st), "descriptors");
-        HS_CU(cudaStreamWaitEvent(st, ctx.ev_sc, 0), "stream wait");
-        HS_CU(launch_sort(ctx, s.hi, bh), "sort");
-        HS_CU(launch_sort(ctx, s.lo, bl), "sort");
-        // upper half on the second stream once both sorts are in (the accumulations
-        // wait for the bases)
-        HS_CU(cudaEventRecord(ctx.ev_fork, st), "event");
-        HS_CU(cudaStreamWaitEvent(s2, ctx.ev_fork, 0), "stream wait");
-        ctx.stream = s2;
-        const cudaError_t te = ops.msm_tail(ctx, s.hi, bh);
-        ctx.stream = st;
-        HS_CU(te, "MSM tail");
-        HS_CU(cudaEventRecord(ctx.ev_join, s2), "event");
-        HS_CU(ops.msm_tail(ctx, s.lo, bl), "MSM tail");
-        HS_CU(cudaStreamWaitEvent(st, ctx.ev_join, 0), "stream wait");
-        HS_CU(ops.join(ctx, bh.out_jac, bl.out_jac, d_final), "join");
-        HS_CU(ops.format_out(ctx, d_final, 1, out_fmt, d_out), "format");
     } else {
-        BatchBuffers b;
         if (!carve(ctx.arena, p, b))
             return fail_msg(ctx, HS_ENOMEM, "workspace carve");
         b.scalars = (const uint32_t *)d_sc;
         b.points = (const uint4 *)d_pts;
         b.ready[0] = ready[0];
         b.ready[1] = ready[1];
-        HS_CU(cudaMemcpyAsync(b.desc, p.msms.data(), sizeof(MsmDesc), cudaMemcpyHostToDevice, st), "descriptors");
-        HS_CU(cudaStreamWaitEvent(st, ctx.ev_sc, 0), "stream wait");
-        HS_CU(launch_sort(ctx, p, b), "sort");
-        HS_CU(ops.msm_tail(ctx, p, b), "MSM tail");
-        HS_CU(ops.format_out(ctx, b.out_jac, 1, out_fmt, d_out), "format");
     }
-    if (rc != HS_OK)
-        return rc;
+    auto device_work = [&](MsmDesc *desc_hi, MsmDesc *desc_lo) -> cudaError_t {
+        cudaError_t e;
+        const unsigned wflags = ctx.capturing_host ? cudaEventWaitExternal : 0;
+        if ((e = cudaStreamWaitEvent(st, ctx.ev_sc, wflags)) != cudaSuccess)
+            return e;
+        if (split) {
+            BatchBuffers h = bh, l = bl;
+            h.desc = desc_hi;
+            l.desc = desc_lo;
+            if ((e = launch_sort(ctx, s.hi, h)) != cudaSuccess || (e = launch_sort(ctx, s.lo, l)) != cudaSuccess)
+                return e;
+            // upper half on the second stream once both sorts are in (the accumulations
+            // wait for the bases)
+            if ((e = cudaEventRecord(ctx.ev_fork, st)) != cudaSuccess ||
+                (e = cudaStreamWaitEvent(s2, ctx.ev_fork, 0)) != cudaSuccess)
+                return e;
+            ctx.stream = s2;
+            e = ops.msm_tail(ctx, s.hi, h);
+            ctx.stream = st;
+            if (e != cudaSuccess)
+                return e;
+            if ((e = cudaEventRecord(ctx.ev_join, s2)) != cudaSuccess || (e = ops.msm_tail(ctx, s.lo, l)) != cudaSuccess ||
+                (e = cudaStreamWaitEvent(st, ctx.ev_join, 0)) != cudaSuccess)
+                return e;
+            if ((e = ops.join(ctx, h.out_jac, l.out_jac, d_final)) != cudaSuccess)
+                return e;
+            return ops.format_out(ctx, d_final, 1, out_fmt, d_out);
+        }
+        BatchBuffers one = b;
+        one.desc = desc_hi;
+        if ((e = launch_sort(ctx, p, one)) != cudaSuccess || (e = ops.msm_tail(ctx, p, one)) != cudaSuccess)
+            return e;
+        return ops.format_out(ctx, one.out_jac, 1, out_fmt, d_out);
+    };
+    if (!ctx.use_graphs || ctx.profile) {
+        if (split) {
+            HS_CU(cudaMemcpyAsync(bh.desc, s.hi.msms.data(), sizeof(MsmDesc), cudaMemcpyHostToDevice, st), "descriptors");
+            HS_CU(cudaMemcpyAsync(bl.desc, s.lo.msms.data(), sizeof(MsmDesc), cudaMemcpyHostToDevice, st), "descriptors");
+            HS_CU(device_work(bh.desc, bl.desc), "MSM launch");
+        } else {
+            HS_CU(cudaMemcpyAsync(b.desc, p.msms.data(), sizeof(MsmDesc), cudaMemcpyHostToDevice, st), "descriptors");
+            HS_CU(device_work(b.desc, nullptr), "MSM launch");
+        }
+    } else {
+        const BatchPlan &p0 = split ? s.hi : p;
+        std::vector<uint64_t> key = {0x484f5354u, (uint64_t)curve, (uint64_t)total, (uint64_t)out_fmt,
+                                     (uint64_t)split, (uint64_t)nparts, (uint64_t)bound[1], (uint64_t)p0.msms[0].c,
+                                     (uint64_t)p0.ba_rounds, (uint64_t)(split ? s.lo.ba_rounds : 0),
+                                     (uint64_t)(uintptr_t)ctx.arena.base, (uint64_t)ctx.arena.cap,
+                                     (uint64_t)(uintptr_t)d_sc, (uint64_t)(uintptr_t)d_out, (uint64_t)(uintptr_t)st,
+                                     (uint64_t)(uintptr_t)s2, (uint64_t)(uintptr_t)ready[0],
+                                     (uint64_t)(uintptr_t)ready[1]};
+        GraphEntry *hit = nullptr;
+        for (GraphEntry &g : ctx.graphs)
+            if (g.key == key)
+                hit = &g;
+        if (!hit) {
+            // descriptors in a buffer owned by the graph, uploaded once here
+            GraphEntry ent;
+            HS_CU(cudaMalloc(&ent.d_desc, 2 * sizeof(MsmDesc)), "descriptor allocation");
+            const MsmDesc both[2] = {p0.msms[0], split ? s.lo.msms[0] : p0.msms[0]};
+            cudaError_t ue = cudaMemcpy(ent.d_desc, both, sizeof(both), cudaMemcpyHostToDevice);
+            if (ue != cudaSuccess) {
+                cudaFree(ent.d_desc);
+                return fail(ctx, ue, "descriptor upload");
+            }
+            cudaGraph_t graph = nullptr;
+            const uint64_t before = ctx.launches;
+            cudaError_t ce = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+            ctx.capturing_host = true;
+            cudaError_t le = ce == cudaSuccess ? device_work((MsmDesc *)ent.d_desc, (MsmDesc *)ent.d_desc + 1) : ce;
+            ctx.capturing_host = false;
+            if (ce == cudaSuccess)
+                ce = cudaStreamEndCapture(st, &graph);
+            cudaGraphExec_t exec = nullptr;
+            cudaError_t ie = (le == cudaSuccess && ce == cudaSuccess)
+                                 ? cudaGraphInstantiateWithFlags(&exec, graph, cudaGraphInstantiateFlagUseNodePriority)
+                                 : cudaSuccess;
+            if (graph)
+                cudaGraphDestroy(graph);
+            if (le != cudaSuccess || ce != cudaSuccess || ie != cudaSuccess) {
+                cudaFree(ent.d_desc);
+                return fail(ctx, le != cudaSuccess ? le : (ce != cudaSuccess ? ce : ie), "graph capture");
+            }
+            ent.key = std::move(key);
+            ent.exec = exec;
+            ent.kernels = ctx.launches - before;
+            if (ctx.graphs.size() >= 64) {
+                cudaStreamSynchronize(st);
+                cudaGraphExecDestroy(ctx.graphs.front().exec);
+                cudaFree(ctx.graphs.front().d_desc);
+                ctx.graphs.erase(ctx.graphs.begin());
+            }
+            ctx.graphs.push_back(std::move(ent));
+            hit = &ctx.graphs.back();
+            ctx.launches = before;  // counted again at the launch below
+        }
+        HS_CU(cudaGraphLaunch(hit->exec, st), "graph launch");
+        ctx.launches += hit->kernels;
+    }
     HS_CU(cudaMemcpyAsync(out, d_out, fmt_bytes(out_fmt), cudaMemcpyDeviceToHost, st), "D2H result");
     HS_CU(cudaStreamSynchronize(st), "MSM");
     if (point_fmt == HS_FMT_COMPRESSED)
