@@ -98,11 +98,17 @@ class Context:
         """single MSMs of >= min_points run as two window halves on two streams (0: off)"""
         self._check(self._lib.hs_context_set_split(self._h, int(min_points)), "set_split")
 
-    def set_batch_affine(self, rounds: int, min_entries: int = 1 << 21) -> None:
+    def set_batch_affine(self, rounds: int, min_entries: int = 1 << 21, curve: int = None) -> None:
         """bucket accumulation by `rounds` rounds of batch-affine additions for plans of at
-        least min_entries entries (0: XYZZ mixed additions throughout)"""
-        self._check(self._lib.hs_context_set_batch_affine(self._h, int(rounds), int(min_entries)),
-                    "set_batch_affine")
+        least min_entries entries (0: XYZZ mixed additions throughout), for one curve or both"""
+        for c in ((L.HELIOS, L.SELENE) if curve is None else (curve,)):
+            self._check(self._lib.hs_context_set_batch_affine(self._h, c, int(rounds), int(min_entries)),
+                        "set_batch_affine")
+
+    def default_batch_affine(self) -> None:
+        """the library's default accumulation form per curve (Helios XYZZ, Selene one round)"""
+        self.set_batch_affine(0, 1 << 21, L.HELIOS)
+        self.set_batch_affine(1, 1 << 21, L.SELENE)
 
     # -- instrumentation --
     def profile(self, on: bool = True) -> None:

@@ -61,9 +61,13 @@ struct Context {
     // input events (recorded outside the capture) become external event waits
     bool capturing_host = false;
     size_t split_min = size_t(1) << 18;  // single MSMs this large run as two window halves (0: never)
-    // batch-affine accumulation: rounds (0: off) for plans of at least ba_min_entries entries
-    uint32_t ba_rounds = 0;
-    uint64_t ba_min_entries = uint64_t(1) << 21;
+    // Batch-affine accumulation per curve: rounds (0: off) for plans of at least
+    // ba_min_entries entries.  Measured at n = 2^20 on GB300: one round is faster
+    // on Selene (F_q, whose products cost 1.6x F_p's: 2.39 vs 2.54 ms per
+    // accumulation), none on Helios (F_p: 1.61 vs 1.54 ms), where the round's
+    // extra memory passes cost as much as the products it saves.
+    uint32_t ba_rounds[2] = {0, 1};
+    uint64_t ba_min_entries[2] = {uint64_t(1) << 21, uint64_t(1) << 21};
     std::vector<GraphEntry> graphs;
     DeviceArena arena;
     std::mutex mu;

@@ -102,7 +102,7 @@ int hs_msm_device_noalloc(int curve, const void *d_scalars, const void *d_points
     ctx.device = device;
     ctx.stream = static_cast<cudaStream_t>(stream);
     ctx.use_graphs = false;
-    ctx.ba_rounds = 0;  // the entries' XYZZ accumulation: the smallest workspace
+    ctx.ba_rounds[0] = ctx.ba_rounds[1] = 0;  // the entries' XYZZ accumulation: the smallest workspace
     if ((e = cudaDeviceGetAttribute(&ctx.sm_count, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess)
         return noalloc_fail(e, "device attribute");
     if ((e = sort_smem_attrs(device)) != cudaSuccess)

@@ -270,7 +270,7 @@ BatchPlan make_batch_plan(const Context &ctx, int curve, const size_t *sizes, ui
     p.hist_blocks = (p.NB + SEG_HIST_THREADS - 1) / SEG_HIST_THREADS;
     plan_chunks(p);
     plan_sort(p);
-    plan_batch_affine(p, ctx.ba_rounds, ctx.ba_min_entries);
+    plan_batch_affine(p, ctx.ba_rounds[curve == HS_SELENE], ctx.ba_min_entries[curve == HS_SELENE]);
     return p;
 }
 
@@ -1423,8 +1423,8 @@ static SplitPlan make_split(const Context &ctx, int curve, size_t n)
     const uint32_t W = (uint32_t)((257 + c - 1) / c);
     const uint32_t h = W / 2;
     SplitPlan sp{make_window_plan(curve, n, c, h, W - h), make_window_plan(curve, n, c, 0, h)};
-    plan_batch_affine(sp.hi, ctx.ba_rounds, ctx.ba_min_entries);
-    plan_batch_affine(sp.lo, ctx.ba_rounds, ctx.ba_min_entries);
+    plan_batch_affine(sp.hi, ctx.ba_rounds[curve == HS_SELENE], ctx.ba_min_entries[curve == HS_SELENE]);
+    plan_batch_affine(sp.lo, ctx.ba_rounds[curve == HS_SELENE], ctx.ba_min_entries[curve == HS_SELENE]);
     return sp;
 }
 
@@ -1701,16 +1701,16 @@ int hs_context_set_split(hs_context *h, size_t min_points)
     return HS_OK;
 }
 
-int hs_context_set_batch_affine(hs_context *h, int rounds, size_t min_entries)
+int hs_context_set_batch_affine(hs_context *h, int curve, int rounds, size_t min_entries)
 {
-    if (!h || rounds < 0 || rounds > (int)BA_MAX_ROUNDS)
+    if (!h || !valid_curve(curve) || rounds < 0 || rounds > (int)BA_MAX_ROUNDS)
         return HS_EINVAL;
     Context &ctx = h->c;
     std::lock_guard<std::mutex> lk(ctx.mu);
     DeviceGuard g(ctx.device);
     drop_graphs(ctx);
-    ctx.ba_rounds = (uint32_t)rounds;
-    ctx.ba_min_entries = min_entries;
+    ctx.ba_rounds[curve == HS_SELENE] = (uint32_t)rounds;
+    ctx.ba_min_entries[curve == HS_SELENE] = min_entries;
     return HS_OK;
 }
 

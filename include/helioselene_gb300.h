@@ -85,15 +85,16 @@ const char *hs_strerror(int status);
 uint64_t hs_context_launches(const hs_context *ctx);
 /* the context's cudaStream_t, as an opaque pointer */
 void *hs_context_stream(hs_context *ctx);
-/* Bucket accumulation form for plans of at least min_entries (point, window)
- * entries: `rounds` (1..3) rounds of pairwise affine additions, each round
- * sharing one field inversion per 2048 additions (Montgomery's trick,
- * fp/include/fp_batch_invert.h:61-114, across a wave of bucket additions),
- * then an XYZZ fold of what is left; 0 keeps the XYZZ mixed additions of
- * every entry (helios/src/x64/helios_msm_vartime.cpp:296-325 is the bucket
- * loop both replace).  Results are identical either way.  Host-input calls of
- * a batch-affine plan send their bases in one part. */
-int hs_context_set_batch_affine(hs_context *ctx, int rounds, size_t min_entries);
+/* Bucket accumulation form of one curve's plans of at least min_entries
+ * (point, window) entries: `rounds` (1..3) rounds of pairwise affine
+ * additions, each round sharing one field inversion per 2048 additions
+ * (Montgomery's trick, fp/include/fp_batch_invert.h:61-114, across a wave of
+ * bucket additions), then an XYZZ fold of what is left; 0 keeps the XYZZ mixed
+ * additions of every entry (helios/src/x64/helios_msm_vartime.cpp:296-325 is
+ * the bucket loop both replace).  Results are identical either way.  Defaults:
+ * Helios 0, Selene 1 round, from 2^21 entries.  Host-input calls of a
+ * batch-affine plan send their bases in one part. */
+int hs_context_set_batch_affine(hs_context *ctx, int curve, int rounds, size_t min_entries);
 /* set the Pippenger window width for one curve; 0 restores the built-in
  * cost model (the autotuner writes this) */
 int hs_context_set_window(hs_context *ctx, int curve, size_t n_min, size_t n_max, int window);

@@ -16,8 +16,6 @@ for p in (ROOT, ROOT / "oracle"):
 import oracle  # noqa: E402  (checker)
 
 GOLDEN = ROOT / "tests" / "golden" / "vectors.json"
-# the library's default bucket accumulation (hs_context_set_batch_affine): rounds, min entries
-BA_DEFAULT = (0, 1 << 21)
 CURVES = {"helios": 0, "selene": 1}
 
 

@@ -11,7 +11,7 @@ import pytest
 
 import oracle
 import pyref
-from conftest import BA_DEFAULT, oracle_inputs
+from conftest import oracle_inputs
 
 pytestmark = pytest.mark.gpu
 
@@ -29,7 +29,7 @@ def _neg(curve, pts, i):
 @pytest.fixture
 def ba_ctx(ctx):
     yield ctx
-    ctx.set_batch_affine(*BA_DEFAULT)
+    ctx.default_batch_affine()
 
 
 @pytest.mark.parametrize("curve", [0, 1])
@@ -74,8 +74,9 @@ def test_doubling_cancellation_and_identity_cases(ba_ctx, curve):
 
 @pytest.mark.parametrize("curve", [0, 1])
 def test_default_rule_at_2p20_against_xyzz_and_oracle(ba_ctx, curve):
-    """n = 2^20 with the 1% edge slices (the headline size): the default rule
-    (two rounds), one and three rounds, and the XYZZ path, split and unsplit"""
+    """n = 2^20 with the 1% edge slices (the headline size): one, two and three
+    rounds and the XYZZ path, split and unsplit, and the library default
+    (Selene one round, Helios none)"""
     from helioselene_gb300.workload import make_workload
     n = 1 << 20
     w = make_workload(curve, n, seed=2024 + curve, edge_fraction=0.01)
@@ -87,6 +88,8 @@ def test_default_rule_at_2p20_against_xyzz_and_oracle(ba_ctx, curve):
             for rounds in (0, 1, 2, 3):
                 ba_ctx.set_batch_affine(rounds, 1 << 21)
                 assert ba_ctx.msm(curve, w.scalars, pts) == want, f"rounds={rounds} split={split}"
+            ba_ctx.default_batch_affine()
+            assert ba_ctx.msm(curve, w.scalars, pts) == want, f"default split={split}"
     finally:
         ba_ctx.set_split(1 << 18)
 

@@ -15,7 +15,7 @@ import pytest
 
 import oracle
 import pyref
-from conftest import BA_DEFAULT, CURVES, oracle_inputs
+from conftest import CURVES, oracle_inputs
 
 pytestmark = pytest.mark.gpu
 
@@ -363,7 +363,7 @@ def test_host_inputs_every_format(ctx, curve):
                                     HS_JAC51) == want_id, f"pedersen jacobian51, {tag}"
     finally:
         ctx.set_split(1 << 18)
-        ctx.set_batch_affine(*BA_DEFAULT)
+        ctx.default_batch_affine()
 
 
 @pytest.mark.parametrize("curve", [0, 1])
@@ -403,4 +403,4 @@ def test_host_parts_edge_cases(ctx, curve):
                         f"{name}, split {split}, rounds {rounds}"
     finally:
         ctx.set_split(1 << 18)
-        ctx.set_batch_affine(*BA_DEFAULT)
+        ctx.default_batch_affine()
