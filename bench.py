@@ -853,8 +853,11 @@ def run_ours(args) -> None:
     ctx2.set_split(head_split)
     ctx2.set_priority(True)
     if args.ba_rounds is not None:
+        rr = [int(x) for x in str(args.ba_rounds).split(",")]
+        rr = rr * 2 if len(rr) == 1 else rr
         for c in (ctx, ctx2):
-            c.set_batch_affine(args.ba_rounds, 1 << 21)
+            for curve in (hs.HELIOS, hs.SELENE):
+                c.set_batch_affine(rr[curve], 1 << 21, curve)
     ctxs = {hs.HELIOS: ctx, hs.SELENE: ctx2}
     n = args.n
     data = make_inputs(hs, ctx, torch, n, device)
@@ -1227,9 +1230,9 @@ def main() -> None:
     ap.add_argument("--no-tree", action="store_true", help="skip the FCMP++ tree-hash layer section")
     ap.add_argument("--no-verify", action="store_true", help="skip the FCMP++ verification-batch section")
     ap.add_argument("--no-scalar-mul", action="store_true", help="skip the independent scalar-multiplication section")
-    ap.add_argument("--ba-rounds", type=int, default=None,
-                    help="batch-affine accumulation rounds for plans of >= 2^21 entries (0: XYZZ; default: the "
-                         "library's)")
+    ap.add_argument("--ba-rounds", default=None,
+                    help="batch-affine accumulation rounds for plans of >= 2^21 entries, one value for both curves "
+                         "or 'helios,selene' (0: XYZZ; default: the library's)")
     ap.add_argument("--split", type=int, default=None,
                     help="window-split threshold in points for single MSMs (0: off; default: the library's)")
     args = ap.parse_args()
