@@ -106,9 +106,8 @@ class Context:
                         "set_batch_affine")
 
     def default_batch_affine(self) -> None:
-        """the library's default accumulation form per curve (Helios XYZZ, Selene one round)"""
-        self.set_batch_affine(0, 1 << 21, L.HELIOS)
-        self.set_batch_affine(1, 1 << 21, L.SELENE)
+        """the library's default accumulation form (one batch-affine round on both curves)"""
+        self.set_batch_affine(1, 1 << 21)
 
     # -- instrumentation --
     def profile(self, on: bool = True) -> None:

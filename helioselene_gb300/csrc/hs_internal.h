@@ -62,11 +62,13 @@ struct Context {
     bool capturing_host = false;
     size_t split_min = size_t(1) << 18;  // single MSMs this large run as two window halves (0: never)
     // Batch-affine accumulation per curve: rounds (0: off) for plans of at least
-    // ba_min_entries entries.  Measured at n = 2^20 on GB300: one round is faster
-    // on Selene (F_q, whose products cost 1.6x F_p's: 2.39 vs 2.54 ms per
-    // accumulation), none on Helios (F_p: 1.61 vs 1.54 ms), where the round's
-    // extra memory passes cost as much as the products it saves.
-    uint32_t ba_rounds[2] = {0, 1};
+    // ba_min_entries entries.  Measured at n = 2^20 on GB300 (accumulation per
+    // MSM, ms): Selene 2.54 -> 2.39 with one round, Helios 1.54 -> 1.61; for a
+    // Helios and a Selene MSM side by side on two streams (the throughput form)
+    // one round on both curves is fastest (5.15 ms per pair against 5.37 with
+    // none): one curve's memory-bound round overlaps the other's
+    // multiply-bound work.
+    uint32_t ba_rounds[2] = {1, 1};
     uint64_t ba_min_entries[2] = {uint64_t(1) << 21, uint64_t(1) << 21};
     std::vector<GraphEntry> graphs;
     DeviceArena arena;

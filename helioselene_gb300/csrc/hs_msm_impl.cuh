@@ -124,8 +124,8 @@ __global__ void __launch_bounds__(128) k_accumulate(const uint4 *__restrict__ se
 //                1/d = (1/prefix through d) * (prefix before d), and the sum.
 // Pairs with equal x double (d = 2 y_a) or cancel (the identity, d = 1); an
 // identity operand (affine (0,0), or a padding entry) takes d = 1 and the
-// other operand is copied.  A plan of R rounds materializes R - 1 of them this
-// way; its last round is fused into the XYZZ accumulation (k_pair_*, below).
+// other operand is copied.  The last round's sums are folded into XYZZ bucket
+// sums by k_accumulate_level.
 constexpr int BA_K = (int)BA_PLAN_K;    // outputs per thread
 constexpr int BA_BT = (int)BA_PLAN_BT;  // threads per block: one shared inversion per BA_K * BA_BT outputs
 constexpr uint32_t PAD_ENTRY = 0xffffffffu;
@@ -168,16 +168,21 @@ __device__ __forceinline__ Fe ba_load_y(const uint4 *src, bool neg, const Fe &x)
 // Kind and denominator of output q (items 2q and 2q+1).  With FULL every
 // coordinate is loaded (for the sum); without, a y coordinate only when the
 // case needs it (identity check, equal x).
-// The items at positions i and i + 1 (round 1 / entries: ea and eb).
 template <class C, bool FIRST, bool FULL>
-__device__ __forceinline__ int ba_item_at(uint32_t ea, uint32_t eb, const uint4 *__restrict__ pts,
-                                          const uint4 *__restrict__ lvl, uint32_t i, Fe &xa, Fe &ya, Fe &xb, Fe &yb,
-                                          Fe &d)
+__device__ __forceinline__ int ba_item(const uint32_t *__restrict__ sorted, const uint4 *__restrict__ pts,
+                                       const uint4 *__restrict__ lvl, uint32_t q, Fe &xa, Fe &ya, Fe &xb, Fe &yb,
+                                       Fe &d)
 {
     using F = typename C::F;
+    uint32_t ea = 0, eb = 0;
+    if (FIRST) {
+        const uint2 e = __ldg(reinterpret_cast<const uint2 *>(sorted) + q);
+        ea = e.x;
+        eb = e.y;
+    }
     bool na, nb;
-    const uint4 *sa = ba_src<FIRST>(ea, pts, lvl, i, na);
-    const uint4 *sb = ba_src<FIRST>(eb, pts, lvl, i + 1, nb);
+    const uint4 *sa = ba_src<FIRST>(ea, pts, lvl, 2 * q, na);
+    const uint4 *sb = ba_src<FIRST>(eb, pts, lvl, 2 * q + 1, nb);
     d = F::one();
     xa = sa ? ba_ld(sa) : F::zero();
     xb = sb ? ba_ld(sb) : F::zero();
@@ -201,21 +206,6 @@ __device__ __forceinline__ int ba_item_at(uint32_t ea, uint32_t eb, const uint4 
     }
     d = dx;
     return BA_ADD;
-}
-
-// output q of a flat round: items 2q and 2q + 1 (round 1: one 8-byte entry pair load)
-template <class C, bool FIRST, bool FULL>
-__device__ __forceinline__ int ba_item(const uint32_t *__restrict__ sorted, const uint4 *__restrict__ pts,
-                                       const uint4 *__restrict__ lvl, uint32_t q, Fe &xa, Fe &ya, Fe &xb, Fe &yb,
-                                       Fe &d)
-{
-    uint32_t ea = 0, eb = 0;
-    if (FIRST) {
-        const uint2 e = __ldg(reinterpret_cast<const uint2 *>(sorted) + q);
-        ea = e.x;
-        eb = e.y;
-    }
-    return ba_item_at<C, FIRST, FULL>(ea, eb, pts, lvl, 2 * q, xa, ya, xb, yb, d);
 }
 
 // first output of this thread's warp tile, plus its lane (outputs base + 32 k)
@@ -346,163 +336,30 @@ __global__ void __launch_bounds__(BA_BT) k_ba_finish(const uint32_t *__restrict_
     }
 }
 
-// ---------------------------------------------------------------------------
-// 2''. the last batch-affine round fused into the XYZZ accumulation
-// ---------------------------------------------------------------------------
-// Over the segments of the accumulation (entries, or the last level round's
-// sums), each segment's items are taken in pairs (2j, 2j+1):
-//   k_pair_prefix  per segment: every pair's denominator and the segment's
-//                  running product (each pair's exclusive prefix at pre[p >> 1],
-//                  p its first position: pairs are disjoint, so p >> 1 is
-//                  distinct), then the block's product tree (one segment per
-//                  thread, BA_BT segments share one inversion);
-//   k_pair_invert  one inversion per block total;
-//   k_pair_finish  per segment, walking back: each pair's affine sum, added into
-//                  the segment's XYZZ sum; an odd last item is added as it is.
-// So each pair costs the affine sum (5M + 1S with the shared inversion) and one
-// mixed addition, against two mixed additions, and no sum goes through memory.
-template <bool FIRST>
-__device__ __forceinline__ void pair_entries(const uint32_t *__restrict__ sorted, uint32_t p, uint32_t &ea, uint32_t &eb)
-{
-    if (FIRST) {
-        ea = __ldg(sorted + p);
-        eb = __ldg(sorted + p + 1);
-    } else {
-        ea = eb = 0;
-    }
-}
-
-template <class C, bool FIRST>
-__global__ void __launch_bounds__(BA_BT) k_pair_prefix(const uint4 *__restrict__ segs,
-                                                      const uint32_t *__restrict__ seg_lo,
-                                                      const uint32_t *__restrict__ seg_hi,
-                                                      const uint32_t *__restrict__ sorted, const uint4 *__restrict__ pts,
-                                                      const uint4 *__restrict__ lvl, uint4 *__restrict__ pre,
-                                                      uint4 *__restrict__ co, uint4 *__restrict__ tot)
-{
-    using F = typename C::F;
-    __shared__ Fe tree[2 * BA_BT];
-    __shared__ Fe cop[2 * BA_BT];
-    const uint32_t S0 = *seg_lo, S = *seg_hi;
-    const uint32_t t = threadIdx.x;
-    if (S0 + blockIdx.x * BA_BT >= S)
-        return;  // the whole block is past this list's segments
-    const uint32_t s = S0 + blockIdx.x * BA_BT + t;
-    Fe run = F::one();
-    if (s < S) {
-        const uint4 dsc = segs[s];  // start, length, destination slot, continue
-        bool any = false;
-        for (uint32_t j = 0; 2 * j + 1 < dsc.y; j++) {
-            const uint32_t p = dsc.x + 2 * j;
-            uint32_t ea, eb;
-            pair_entries<FIRST>(sorted, p, ea, eb);
-            Fe xa, ya, xb, yb, d;
-            const int kind = ba_item_at<C, FIRST, false>(ea, eb, pts, lvl, p, xa, ya, xb, yb, d);
-            if (kind == BA_ADD || kind == BA_DBL) {
-                store_fe(pre + 2 * (size_t)(p >> 1), run);  // exclusive prefix (1 for the first)
-                run = any ? F::mul(run, d) : d;
-                any = true;
-            }
-        }
-    }
-    tree[BA_BT + t] = run;
-    __syncthreads();
-    for (uint32_t s2 = BA_BT / 2; s2 >= 1; s2 >>= 1) {
-        if (t < s2)
-            tree[s2 + t] = F::mul(tree[2 * (s2 + t)], tree[2 * (s2 + t) + 1]);
-        __syncthreads();
-    }
-    if (t == 0)
-        cop[1] = F::one();
-    __syncthreads();
-    for (uint32_t s2 = 1; s2 < BA_BT; s2 <<= 1) {
-        if (t < s2) {
-            const uint32_t nd = s2 + t;
-            const Fe c = cop[nd];
-            cop[2 * nd] = F::mul(c, tree[2 * nd + 1]);
-            cop[2 * nd + 1] = F::mul(c, tree[2 * nd]);
-        }
-        __syncthreads();
-    }
-    store_fe(co + 2 * ((size_t)blockIdx.x * BA_BT + t), cop[BA_BT + t]);
-    if (t == 0)
-        store_fe(tot + 2 * (size_t)blockIdx.x, tree[1]);
-}
-
+// The batch-affine rounds' last sums, folded per segment into XYZZ bucket sums
+// (segments of a bucket's list in the last level buffer, longest first, as in
+// k_accumulate; the items are affine points, (0,0) the identity).
 template <class C>
-__global__ void k_pair_invert(const uint32_t *__restrict__ seg_lo, const uint32_t *__restrict__ seg_hi,
-                              const uint4 *__restrict__ tot, uint4 *__restrict__ inv)
-{
-    using F = typename C::F;
-    const uint32_t nblk = (*seg_hi - *seg_lo + BA_BT - 1) / BA_BT;
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nblk)
-        return;
-    store_fe(inv + 2 * (size_t)i, F::inv(load_fe(tot + 2 * (size_t)i)));
-}
-
-template <class C, bool FIRST, bool RESUME>
-__global__ void __launch_bounds__(BA_BT, 4) k_pair_finish(const uint4 *__restrict__ segs,
-                                                      const uint32_t *__restrict__ seg_lo,
-                                                      const uint32_t *__restrict__ seg_hi,
-                                                      const uint32_t *__restrict__ sorted, const uint4 *__restrict__ pts,
-                                                      const uint4 *__restrict__ lvl, const uint4 *__restrict__ pre,
-                                                      const uint4 *__restrict__ co, const uint4 *__restrict__ inv,
-                                                      uint4 *__restrict__ seg_sum)
+__global__ void __launch_bounds__(128) k_accumulate_level(const uint4 *__restrict__ segs,
+                                                         const uint32_t *__restrict__ seg_lo,
+                                                         const uint32_t *__restrict__ seg_hi,
+                                                         const uint4 *__restrict__ lvl, uint4 *__restrict__ seg_sum)
 {
     using G = Group<C>;
     using F = typename C::F;
     const uint32_t S0 = *seg_lo, S = *seg_hi;
-    const uint32_t s = S0 + blockIdx.x * BA_BT + threadIdx.x;
-    if (s >= S)
-        return;
-    const uint4 dsc = segs[s];
-    Xyzz acc = (RESUME && dsc.w) ? load_xyzz(seg_sum + 8 * (size_t)dsc.z) : G::inf();
-    if (dsc.y & 1) {  // the odd last item
-        const uint32_t p = dsc.x + dsc.y - 1;
-        bool neg;
-        const uint32_t e = FIRST ? __ldg(sorted + p) : 0u;
-        const uint4 *src = ba_src<FIRST>(e, pts, lvl, p, neg);
-        if (src) {
-            const Fe x = ba_ld(src);
-            const Fe y = ba_load_y<C>(src, neg, x);
-            if (!(F::is_exact_zero(x) && F::is_exact_zero(y)))
-                G::add_affine(acc, x, y);
+    for (uint32_t s = S0 + blockIdx.x * blockDim.x + threadIdx.x; s < S; s += gridDim.x * blockDim.x) {
+        const uint4 d = segs[s];  // start, length, destination slot
+        Xyzz acc = G::inf();
+        for (uint32_t i = 0; i < d.y; i++) {
+            Fe x, y;
+            load_affine(lvl, d.x + i, x, y);
+            if (F::is_exact_zero(x) && F::is_exact_zero(y))
+                continue;
+            G::add_affine(acc, x, y);
         }
+        store_xyzz(seg_sum + 8 * (size_t)d.z, acc);
     }
-    if (dsc.y >= 2) {
-        Fe inv_run = F::mul(load_fe(inv + 2 * (size_t)blockIdx.x),
-                            load_fe(co + 2 * ((size_t)blockIdx.x * BA_BT + threadIdx.x)));
-        for (uint32_t j = dsc.y / 2; j-- > 0;) {
-            const uint32_t p = dsc.x + 2 * j;
-            uint32_t ea, eb;
-            pair_entries<FIRST>(sorted, p, ea, eb);
-            Fe xa, ya, xb, yb, d;
-            const int kind = ba_item_at<C, FIRST, true>(ea, eb, pts, lvl, p, xa, ya, xb, yb, d);
-            if (kind == BA_ADD || kind == BA_DBL) {
-                const Fe inv_d = F::mul(inv_run, load_fe(pre + 2 * (size_t)(p >> 1)));
-                inv_run = F::mul(inv_run, d);
-                Fe num;
-                if (kind == BA_ADD) {
-                    num = F::sub(yb, ya);
-                } else {
-                    const Fe t = F::sub(F::sqr(xa), F::one());
-                    num = F::add(F::dbl(t), t);  // 3 x^2 + a, a = -3
-                    xb = xa;
-                }
-                const Fe lam = F::mul(num, inv_d);
-                const Fe x3 = F::sub(F::sub(F::sqr(lam), xa), xb);
-                const Fe y3 = F::sub(F::mul(lam, F::sub(xa, x3)), ya);
-                G::add_affine(acc, x3, y3);
-            } else if (kind == BA_COPY_A) {
-                if (!(F::is_exact_zero(xa) && F::is_exact_zero(ya)))
-                    G::add_affine(acc, xa, ya);
-            } else if (kind == BA_COPY_B) {
-                G::add_affine(acc, xb, yb);
-            }
-        }
-    }
-    store_xyzz(seg_sum + 8 * (size_t)dsc.z, acc);
 }
 
 // Out-of-line point operations for the latency-bound level-2 reduction kernels
@@ -1027,21 +884,14 @@ cudaError_t msm_tail(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
     //    wave by wave, so kernels of other streams (another MSM's tail) get SM
     //    slots while this one runs.  Threads past the device-side count exit.
     if (p.ba_rounds) {
-        // R - 1 materialized rounds over the padded lists (bases in one part),
-        // then the last round fused into the accumulation of the segments
-        const uint32_t lv = p.ba_rounds - 1;
-        const size_t nh = (size_t)(p.L + 1) * p.hist_blocks * (p.part_slice ? 2 : 1);
-        const int parts = p.part_slice ? 2 : 1;
-        const uint32_t *bound[3] = {b.len_scan, b.len_scan + (p.part_slice ? nh / 2 : nh), b.len_scan + nh};
-        const unsigned wflags = ctx.capturing_host ? cudaEventWaitExternal : 0;
-        if (lv && b.ready[0]) {  // host inputs: the bases arrive on another stream (one part)
-            const cudaError_t e = cudaStreamWaitEvent(st, b.ready[0], wflags);
+        if (b.ready[0]) {  // host inputs: the bases arrive on another stream (one part: no part split here)
+            const cudaError_t e = cudaStreamWaitEvent(st, b.ready[0], ctx.capturing_host ? cudaEventWaitExternal : 0);
             if (e != cudaSuccess)
                 return e;
         }
         cudaEvent_t ev0 = nullptr;
         prof_begin(ctx, &ev0);
-        for (uint32_t r = 1; r <= lv; r++) {
+        for (uint32_t r = 1; r <= p.ba_rounds; r++) {
             const uint4 *in_lvl = r == 1 ? nullptr : b.ba_lvl[(r - 2) & 1];
             uint4 *out_lvl = b.ba_lvl[(r - 1) & 1];
             const uint32_t blocks = std::max<uint32_t>(1, p.ba_blocks[r - 1]);
@@ -1062,37 +912,13 @@ cudaError_t msm_tail(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
                                                                 b.ba_pre, b.ba_co, b.ba_inv, out_lvl);
             HS_LAUNCH_CHECK(ctx);
         }
-        const uint4 *lvl = lv ? b.ba_lvl[(lv - 1) & 1] : nullptr;
-        const uint32_t pblocks = (uint32_t)std::max<uint64_t>(1, ((uint64_t)p.max_segs + BA_BT - 1) / BA_BT);
-        for (int j = 0; j < parts; j++) {
-            if (!lv && b.ready[j]) {  // host inputs: this part of the bases arrives on another stream
-                const cudaError_t e = cudaStreamWaitEvent(st, b.ready[j], wflags);
-                if (e != cudaSuccess)
-                    return e;
-            }
-            if (lv)
-                k_pair_prefix<C, false><<<pblocks, BA_BT, 0, st>>>(b.segs, bound[j], bound[j + 1], b.sorted,
-                                                                   b.points, lvl, b.ba_pre, b.ba_co, b.ba_tot);
-            else
-                k_pair_prefix<C, true><<<pblocks, BA_BT, 0, st>>>(b.segs, bound[j], bound[j + 1], b.sorted,
-                                                                  b.points, lvl, b.ba_pre, b.ba_co, b.ba_tot);
-            HS_LAUNCH_CHECK(ctx);
-            k_pair_invert<C><<<(pblocks + 63) / 64, 64, 0, st>>>(bound[j], bound[j + 1], b.ba_tot, b.ba_inv);
-            HS_LAUNCH_CHECK(ctx);
-            if (lv)
-                k_pair_finish<C, false, false><<<pblocks, BA_BT, 0, st>>>(b.segs, bound[j], bound[j + 1], b.sorted,
-                                                                          b.points, lvl, b.ba_pre, b.ba_co, b.ba_inv,
-                                                                          b.seg_sum);
-            else if (j == 0)
-                k_pair_finish<C, true, false><<<pblocks, BA_BT, 0, st>>>(b.segs, bound[j], bound[j + 1], b.sorted,
-                                                                         b.points, lvl, b.ba_pre, b.ba_co, b.ba_inv,
-                                                                         b.seg_sum);
-            else
-                k_pair_finish<C, true, true><<<pblocks, BA_BT, 0, st>>>(b.segs, bound[j], bound[j + 1], b.sorted,
-                                                                        b.points, lvl, b.ba_pre, b.ba_co, b.ba_inv,
-                                                                        b.seg_sum);
-            HS_LAUNCH_CHECK(ctx);
-        }
+        const int threads = 128;
+        const uint64_t want = (p.max_segs + threads - 1) / threads;
+        const int blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)ctx.sm_count * 32));
+        const size_t nh = (size_t)(p.L + 1) * p.hist_blocks;
+        k_accumulate_level<C><<<blocks, threads, 0, st>>>(b.segs, b.len_scan, b.len_scan + nh,
+                                                          b.ba_lvl[(p.ba_rounds - 1) & 1], b.seg_sum);
+        HS_LAUNCH_CHECK(ctx);
         prof_end(ctx, ev0, p.entries_pinned);
     } else {
         const int threads = 128;

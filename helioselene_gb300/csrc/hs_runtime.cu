@@ -365,47 +365,26 @@ BatchPlan make_window_plan(int curve, size_t n, int c, uint32_t w_lo, uint32_t w
     return p;
 }
 
-// Batch-affine rounds: R - 1 rounds are materialized, the last one is fused
-// into the accumulation of the segments (pairs of items per segment).  For the
-// materialized rounds every bucket's entry list is padded to a multiple of
-// 2^(R-1) (at most NB (2^(R-1) - 1) padding entries), so round r's lists are
-// the padded offsets shifted right by r and need no scan; the segments then
-// cut the lists of the last materialized round, with the cap of an entry count
-// that size.  With R = 1 nothing is padded and the segments are the entries'.
+// Batch-affine rounds: every bucket's entry list is padded to a multiple of
+// 2^R (at most NB (2^R - 1) padding entries), so round r's lists are the
+// padded offsets shifted right by r and need no scan; the fold's segments cut
+// the last round's lists with the cap of an entry count that size.
 void plan_batch_affine(BatchPlan &p, uint32_t rounds, uint64_t min_entries)
 {
     rounds = std::min<uint32_t>(rounds, BA_MAX_ROUNDS);
-    if (rounds == 0 || p.entries_bound < min_entries)
-        return;
-    const uint32_t lv = rounds - 1;
-    const uint64_t padded = (uint64_t)p.max_entries + (uint64_t)p.NB * ((1u << lv) - 1);
-    if (padded >= 0x80000000ull || (lv && p.part_slice))
+    const uint64_t padded = (uint64_t)p.max_entries + (uint64_t)p.NB * ((1u << rounds) - 1);
+    if (rounds == 0 || p.entries_bound < min_entries || p.part_slice || padded >= 0x80000000ull)
         return;
     p.ba_rounds = rounds;
-    if (!lv)
-        return;
     p.max_entries = (uint32_t)padded;
     const uint64_t per_block = (uint64_t)BA_PLAN_K * BA_PLAN_BT;
-    for (uint32_t r = 1; r <= lv; r++) {
+    for (uint32_t r = 1; r <= rounds; r++) {
         p.ba_items[r - 1] = (padded >> r) + 1;
         p.ba_blocks[r - 1] = (uint32_t)((p.ba_items[r - 1] + per_block - 1) / per_block);
     }
-    const uint64_t ent = p.ba_items[lv - 1];
+    const uint64_t ent = p.ba_items[rounds - 1];
     p.L = seg_cap(ent, p.NB);
     p.max_segs = (uint32_t)(std::min<uint64_t>(ent, p.NB) + ent / p.L + 1);
-}
-
-// batch-affine work buffers: level buffers, prefixes, per-thread co-products
-// and per-block totals and inverses, for the larger of the materialized rounds
-// and the fused one
-static void ba_sizes(const BatchPlan &p, size_t &lvl0, size_t &lvl1, size_t &pre, size_t &blocks)
-{
-    const uint32_t lv = p.ba_rounds ? p.ba_rounds - 1 : 0;
-    lvl0 = lv >= 1 ? (size_t)p.ba_items[0] : 0;
-    lvl1 = lv >= 2 ? (size_t)p.ba_items[1] : 0;
-    const size_t fused_items = (lv ? (size_t)p.ba_items[lv - 1] : (size_t)p.max_entries) / 2 + 1;
-    pre = std::max<size_t>(lvl0, fused_items);
-    blocks = std::max<size_t>(lv ? p.ba_blocks[0] : 0, ((size_t)p.max_segs + BA_PLAN_BT - 1) / BA_PLAN_BT);
 }
 
 static constexpr int SCAN_THREADS = 1024;
@@ -436,12 +415,11 @@ size_t batch_bytes(const BatchPlan &p)
     b += align256((size_t)std::max<uint32_t>(1, p.M) * 96);                                // results
     b += p.part_slice ? align256((size_t)(p.NB + 1) * 4) : 0;                                // part-0 counts
     if (p.ba_rounds) {
-        size_t lvl0, lvl1, pre, blocks;
-        ba_sizes(p, lvl0, lvl1, pre, blocks);
-        b += align256(lvl0 * 64) + align256(lvl1 * 64);  // odd / even materialized rounds
-        b += align256(pre * 32);                         // prefixes
-        b += align256(blocks * BA_PLAN_BT * 32);         // co-products
-        b += 2 * align256(blocks * 32);                  // totals, inverses
+        b += align256((size_t)p.ba_items[0] * 64);                                            // odd rounds
+        b += p.ba_rounds > 1 ? align256((size_t)p.ba_items[1] * 64) : 0;                      // even rounds
+        b += align256((size_t)p.ba_items[0] * 32);                                            // prefixes
+        b += align256((size_t)p.ba_blocks[0] * BA_PLAN_BT * 32);                              // co-products
+        b += 2 * align256((size_t)p.ba_blocks[0] * 32);                                       // totals, inverses
         b += 8 * 256;
     }
     return b + 16 * 256;
@@ -471,16 +449,13 @@ bool carve(DeviceArena &a, const BatchPlan &p, BatchBuffers &b)
     b.counts0 = p.part_slice ? (uint32_t *)a.take((size_t)(p.NB + 1) * 4) : nullptr;
     bool ba_ok = true;
     if (p.ba_rounds) {
-        size_t lvl0, lvl1, pre, blocks;
-        ba_sizes(p, lvl0, lvl1, pre, blocks);
-        if (lvl0)
-            ba_ok = ba_ok && (b.ba_lvl[0] = (uint4 *)a.take(lvl0 * 64));
-        if (lvl1)
-            ba_ok = ba_ok && (b.ba_lvl[1] = (uint4 *)a.take(lvl1 * 64));
-        ba_ok = ba_ok && (b.ba_pre = (uint4 *)a.take(pre * 32));
-        ba_ok = ba_ok && (b.ba_co = (uint4 *)a.take(blocks * BA_PLAN_BT * 32));
-        ba_ok = ba_ok && (b.ba_tot = (uint4 *)a.take(blocks * 32));
-        ba_ok = ba_ok && (b.ba_inv = (uint4 *)a.take(blocks * 32));
+        ba_ok = ba_ok && (b.ba_lvl[0] = (uint4 *)a.take((size_t)p.ba_items[0] * 64));
+        if (p.ba_rounds > 1)
+            ba_ok = ba_ok && (b.ba_lvl[1] = (uint4 *)a.take((size_t)p.ba_items[1] * 64));
+        ba_ok = ba_ok && (b.ba_pre = (uint4 *)a.take((size_t)p.ba_items[0] * 32));
+        ba_ok = ba_ok && (b.ba_co = (uint4 *)a.take((size_t)p.ba_blocks[0] * BA_PLAN_BT * 32));
+        ba_ok = ba_ok && (b.ba_tot = (uint4 *)a.take((size_t)p.ba_blocks[0] * 32));
+        ba_ok = ba_ok && (b.ba_inv = (uint4 *)a.take((size_t)p.ba_blocks[0] * 32));
     }
     return b.desc && b.counts && b.offsets && b.seg_off && b.scan_tmp && b.len_hist && b.len_scan && b.sorted &&
            b.segs && b.seg_sum && b.heavy && b.heavy_n && b.redA && b.redC && b.redS && b.out_jac &&
@@ -1076,10 +1051,9 @@ cudaError_t launch_sort(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
     // batch-affine plans: every bucket's list padded to a multiple of 2^R with
     // PAD_ENTRY (the identity), and the fold's segments counted on lists 2^R
     // times shorter
-    const uint32_t lv = p.ba_rounds ? p.ba_rounds - 1 : 0;  // materialized batch-affine rounds
-    const uint32_t pad = (1u << lv) - 1;
-    const uint32_t seg_L = p.L << lv;
-    if (lv && (e = cudaMemsetAsync(b.sorted, 0xff, (size_t)p.max_entries * 4, st)) != cudaSuccess)
+    const uint32_t pad = p.ba_rounds ? (1u << p.ba_rounds) - 1 : 0u;
+    const uint32_t seg_L = p.L << p.ba_rounds;
+    if (p.ba_rounds && (e = cudaMemsetAsync(b.sorted, 0xff, (size_t)p.max_entries * 4, st)) != cudaSuccess)
         return e;
     if (p.smem_sort()) {
         if ((e = sort_smem_attrs(ctx.device)) != cudaSuccess)
@@ -1123,12 +1097,12 @@ cudaError_t launch_sort(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
     const uint32_t *c0 = (p.part_slice && p.smem_sort()) ? b.counts0 : nullptr;
     const size_t hsm = (size_t)(p.L + 1) * 4 * (c0 ? 2 : 1);
     k_seg_hist<<<p.hist_blocks, SEG_HIST_THREADS, hsm, st>>>(b.offsets, p.NB, p.L, p.hist_blocks, b.len_hist, c0,
-                                                             lv);
+                                                             p.ba_rounds);
     HS_LAUNCH_CHECK(ctx);
     if ((e = launch_scan(ctx, b.len_hist, nh, 1u, b.len_scan, nullptr, b.scan_tmp)) != cudaSuccess)
         return e;
     k_seg_scatter<<<p.hist_blocks, SEG_HIST_THREADS, hsm, st>>>(b.offsets, b.seg_off, p.NB, p.L, p.hist_blocks,
-                                                                 b.len_scan, b.segs, c0, lv);
+                                                                 b.len_scan, b.segs, c0, p.ba_rounds);
     HS_LAUNCH_CHECK(ctx);
     return cudaSuccess;
 }
@@ -1821,11 +1795,11 @@ static int msm_host(Context &ctx, int curve, const uint8_t *lead_scalar, const v
     // entries of a bucket are contiguous and get their own segments, and the
     // accumulation of part 0 runs while part 1 is still on the link.
     const MsmDesc &d0 = split ? s.lo.msms[0] : p.msms[0];
-    // (a plan with materialized batch-affine rounds takes its bases in one part:
-    // its rounds pair entries of both parts)
+    // (a batch-affine plan takes its bases in one part: its rounds pair entries
+    // of both parts)
     const bool two = point_fmt != HS_FMT_COMPRESSED && d0.slices >= 2 &&
-                     (split ? (s.hi.smem_sort() && s.lo.smem_sort() && s.hi.ba_rounds <= 1 && s.lo.ba_rounds <= 1)
-                            : (p.smem_sort() && p.ba_rounds <= 1));
+                     (split ? (s.hi.smem_sort() && s.lo.smem_sort() && !s.hi.ba_rounds && !s.lo.ba_rounds)
+                            : (p.smem_sort() && !p.ba_rounds));
     size_t bound[3] = {0, total, total};
     if (two) {
         const uint32_t cut = d0.slices / 2;

@@ -91,8 +91,8 @@ void *hs_context_stream(hs_context *ctx);
  * (Montgomery's trick, fp/include/fp_batch_invert.h:61-114, across a wave of
  * bucket additions), then an XYZZ fold of what is left; 0 keeps the XYZZ mixed
  * additions of every entry (helios/src/x64/helios_msm_vartime.cpp:296-325 is
- * the bucket loop both replace).  Results are identical either way.  Defaults:
- * Helios 0, Selene 1 round, from 2^21 entries.  Host-input calls of a
+ * the bucket loop both replace).  Results are identical either way.  Default:
+ * one round on both curves, from 2^21 entries.  Host-input calls of a
  * batch-affine plan send their bases in one part. */
 int hs_context_set_batch_affine(hs_context *ctx, int curve, int rounds, size_t min_entries);
 /* set the Pippenger window width for one curve; 0 restores the built-in

@@ -75,8 +75,7 @@ def test_doubling_cancellation_and_identity_cases(ba_ctx, curve):
 @pytest.mark.parametrize("curve", [0, 1])
 def test_default_rule_at_2p20_against_xyzz_and_oracle(ba_ctx, curve):
     """n = 2^20 with the 1% edge slices (the headline size): one, two and three
-    rounds and the XYZZ path, split and unsplit, and the library default
-    (Selene one round, Helios none)"""
+    rounds and the XYZZ path, split and unsplit, and the library default"""
     from helioselene_gb300.workload import make_workload
     n = 1 << 20
     w = make_workload(curve, n, seed=2024 + curve, edge_fraction=0.01)
