@@ -531,11 +531,155 @@ struct Field {
         return acc;
     }
 
-    // a^(m-2); 0 -> 0
+    // ---- inversion by batched divsteps ----------------------------------------
+    // The variable-time binary-GCD inversion of Bernstein and Yang ("Fast
+    // constant-time gcd computation and modular inversion", 2019), with the
+    // half-delta divstep: starting from (f, g) = (m, a), each divstep maps
+    //     delta > 0 and g odd:  (delta, f, g) -> (1 - delta, g, (g - f) / 2)
+    //     g odd:                (delta, f, g) -> (1 + delta, f, (g + f) / 2)
+    //     g even:               (delta, f, g) -> (1 + delta, f, g / 2)
+    // until g = 0, where f = +-gcd = +-1.  Steps run in batches of 30 on the low
+    // 32 bits of f and g, which give a transition matrix T (entries at most 2^30)
+    // with 2^30 (f', g') = T (f, g); T is then applied to the full f and g, held
+    // in nine signed 30-bit limbs, and to (d, e) with f = d a, g = e a (mod m),
+    // where the division by 2^30 is made exact by adding a multiple of m.  At the
+    // end a^-1 = +-d.  A 256-bit input needs at most 590 divsteps (20 batches);
+    // the loop is capped at 40.  Against Fermat's a^(m-2) (255 dependent
+    // squarings) the dependent chain is about a tenth as long.
+    struct L30 {
+        int32_t l[9];  // value = sum l[i] 2^(30 i); l[0..7] in [0, 2^30), l[8] signed
+    };
+
+    __device__ __forceinline__ static L30 to_l30(const Fe &a)
+    {
+        L30 r;
+#pragma unroll
+        for (int i = 0; i < 9; i++) {
+            const int b = 30 * i, k = b >> 5, sh = b & 31;
+            const uint64_t lo = a.w[k], hi = k + 1 < 8 ? a.w[k + 1] : 0u;
+            r.l[i] = (int32_t)(((lo | (hi << 32)) >> sh) & 0x3fffffffu);
+        }
+        return r;
+    }
+
+    // (x, y) <- (s x + t y + k m) / 2^30 for one row; the low 30 bits vanish
+    __device__ __forceinline__ static void l30_row(L30 &out, const L30 &x, const L30 &y, int32_t s, int32_t t,
+                                                   int32_t k, const L30 &m)
+    {
+        int64_t c = (int64_t)s * x.l[0] + (int64_t)t * y.l[0] + (int64_t)k * m.l[0];
+        c >>= 30;
+#pragma unroll
+        for (int i = 1; i < 9; i++) {
+            c += (int64_t)s * x.l[i] + (int64_t)t * y.l[i] + (int64_t)k * m.l[i];
+            out.l[i - 1] = (int32_t)(c & 0x3fffffff);
+            c >>= 30;
+        }
+        out.l[8] = (int32_t)c;
+    }
+
     __device__ static Fe inv(const Fe &a)
     {
-        const uint32_t e[8] = {M0 - 2u, M1, M2, M3, M4, M5, M6, M7};
-        return pow(a, e);
+        const Fe x = canon(a);
+        if (is_exact_zero(x))
+            return zero();  // 0 -> 0
+        const Fe mf = {{M0, M1, M2, M3, M4, M5, M6, M7}};
+        const L30 m = to_l30(mf);
+        L30 zero30;
+#pragma unroll
+        for (int i = 0; i < 9; i++)
+            zero30.l[i] = 0;
+        // m^-1 mod 2^32 by Newton's iteration (m odd: m m = 1 mod 8 to start)
+        uint32_t minv = M0;
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+            minv *= 2u - M0 * minv;
+        L30 f = m, g = to_l30(x), d = zero30, e = zero30;
+        e.l[0] = 1;
+        int32_t D = 1;  // 2 delta, delta = 1/2
+        for (int batch = 0; batch < 40; batch++) {
+            uint32_t any = 0;
+#pragma unroll
+            for (int i = 0; i < 9; i++)
+                any |= (uint32_t)g.l[i];
+            if (!any)
+                break;
+            uint32_t fl = (uint32_t)f.l[0] | ((uint32_t)f.l[1] << 30);
+            uint32_t gl = (uint32_t)g.l[0] | ((uint32_t)g.l[1] << 30);
+            int32_t u = 1, v = 0, q = 0, r = 1;
+#pragma unroll 1
+            for (int i = 0; i < 30; i++) {
+                if (D > 0 && (gl & 1u)) {
+                    D = 2 - D;
+                    const uint32_t t = fl;
+                    fl = gl;
+                    gl -= t;
+                    const int32_t tu = u, tv = v;
+                    u = q;
+                    v = r;
+                    q -= tu;
+                    r -= tv;
+                } else if (gl & 1u) {
+                    D = 2 + D;
+                    gl += fl;
+                    q += u;
+                    r += v;
+                } else {
+                    D = 2 + D;
+                }
+                gl >>= 1;
+                u *= 2;
+                v *= 2;
+            }
+            L30 nf, ng, nd, ne;
+            l30_row(nf, f, g, u, v, 0, m);
+            l30_row(ng, f, g, q, r, 0, m);
+            const uint32_t td = (uint32_t)u * (uint32_t)d.l[0] + (uint32_t)v * (uint32_t)e.l[0];
+            const uint32_t te = (uint32_t)q * (uint32_t)d.l[0] + (uint32_t)r * (uint32_t)e.l[0];
+            const int32_t md = (int32_t)(((0u - td) * minv) << 2) >> 2;  // in [-2^29, 2^29)
+            const int32_t me = (int32_t)(((0u - te) * minv) << 2) >> 2;
+            l30_row(nd, d, e, u, v, md, m);
+            l30_row(ne, d, e, q, r, me, m);
+            f = nf;
+            g = ng;
+            d = nd;
+            e = ne;
+        }
+        // d + 16 m > 0 (|d| < m here), packed into nine 32-bit words, folded mod m
+        int64_t c = 0;
+        uint32_t w[9];
+        {
+            L30 t;
+#pragma unroll
+            for (int i = 0; i < 9; i++) {
+                c += (int64_t)d.l[i] + 16 * (int64_t)m.l[i];
+                t.l[i] = i < 8 ? (int32_t)(c & 0x3fffffff) : (int32_t)c;
+                c >>= 30;
+            }
+            uint64_t acc = 0;
+            int bits = 0, k = 0;
+#pragma unroll
+            for (int i = 0; i < 9; i++) {
+                acc |= (uint64_t)(uint32_t)t.l[i] << bits;
+                bits += 30;
+                while (bits >= 32 && k < 9) {
+                    w[k++] = (uint32_t)acc;
+                    acc >>= 32;
+                    bits -= 32;
+                }
+            }
+            while (k < 9) {
+                w[k++] = (uint32_t)acc;
+                acc >>= 32;
+            }
+        }
+        Fe lo;
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+            lo.w[i] = w[i];
+        Fe cfe = zero();
+        add_c_masked(cfe, 0xffffffffu);  // 2^256 mod m
+        Fe res = add(lo, mul(from_u32(w[8]), cfe));
+        return f.l[8] < 0 ? neg(res) : res;
     }
 };
 
