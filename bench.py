@@ -45,9 +45,16 @@ WORKLOAD = ("Helios + Selene vartime Pippenger MSM, n=2^20 each; scalars uniform
             "SWU-derived affine bases; 1% edge slices (zero, order-1, repeated base, top-window-only)")
 from helioselene_gb300.workload import BENCH_SEED as SEED  # noqa: E402
 IMAD_PER_MODMUL = {0: 144, 1: 232}  # F_p, F_q: 2 IMAD per 32x32->64 product
-# dram__bytes_read.sum + dram__bytes_write.sum of one k_accumulate launch at
-# n = 2^20, mean of the Helios and Selene launches of one ncu capture
-ACC_TRAFFIC_BYTES = (477.2e6 + 497.5e6) / 2
+# dram__bytes_read.sum + dram__bytes_write.sum of the bucket-accumulation phase of
+# one MSM at n = 2^20 (Helios, Selene), from ncu --set full captures of this
+# workload, by accumulation form (batch-affine rounds): 0 is k_accumulate, 1 is
+# k_ba_pairs + k_ba_invert + k_ba_finish + k_accumulate_level
+ACC_TRAFFIC = {
+    0: {"bytes": (477.2e6, 497.5e6), "capture": "2026-12-04, commit 14d24da, k_accumulate"},
+    1: {"bytes": (2923.5e6, 2941.9e6),
+        "capture": "2026-12-04, commit d2e236f, k_ba_pairs + k_ba_invert + k_ba_finish + k_accumulate_level"},
+}
+DEFAULT_BA_ROUNDS = (1, 1)  # the library's default accumulation form (Helios, Selene)
 SPLIT_DEFAULT = 1 << 18  # the library's window-split threshold for single MSMs
 
 
@@ -789,6 +796,30 @@ def run_decompress(hs, torch, ctxs, data, n: int, flush, imad_peak: float) -> di
     return out
 
 
+def executed_per_entry(rounds: int, curve: int) -> float:
+    """IMAD-equivalents executed per (point, window) entry by the accumulation with
+    `rounds` batch-affine rounds: round r adds 2^-r pairs per entry at 5M + 1S, the
+    fold 2^-rounds items per entry at 8M + 2S"""
+    m, s = IMAD_PER_MODMUL[curve], IMAD_PER_MODSQR[curve]
+    pair, madd = 5 * m + s, 8 * m + 2 * s
+    return sum(pair / 2**r for r in range(1, rounds + 1)) + madd / 2**rounds
+
+
+def traffic_of(rr) -> float:
+    """the captured accumulation-phase DRAM bytes per MSM, mean of the curves (None if not captured)"""
+    vals = [ACC_TRAFFIC[rr[c]]["bytes"][c] for c in (0, 1) if rr[c] in ACC_TRAFFIC]
+    return sum(vals) / len(vals) if len(vals) == 2 else None
+
+
+def traffic_source(rr) -> str:
+    parts = []
+    for c, name in ((0, "Helios"), (1, "Selene")):
+        t = ACC_TRAFFIC.get(rr[c])
+        parts.append(f"{name}: " + (f"{t['bytes'][c] / 1e6:.1f} MB, ncu capture {t['capture']}" if t else
+                                    "no capture of this form"))
+    return "; ".join(parts)
+
+
 def probe_rates(rates: dict, torch, local: int, clk: dict) -> dict:
     """the IMAD probe's instruction rates, per SM per clock at the SM clock seen
     in the timed region (the denominator of every roofline fraction here)"""
@@ -852,12 +883,14 @@ def run_ours(args) -> None:
     ctx.set_split(head_split)
     ctx2.set_split(head_split)
     ctx2.set_priority(True)
+    # the accumulation form of each curve (batch-affine rounds), set explicitly
+    rr = list(DEFAULT_BA_ROUNDS)
     if args.ba_rounds is not None:
         rr = [int(x) for x in str(args.ba_rounds).split(",")]
         rr = rr * 2 if len(rr) == 1 else rr
-        for c in (ctx, ctx2):
-            for curve in (hs.HELIOS, hs.SELENE):
-                c.set_batch_affine(rr[curve], 1 << 21, curve)
+    for c in (ctx, ctx2):
+        for curve in (hs.HELIOS, hs.SELENE):
+            c.set_batch_affine(rr[curve], 1 << 21, curve)
     ctxs = {hs.HELIOS: ctx, hs.SELENE: ctx2}
     n = args.n
     data = make_inputs(hs, ctx, torch, n, device)
@@ -958,7 +991,7 @@ def run_ours(args) -> None:
         prof_total["ms"] += pr["accumulate_ms"]
         prof_total["launches"] += pr["accumulate_launches"]
         prof_total["work"] += pr["entries"] * 6 * IMAD_PER_MODMUL[curve]
-        prof_total["executed"] += pr["entries"] * (8 * IMAD_PER_MODMUL[curve] + 2 * IMAD_PER_MODSQR[curve])
+        prof_total["executed"] += pr["entries"] * executed_per_entry(rr[curve], curve)
 
     # ---- e2e: reference-facing call with host buffers ----
     # Each e2e step is one isolated pair of calls (nothing of the next step
@@ -1077,9 +1110,15 @@ def run_ours(args) -> None:
                                        "api": "hs_msm_batch with both MSMs (HS_FMT_JACOBIAN51 in and out)"}},
             "roofline": {"bound": "imad", "achieved": achieved / 1e12, "peak": imad_peak / 1e12,
                          "unit": "T IMAD/s", "frac": achieved / imad_peak if imad_peak else None,
-                         "traffic": ACC_TRAFFIC_BYTES, "traffic_unit": "bytes per launch (DRAM read + write)",
-                         "traffic_source": "ncu capture of k_accumulate at n=2^20 (Helios 477.2 MB, Selene 497.5 MB)",
-                         "kernel": "k_accumulate",
+                         "traffic": traffic_of(rr), "traffic_unit": "bytes per MSM's accumulation phase "
+                                                                   "(DRAM read + write), mean of the two curves",
+                         "traffic_source": traffic_source(rr),
+                         "kernel": "bucket accumulation phase: " + ("; ".join(
+                             f"{name} " + ("k_accumulate (XYZZ)" if rr[c] == 0 else
+                                          f"{rr[c]} batch-affine round(s) (k_ba_pairs, k_ba_invert, k_ba_finish) "
+                                          "+ XYZZ fold (k_accumulate_level)")
+                             for c, name in ((0, "Helios"), (1, "Selene")))),
+                         "ba_rounds": {"helios": rr[0], "selene": rr[1]},
                          "work": "point-window entries x 6 modmul (batch-affine bucket add) x IMAD-eq per modmul "
                                  "(F_p 144, F_q 232), summed over one Helios and one Selene launch",
                          "peak_source": "measured in this run by hs_measure_imad_peak (the faster of mad.lo/mad.hi "
@@ -1087,8 +1126,10 @@ def run_ours(args) -> None:
                          "accumulate_ms_per_launch": acc_ms,
                          "executed_frac": (prof_total["executed"] / (prof_total["ms"] * 1e-3) / imad_peak
                                            if imad_peak and prof_total["ms"] > 0 else None),
-                         "executed_note": "the same launches counted with the products the kernel executes: "
-                                          "XYZZ mixed addition, 8 products + 2 squares per entry",
+                         "executed_note": "the same launches counted with the products they execute: XYZZ mixed "
+                                          "addition 8 products + 2 squares per item; a batch-affine pair 5 "
+                                          "products + 1 square (prefix, walk back, lambda, y) plus the shared "
+                                          "inversion",
                          "whole_msm_frac": whole / imad_peak if imad_peak else None,
                          "pinned_entries": "n x ceil(256/c) per MSM (c = 16 at n = 2^20: 16 windows), "
                                            "6 modmul each",
