@@ -60,6 +60,7 @@ SIGNATURES = {
     "hs_context_set_graphs": (_int, [_vp, _int]),
     "hs_context_set_split": (_int, [_vp, _sz]),
     "hs_context_set_batch_affine": (_int, [_vp, _int, _int, _sz]),
+    "hs_context_set_rule": (_int, [_vp, _int, _sz, _sz, _int, _int]),
     "hs_context_set_priority": (_int, [_vp, _int]),
     "hs_msm": (_int, [_vp, _int, _vp, _vp, _int, _sz, _vp, _int]),
     "hs_msm_device": (_int, [_vp, _int, _vp, _vp, _sz, _vp, _int]),

@@ -84,8 +84,10 @@ class Context:
     def stream(self) -> int:
         return int(self._lib.hs_context_stream(self._h) or 0)
 
-    def set_window(self, curve: int, n_min: int, n_max: int, window: int) -> None:
-        self._check(self._lib.hs_context_set_window(self._h, curve, n_min, n_max, window), "set_window")
+    def set_window(self, curve: int, n_min: int, n_max: int, window: int, ba_rounds: int = -1) -> None:
+        """window width (and optionally batch-affine rounds) for MSMs of n_min..n_max points; window 0 clears"""
+        self._check(self._lib.hs_context_set_rule(self._h, curve, n_min, n_max, window, int(ba_rounds)),
+                    "set_window")
 
     def set_graphs(self, on: bool) -> None:
         self._check(self._lib.hs_context_set_graphs(self._h, int(on)), "set_graphs")

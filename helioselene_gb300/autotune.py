@@ -1,9 +1,13 @@
-"""Window-width autotuner for the batched and per-call MSM paths.
+"""Window and accumulation autotuner for the batched and per-call MSM paths.
 
 For every size class (powers of two from 2^6 to 2^20) it times, on the GPU, a
 batch of MSMs of that size over candidate window widths c (a hill-climb that
-starts from the previous class's best) and keeps the fastest; the table becomes the context's window rules (hs_context_set_window)
-and can be saved to / loaded from a JSON cache keyed by device name.
+starts from the previous class's best) and keeps the fastest; then, at that c,
+the bucket accumulation form: 0, 1 or 2 batch-affine rounds (the wave of
+pairwise additions that share one inversion, hs_context_set_batch_affine).
+The table becomes the context's rules (hs_context_set_rule: c per class, and
+the rounds of plans whose entries lie mostly in that class) and can be saved
+to / loaded from a JSON cache keyed by device name.
 
 The reference hard-codes its window by n (helios/src/x64/helios_msm_vartime.cpp:248-263)
 and its autotune times only backends at n = 16 (src/dispatch.cpp:381-421); here
@@ -32,12 +36,19 @@ def _classes(n_min: int, n_max: int):
         k += 1
 
 
-def tune(ctx, curve: int, n_min: int = 64, n_max: int = 1 << 20, candidates: Iterable[int] = DEFAULT_CANDIDATES,
-         points_per_class: int = 1 << 20, reps: int = 3, seed: int = 1) -> Dict[str, int]:
-    """Return {"lo-hi": c} for each size class, measured with batched device MSMs.
+ROUND_CANDIDATES = (0, 1, 2)
 
-    Candidates are walked outward from the best of the previous size class (the
-    optimum grows with n), stopping once two neighbours in a row are slower."""
+
+def tune(ctx, curve: int, n_min: int = 64, n_max: int = 1 << 20, candidates: Iterable[int] = DEFAULT_CANDIDATES,
+         points_per_class: int = 1 << 20, reps: int = 3, seed: int = 1) -> Dict[str, dict]:
+    """Return {"lo-hi": {"c": c, "rounds": r}} for each size class, measured with
+    batched device MSMs.
+
+    Window candidates are walked outward from the best of the previous size
+    class (the optimum grows with n), stopping once two neighbours in a row are
+    slower; the accumulation rounds are then timed at the chosen c (a batch
+    below the accumulation's entry threshold runs XYZZ whatever the rounds, so
+    its class keeps 0)."""
     import torch
 
     from .workload import ORDER, random_field_bytes, random_scalars
@@ -59,10 +70,10 @@ def tune(ctx, curve: int, n_min: int = 64, n_max: int = 1 << 20, candidates: Ite
         cands = sorted(set(candidates))
         timed = {}
 
-        def measure(c):
-            if c not in timed:
+        def measure(c, rounds=0):
+            if (c, rounds) not in timed:
                 ctx.set_window(curve, 0, 0, 0)
-                ctx.set_window(curve, 1, 1 << 31, c)
+                ctx.set_window(curve, 1, 1 << 31, c, rounds)
                 ctx.msm_batch_device(curve, sizes, d_sc.data_ptr(), d_pts.data_ptr(), d_out.data_ptr())
                 stream.synchronize()
                 ts = []
@@ -73,8 +84,8 @@ def tune(ctx, curve: int, n_min: int = 64, n_max: int = 1 << 20, candidates: Ite
                     b.record(stream)
                     stream.synchronize()
                     ts.append(a.elapsed_time(b))
-                timed[c] = min(ts)
-            return timed[c]
+                timed[(c, rounds)] = min(ts)
+            return timed[(c, rounds)]
 
         start = min(cands, key=lambda c: abs(c - prev)) if table else cands[0]
         best_c = start
@@ -89,17 +100,22 @@ def tune(ctx, curve: int, n_min: int = 64, n_max: int = 1 << 20, candidates: Ite
                 c += direction
         measure(start)
         prev = best_c
-        table[f"{lo}-{hi}"] = best_c
+        best_r = min(ROUND_CANDIDATES, key=lambda r: measure(best_c, r))
+        table[f"{lo}-{hi}"] = {"c": best_c, "rounds": best_r}
         del d_u, d_pts, d_sc, d_out
     ctx.set_window(curve, 0, 0, 0)
     return table
 
 
-def apply(ctx, curve: int, table: Dict[str, int]) -> None:
+def apply(ctx, curve: int, table: Dict[str, object]) -> None:
+    """install a table: entries {"c", "rounds"} (or a bare window width)"""
     ctx.set_window(curve, 0, 0, 0)
-    for key, c in table.items():
+    for key, v in table.items():
         lo, hi = (int(x) for x in key.split("-"))
-        ctx.set_window(curve, lo, hi, int(c))
+        if isinstance(v, dict):
+            ctx.set_window(curve, lo, hi, int(v["c"]), int(v.get("rounds", -1)))
+        else:
+            ctx.set_window(curve, lo, hi, int(v))
 
 
 def load_or_tune(ctx, cache: Optional[Path] = None, n_max: int = 1 << 20, **kw) -> dict:
@@ -113,7 +129,8 @@ def load_or_tune(ctx, cache: Optional[Path] = None, n_max: int = 1 << 20, **kw) 
         except (OSError, ValueError):
             data = {}
     entry = data.get(dev)
-    if not entry or entry.get("n_max", 0) < n_max:
+    stale = entry and not all(isinstance(v, dict) for k in ("helios", "selene") for v in entry.get(k, {}).values())
+    if not entry or stale or entry.get("n_max", 0) < n_max:
         t0 = time.time()
         entry = {"n_max": n_max, "helios": tune(ctx, L.HELIOS, n_max=n_max, **kw),
                  "selene": tune(ctx, L.SELENE, n_max=n_max, **kw), "seconds": round(time.time() - t0, 2)}

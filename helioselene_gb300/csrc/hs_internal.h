@@ -30,9 +30,12 @@ struct DeviceArena {
     void release();
 };
 
+// A size class's window width and, when ba_rounds >= 0, its batch-affine
+// rounds (a plan takes the rounds of the class holding most of its entries).
 struct WindowRule {
     size_t n_min, n_max;
     int c;
+    int ba_rounds = -1;
 };
 
 // A captured launch sequence, replayed when the same batch shape runs again on

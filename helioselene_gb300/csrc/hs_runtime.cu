@@ -270,7 +270,25 @@ BatchPlan make_batch_plan(const Context &ctx, int curve, const size_t *sizes, ui
     p.hist_blocks = (p.NB + SEG_HIST_THREADS - 1) / SEG_HIST_THREADS;
     plan_chunks(p);
     plan_sort(p);
-    plan_batch_affine(p, ctx.ba_rounds[curve == HS_SELENE], ctx.ba_min_entries[curve == HS_SELENE]);
+    // batch-affine rounds: those of the size class (window rule) holding most of
+    // the plan's entries when that rule names some, else the curve's setting
+    const auto &rules = ctx.rules[curve == HS_SELENE ? 1 : 0];
+    int rounds = (int)ctx.ba_rounds[curve == HS_SELENE];
+    if (!rules.empty()) {
+        std::vector<uint64_t> by_rule(rules.size(), 0);
+        for (uint32_t i = 0; i < M; i++) {
+            int hit = -1;
+            for (size_t k = 0; k < rules.size(); k++)
+                if (sizes[i] >= rules[k].n_min && sizes[i] <= rules[k].n_max)
+                    hit = (int)k;  // the last matching rule wins, as in choose_window
+            if (hit >= 0)
+                by_rule[hit] += (uint64_t)sizes[i] * p.msms[i].W;
+        }
+        const size_t top = (size_t)(std::max_element(by_rule.begin(), by_rule.end()) - by_rule.begin());
+        if (by_rule[top] && rules[top].ba_rounds >= 0)
+            rounds = rules[top].ba_rounds;
+    }
+    plan_batch_affine(p, (uint32_t)rounds, ctx.ba_min_entries[curve == HS_SELENE]);
     return p;
 }
 
@@ -1650,7 +1668,13 @@ void *hs_context_stream(hs_context *h) { return h ? (void *)h->c.stream : nullpt
 
 int hs_context_set_window(hs_context *h, int curve, size_t n_min, size_t n_max, int window)
 {
-    if (!h || !valid_curve(curve) || n_min > n_max || (window != 0 && (window < 4 || window > 20)))
+    return hs_context_set_rule(h, curve, n_min, n_max, window, -1);
+}
+
+int hs_context_set_rule(hs_context *h, int curve, size_t n_min, size_t n_max, int window, int ba_rounds)
+{
+    if (!h || !valid_curve(curve) || n_min > n_max || (window != 0 && (window < 4 || window > 20)) ||
+        ba_rounds < -1 || ba_rounds > (int)BA_MAX_ROUNDS)
         return HS_EINVAL;
     std::lock_guard<std::mutex> lk(h->c.mu);
     auto &rules = h->c.rules[curve == HS_SELENE ? 1 : 0];
@@ -1658,7 +1682,9 @@ int hs_context_set_window(hs_context *h, int curve, size_t n_min, size_t n_max, 
         rules.clear();
         return HS_OK;
     }
-    rules.push_back(WindowRule{n_min, n_max, window});
+    WindowRule r{n_min, n_max, window};
+    r.ba_rounds = ba_rounds;
+    rules.push_back(r);
     return HS_OK;
 }
 

@@ -98,6 +98,10 @@ int hs_context_set_batch_affine(hs_context *ctx, int curve, int rounds, size_t m
 /* set the Pippenger window width for one curve; 0 restores the built-in
  * cost model (the autotuner writes this) */
 int hs_context_set_window(hs_context *ctx, int curve, size_t n_min, size_t n_max, int window);
+/* the same, with the batch-affine rounds (0..3) of plans whose entries lie
+ * mostly in this size class (-1: the curve's setting, hs_context_set_batch_affine);
+ * the autotuner writes both */
+int hs_context_set_rule(hs_context *ctx, int curve, size_t n_min, size_t n_max, int window, int ba_rounds);
 /* capture launch sequences as CUDA graphs and replay them for repeated shapes
  * (on by default); off launches every kernel directly */
 int hs_context_set_graphs(hs_context *ctx, int on);

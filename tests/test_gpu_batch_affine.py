@@ -106,3 +106,24 @@ def test_batched_plan_with_rounds(ba_ctx):
         ba_ctx.set_batch_affine(rounds, 0)
         got = ba_ctx.msm_batch(items)
         assert got == wants, f"rounds={rounds}"
+
+
+@pytest.mark.parametrize("curve", [0, 1])
+def test_rounds_from_size_class_rules(ba_ctx, curve):
+    """window rules that name batch-affine rounds (what the autotuner installs):
+    a batch whose entries lie mostly in one class takes that class's rounds"""
+    items, wants = [], []
+    for i, n in enumerate([70000, 3000, 90000, 17]):
+        sc, pts, _ = oracle_inputs(curve, n, seed=4000 + i, edge_fraction=0.02 if n >= 100 else 0.0)
+        items.append((curve, sc, pts))
+        wants.append(oracle.msm(curve, sc, pts))
+    try:
+        for rounds in (0, 1, 2, 3):
+            ba_ctx.set_window(curve, 0, 0, 0)
+            ba_ctx.set_window(curve, 1, 4095, 9, 0)
+            ba_ctx.set_window(curve, 4096, 1 << 20, 12, rounds)
+            ba_ctx.set_batch_affine(0, 0, curve)  # the rules' rounds, not the curve setting, decide
+            assert ba_ctx.msm_batch(items) == wants, f"rounds={rounds}"
+            assert ba_ctx.msm(curve, items[2][1], items[2][2]) == wants[2], f"single, rounds={rounds}"
+    finally:
+        ba_ctx.set_window(curve, 0, 0, 0)
