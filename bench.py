@@ -1001,7 +1001,7 @@ def run_ours(args) -> None:
     e2e_split = SPLIT_DEFAULT if args.split is None else args.split
     for c in ctxs.values():
         c.set_split(e2e_split)
-    e2e_steps = max(3, min(args.steps, 10))
+    e2e_steps = max(10, min(args.steps, 30))
     for _ in range(2):
         for curve in (hs.HELIOS, hs.SELENE):
             ctxs[curve].msm(curve, data[curve]["h_sc"].numpy(), data[curve]["h_jac"].numpy(), hs.FMT_JACOBIAN51,
@@ -1104,7 +1104,8 @@ def run_ours(args) -> None:
                     "api": "hs_msm(point_fmt=HS_FMT_JACOBIAN51, out_fmt=HS_FMT_JACOBIAN51), pinned host buffers",
                     "calls": "one per curve from a pool of two host threads, Selene first", "window_split_min": e2e_split,
                     "step_ms": {"median": statistics.median(e2e_step_ms), "min": min(e2e_step_ms),
-                                "max": max(e2e_step_ms)},
+                                "max": max(e2e_step_ms), "all": [round(t, 3) for t in e2e_step_ms]},
+                    "median_step_value": ws * 2 * n / (statistics.median(e2e_step_ms) * 1e-3),
                     "h2d_GBps_before": round(statistics.median(h2d_gbps), 1),
                     "one_batch_call": {"value": ws * 2 * n / e2e_batch_s, "unit": "points/s",
                                        "api": "hs_msm_batch with both MSMs (HS_FMT_JACOBIAN51 in and out)"}},
