@@ -208,7 +208,7 @@ def run_batched(hs, torch, device: str, local: int, steps: int, with_oracle: boo
     ctxs = [hs.Context(local), hs.Context(local)]
     t0 = time.time()
     tuned = autotune.load_or_tune(ctxs[0], cache=Path.home() / ".cache" / "helioselene_gb300_autotune.json",
-                                  n_max=65536, points_per_class=1 << 18, reps=2)
+                                  n_max=65536, points_per_class=1 << 20, reps=2)
     for c, name in ((hs.HELIOS, "helios"), (hs.SELENE, "selene")):
         autotune.apply(ctxs[1], c, tuned[name])
     tune_s = time.time() - t0

@@ -2692,6 +2692,15 @@ int hs_fixed_base_create(hs_context *h, int curve, const void *generators, int p
     return HS_OK;
 }
 
+// a chunk of `count` commitments, with the curve's bucket accumulation form
+static BatchPlan fixed_plan(const Context &ctx, const hs_fixed_base *fb, uint32_t count)
+{
+    BatchPlan p = make_fixed_plan(fb->curve, fb->n_gen, fb->c, count);
+    const int k = fb->curve == HS_SELENE ? 1 : 0;
+    plan_batch_affine(p, ctx.ba_rounds[k], ctx.ba_min_entries[k]);
+    return p;
+}
+
 // Run count fixed-base commitments whose scalars are at d_scalars (count x n_gen
 // x 32 bytes on the device) in chunks bounded by the entry count; results to d_out.
 static int fixed_commit_chunks(Context &ctx, const hs_fixed_base *fb, const uint8_t *d_scalars, size_t count,
@@ -2699,7 +2708,7 @@ static int fixed_commit_chunks(Context &ctx, const hs_fixed_base *fb, const uint
 {
     const uint64_t per = (uint64_t)fb->n_gen * fb->W;
     const size_t chunk = (size_t)std::max<uint64_t>(1, std::min<uint64_t>(count, (1ull << 29) / per));
-    const BatchPlan big = make_fixed_plan(fb->curve, fb->n_gen, fb->c, (uint32_t)chunk);
+    const BatchPlan big = fixed_plan(ctx, fb, (uint32_t)chunk);
     const bool aff = out_fmt == HS_FMT_AFFINE;
     // affine results: Jacobian first, then one shared inversion per 16 commitments
     const size_t extra = aff ? align256(count * 120) + align256(count * 32) : 0;
@@ -2709,7 +2718,7 @@ static int fixed_commit_chunks(Context &ctx, const hs_fixed_base *fb, const uint
     void *d_scr = nullptr;
     for (size_t j0 = 0; j0 < count; j0 += chunk) {
         const size_t cnt = std::min(chunk, count - j0);
-        const BatchPlan p = make_fixed_plan(fb->curve, fb->n_gen, fb->c, (uint32_t)cnt);
+        const BatchPlan p = fixed_plan(ctx, fb, (uint32_t)cnt);
         ctx.arena.reset();
         if (aff) {  // results and scratch live at the front of the arena, below the batch workspace
             d_jac = (uint8_t *)ctx.arena.take(count * 120);
@@ -2770,9 +2779,9 @@ int hs_fixed_base_commit(hs_context *h, const hs_fixed_base *fb, const uint8_t *
     std::vector<uint8_t> host(count * ob);
     for (size_t j0 = 0; j0 < count; j0 += chunk) {
         const size_t cnt = std::min(chunk, count - j0);
-        const BatchPlan big = make_fixed_plan(fb->curve, fb->n_gen, fb->c, (uint32_t)chunk);
+        const BatchPlan big = fixed_plan(ctx, fb, (uint32_t)chunk);
         HS_CU(ctx.arena.reserve(batch_bytes(big) + align256(extra) + 1024), "workspace allocation");
-        const BatchPlan p = make_fixed_plan(fb->curve, fb->n_gen, fb->c, (uint32_t)cnt);
+        const BatchPlan p = fixed_plan(ctx, fb, (uint32_t)cnt);
         BatchBuffers b;
         if (!carve(ctx.arena, p, b))
             return fail_msg(ctx, HS_ENOMEM, "workspace carve");

@@ -127,3 +127,27 @@ def test_rounds_from_size_class_rules(ba_ctx, curve):
             assert ba_ctx.msm(curve, items[2][1], items[2][2]) == wants[2], f"single, rounds={rounds}"
     finally:
         ba_ctx.set_window(curve, 0, 0, 0)
+
+
+@pytest.mark.parametrize("curve", [0, 1])
+def test_fixed_base_commitments_with_rounds(ba_ctx, curve):
+    """fixed-base commitments (every window of every generator into one set of
+    buckets, so buckets of thousands of entries) with the rounds forced on"""
+    import helioselene_gb300 as hs
+    from helioselene_gb300.workload import ORDER, random_scalars
+    n, count = 500, 5
+    _, gens, _ = oracle_inputs(curve, n + 1, seed=61 + curve)
+    H, G = gens[n], gens[:n]
+    rng = np.random.default_rng(17 + curve)
+    vals = random_scalars(rng, count * n, ORDER[curve]).reshape(count, n, 32)
+    vals[1, :100] = vals[1, 0]          # repeated scalars on distinct generators
+    vals[2] = 0
+    blinds = random_scalars(rng, count, ORDER[curve])
+    want = [oracle.pedersen(curve, blinds[j], H, vals[j], G) for j in range(count)]
+    fb = hs.FixedBase(ba_ctx, curve, G, H=H, window=12)
+    try:
+        for rounds in (0, 1, 2, 3):
+            ba_ctx.set_batch_affine(rounds, 0, curve)
+            assert fb.commit(vals, blinds) == want, f"rounds={rounds}"
+    finally:
+        fb.close()
