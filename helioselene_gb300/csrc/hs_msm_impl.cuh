@@ -129,7 +129,6 @@ __global__ void __launch_bounds__(128) k_accumulate(const uint4 *__restrict__ se
 constexpr int BA_K = (int)BA_PLAN_K;    // outputs per thread
 constexpr int BA_BT = (int)BA_PLAN_BT;  // threads per block: one shared inversion per BA_K * BA_BT outputs
 constexpr uint32_t PAD_ENTRY = 0xffffffffu;
-constexpr int BA_PF = 4;  // outputs whose loads k_ba_pairs keeps in flight together
 
 enum BaKind : int { BA_ADD, BA_DBL, BA_COPY_A, BA_COPY_B, BA_ZERO };
 
@@ -166,57 +165,30 @@ __device__ __forceinline__ Fe ba_load_y(const uint4 *src, bool neg, const Fe &x)
     return (neg && !(F::is_exact_zero(x) && F::is_exact_zero(y))) ? F::neg(y) : y;
 }
 
-// Where the two items of output q are (round 1 reads the 8-byte entry pair;
-// a PAD_ENTRY is the identity, src null); `valid` is false past the round's end.
-struct BaSrc {
-    const uint4 *sa, *sb;
-    bool na, nb, valid;
-};
-
-template <bool FIRST>
-__device__ __forceinline__ BaSrc ba_locate(const uint32_t *__restrict__ sorted, const uint4 *__restrict__ pts,
-                                           const uint4 *__restrict__ lvl, uint64_t q, uint32_t E)
+// Kind and denominator of output q (items 2q and 2q+1).  With FULL every
+// coordinate is loaded (for the sum); without, a y coordinate only when the
+// case needs it (identity check, equal x).
+template <class C, bool FIRST, bool FULL>
+__device__ __forceinline__ int ba_item(const uint32_t *__restrict__ sorted, const uint4 *__restrict__ pts,
+                                       const uint4 *__restrict__ lvl, uint32_t q, Fe &xa, Fe &ya, Fe &xb, Fe &yb,
+                                       Fe &d)
 {
-    BaSrc r;
-    r.valid = q < E;
+    using F = typename C::F;
     uint32_t ea = 0, eb = 0;
-    if (FIRST && r.valid) {
+    if (FIRST) {
         const uint2 e = __ldg(reinterpret_cast<const uint2 *>(sorted) + q);
         ea = e.x;
         eb = e.y;
     }
-    r.sa = r.valid ? ba_src<FIRST>(ea, pts, lvl, 2 * (uint32_t)q, r.na) : nullptr;
-    r.sb = r.valid ? ba_src<FIRST>(eb, pts, lvl, 2 * (uint32_t)q + 1, r.nb) : nullptr;
-    if (!r.valid)
-        r.na = r.nb = false;
-    return r;
-}
-
-// y as the item's point has it: negated for a negative round-1 digit, the identity left (0,0)
-template <class C>
-__device__ __forceinline__ Fe ba_sign_y(const Fe &y, bool neg, const Fe &x)
-{
-    using F = typename C::F;
-    return (neg && !(F::is_exact_zero(x) && F::is_exact_zero(y))) ? F::neg(y) : y;
-}
-
-// Kind and denominator of an output from its items' x coordinates (xa, xb as
-// loaded; zero for a null source) and, with FULL, their y coordinates as loaded
-// (ya, yb unsigned on entry, signed on return); without FULL a y coordinate is
-// loaded only when the case needs it (identity check, equal x).
-template <class C, bool FULL>
-__device__ __forceinline__ int ba_decide(const BaSrc &s, const Fe &xa, Fe &ya, const Fe &xb, Fe &yb, Fe &d)
-{
-    using F = typename C::F;
+    bool na, nb;
+    const uint4 *sa = ba_src<FIRST>(ea, pts, lvl, 2 * q, na);
+    const uint4 *sb = ba_src<FIRST>(eb, pts, lvl, 2 * q + 1, nb);
     d = F::one();
+    xa = sa ? ba_ld(sa) : F::zero();
+    xb = sb ? ba_ld(sb) : F::zero();
     const bool xa0 = F::is_exact_zero(xa), xb0 = F::is_exact_zero(xb);
-    if (FULL) {
-        ya = s.sa ? ba_sign_y<C>(ya, s.na, xa) : F::zero();
-        yb = s.sb ? ba_sign_y<C>(yb, s.nb, xb) : F::zero();
-    } else {
-        ya = (s.sa && xa0) ? ba_load_y<C>(s.sa, s.na, xa) : F::zero();
-        yb = (s.sb && xb0) ? ba_load_y<C>(s.sb, s.nb, xb) : F::zero();
-    }
+    ya = (sa && (FULL || xa0)) ? ba_load_y<C>(sa, na, xa) : F::zero();
+    yb = (sb && (FULL || xb0)) ? ba_load_y<C>(sb, nb, xb) : F::zero();
     if (xb0 && F::is_exact_zero(yb))
         return BA_COPY_A;  // b is the identity
     if (xa0 && F::is_exact_zero(ya))
@@ -224,8 +196,8 @@ __device__ __forceinline__ int ba_decide(const BaSrc &s, const Fe &xa, Fe &ya, c
     const Fe dx = F::sub(xb, xa);
     if (F::is_zero(dx)) {
         if (!FULL) {
-            ya = ba_load_y<C>(s.sa, s.na, xa);
-            yb = ba_load_y<C>(s.sb, s.nb, xb);
+            ya = ba_load_y<C>(sa, na, xa);
+            yb = ba_load_y<C>(sb, nb, xb);
         }
         if (!F::is_zero(F::sub(yb, ya)) || F::is_zero(ya))
             return BA_ZERO;  // b = -a (or a point of order 2, which doubles to the identity)
@@ -259,34 +231,17 @@ __global__ void __launch_bounds__(BA_BT) k_ba_pairs(const uint32_t *__restrict__
     const uint64_t base = ba_tile_base();
     Fe run = F::one();
     bool any = false;
-    // BA_PF outputs at a time: their entries, then their x coordinates, are all in
-    // flight before the first denominator is formed (the gathers are random)
 #pragma unroll 1
-    for (int k0 = 0; k0 < BA_K; k0 += BA_PF) {
-        if (base + 32 * (uint64_t)k0 >= E)
+    for (int k = 0; k < BA_K; k++) {
+        const uint64_t q = base + 32 * (uint64_t)k;
+        if (q >= E)
             break;
-        BaSrc src[BA_PF];
-        Fe xa[BA_PF], xb[BA_PF];
-#pragma unroll
-        for (int j = 0; j < BA_PF; j++)
-            src[j] = ba_locate<FIRST>(sorted, pts, lvl, base + 32 * (uint64_t)(k0 + j), E);
-#pragma unroll
-        for (int j = 0; j < BA_PF; j++) {
-            xa[j] = src[j].sa ? ba_ld(src[j].sa) : F::zero();
-            xb[j] = src[j].sb ? ba_ld(src[j].sb) : F::zero();
-        }
-#pragma unroll
-        for (int j = 0; j < BA_PF; j++) {
-            if (!src[j].valid)
-                continue;
-            Fe ya, yb, d;
-            const int kind = ba_decide<C, false>(src[j], xa[j], ya, xb[j], yb, d);
-            if (kind == BA_ADD || kind == BA_DBL) {
-                const uint64_t q = base + 32 * (uint64_t)(k0 + j);
-                store_fe(pre + 2 * q, run);  // exclusive prefix of this output (1 for the first)
-                run = any ? F::mul(run, d) : d;
-                any = true;
-            }
+        Fe xa, ya, xb, yb, d;
+        const int kind = ba_item<C, FIRST, false>(sorted, pts, lvl, (uint32_t)q, xa, ya, xb, yb, d);
+        if (kind == BA_ADD || kind == BA_DBL) {
+            store_fe(pre + 2 * q, run);  // exclusive prefix of this output (1 for the first)
+            run = any ? F::mul(run, d) : d;
+            any = true;
         }
     }
     // product tree over the block's thread totals (leaf t at BA_BT + t)
@@ -330,7 +285,7 @@ __global__ void k_ba_invert(const uint32_t *__restrict__ offsets, uint32_t NB, u
 }
 
 template <class C, bool FIRST>
-__global__ void __launch_bounds__(BA_BT, 4) k_ba_finish(const uint32_t *__restrict__ offsets, uint32_t NB, uint32_t r,
+__global__ void __launch_bounds__(BA_BT) k_ba_finish(const uint32_t *__restrict__ offsets, uint32_t NB, uint32_t r,
                                                     const uint32_t *__restrict__ sorted, const uint4 *__restrict__ pts,
                                                     const uint4 *__restrict__ lvl, const uint4 *__restrict__ pre,
                                                     const uint4 *__restrict__ co, const uint4 *__restrict__ inv,
@@ -345,24 +300,11 @@ __global__ void __launch_bounds__(BA_BT, 4) k_ba_finish(const uint32_t *__restri
     Fe inv_run = F::mul(load_fe(inv + 2 * (size_t)blockIdx.x),
                         load_fe(co + 2 * ((size_t)blockIdx.x * BA_BT + threadIdx.x)));
     const int kmax = (int)((E - 1 - base) / 32) < BA_K - 1 ? (int)((E - 1 - base) / 32) : BA_K - 1;
-    // the next output's points are loaded while this one is computed
-    BaSrc cs = ba_locate<FIRST>(sorted, pts, lvl, base + 32 * (uint64_t)kmax, E);
-    Fe cxa = cs.sa ? ba_ld(cs.sa) : F::zero(), cya = cs.sa ? ba_ld(cs.sa + 2) : F::zero();
-    Fe cxb = cs.sb ? ba_ld(cs.sb) : F::zero(), cyb = cs.sb ? ba_ld(cs.sb + 2) : F::zero();
 #pragma unroll 1
     for (int k = kmax; k >= 0; k--) {
         const uint64_t q = base + 32 * (uint64_t)k;
-        BaSrc ns;
-        Fe nxa, nya, nxb, nyb;
-        if (k > 0) {
-            ns = ba_locate<FIRST>(sorted, pts, lvl, q - 32, E);
-            nxa = ns.sa ? ba_ld(ns.sa) : F::zero();
-            nya = ns.sa ? ba_ld(ns.sa + 2) : F::zero();
-            nxb = ns.sb ? ba_ld(ns.sb) : F::zero();
-            nyb = ns.sb ? ba_ld(ns.sb + 2) : F::zero();
-        }
-        Fe xa = cxa, ya = cya, xb = cxb, yb = cyb, d;
-        const int kind = ba_decide<C, true>(cs, xa, ya, xb, yb, d);
+        Fe xa, ya, xb, yb, d;
+        const int kind = ba_item<C, FIRST, true>(sorted, pts, lvl, (uint32_t)q, xa, ya, xb, yb, d);
         Fe x3, y3;
         if (kind == BA_ADD || kind == BA_DBL) {
             const Fe inv_d = F::mul(inv_run, load_fe(pre + 2 * q));
@@ -387,13 +329,6 @@ __global__ void __launch_bounds__(BA_BT, 4) k_ba_finish(const uint32_t *__restri
         } else {
             x3 = F::zero();
             y3 = F::zero();
-        }
-        if (k > 0) {
-            cs = ns;
-            cxa = nxa;
-            cya = nya;
-            cxb = nxb;
-            cyb = nyb;
         }
         uint4 *dst = out + 4 * q;
         store_fe(dst, x3);
