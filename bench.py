@@ -311,7 +311,10 @@ def run_serving(hs, torch, device: str, local: int, requests_per_rate: int = 100
     25% are fresh points sent with the request.  Continuous batching (8 slots,
     batches of up to 2^23 points)
     against the plain path: the same requests one MSM per launch sequence, one
-    at a time (a server with one slot and one request per batch)."""
+    at a time (a server with one slot and one request per batch, the pooled
+    bases gathered as variable bases, as a per-call MSM would take them).  The
+    batching server keeps each pool as a table of window multiples; at
+    saturation it is also timed with the pool gathered instead (window 0)."""
     from helioselene_gb300.workload import ORDER, random_field_bytes, random_scalars, serving_sizes
     rng = np.random.default_rng(SEED + 4)
     pool_n = 1 << 18
@@ -383,12 +386,16 @@ def run_serving(hs, torch, device: str, local: int, requests_per_rate: int = 100
            "plain": "the same requests at the same arrival times, one MSM per launch sequence, one at a time",
            "rates": []}
     srv = hs.Server(local, slots=8, max_batch_points=1 << 23, max_batch_msms=1024)
+    gathered = hs.Server(local, slots=8, max_batch_points=1 << 23, max_batch_msms=1024)
     plain = hs.Server(local, slots=1, max_batch_msms=1)
-    for s in (srv, plain):
+    for s in (srv, gathered, plain):
         for c in (hs.HELIOS, hs.SELENE):
+            if s is not srv:
+                s.set_pool_window(c, 0)
             s.set_pool(c, pools[c])
     warm = draw(64)
     run(srv, warm, 0)
+    run(gathered, warm, 0)
     run(plain, warm[:16], 0)
     checked = None
     for rate in (1000, 3000, 9000, 0):
@@ -401,6 +408,11 @@ def run_serving(hs, torch, device: str, local: int, requests_per_rate: int = 100
         out["rates"].append({"serving": a, "plain": bsec})
         if rate == 0:
             checked = (reqs, res_srv)
+            res_g = []
+            g = run(gathered, reqs, rate, arrivals, res_g)
+            out["pool_table"] = {"window": 12, "table_msms_per_s": a["msms_per_s"],
+                                 "gathered_msms_per_s": g["msms_per_s"], "gathered_p50_ms": g["p50_ms"],
+                                 "gathered_p99_ms": g["p99_ms"], "same_results": res_g == res_srv}
     # a sample of the all-at-once requests against the oracle (pooled + fresh bases)
     if with_oracle and checked:
         sys.path.insert(0, str(ROOT / "oracle"))
@@ -425,12 +437,13 @@ def run_serving(hs, torch, device: str, local: int, requests_per_rate: int = 100
     out["plain_msms_per_s"] = peak["plain"]["msms_per_s"]
     out["speedup_vs_plain"] = out["msms_per_s"] / out["plain_msms_per_s"]
     srv.close()
+    gathered.close()
     plain.close()
     return out
 
 
 def run_fixed(hs, torch, device: str, local: int, count: int = 4096, chunk: int = 256,
-              with_oracle: bool = True) -> dict:
+              with_oracle: bool = True, ba_rounds=None) -> dict:
     """Config 5: Pedersen-style commitments r*H + sum v_i G_i over n = 2^20 resident
     generators per curve with device window tables; 4096 commitments per curve,
     submitted 256 at a time from two device scalar buffers used alternately;
@@ -444,6 +457,9 @@ def run_fixed(hs, torch, device: str, local: int, count: int = 4096, chunk: int 
     gen = torch.Generator(device=device)
     gen.manual_seed(SEED + 5)
     ctx = hs.Context(local)
+    if ba_rounds is not None:
+        for curve in (hs.HELIOS, hs.SELENE):
+            ctx.set_batch_affine(ba_rounds[curve], 1 << 21, curve)
     stream = torch.cuda.ExternalStream(ctx.stream, device=device)
     nsparse = max(1, chunk // 10)
     out = {"generators": n, "commitments": count, "chunk": chunk, "sparse_fraction": nsparse / chunk}
@@ -1064,7 +1080,7 @@ def run_ours(args) -> None:
         serving = run_serving(hs, torch, device, local, with_oracle=not args.no_cpu)
     fixed = None
     if not args.no_fixed:
-        fixed = run_fixed(hs, torch, device, local, with_oracle=not args.no_cpu)
+        fixed = run_fixed(hs, torch, device, local, with_oracle=not args.no_cpu, ba_rounds=rr)
     smul = None
     if not args.no_scalar_mul:
         smul = run_scalar_mul(hs, torch, ctxs, data, n, flush)

@@ -88,6 +88,7 @@ SIGNATURES = {
     "hs_fixed_base_destroy": (None, [_vp]),
     "hs_server_create": (_int, [_c.POINTER(_vp), _c.POINTER(hs_server_config)]),
     "hs_server_set_pool": (_int, [_vp, _int, _vp, _sz]),
+    "hs_server_set_pool_window": (_int, [_vp, _int, _int]),
     "hs_server_set_window": (_int, [_vp, _int, _sz, _sz, _int]),
     "hs_server_submit": (_int, [_vp, _c.POINTER(hs_request), _c.POINTER(_c.c_uint64)]),
     "hs_server_wait": (_int, [_vp, _c.c_uint64, _int, _c.POINTER(_c.c_double)]),

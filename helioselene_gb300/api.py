@@ -315,10 +315,19 @@ class Server:
         self._live = {}
 
     def set_pool(self, curve: int, affine_points) -> None:
+        """resident base pool of one curve (and, unless its pool window is 0,
+        the table of window multiples its pooled requests are computed from)"""
         p = _u8(affine_points)
         rc = self._lib.hs_server_set_pool(self._h, curve, _ptr(p), p.size // 64)
         if rc != L.HS_OK:
             raise L.HsError(rc, "hs_server_set_pool")
+
+    def set_pool_window(self, curve: int, window: int) -> None:
+        """window width of the curve's pool table from the next set_pool (4..16;
+        0: no table, pooled bases gathered as variable bases)"""
+        rc = self._lib.hs_server_set_pool_window(self._h, curve, int(window))
+        if rc != L.HS_OK:
+            raise L.HsError(rc, "hs_server_set_pool_window")
 
     def set_window(self, curve: int, n_min: int, n_max: int, window: int) -> None:
         """window rule for every slot's batches (hs_server_set_window; window 0 clears)"""

@@ -104,13 +104,16 @@ constexpr uint32_t RED_CHUNK = 256;
 // A fixed-base MSM (fixed = 1) reads its bases from a table of window
 // multiples 2^(c k) G_i stored at index i*W + k: every window then adds into
 // the same B buckets, so it reduces Wr = 1 window and needs no Horner step.
+// With fixed = 2 its points are rows of such a table named by an index list
+// (BatchBuffers::pt_idx): point pt_off + j of the batch is generator
+// pt_idx[pt_off + j] of the table.
 struct MsmDesc {
     uint32_t pt_off, n;
     uint32_t c, W, B;
     uint32_t bucket_base;
     uint32_t group_base, m0, log2m0, T;  // T = B / m0 groups per window
     uint32_t win_base;
-    uint32_t fixed;   // 1: bases from a window-multiple table
+    uint32_t fixed;   // 1: bases from a window-multiple table, 2: table rows named by BatchBuffers::pt_idx
     uint32_t Wr;      // windows that are reduced and combined (W, or 1 for fixed-base)
     uint32_t w_lo;    // first window this descriptor emits (a window-split half starts above 0)
     uint32_t w_cnt;   // windows emitted: [w_lo, w_lo + w_cnt)
@@ -183,7 +186,8 @@ constexpr uint32_t BA_MAX_ROUNDS = 3;
 // Device buffers of one batch (carved from the arena).
 struct BatchBuffers {
     const uint32_t *scalars = nullptr;  // n_total * 8 words
-    const uint4 *points = nullptr;      // n_total * 4 uint4 (affine x || y)
+    const uint4 *points = nullptr;      // n_total * 4 uint4 (affine x || y), or a window-multiple table
+    const uint32_t *pt_idx = nullptr;   // n_total table generators of the MSMs with fixed = 2
     MsmDesc *desc = nullptr;            // M descriptors
     uint32_t *counts = nullptr;         // NB + 1 (later reused as fill cursors)
     uint32_t *offsets = nullptr;        // NB + 1, exclusive scan of counts
@@ -233,6 +237,9 @@ int choose_window(const Context &ctx, int curve, size_t n);
 BatchPlan make_batch_plan(const Context &ctx, int curve, const size_t *sizes, uint32_t M);
 // count fixed-base MSMs of n table generators each (window c), scalars back to back
 BatchPlan make_fixed_plan(int curve, size_t n, int c, uint32_t count);
+// M MSMs over rows of one window-multiple table (window c) named by index lists
+// (fixed = 2): sizes[i] generators each, scalars and indices back to back
+BatchPlan make_indexed_plan(const Context &ctx, int curve, const size_t *sizes, uint32_t M, int c);
 // one MSM of n points restricted to windows [w_lo, w_lo + w_cnt) of width c
 BatchPlan make_window_plan(int curve, size_t n, int c, uint32_t w_lo, uint32_t w_cnt);
 // switch a plan to batch-affine accumulation with `rounds` rounds (0 or a plan
@@ -243,6 +250,10 @@ bool carve(DeviceArena &a, const BatchPlan &p, BatchBuffers &b);
 
 // curve-independent launches (hs_runtime.cu): descriptor upload, recode, sort, segments
 cudaError_t launch_sort(Context &ctx, const BatchPlan &p, const BatchBuffers &b);
+// two plans over the same M requests (a request's MSM cut in two parts), their
+// results added per request into d_jac (M canonical Jacobians) and formatted
+int execute_joined(Context &ctx, const BatchPlan &pa, const BatchBuffers &ba, const BatchPlan &pb,
+                   const BatchBuffers &bb, uint32_t *d_jac, void *d_out, int out_fmt);
 
 // per-curve entry points (hs_curve_helios.cu / hs_curve_selene.cu)
 struct CurveOps {
@@ -262,8 +273,8 @@ struct CurveOps {
     // window-multiple table: table[i*W + k] = 2^(c k) * gens[i] (affine), tmp holds n*W XYZZ points
     cudaError_t (*fixed_table)(Context &ctx, const uint4 *d_gens, size_t n, int c, int W, uint4 *d_tmp,
                                uint4 *d_table);
-    // out = a + b for canonical Jacobians (24 words each)
-    cudaError_t (*join)(Context &ctx, const uint32_t *d_a, const uint32_t *d_b, uint32_t *d_out);
+    // out[i] = a[i] + b[i] for count canonical Jacobians (24 words each)
+    cudaError_t (*join)(Context &ctx, const uint32_t *d_a, const uint32_t *d_b, size_t count, uint32_t *d_out);
     // 32-byte encodings -> canonical affine; invalid ones give (0, 0), d_valid[i] = 0
     // (d_valid may be null) and a count in *d_bad (not cleared here)
     cudaError_t (*decompress)(Context &ctx, const void *d_in, size_t n, uint4 *d_out, uint8_t *d_valid,

@@ -1571,18 +1571,23 @@ __device__ Xyzz xyzz_from_jac24(const uint32_t *j)
 }
 
 template <class C>
-__global__ void k_join(const uint32_t *__restrict__ a, const uint32_t *__restrict__ b, uint32_t *__restrict__ out)
+__global__ void k_join(const uint32_t *__restrict__ a, const uint32_t *__restrict__ b, size_t count,
+                       uint32_t *__restrict__ out)
 {
     using G = Group<C>;
-    if (blockIdx.x != 0 || threadIdx.x != 0)
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= count)
         return;
-    store_jacobian_canon<C>(out, G::add(xyzz_from_jac24<C>(a), xyzz_from_jac24<C>(b)));
+    store_jacobian_canon<C>(out + 24 * i, G::add(xyzz_from_jac24<C>(a + 24 * i), xyzz_from_jac24<C>(b + 24 * i)));
 }
 
 template <class C>
-cudaError_t join(Context &ctx, const uint32_t *d_a, const uint32_t *d_b, uint32_t *d_out)
+cudaError_t join(Context &ctx, const uint32_t *d_a, const uint32_t *d_b, size_t count, uint32_t *d_out)
 {
-    k_join<C><<<1, 32, 0, ctx.stream>>>(d_a, d_b, d_out);
+    if (count == 0)
+        return cudaSuccess;
+    const int threads = 64;
+    k_join<C><<<(unsigned)((count + threads - 1) / threads), threads, 0, ctx.stream>>>(d_a, d_b, count, d_out);
     HS_LAUNCH_CHECK(ctx);
     return cudaSuccess;
 }

@@ -338,6 +338,56 @@ BatchPlan make_fixed_plan(int curve, size_t n, int c, uint32_t count)
     return p;
 }
 
+BatchPlan make_indexed_plan(const Context &ctx, int curve, const size_t *sizes, uint32_t M, int c)
+{
+    BatchPlan p;
+    p.curve = curve;
+    p.M = M;
+    p.msms.resize(M);
+    const uint32_t W = (uint32_t)((257 + c - 1) / c), B = 1u << (c - 1);
+    const uint32_t m0 = std::min<uint32_t>(group_size((uint64_t)M * B), B);
+    uint32_t log2m0 = 0;
+    while ((1u << log2m0) < m0)
+        log2m0++;
+    uint64_t pt = 0;
+    for (uint32_t j = 0; j < M; j++) {
+        MsmDesc &d = p.msms[j];
+        d.pt_off = (uint32_t)pt;
+        d.n = (uint32_t)sizes[j];
+        d.c = (uint32_t)c;
+        d.W = W;
+        d.B = B;
+        d.m0 = m0;
+        d.log2m0 = log2m0;
+        d.T = B / m0;
+        d.bucket_base = j * B;
+        d.group_base = j * d.T;
+        d.win_base = j;
+        d.fixed = 2;
+        d.Wr = 1;
+        d.w_lo = 0;
+        d.w_cnt = W;
+        d.shift = 0;
+        pt += sizes[j];
+    }
+    const uint64_t ent = pt * W;
+    p.entries_pinned = pt * (uint64_t)((256 + c - 1) / c);
+    p.n_total = (uint32_t)pt;
+    p.NB = M * B;
+    p.G = M * (B / m0);
+    p.WS = M;
+    p.entries_bound = ent;
+    p.max_entries = (uint32_t)std::max<uint64_t>(1, ent);
+    p.L = seg_cap(ent, p.NB);
+    p.max_segs = (uint32_t)(std::min<uint64_t>(ent, p.NB) + ent / p.L + 1);
+    p.hist_blocks = (p.NB + SEG_HIST_THREADS - 1) / SEG_HIST_THREADS;
+    plan_chunks(p);
+    plan_sort(p);
+    const int cv = curve == HS_SELENE;
+    plan_batch_affine(p, ctx.ba_rounds[cv], ctx.ba_min_entries[cv]);
+    return p;
+}
+
 BatchPlan make_window_plan(int curve, size_t n, int c, uint32_t w_lo, uint32_t w_cnt)
 {
     BatchPlan p;
@@ -498,7 +548,8 @@ __device__ __forceinline__ uint32_t window_bits(const uint32_t s[8], int k)
 // bucket keys; scatter pass: place "index | sign" at offsets[key] + running fill.
 // Normal MSMs: window k uses buckets bucket_base + k*B + ..., entries name the
 // point (pbase = i, pstep = 0).  Fixed-base MSMs: every window uses the same B
-// buckets (wstep = 0), entries name table row (i - pt_off)*W + k (pstep = 1).
+// buckets (wstep = 0), entries name table row g*W + k (pstep = 1) of generator
+// g = i - pt_off, or g = pt_idx[i] for an indexed MSM.
 // The digits are always computed from window 0 (the carries run upward), but
 // only windows [w_lo, w_lo + w_cnt) are emitted (a window-split half).
 template <int CB, bool SCATTER>
@@ -536,10 +587,16 @@ __device__ __forceinline__ void recode_one(const uint32_t s[8], uint32_t pbase, 
 }
 
 // One thread per point of the batch; the window width is per MSM.
+// table generator of batch point i of a fixed-base MSM
+__device__ __forceinline__ uint32_t table_gen(const MsmDesc &d, const uint32_t *__restrict__ pt_idx, uint32_t i)
+{
+    return d.fixed == 2 ? __ldg(pt_idx + i) : i - d.pt_off;
+}
+
 template <bool SCATTER>
 __global__ void k_recode(const uint4 *__restrict__ scalars, uint32_t n_total, const MsmDesc *__restrict__ desc,
                          uint32_t M, uint32_t *__restrict__ counts, const uint32_t *__restrict__ offsets,
-                         uint32_t *__restrict__ sorted)
+                         uint32_t *__restrict__ sorted, const uint32_t *__restrict__ pt_idx)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_total)
@@ -547,7 +604,7 @@ __global__ void k_recode(const uint4 *__restrict__ scalars, uint32_t n_total, co
     const uint32_t m = find_msm(M, i, [&](uint32_t k) { return desc[k].pt_off; });
     const uint32_t c = desc[m].c, base = desc[m].bucket_base;
     const bool fixed = desc[m].fixed != 0;
-    const uint32_t pbase = fixed ? (i - desc[m].pt_off) * desc[m].W : i;
+    const uint32_t pbase = fixed && SCATTER ? table_gen(desc[m], pt_idx, i) * desc[m].W : i;
     const uint32_t pstep = fixed ? 1u : 0u;
     const uint32_t wstep = fixed ? 0u : desc[m].B;
     const uint32_t w_lo = desc[m].w_lo, w_cnt = desc[m].w_cnt;
@@ -758,7 +815,8 @@ __global__ void k_sort_rows(const MsmDesc *__restrict__ desc, uint32_t M, uint32
 __global__ void __launch_bounds__(SORT_THREADS) k_sort_scatter(const uint32_t *__restrict__ digits,
                                                              const MsmDesc *__restrict__ desc, uint32_t M,
                                                              const uint32_t *__restrict__ cnt,
-                                                             uint32_t *__restrict__ sorted)
+                                                             uint32_t *__restrict__ sorted,
+                                                             const uint32_t *__restrict__ pt_idx)
 {
     extern __shared__ uint32_t slot[];
     const SortBlock sb = sort_block(desc, M, blockIdx.x);
@@ -782,7 +840,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_scatter(const uint32_t *_
             if (mag) {
                 const uint32_t ii = i + u * step;
                 const uint32_t pos = atomicAdd(slot + mag - 1, 1u);
-                const uint32_t v = d.fixed ? (ii - d.pt_off) * d.W + sb.k_abs : ii;
+                const uint32_t v = d.fixed ? table_gen(d, pt_idx, ii) * d.W + sb.k_abs : ii;
                 sorted[pos] = v | (dv[u] & 0x80000000u);
             }
         }
@@ -791,7 +849,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_scatter(const uint32_t *_
         const uint32_t dv = __ldg(dg + (i - d.pt_off)), mag = dv & 0x7fffffffu;
         if (mag) {
             const uint32_t pos = atomicAdd(slot + mag - 1, 1u);
-            const uint32_t v = d.fixed ? (i - d.pt_off) * d.W + sb.k_abs : i;
+            const uint32_t v = d.fixed ? table_gen(d, pt_idx, i) * d.W + sb.k_abs : i;
             sorted[pos] = v | (dv & 0x80000000u);
         }
     }
@@ -1092,12 +1150,14 @@ cudaError_t launch_sort(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
             return e;
         k_sort_rows<1><<<tb, 256, 0, st>>>(b.desc, p.M, p.NB, b.sort_cnt, nullptr, b.offsets, 0u, nullptr);
         HS_LAUNCH_CHECK(ctx);
-        k_sort_scatter<<<p.sort_blocks, SORT_THREADS, smem, st>>>(b.digits, b.desc, p.M, b.sort_cnt, b.sorted);
+        k_sort_scatter<<<p.sort_blocks, SORT_THREADS, smem, st>>>(b.digits, b.desc, p.M, b.sort_cnt, b.sorted,
+                                                                  b.pt_idx);
         HS_LAUNCH_CHECK(ctx);
     } else {
         const unsigned rblocks = (p.n_total + 255) / 256;
         if (p.n_total) {
-            k_recode<false><<<rblocks, 256, 0, st>>>(sc, p.n_total, b.desc, p.M, b.counts, b.offsets, b.sorted);
+            k_recode<false><<<rblocks, 256, 0, st>>>(sc, p.n_total, b.desc, p.M, b.counts, b.offsets, b.sorted,
+                                                      b.pt_idx);
             HS_LAUNCH_CHECK(ctx);
         }
         if ((e = launch_scan(ctx, b.counts, p.NB, seg_L, b.offsets, b.seg_off, b.scan_tmp, nullptr, pad)) !=
@@ -1106,7 +1166,8 @@ cudaError_t launch_sort(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
         if ((e = cudaMemsetAsync(b.counts, 0, (size_t)(p.NB + 1) * 4, st)) != cudaSuccess)
             return e;
         if (p.n_total) {
-            k_recode<true><<<rblocks, 256, 0, st>>>(sc, p.n_total, b.desc, p.M, b.counts, b.offsets, b.sorted);
+            k_recode<true><<<rblocks, 256, 0, st>>>(sc, p.n_total, b.desc, p.M, b.counts, b.offsets, b.sorted,
+                                                     b.pt_idx);
             HS_LAUNCH_CHECK(ctx);
         }
     }
@@ -1362,6 +1423,27 @@ int execute_batch(Context &ctx, const BatchPlan &p, const BatchBuffers &b, void 
     return HS_OK;
 }
 
+// Two plans over the same M requests -- each request's MSM cut in two parts,
+// one per plan -- run one after the other on the context stream; then
+// out[i] = a[i] + b[i], formatted.  d_jac holds M canonical Jacobians.
+int execute_joined(Context &ctx, const BatchPlan &pa, const BatchBuffers &ba, const BatchPlan &pb,
+                   const BatchBuffers &bb, uint32_t *d_jac, void *d_out, int out_fmt)
+{
+    cudaStream_t st = ctx.stream;
+    const CurveOps &ops = curve_ops(pa.curve);
+    for (int k = 0; k < 2; k++) {
+        const BatchPlan &p = k ? pb : pa;
+        const BatchBuffers &b = k ? bb : ba;
+        HS_CU(cudaMemcpyAsync(b.desc, p.msms.data(), (size_t)p.M * sizeof(MsmDesc), cudaMemcpyHostToDevice, st),
+              "descriptor upload");
+        HS_CU(launch_sort(ctx, p, b), "MSM launch");
+        HS_CU(ops.msm_tail(ctx, p, b), "MSM launch");
+    }
+    HS_CU(ops.join(ctx, ba.out_jac, bb.out_jac, pa.M, d_jac), "join");
+    HS_CU(ops.format_out(ctx, d_jac, pa.M, out_fmt, d_out), "output format");
+    return HS_OK;
+}
+
 // ---------------------------------------------------------------------------
 // window-split MSM: the upper windows on the context stream, the lower windows
 // on a second, lower-priority stream, joined by one point addition.  The upper
@@ -1467,7 +1549,7 @@ static cudaError_t launch_split(Context &ctx, const SplitPlan &s, const BatchBuf
         return e;
     if ((e = cudaEventRecord(ctx.ev_join, b)) != cudaSuccess || (e = cudaStreamWaitEvent(a, ctx.ev_join, 0)) != cudaSuccess)
         return e;
-    if ((e = ops.join(ctx, bh.out_jac, bl.out_jac, d_final)) != cudaSuccess)
+    if ((e = ops.join(ctx, bh.out_jac, bl.out_jac, 1, d_final)) != cudaSuccess)
         return e;
     return ops.format_out(ctx, d_final, 1, out_fmt, d_out);
 }
@@ -1941,7 +2023,7 @@ static int msm_host(Context &ctx, int curve, const uint8_t *lead_scalar, const v
             if ((e = cudaEventRecord(ctx.ev_join, s2)) != cudaSuccess || (e = ops.msm_tail(ctx, s.lo, l)) != cudaSuccess ||
                 (e = cudaStreamWaitEvent(st, ctx.ev_join, 0)) != cudaSuccess)
                 return e;
-            if ((e = ops.join(ctx, h.out_jac, l.out_jac, d_final)) != cudaSuccess)
+            if ((e = ops.join(ctx, h.out_jac, l.out_jac, 1, d_final)) != cudaSuccess)
                 return e;
             return ops.format_out(ctx, d_final, 1, out_fmt, d_out);
         }

@@ -7,8 +7,13 @@
 // event fired, copying results out and waking waiters; (2) while a slot is
 // free and requests are queued, takes the oldest request's curve, collects up
 // to the caps of queued requests of that curve (FIFO), checks the batch's
-// workspace against the HBM budget, stages scalars / fresh bases, gathers pool
-// bases on the device, and launches the batched MSM pipeline on that slot.
+// workspace against the HBM budget, stages scalars / fresh bases, and launches
+// the batched MSM pipeline on that slot.  A curve's resident pool is kept as
+// a table of window multiples 2^(c k) P_i (built once by hs_server_set_pool):
+// the pooled part of every request is then a fixed-base MSM over table rows
+// named by its indices (one reduced window, no Horner chain), the fresh part a
+// variable-base MSM, and the two are added per request.  With the table off
+// (window 0) the pooled bases are gathered into the batch instead.
 // All waits are host-side and bounded.
 #include <cuda_runtime.h>
 
@@ -73,10 +78,20 @@ struct Slot {
 };
 
 struct Pool {
-    uint4 *d = nullptr;
+    uint4 *d = nullptr;      // affine bases (pools without a table)
+    uint4 *table = nullptr;  // n * W window multiples, affine: row i*W + k = 2^(c k) P_i
+    int c = 0;
+    uint32_t W = 0;
     size_t n = 0;
     uint64_t gen = 0;  // bumped by every replacement
+    int window = -1;   // for the next replacement: table width, 0 = no table, -1 = POOL_WINDOW_AUTO
 };
+
+// width of a pool's window-multiple table unless set: for pooled parts of a
+// few hundred to a few hundred thousand bases, c = 12 (22 rows per base) takes
+// fewer (point, window) entries than the variable-base windows of parts up to
+// ~2^17 bases and reduces 2048 buckets per request
+constexpr int POOL_WINDOW_AUTO = 12;
 
 struct Server {
     hs_server_config cfg{};
@@ -94,6 +109,22 @@ struct Server {
     std::string last_error;
 };
 
+// (point, window) entries of a request under the slots' window rules and the
+// curve's pool table
+static uint64_t request_entries(const Server &S, const hs_request &q)
+{
+    const Context &ctx = S.slots[0]->ctx;
+    const Pool &p = S.pools[q.curve];
+    const size_t n = q.n_pool + q.n_fresh;
+    const int c = choose_window(ctx, q.curve, n ? n : 1);
+    uint64_t e = (uint64_t)n * (uint64_t)((257 + c - 1) / c);
+    if (p.table && q.n_pool) {
+        const int cf = choose_window(ctx, q.curve, q.n_fresh ? q.n_fresh : 1);
+        e = std::max<uint64_t>(e, (uint64_t)q.n_pool * p.W + (uint64_t)q.n_fresh * ((257 + cf - 1) / cf));
+    }
+    return e;
+}
+
 static size_t batch_stage_bytes(size_t total, size_t total_pool, size_t msms, size_t ob)
 {
     return align256(std::max<size_t>(1, total) * 32) + align256(std::max<size_t>(1, total) * 64) +
@@ -101,9 +132,148 @@ static size_t batch_stage_bytes(size_t total, size_t total_pool, size_t msms, si
            align256(std::max<size_t>(1, msms) * ob);
 }
 
+static void finish_launch(Server &S, Slot &s, std::vector<uint64_t> &batch, int curve, size_t bytes)
+{
+    s.busy = true;
+    s.curve = curve;
+    s.bytes = bytes;
+    s.tickets = batch;
+    S.in_flight += bytes;
+    S.stats.peak_bytes = std::max<uint64_t>(S.stats.peak_bytes, S.in_flight);
+    S.stats.batches++;
+    S.stats.max_batch_msms = std::max<uint64_t>(S.stats.max_batch_msms, batch.size());
+}
+
+static bool fail_requests(Server &S, Slot &s, const std::vector<uint64_t> &batch, int code)
+{
+    for (uint64_t t : batch) {
+        ReqState &r = S.reqs[t];
+        r.status = code;
+        S.stats.failed++;
+    }
+    S.last_error = s.ctx.last_error;
+    S.cv_done.notify_all();
+    return true;
+}
+
+static bool ensure_pinned_out(Slot &s, size_t bytes)
+{
+    if (s.pinned_cap >= bytes)
+        return true;
+    if (s.pinned_out)
+        cudaFreeHost(s.pinned_out);
+    s.pinned_cap = std::max<size_t>(bytes, 1024 * 120);
+    if (cudaMallocHost((void **)&s.pinned_out, s.pinned_cap) != cudaSuccess) {
+        s.pinned_out = nullptr;
+        s.pinned_cap = 0;
+        cudaGetLastError();
+        return false;
+    }
+    return true;
+}
+
+// A batch over a curve with a pool table: the fresh parts as one variable-base
+// batch plan, the pooled parts as one plan over the table's rows, added per
+// request.  Called with the server lock held; false = deferred (budget).
+static bool launch_with_table(Server &S, Slot &s, std::vector<uint64_t> &batch, int curve)
+{
+    const Pool &pool = S.pools[curve];
+    const size_t ob = fmt_bytes(S.cfg.out_fmt);
+    const uint32_t M = (uint32_t)batch.size();
+    std::vector<size_t> fresh(M), pooled(M);
+    size_t tf = 0, tp = 0;
+    for (uint32_t j = 0; j < M; j++) {
+        const hs_request &q = S.reqs[batch[j]].req;
+        fresh[j] = q.n_fresh;
+        pooled[j] = q.n_pool;
+        tf += q.n_fresh;
+        tp += q.n_pool;
+    }
+    Context &ctx = s.ctx;
+    const BatchPlan pv = make_batch_plan(ctx, curve, fresh.data(), M);
+    const BatchPlan pp = make_indexed_plan(ctx, curve, pooled.data(), M, pool.c);
+    if (pv.entries_bound > BATCH_ENTRIES_MAX || pp.entries_bound > BATCH_ENTRIES_MAX)  // rules changed since submission
+        return fail_requests(S, s, batch, HS_ERANGE);
+    // staging: fresh scalars and bases, pooled scalars and indices, M joined
+    // Jacobians, M results
+    const size_t st_bytes = align256(std::max<size_t>(1, tf) * 32) + align256(std::max<size_t>(1, tf) * 64) +
+                            align256(std::max<size_t>(1, tp) * 32) + align256(std::max<size_t>(1, tp) * 4) +
+                            align256((size_t)M * 96) + align256((size_t)M * ob);
+    const size_t bytes = batch_bytes(pv) + batch_bytes(pp) + st_bytes + 4096;
+    if (S.in_flight > 0 && S.in_flight + bytes > S.cfg.hbm_budget) {
+        S.stats.deferred++;
+        return false;
+    }
+    BatchBuffers bv, bp;
+    if (ctx.arena.reserve(bytes) != cudaSuccess) {
+        cudaGetLastError();
+        ctx.last_error = "workspace allocation";
+        return fail_requests(S, s, batch, HS_ENOMEM);
+    }
+    uint8_t *d_fsc = nullptr, *d_fpts = nullptr, *d_psc = nullptr, *d_out = nullptr;
+    uint32_t *d_idx = nullptr, *d_jac = nullptr;
+    if (!carve(ctx.arena, pv, bv) || !carve(ctx.arena, pp, bp) ||
+        !(d_fsc = (uint8_t *)ctx.arena.take(std::max<size_t>(1, tf) * 32)) ||
+        !(d_fpts = (uint8_t *)ctx.arena.take(std::max<size_t>(1, tf) * 64)) ||
+        !(d_psc = (uint8_t *)ctx.arena.take(std::max<size_t>(1, tp) * 32)) ||
+        !(d_idx = (uint32_t *)ctx.arena.take(std::max<size_t>(1, tp) * 4)) ||
+        !(d_jac = (uint32_t *)ctx.arena.take((size_t)M * 96)) || !(d_out = (uint8_t *)ctx.arena.take((size_t)M * ob))) {
+        ctx.last_error = "workspace carve";
+        return fail_requests(S, s, batch, HS_ENOMEM);
+    }
+    if (!ensure_pinned_out(s, (size_t)M * ob))
+        return fail_requests(S, s, batch, HS_ENOMEM);
+    cudaStream_t st = ctx.stream;
+    cudaError_t e = cudaSuccess;
+    size_t fo = 0, po = 0;
+    for (uint64_t t : batch) {
+        const hs_request &q = S.reqs[t].req;
+        if (q.n_pool && e == cudaSuccess)
+            e = cudaMemcpyAsync(d_psc + 32 * po, q.scalars, 32 * q.n_pool, cudaMemcpyHostToDevice, st);
+        if (q.n_pool && e == cudaSuccess)
+            e = cudaMemcpyAsync(d_idx + po, q.pool_idx, 4 * q.n_pool, cudaMemcpyHostToDevice, st);
+        if (q.n_fresh && e == cudaSuccess)
+            e = cudaMemcpyAsync(d_fsc + 32 * fo, q.scalars + 32 * q.n_pool, 32 * q.n_fresh, cudaMemcpyHostToDevice, st);
+        if (q.n_fresh && e == cudaSuccess)
+            e = cudaMemcpyAsync(d_fpts + 64 * fo, q.fresh_points, 64 * q.n_fresh, cudaMemcpyHostToDevice, st);
+        fo += q.n_fresh;
+        po += q.n_pool;
+    }
+    if (e != cudaSuccess) {
+        ctx.last_error = std::string("staging: ") + cudaGetErrorString(e);
+        return fail_requests(S, s, batch, HS_ECUDA);
+    }
+    bv.scalars = (const uint32_t *)d_fsc;
+    bv.points = (const uint4 *)d_fpts;
+    bp.scalars = (const uint32_t *)d_psc;
+    bp.points = pool.table;
+    bp.pt_idx = d_idx;
+    // a batch of pooled parts only runs the table plan alone
+    const int rc = tf ? execute_joined(ctx, pv, bv, pp, bp, d_jac, d_out, S.cfg.out_fmt)
+                      : execute_batch(ctx, pp, bp, d_out, S.cfg.out_fmt);
+    if (rc != HS_OK)
+        return fail_requests(S, s, batch, HS_ECUDA);
+    e = cudaMemcpyAsync(s.pinned_out, d_out, (size_t)M * ob, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+        e = cudaEventRecord(s.done, st);
+    if (e != cudaSuccess) {
+        ctx.last_error = std::string("result copy: ") + cudaGetErrorString(e);
+        return fail_requests(S, s, batch, HS_ECUDA);
+    }
+    finish_launch(S, s, batch, curve, bytes);
+    return true;
+}
+
 // launch one batch on slot s; called with the server lock held; false = deferred (budget)
 static bool launch(Server &S, Slot &s, std::vector<uint64_t> &batch, int curve)
 {
+    if (S.pools[curve].table) {
+        bool pooled = false;
+        for (uint64_t t : batch)
+            pooled = pooled || S.reqs[t].req.n_pool;
+        if (pooled)
+            return launch_with_table(S, s, batch, curve);
+    }
     const size_t ob = fmt_bytes(S.cfg.out_fmt);
     std::vector<size_t> sizes;
     size_t total = 0, total_pool = 0;
@@ -129,16 +299,7 @@ static bool launch(Server &S, Slot &s, std::vector<uint64_t> &batch, int curve)
         S.stats.deferred++;
         return false;
     }
-    auto fail_batch = [&](int code) {
-        for (uint64_t t : batch) {
-            ReqState &r = S.reqs[t];
-            r.status = code;
-            S.stats.failed++;
-        }
-        S.last_error = ctx.last_error;
-        S.cv_done.notify_all();
-        return true;
-    };
+    auto fail_batch = [&](int code) { return fail_requests(S, s, batch, code); };
     BatchBuffers b;
     void *ext = nullptr;
     if (reserve_batch(ctx, p, extra, b, &ext) != HS_OK)
@@ -148,17 +309,8 @@ static bool launch(Server &S, Slot &s, std::vector<uint64_t> &batch, int curve)
     uint32_t *d_src = (uint32_t *)(d_pts + align256(std::max<size_t>(1, total) * 64));
     uint4 *d_seg = (uint4 *)((uint8_t *)d_src + align256(std::max<size_t>(1, total_pool) * 4));
     uint8_t *d_out = (uint8_t *)d_seg + align256(std::max<size_t>(1, batch.size()) * 16);
-    if (s.pinned_cap < batch.size() * ob) {
-        if (s.pinned_out)
-            cudaFreeHost(s.pinned_out);
-        s.pinned_cap = std::max<size_t>(batch.size() * ob, 1024 * 120);
-        if (cudaMallocHost((void **)&s.pinned_out, s.pinned_cap) != cudaSuccess) {
-            s.pinned_out = nullptr;
-            s.pinned_cap = 0;
-            cudaGetLastError();
-            return fail_batch(HS_ENOMEM);
-        }
-    }
+    if (!ensure_pinned_out(s, batch.size() * ob))
+        return fail_batch(HS_ENOMEM);
     cudaStream_t st = ctx.stream;
     // per request: its scalars, fresh bases and pool indices copied straight from
     // the caller's buffers, plus one table row; the pooled bases are gathered on
@@ -204,14 +356,7 @@ static bool launch(Server &S, Slot &s, std::vector<uint64_t> &batch, int curve)
         ctx.last_error = std::string("result copy: ") + cudaGetErrorString(e);
         return fail_batch(HS_ECUDA);
     }
-    s.busy = true;
-    s.curve = curve;
-    s.bytes = bytes;
-    s.tickets = batch;
-    S.in_flight += bytes;
-    S.stats.peak_bytes = std::max<uint64_t>(S.stats.peak_bytes, S.in_flight);
-    S.stats.batches++;
-    S.stats.max_batch_msms = std::max<uint64_t>(S.stats.max_batch_msms, batch.size());
+    finish_launch(S, s, batch, curve, bytes);
     return true;
 }
 
@@ -407,8 +552,12 @@ int hs_server_set_pool(hs_server *h, int curve, const void *pts, size_t n)
     Pool &p = S.pools[curve];
     if (p.d)
         cudaFree(p.d);
-    p.d = nullptr;
+    if (p.table)
+        cudaFree(p.table);
+    p.d = p.table = nullptr;
     p.n = 0;
+    p.c = 0;
+    p.W = 0;
     p.gen++;
     if (!n)
         return HS_OK;
@@ -421,7 +570,50 @@ int hs_server_set_pool(hs_server *h, int curve, const void *pts, size_t n)
         cudaGetLastError();
         return HS_ECUDA;
     }
+    const int c = p.window < 0 ? POOL_WINDOW_AUTO : p.window;
+    if (c) {
+        // the table of window multiples, built with the first slot's context
+        // (idle: pools are replaced only while nothing is queued or in flight)
+        const uint32_t W = (uint32_t)((257 + c - 1) / c);
+        const size_t m = n * W;
+        if (m >= 0x80000000ull)
+            return HS_ERANGE;
+        Context &ctx = S.slots[0]->ctx;
+        if (cudaMalloc((void **)&p.table, m * 64) != cudaSuccess) {
+            cudaGetLastError();
+            p.table = nullptr;
+            return HS_ENOMEM;
+        }
+        cudaError_t e = ctx.arena.reserve(align256(m * 160) + 1024);
+        uint4 *d_tmp = e == cudaSuccess ? (uint4 *)ctx.arena.take(m * 160) : nullptr;
+        if (e == cudaSuccess && !d_tmp)
+            e = cudaErrorMemoryAllocation;
+        if (e == cudaSuccess)
+            e = curve_ops(curve).fixed_table(ctx, p.d, n, c, (int)W, d_tmp, p.table);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(ctx.stream);
+        ctx.arena.release();  // the build's scratch is not kept as the slot's workspace
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            cudaFree(p.table);
+            p.table = nullptr;
+            S.last_error = std::string("pool table: ") + cudaGetErrorString(e);
+            return e == cudaErrorMemoryAllocation ? HS_ENOMEM : HS_ECUDA;
+        }
+        p.c = c;
+        p.W = W;
+    }
     p.n = n;
+    return HS_OK;
+}
+
+int hs_server_set_pool_window(hs_server *h, int curve, int window)
+{
+    if (!h || (curve != HS_HELIOS && curve != HS_SELENE) || (window != 0 && (window < 4 || window > 16)))
+        return HS_EINVAL;
+    Server &S = h->s;
+    std::lock_guard<std::mutex> lk(S.mu);
+    S.pools[curve].window = window;
     return HS_OK;
 }
 
@@ -471,8 +663,7 @@ int hs_server_submit(hs_server *h, const hs_request *req, uint64_t *ticket)
         if (S.pools[req->curve].gen == gen)
             break;
     }
-    const int c = choose_window(S.slots[0]->ctx, req->curve, n);
-    const uint64_t entries = (uint64_t)n * (uint64_t)((257 + c - 1) / c);
+    const uint64_t entries = request_entries(S, *req);
     if (entries > BATCH_ENTRIES_MAX)
         return HS_ERANGE;
     const uint64_t t = S.next_ticket++;
@@ -545,9 +736,12 @@ void hs_server_destroy(hs_server *h)
             if (s.pinned_out)
                 cudaFreeHost(s.pinned_out);
         }
-        for (Pool &p : S.pools)
+        for (Pool &p : S.pools) {
             if (p.d)
                 cudaFree(p.d);
+            if (p.table)
+                cudaFree(p.table);
+        }
     }
     delete h;
 }

@@ -283,8 +283,19 @@ typedef struct hs_server_stats {
 } hs_server_stats;
 
 int hs_server_create(hs_server **srv, const hs_server_config *cfg);
-/* upload (replace) the resident base pool of one curve: n HS_FMT_AFFINE points */
+/* upload (replace) the resident base pool of one curve: n HS_FMT_AFFINE points.
+ * Unless the curve's pool window is 0, the pool is also expanded once into a
+ * resident table of window multiples 2^(c k) P_i (n * ceil(257/c) affine
+ * points, 64 bytes each; a scratch of 160 bytes per table point while it is
+ * built): the pooled bases of every request then form a fixed-base MSM over
+ * that table (one reduced window, no doubling chain), added to the
+ * variable-base MSM of its fresh bases.  Only while nothing is queued or in
+ * flight (HS_EBUSY otherwise). */
 int hs_server_set_pool(hs_server *srv, int curve, const void *affine_points, size_t n);
+/* window width c of the curve's pool table from the next hs_server_set_pool:
+ * 4..16, or 0 for no table (pooled bases are gathered into each batch as
+ * variable bases).  The default is 12. */
+int hs_server_set_pool_window(hs_server *srv, int curve, int window);
 /* window rule for the batches of every slot, as hs_context_set_window (window 0
  * clears the curve's rules); applies to batches planned after the call */
 int hs_server_set_window(hs_server *srv, int curve, size_t n_min, size_t n_max, int window);

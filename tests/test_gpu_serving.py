@@ -119,3 +119,51 @@ def test_bad_requests_are_refused(pools):
         assert e.value.status == -6
         t = srv.submit(0, sc, np.array([0, 1, 2, 3], np.uint32))
         assert srv.wait(t)[0] == bytes(32)  # zero scalars -> identity
+
+
+@pytest.mark.parametrize("window", [0, 6, 12, 16])
+def test_pool_table_widths_and_part_shapes(pools, window):
+    """the pool as a table of window multiples (pooled parts as fixed-base MSMs
+    over indexed rows, added to the fresh parts), or gathered (window 0): every
+    request shape -- pooled only, fresh only, both, empty, repeated and
+    identity-cancelling indices -- matches the oracle"""
+    import helioselene_gb300 as hs
+    from helioselene_gb300.workload import ORDER, random_scalars
+    rng = np.random.default_rng(40 + window)
+    reqs = make_requests(rng, pools, 30, 4096)
+    for curve in (0, 1):
+        for n_pool, n_fresh in ((700, 0), (0, 300), (0, 0), (1, 0), (5000, 20)):
+            idx = rng.integers(0, 4096, n_pool).astype(np.uint32)
+            if n_pool >= 700:
+                idx[: n_pool // 4] = 17  # one pool point many times: doubling and cancelling cases
+            _, fresh, _ = oracle_inputs(curve, max(1, n_fresh), seed=90 + n_fresh)
+            fresh = fresh[:n_fresh]
+            scal = random_scalars(rng, n_pool + n_fresh, ORDER[curve])
+            if n_pool >= 700:
+                # s and order - s on the same pool point cancel
+                s0 = int.from_bytes(scal[0].tobytes(), "little")
+                scal[1] = np.frombuffer((ORDER[curve] - s0).to_bytes(32, "little"), np.uint8)
+                idx[1] = idx[0]
+            pts = np.concatenate([pools[curve][idx], fresh]) if n_pool + n_fresh else np.zeros((0, 64), np.uint8)
+            reqs.append({"curve": curve, "scalars": scal, "idx": idx, "fresh": fresh,
+                         "want": oracle.msm(curve, scal, pts)})
+    with hs.Server(0, slots=3) as srv:
+        for c in (0, 1):
+            srv.set_pool_window(c, window)
+            srv.set_pool(c, pools[c])
+        tickets = [srv.submit(r["curve"], r["scalars"], r["idx"], r["fresh"]) for r in reqs]
+        got = [srv.wait(t)[0] for t in tickets]
+        alone = [srv.wait(srv.submit(r["curve"], r["scalars"], r["idx"], r["fresh"]))[0] for r in reqs[-10:]]
+        st = srv.stats()
+    bad = [i for i, (g, r) in enumerate(zip(got, reqs)) if g != r["want"]]
+    assert not bad, f"mismatches {bad[:8]}"
+    assert alone == got[-10:]
+    assert st["failed"] == 0
+
+
+def test_pool_window_refused_outside_range(pools):
+    import helioselene_gb300 as hs
+    with hs.Server(0, slots=1) as srv:
+        for bad in ((2, 12), (0, 3), (0, 17), (1, -1)):
+            with pytest.raises(hs.HsError):
+                srv.set_pool_window(*bad)
