@@ -313,8 +313,10 @@ def run_serving(hs, torch, device: str, local: int, requests_per_rate: int = 100
     against the plain path: the same requests one MSM per launch sequence, one
     at a time (a server with one slot and one request per batch, the pooled
     bases gathered as variable bases, as a per-call MSM would take them).  The
-    batching server keeps each pool as a table of window multiples; at
-    saturation it is also timed with the pool gathered instead (window 0)."""
+    batching server also keeps each pool as a table of window multiples, which
+    requests with pooled bases only run over: a second stream of such requests
+    (same sizes, no fresh bases) is timed on it, on a server without tables
+    (window 0) and on the plain arm."""
     from helioselene_gb300.workload import ORDER, random_field_bytes, random_scalars, serving_sizes
     rng = np.random.default_rng(SEED + 4)
     pool_n = 1 << 18
@@ -339,13 +341,13 @@ def run_serving(hs, torch, device: str, local: int, requests_per_rate: int = 100
     perm = torch.empty(2 * res_n * 4, dtype=torch.uint8, pin_memory=True)
     perm.numpy().view(np.uint32)[:] = rng.integers(0, pool_n, 2 * res_n).astype(np.uint32)
 
-    def draw(count):
+    def draw(count, pool_share=0.75):
         n = serving_sizes(rng, count)
         reqs = []
         for i in range(count):
             curve = i % 2
             k = int(n[i])
-            npool = (3 * k) // 4
+            npool = int(k * pool_share)
             nfresh = k - npool
             so = int(rng.integers(0, 2 * res_n - k))
             fo = int(rng.integers(0, res_n - nfresh + 1))
@@ -386,7 +388,7 @@ def run_serving(hs, torch, device: str, local: int, requests_per_rate: int = 100
            "plain": "the same requests at the same arrival times, one MSM per launch sequence, one at a time",
            "rates": []}
     srv = hs.Server(local, slots=8, max_batch_points=1 << 23, max_batch_msms=1024)
-    gathered = hs.Server(local, slots=8, max_batch_points=1 << 23, max_batch_msms=1024)
+    gathered = hs.Server(local, slots=8, max_batch_points=1 << 23, max_batch_msms=1024)  # no pool tables
     plain = hs.Server(local, slots=1, max_batch_msms=1)
     for s in (srv, gathered, plain):
         for c in (hs.HELIOS, hs.SELENE):
@@ -394,6 +396,9 @@ def run_serving(hs, torch, device: str, local: int, requests_per_rate: int = 100
                 s.set_pool_window(c, 0)
             s.set_pool(c, pools[c])
     warm = draw(64)
+    run(srv, warm, 0)
+    run(plain, warm[:16], 0)
+    warm = draw(64, pool_share=1.0)
     run(srv, warm, 0)
     run(gathered, warm, 0)
     run(plain, warm[:16], 0)
@@ -408,11 +413,31 @@ def run_serving(hs, torch, device: str, local: int, requests_per_rate: int = 100
         out["rates"].append({"serving": a, "plain": bsec})
         if rate == 0:
             checked = (reqs, res_srv)
-            res_g = []
-            g = run(gathered, reqs, rate, arrivals, res_g)
-            out["pool_table"] = {"window": 12, "table_msms_per_s": a["msms_per_s"],
-                                 "gathered_msms_per_s": g["msms_per_s"], "gathered_p50_ms": g["p50_ms"],
-                                 "gathered_p99_ms": g["p99_ms"], "same_results": res_g == res_srv}
+    # requests with pooled bases only: over the pool tables, gathered, plain
+    out["pool_only"] = {"mix": "the same size mixture, every base from the pool", "table_window": 12, "rates": []}
+    for rate in (9000, 0):
+        reqs = draw(requests_per_rate, pool_share=1.0)
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, len(reqs))) if rate else np.zeros(len(reqs))
+        res_t, res_g, res_p = [], [], []
+        t = run(srv, reqs, rate, arrivals, res_t)
+        g = run(gathered, reqs, rate, arrivals, res_g)
+        pl = run(plain, reqs, rate, arrivals, res_p)
+        t["same_as_plain"] = res_t == res_p
+        g["same_as_plain"] = res_g == res_p
+        out["pool_only"]["rates"].append({"table": t, "gathered": g, "plain": pl})
+        if rate == 0 and with_oracle:
+            sys.path.insert(0, str(ROOT / "oracle"))
+            import oracle
+            sample = list(range(0, len(reqs), max(1, len(reqs) // 32)))
+            ok = True
+            for curve in (hs.HELIOS, hs.SELENE):
+                sel = [i for i in sample if reqs[i][0] == curve]
+                sc = np.concatenate([views(reqs[i])[1].reshape(-1, 32) for i in sel])
+                pts = np.concatenate([pools[curve][views(reqs[i])[2]] for i in sel])
+                want = oracle.msm_many(curve, sc, pts, [reqs[i][2] for i in sel])
+                ok = ok and all(res_t[i] == want[j] for j, i in enumerate(sel))
+            out["pool_only"]["bit_exact_vs_oracle"] = ok
+            out["pool_only"]["oracle_check"] = f"{len(sample)} of the {len(reqs)} all-at-once requests
     # a sample of the all-at-once requests against the oracle (pooled + fresh bases)
     if with_oracle and checked:
         sys.path.insert(0, str(ROOT / "oracle"))
@@ -1080,7 +1105,8 @@ def run_ours(args) -> None:
         serving = run_serving(hs, torch, device, local, with_oracle=not args.no_cpu)
     fixed = None
     if not args.no_fixed:
-        fixed = run_fixed(hs, torch, device, local, with_oracle=not args.no_cpu, ba_rounds=rr)
+        fixed = run_fixed(hs, torch, device, local, with_oracle=not args.no_cpu,
+                          ba_rounds=rr if args.ba_rounds is not None else None)
     smul = None
     if not args.no_scalar_mul:
         smul = run_scalar_mul(hs, torch, ctxs, data, n, flush)

@@ -316,7 +316,8 @@ class Server:
 
     def set_pool(self, curve: int, affine_points) -> None:
         """resident base pool of one curve (and, unless its pool window is 0,
-        the table of window multiples its pooled requests are computed from)"""
+        the table of window multiples that requests with pooled bases only are
+        computed from)"""
         p = _u8(affine_points)
         rc = self._lib.hs_server_set_pool(self._h, curve, _ptr(p), p.size // 64)
         if rc != L.HS_OK:

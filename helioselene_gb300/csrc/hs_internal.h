@@ -73,6 +73,13 @@ struct Context {
     // multiply-bound work.
     uint32_t ba_rounds[2] = {1, 1};
     uint64_t ba_min_entries[2] = {uint64_t(1) << 21, uint64_t(1) << 21};
+    // Fixed-base commitments run one curve at a time, where the round pays on
+    // Selene only (4096 commitments over 2^20 generators on GB300: Helios 617
+    // commitments/s without it, 568 with; Selene 397 without, 427 with), so
+    // until hs_context_set_batch_affine sets a curve, its fixed-base plans
+    // take these rounds.
+    bool ba_set[2] = {false, false};
+    uint32_t fixed_ba_rounds[2] = {0, 1};
     std::vector<GraphEntry> graphs;
     DeviceArena arena;
     std::mutex mu;
@@ -250,10 +257,6 @@ bool carve(DeviceArena &a, const BatchPlan &p, BatchBuffers &b);
 
 // curve-independent launches (hs_runtime.cu): descriptor upload, recode, sort, segments
 cudaError_t launch_sort(Context &ctx, const BatchPlan &p, const BatchBuffers &b);
-// two plans over the same M requests (a request's MSM cut in two parts), their
-// results added per request into d_jac (M canonical Jacobians) and formatted
-int execute_joined(Context &ctx, const BatchPlan &pa, const BatchBuffers &ba, const BatchPlan &pb,
-                   const BatchBuffers &bb, uint32_t *d_jac, void *d_out, int out_fmt);
 
 // per-curve entry points (hs_curve_helios.cu / hs_curve_selene.cu)
 struct CurveOps {

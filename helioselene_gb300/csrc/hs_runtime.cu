@@ -1423,27 +1423,6 @@ int execute_batch(Context &ctx, const BatchPlan &p, const BatchBuffers &b, void 
     return HS_OK;
 }
 
-// Two plans over the same M requests -- each request's MSM cut in two parts,
-// one per plan -- run one after the other on the context stream; then
-// out[i] = a[i] + b[i], formatted.  d_jac holds M canonical Jacobians.
-int execute_joined(Context &ctx, const BatchPlan &pa, const BatchBuffers &ba, const BatchPlan &pb,
-                   const BatchBuffers &bb, uint32_t *d_jac, void *d_out, int out_fmt)
-{
-    cudaStream_t st = ctx.stream;
-    const CurveOps &ops = curve_ops(pa.curve);
-    for (int k = 0; k < 2; k++) {
-        const BatchPlan &p = k ? pb : pa;
-        const BatchBuffers &b = k ? bb : ba;
-        HS_CU(cudaMemcpyAsync(b.desc, p.msms.data(), (size_t)p.M * sizeof(MsmDesc), cudaMemcpyHostToDevice, st),
-              "descriptor upload");
-        HS_CU(launch_sort(ctx, p, b), "MSM launch");
-        HS_CU(ops.msm_tail(ctx, p, b), "MSM launch");
-    }
-    HS_CU(ops.join(ctx, ba.out_jac, bb.out_jac, pa.M, d_jac), "join");
-    HS_CU(ops.format_out(ctx, d_jac, pa.M, out_fmt, d_out), "output format");
-    return HS_OK;
-}
-
 // ---------------------------------------------------------------------------
 // window-split MSM: the upper windows on the context stream, the lower windows
 // on a second, lower-priority stream, joined by one point addition.  The upper
@@ -1819,6 +1798,7 @@ int hs_context_set_batch_affine(hs_context *h, int curve, int rounds, size_t min
     drop_graphs(ctx);
     ctx.ba_rounds[curve == HS_SELENE] = (uint32_t)rounds;
     ctx.ba_min_entries[curve == HS_SELENE] = min_entries;
+    ctx.ba_set[curve == HS_SELENE] = true;
     return HS_OK;
 }
 
@@ -2779,7 +2759,7 @@ static BatchPlan fixed_plan(const Context &ctx, const hs_fixed_base *fb, uint32_
 {
     BatchPlan p = make_fixed_plan(fb->curve, fb->n_gen, fb->c, count);
     const int k = fb->curve == HS_SELENE ? 1 : 0;
-    plan_batch_affine(p, ctx.ba_rounds[k], ctx.ba_min_entries[k]);
+    plan_batch_affine(p, ctx.ba_set[k] ? ctx.ba_rounds[k] : ctx.fixed_ba_rounds[k], ctx.ba_min_entries[k]);
     return p;
 }
 

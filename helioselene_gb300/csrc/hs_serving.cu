@@ -8,12 +8,13 @@
 // free and requests are queued, takes the oldest request's curve, collects up
 // to the caps of queued requests of that curve (FIFO), checks the batch's
 // workspace against the HBM budget, stages scalars / fresh bases, and launches
-// the batched MSM pipeline on that slot.  A curve's resident pool is kept as
-// a table of window multiples 2^(c k) P_i (built once by hs_server_set_pool):
-// the pooled part of every request is then a fixed-base MSM over table rows
-// named by its indices (one reduced window, no Horner chain), the fresh part a
-// variable-base MSM, and the two are added per request.  With the table off
-// (window 0) the pooled bases are gathered into the batch instead.
+// the batched MSM pipeline on that slot.  A curve's resident pool is also kept
+// as a table of window multiples 2^(c k) P_i (built once by
+// hs_server_set_pool): a request whose bases all come from the pool is a
+// fixed-base MSM over the table rows its indices name (one reduced window, no
+// Horner chain), batched with other such requests.  A request with fresh bases
+// is a variable-base MSM whose pooled bases are gathered into its batch on the
+// device.  A batch holds one curve and one of the two forms.
 // All waits are host-side and bounded.
 #include <cuda_runtime.h>
 
@@ -59,6 +60,7 @@ constexpr uint64_t BATCH_ENTRIES_MAX = 0x7fffffffull;
 struct ReqState {
     hs_request req;
     size_t n = 0;
+    bool table = false;    // pooled bases only, computed over the pool's window table
     uint64_t entries = 0;  // n x windows under the slots' window rules at submission
     Clock::time_point submitted;
     double latency_ms = 0.0;
@@ -87,10 +89,10 @@ struct Pool {
     int window = -1;   // for the next replacement: table width, 0 = no table, -1 = POOL_WINDOW_AUTO
 };
 
-// width of a pool's window-multiple table unless set: for pooled parts of a
-// few hundred to a few hundred thousand bases, c = 12 (22 rows per base) takes
-// fewer (point, window) entries than the variable-base windows of parts up to
-// ~2^17 bases and reduces 2048 buckets per request
+// width of a pool's window-multiple table unless set: for requests of a few
+// hundred to a few hundred thousand pooled bases, c = 12 (22 rows per base)
+// takes fewer (point, window) entries than the variable-base windows of
+// requests up to ~2^17 bases and reduces 2048 buckets per request
 constexpr int POOL_WINDOW_AUTO = 12;
 
 struct Server {
@@ -109,20 +111,21 @@ struct Server {
     std::string last_error;
 };
 
-// (point, window) entries of a request under the slots' window rules and the
-// curve's pool table
+// whether a request runs over its curve's pool table
+static bool table_form(const Server &S, const hs_request &q)
+{
+    return S.pools[q.curve].table && q.n_pool && !q.n_fresh;
+}
+
+// (point, window) entries of a request under the slots' window rules, or the
+// pool table's windows
 static uint64_t request_entries(const Server &S, const hs_request &q)
 {
-    const Context &ctx = S.slots[0]->ctx;
-    const Pool &p = S.pools[q.curve];
     const size_t n = q.n_pool + q.n_fresh;
-    const int c = choose_window(ctx, q.curve, n ? n : 1);
-    uint64_t e = (uint64_t)n * (uint64_t)((257 + c - 1) / c);
-    if (p.table && q.n_pool) {
-        const int cf = choose_window(ctx, q.curve, q.n_fresh ? q.n_fresh : 1);
-        e = std::max<uint64_t>(e, (uint64_t)q.n_pool * p.W + (uint64_t)q.n_fresh * ((257 + cf - 1) / cf));
-    }
-    return e;
+    if (table_form(S, q))
+        return (uint64_t)n * S.pools[q.curve].W;
+    const int c = choose_window(S.slots[0]->ctx, q.curve, n ? n : 1);
+    return (uint64_t)n * (uint64_t)((257 + c - 1) / c);
 }
 
 static size_t batch_stage_bytes(size_t total, size_t total_pool, size_t msms, size_t ob)
@@ -172,86 +175,60 @@ static bool ensure_pinned_out(Slot &s, size_t bytes)
     return true;
 }
 
-// A batch over a curve with a pool table: the fresh parts as one variable-base
-// batch plan, the pooled parts as one plan over the table's rows, added per
-// request.  Called with the server lock held; false = deferred (budget).
-static bool launch_with_table(Server &S, Slot &s, std::vector<uint64_t> &batch, int curve)
+// A batch of pool-only requests: fixed-base MSMs over the rows of the curve's
+// pool table that their indices name.  Called with the server lock held;
+// false = deferred (budget).
+static bool launch_table(Server &S, Slot &s, std::vector<uint64_t> &batch, int curve)
 {
     const Pool &pool = S.pools[curve];
     const size_t ob = fmt_bytes(S.cfg.out_fmt);
     const uint32_t M = (uint32_t)batch.size();
-    std::vector<size_t> fresh(M), pooled(M);
-    size_t tf = 0, tp = 0;
+    std::vector<size_t> sizes(M);
+    size_t tp = 0;
     for (uint32_t j = 0; j < M; j++) {
-        const hs_request &q = S.reqs[batch[j]].req;
-        fresh[j] = q.n_fresh;
-        pooled[j] = q.n_pool;
-        tf += q.n_fresh;
-        tp += q.n_pool;
+        sizes[j] = S.reqs[batch[j]].req.n_pool;
+        tp += sizes[j];
     }
     Context &ctx = s.ctx;
-    const BatchPlan pv = make_batch_plan(ctx, curve, fresh.data(), M);
-    const BatchPlan pp = make_indexed_plan(ctx, curve, pooled.data(), M, pool.c);
-    if (pv.entries_bound > BATCH_ENTRIES_MAX || pp.entries_bound > BATCH_ENTRIES_MAX)  // rules changed since submission
+    const BatchPlan p = make_indexed_plan(ctx, curve, sizes.data(), M, pool.c);
+    if (p.entries_bound > BATCH_ENTRIES_MAX)
         return fail_requests(S, s, batch, HS_ERANGE);
-    // staging: fresh scalars and bases, pooled scalars and indices, M joined
-    // Jacobians, M results
-    const size_t st_bytes = align256(std::max<size_t>(1, tf) * 32) + align256(std::max<size_t>(1, tf) * 64) +
-                            align256(std::max<size_t>(1, tp) * 32) + align256(std::max<size_t>(1, tp) * 4) +
-                            align256((size_t)M * 96) + align256((size_t)M * ob);
-    const size_t bytes = batch_bytes(pv) + batch_bytes(pp) + st_bytes + 4096;
+    // staging: scalars, indices, M results
+    const size_t extra = align256(std::max<size_t>(1, tp) * 32) + align256(std::max<size_t>(1, tp) * 4) +
+                         align256((size_t)M * ob);
+    const size_t bytes = batch_bytes(p) + extra + 2048;
     if (S.in_flight > 0 && S.in_flight + bytes > S.cfg.hbm_budget) {
         S.stats.deferred++;
         return false;
     }
-    BatchBuffers bv, bp;
-    if (ctx.arena.reserve(bytes) != cudaSuccess) {
-        cudaGetLastError();
-        ctx.last_error = "workspace allocation";
+    BatchBuffers b;
+    void *ext = nullptr;
+    if (reserve_batch(ctx, p, extra, b, &ext) != HS_OK)
         return fail_requests(S, s, batch, HS_ENOMEM);
-    }
-    uint8_t *d_fsc = nullptr, *d_fpts = nullptr, *d_psc = nullptr, *d_out = nullptr;
-    uint32_t *d_idx = nullptr, *d_jac = nullptr;
-    if (!carve(ctx.arena, pv, bv) || !carve(ctx.arena, pp, bp) ||
-        !(d_fsc = (uint8_t *)ctx.arena.take(std::max<size_t>(1, tf) * 32)) ||
-        !(d_fpts = (uint8_t *)ctx.arena.take(std::max<size_t>(1, tf) * 64)) ||
-        !(d_psc = (uint8_t *)ctx.arena.take(std::max<size_t>(1, tp) * 32)) ||
-        !(d_idx = (uint32_t *)ctx.arena.take(std::max<size_t>(1, tp) * 4)) ||
-        !(d_jac = (uint32_t *)ctx.arena.take((size_t)M * 96)) || !(d_out = (uint8_t *)ctx.arena.take((size_t)M * ob))) {
-        ctx.last_error = "workspace carve";
-        return fail_requests(S, s, batch, HS_ENOMEM);
-    }
+    uint8_t *d_sc = (uint8_t *)ext;
+    uint32_t *d_idx = (uint32_t *)(d_sc + align256(std::max<size_t>(1, tp) * 32));
+    uint8_t *d_out = (uint8_t *)d_idx + align256(std::max<size_t>(1, tp) * 4);
     if (!ensure_pinned_out(s, (size_t)M * ob))
         return fail_requests(S, s, batch, HS_ENOMEM);
     cudaStream_t st = ctx.stream;
     cudaError_t e = cudaSuccess;
-    size_t fo = 0, po = 0;
+    size_t off = 0;
     for (uint64_t t : batch) {
         const hs_request &q = S.reqs[t].req;
-        if (q.n_pool && e == cudaSuccess)
-            e = cudaMemcpyAsync(d_psc + 32 * po, q.scalars, 32 * q.n_pool, cudaMemcpyHostToDevice, st);
-        if (q.n_pool && e == cudaSuccess)
-            e = cudaMemcpyAsync(d_idx + po, q.pool_idx, 4 * q.n_pool, cudaMemcpyHostToDevice, st);
-        if (q.n_fresh && e == cudaSuccess)
-            e = cudaMemcpyAsync(d_fsc + 32 * fo, q.scalars + 32 * q.n_pool, 32 * q.n_fresh, cudaMemcpyHostToDevice, st);
-        if (q.n_fresh && e == cudaSuccess)
-            e = cudaMemcpyAsync(d_fpts + 64 * fo, q.fresh_points, 64 * q.n_fresh, cudaMemcpyHostToDevice, st);
-        fo += q.n_fresh;
-        po += q.n_pool;
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(d_sc + 32 * off, q.scalars, 32 * q.n_pool, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(d_idx + off, q.pool_idx, 4 * q.n_pool, cudaMemcpyHostToDevice, st);
+        off += q.n_pool;
     }
     if (e != cudaSuccess) {
         ctx.last_error = std::string("staging: ") + cudaGetErrorString(e);
         return fail_requests(S, s, batch, HS_ECUDA);
     }
-    bv.scalars = (const uint32_t *)d_fsc;
-    bv.points = (const uint4 *)d_fpts;
-    bp.scalars = (const uint32_t *)d_psc;
-    bp.points = pool.table;
-    bp.pt_idx = d_idx;
-    // a batch of pooled parts only runs the table plan alone
-    const int rc = tf ? execute_joined(ctx, pv, bv, pp, bp, d_jac, d_out, S.cfg.out_fmt)
-                      : execute_batch(ctx, pp, bp, d_out, S.cfg.out_fmt);
-    if (rc != HS_OK)
+    b.scalars = (const uint32_t *)d_sc;
+    b.points = pool.table;
+    b.pt_idx = d_idx;
+    if (execute_batch(ctx, p, b, d_out, S.cfg.out_fmt) != HS_OK)
         return fail_requests(S, s, batch, HS_ECUDA);
     e = cudaMemcpyAsync(s.pinned_out, d_out, (size_t)M * ob, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess)
@@ -267,13 +244,8 @@ static bool launch_with_table(Server &S, Slot &s, std::vector<uint64_t> &batch, 
 // launch one batch on slot s; called with the server lock held; false = deferred (budget)
 static bool launch(Server &S, Slot &s, std::vector<uint64_t> &batch, int curve)
 {
-    if (S.pools[curve].table) {
-        bool pooled = false;
-        for (uint64_t t : batch)
-            pooled = pooled || S.reqs[t].req.n_pool;
-        if (pooled)
-            return launch_with_table(S, s, batch, curve);
-    }
+    if (S.reqs[batch.front()].table)
+        return launch_table(S, s, batch, curve);
     const size_t ob = fmt_bytes(S.cfg.out_fmt);
     std::vector<size_t> sizes;
     size_t total = 0, total_pool = 0;
@@ -423,8 +395,10 @@ static void scheduler(Server *Sp)
                 }
             if (!free_slot)
                 break;
-            // oldest request decides the curve; take queued requests of that curve, FIFO, up to the caps
+            // the oldest request decides the curve and the form (pool table or
+            // not); take queued requests of both, FIFO, up to the caps
             const int curve = S.reqs[S.queue.front()].req.curve;
+            const bool form = S.reqs[S.queue.front()].table;
             std::vector<uint64_t> batch;
             size_t pts = 0;
             uint64_t ent = 0;
@@ -433,7 +407,7 @@ static void scheduler(Server *Sp)
                 const uint64_t t = S.queue.front();
                 S.queue.pop_front();
                 const ReqState &r = S.reqs[t];
-                if (r.req.curve == curve && batch.size() < S.cfg.max_batch_msms &&
+                if (r.req.curve == curve && r.table == form && batch.size() < S.cfg.max_batch_msms &&
                     (batch.empty() || (pts + r.n <= S.cfg.max_batch_points && ent + r.entries <= BATCH_ENTRIES_MAX))) {
                     batch.push_back(t);
                     pts += r.n;
@@ -670,6 +644,7 @@ int hs_server_submit(hs_server *h, const hs_request *req, uint64_t *ticket)
     ReqState &r = S.reqs[t];
     r.req = *req;
     r.n = n;
+    r.table = table_form(S, *req);
     r.entries = entries;
     r.submitted = Clock::now();
     S.queue.push_back(t);

@@ -92,8 +92,9 @@ void *hs_context_stream(hs_context *ctx);
  * bucket additions), then an XYZZ fold of what is left; 0 keeps the XYZZ mixed
  * additions of every entry (helios/src/x64/helios_msm_vartime.cpp:296-325 is
  * the bucket loop both replace).  Results are identical either way.  Default:
- * one round on both curves, from 2^21 entries.  Host-input calls of a
- * batch-affine plan send their bases in one part. */
+ * one round on both curves, from 2^21 entries; fixed-base commitments of a
+ * curve that this call has not set take no round on Helios and one on Selene.
+ * Host-input calls of a batch-affine plan send their bases in one part. */
 int hs_context_set_batch_affine(hs_context *ctx, int curve, int rounds, size_t min_entries);
 /* set the Pippenger window width for one curve; 0 restores the built-in
  * cost model (the autotuner writes this) */
@@ -287,14 +288,15 @@ int hs_server_create(hs_server **srv, const hs_server_config *cfg);
  * Unless the curve's pool window is 0, the pool is also expanded once into a
  * resident table of window multiples 2^(c k) P_i (n * ceil(257/c) affine
  * points, 64 bytes each; a scratch of 160 bytes per table point while it is
- * built): the pooled bases of every request then form a fixed-base MSM over
- * that table (one reduced window, no doubling chain), added to the
- * variable-base MSM of its fresh bases.  Only while nothing is queued or in
- * flight (HS_EBUSY otherwise). */
+ * built): a request whose bases all come from the pool is then a fixed-base
+ * MSM over that table (one reduced window, no doubling chain), batched with
+ * other such requests; requests with fresh bases gather their pooled bases
+ * into a variable-base batch.  Only while nothing is queued or in flight
+ * (HS_EBUSY otherwise). */
 int hs_server_set_pool(hs_server *srv, int curve, const void *affine_points, size_t n);
 /* window width c of the curve's pool table from the next hs_server_set_pool:
- * 4..16, or 0 for no table (pooled bases are gathered into each batch as
- * variable bases).  The default is 12. */
+ * 4..16, or 0 for no table (every request's pooled bases are gathered into
+ * its batch as variable bases).  The default is 12. */
 int hs_server_set_pool_window(hs_server *srv, int curve, int window);
 /* window rule for the batches of every slot, as hs_context_set_window (window 0
  * clears the curve's rules); applies to batches planned after the call */

@@ -123,10 +123,11 @@ def test_bad_requests_are_refused(pools):
 
 @pytest.mark.parametrize("window", [0, 6, 12, 16])
 def test_pool_table_widths_and_part_shapes(pools, window):
-    """the pool as a table of window multiples (pooled parts as fixed-base MSMs
-    over indexed rows, added to the fresh parts), or gathered (window 0): every
-    request shape -- pooled only, fresh only, both, empty, repeated and
-    identity-cancelling indices -- matches the oracle"""
+    """the pool as a table of window multiples (pool-only requests as fixed-base
+    MSMs over indexed rows, batched apart from the requests with fresh bases), or
+    gathered (window 0): every request shape -- pooled only, fresh only, both,
+    empty, repeated and identity-cancelling indices -- matches the oracle, in
+    the mix and alone"""
     import helioselene_gb300 as hs
     from helioselene_gb300.workload import ORDER, random_scalars
     rng = np.random.default_rng(40 + window)
