@@ -437,7 +437,7 @@ def run_serving(hs, torch, device: str, local: int, requests_per_rate: int = 100
                 want = oracle.msm_many(curve, sc, pts, [reqs[i][2] for i in sel])
                 ok = ok and all(res_t[i] == want[j] for j, i in enumerate(sel))
             out["pool_only"]["bit_exact_vs_oracle"] = ok
-            out["pool_only"]["oracle_check"] = f"{len(sample)} of the {len(reqs)} all-at-once requests
+            out["pool_only"]["oracle_check"] = f"{len(sample)} of the {len(reqs)} all-at-once requests"
     # a sample of the all-at-once requests against the oracle (pooled + fresh bases)
     if with_oracle and checked:
         sys.path.insert(0, str(ROOT / "oracle"))
