@@ -208,27 +208,33 @@ __device__ __forceinline__ int ba_item(const uint32_t *__restrict__ sorted, cons
     return BA_ADD;
 }
 
-// first output of this thread's warp tile, plus its lane (outputs base + 32 k)
-__device__ __forceinline__ uint64_t ba_tile_base()
+// first output of this thread's warp tile, plus its lane (outputs base + 32 k),
+// in a launch over outputs [E0, E)
+__device__ __forceinline__ uint64_t ba_tile_base(uint32_t E0)
 {
     const uint64_t tile = (uint64_t)blockIdx.x * (BA_BT / 32) + (threadIdx.x >> 5);
-    return tile * 32 * BA_K + (threadIdx.x & 31);
+    return E0 + tile * 32 * BA_K + (threadIdx.x & 31);
 }
 
+// A launch covers round r's outputs [*lo >> r, *hi >> r) (lo null: from 0):
+// the whole level, or the lists of one part of host inputs in two parts.
+__device__ __forceinline__ uint32_t ba_first(const uint32_t *lo, uint32_t r) { return lo ? __ldg(lo) >> r : 0u; }
+
 template <class C, bool FIRST>
-__global__ void __launch_bounds__(BA_BT) k_ba_pairs(const uint32_t *__restrict__ offsets, uint32_t NB, uint32_t r,
-                                                   const uint32_t *__restrict__ sorted, const uint4 *__restrict__ pts,
-                                                   const uint4 *__restrict__ lvl, uint4 *__restrict__ pre,
-                                                   uint4 *__restrict__ co, uint4 *__restrict__ tot)
+__global__ void __launch_bounds__(BA_BT) k_ba_pairs(const uint32_t *__restrict__ lo, const uint32_t *__restrict__ hi,
+                                                   uint32_t r, const uint32_t *__restrict__ sorted,
+                                                   const uint4 *__restrict__ pts, const uint4 *__restrict__ lvl,
+                                                   uint4 *__restrict__ pre, uint4 *__restrict__ co,
+                                                   uint4 *__restrict__ tot)
 {
     using F = typename C::F;
     __shared__ Fe tree[2 * BA_BT];
     __shared__ Fe cop[2 * BA_BT];
-    const uint32_t E = __ldg(offsets + NB) >> r;  // outputs of this round
+    const uint32_t E0 = ba_first(lo, r), E = __ldg(hi) >> r;  // outputs of this launch
     const uint32_t t = threadIdx.x;
-    if ((uint64_t)blockIdx.x * BA_BT * BA_K >= E)
-        return;  // the whole block is past the round's outputs
-    const uint64_t base = ba_tile_base();
+    if (E0 + (uint64_t)blockIdx.x * BA_BT * BA_K >= E)
+        return;  // the whole block is past the launch's outputs
+    const uint64_t base = ba_tile_base(E0);
     Fe run = F::one();
     bool any = false;
 #pragma unroll 1
@@ -272,12 +278,12 @@ __global__ void __launch_bounds__(BA_BT) k_ba_pairs(const uint32_t *__restrict__
 
 // one inversion per block total (a block total is never zero: every factor is)
 template <class C>
-__global__ void k_ba_invert(const uint32_t *__restrict__ offsets, uint32_t NB, uint32_t r,
+__global__ void k_ba_invert(const uint32_t *__restrict__ lo, const uint32_t *__restrict__ hi, uint32_t r,
                             const uint4 *__restrict__ tot, uint4 *__restrict__ inv)
 {
     using F = typename C::F;
-    const uint32_t E = __ldg(offsets + NB) >> r;
-    const uint32_t nblk = (uint32_t)(((uint64_t)E + BA_BT * BA_K - 1) / (BA_BT * BA_K));
+    const uint32_t E0 = ba_first(lo, r), E = __ldg(hi) >> r;
+    const uint32_t nblk = (uint32_t)(((uint64_t)(E - E0) + BA_BT * BA_K - 1) / (BA_BT * BA_K));
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nblk)
         return;
@@ -285,15 +291,15 @@ __global__ void k_ba_invert(const uint32_t *__restrict__ offsets, uint32_t NB, u
 }
 
 template <class C, bool FIRST>
-__global__ void __launch_bounds__(BA_BT) k_ba_finish(const uint32_t *__restrict__ offsets, uint32_t NB, uint32_t r,
-                                                    const uint32_t *__restrict__ sorted, const uint4 *__restrict__ pts,
-                                                    const uint4 *__restrict__ lvl, const uint4 *__restrict__ pre,
-                                                    const uint4 *__restrict__ co, const uint4 *__restrict__ inv,
-                                                    uint4 *__restrict__ out)
+__global__ void __launch_bounds__(BA_BT) k_ba_finish(const uint32_t *__restrict__ lo, const uint32_t *__restrict__ hi,
+                                                    uint32_t r, const uint32_t *__restrict__ sorted,
+                                                    const uint4 *__restrict__ pts, const uint4 *__restrict__ lvl,
+                                                    const uint4 *__restrict__ pre, const uint4 *__restrict__ co,
+                                                    const uint4 *__restrict__ inv, uint4 *__restrict__ out)
 {
     using F = typename C::F;
-    const uint32_t E = __ldg(offsets + NB) >> r;
-    const uint64_t base = ba_tile_base();
+    const uint32_t E0 = ba_first(lo, r), E = __ldg(hi) >> r;
+    const uint64_t base = ba_tile_base(E0);
     if (base >= E)
         return;
     // 1 / (this thread's total)
@@ -338,8 +344,10 @@ __global__ void __launch_bounds__(BA_BT) k_ba_finish(const uint32_t *__restrict_
 
 // The batch-affine rounds' last sums, folded per segment into XYZZ bucket sums
 // (segments of a bucket's list in the last level buffer, longest first, as in
-// k_accumulate; the items are affine points, (0,0) the identity).
-template <class C>
+// k_accumulate; the items are affine points, (0,0) the identity).  With
+// RESUME (part 1 of host inputs in two parts), a descriptor with d.w set
+// continues the sum stored in its slot by part 0.
+template <class C, bool RESUME>
 __global__ void __launch_bounds__(128) k_accumulate_level(const uint4 *__restrict__ segs,
                                                          const uint32_t *__restrict__ seg_lo,
                                                          const uint32_t *__restrict__ seg_hi,
@@ -349,8 +357,8 @@ __global__ void __launch_bounds__(128) k_accumulate_level(const uint4 *__restric
     using F = typename C::F;
     const uint32_t S0 = *seg_lo, S = *seg_hi;
     for (uint32_t s = S0 + blockIdx.x * blockDim.x + threadIdx.x; s < S; s += gridDim.x * blockDim.x) {
-        const uint4 d = segs[s];  // start, length, destination slot
-        Xyzz acc = G::inf();
+        const uint4 d = segs[s];  // start, length, destination slot, continue
+        Xyzz acc = (RESUME && d.w) ? load_xyzz(seg_sum + 8 * (size_t)d.z) : G::inf();
         for (uint32_t i = 0; i < d.y; i++) {
             Fe x, y;
             load_affine(lvl, d.x + i, x, y);
@@ -884,42 +892,56 @@ cudaError_t msm_tail(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
     //    wave by wave, so kernels of other streams (another MSM's tail) get SM
     //    slots while this one runs.  Threads past the device-side count exit.
     if (p.ba_rounds) {
-        if (b.ready[0]) {  // host inputs: the bases arrive on another stream (one part: no part split here)
-            const cudaError_t e = cudaStreamWaitEvent(st, b.ready[0], ctx.capturing_host ? cudaEventWaitExternal : 0);
-            if (e != cudaSuccess)
-                return e;
-        }
-        cudaEvent_t ev0 = nullptr;
-        prof_begin(ctx, &ev0);
-        for (uint32_t r = 1; r <= p.ba_rounds; r++) {
-            const uint4 *in_lvl = r == 1 ? nullptr : b.ba_lvl[(r - 2) & 1];
-            uint4 *out_lvl = b.ba_lvl[(r - 1) & 1];
-            const uint32_t blocks = std::max<uint32_t>(1, p.ba_blocks[r - 1]);
-            if (r == 1)
-                k_ba_pairs<C, true><<<blocks, BA_BT, 0, st>>>(b.offsets, p.NB, r, b.sorted, b.points, in_lvl,
-                                                              b.ba_pre, b.ba_co, b.ba_tot);
+        // Host inputs in two parts: bucket k's part-j entries form list NB*j + k
+        // (offsets has 2 NB + 1 entries), so each part's lists are one range of
+        // every level; its rounds and its fold run once that part is in, and
+        // the first part-1 segment of a bucket continues its part-0 sum.
+        const int parts = p.part_slice ? 2 : 1;
+        const size_t nh = (size_t)(p.L + 1) * p.hist_blocks * (p.part_slice ? 2 : 1);
+        const uint32_t *bound[3] = {b.len_scan, b.len_scan + (p.part_slice ? nh / 2 : nh), b.len_scan + nh};
+        const uint4 *last = b.ba_lvl[(p.ba_rounds - 1) & 1];
+        for (int j = 0; j < parts; j++) {
+            if (b.ready[j]) {  // host inputs: this part of the bases arrives on another stream
+                const cudaError_t e =
+                    cudaStreamWaitEvent(st, b.ready[j], ctx.capturing_host ? cudaEventWaitExternal : 0);
+                if (e != cudaSuccess)
+                    return e;
+            }
+            cudaEvent_t ev0 = nullptr;
+            prof_begin(ctx, &ev0);
+            const uint32_t *lo = j ? b.offsets + p.NB : nullptr;
+            const uint32_t *hi = b.offsets + (size_t)p.NB * (j + 1);
+            for (uint32_t r = 1; r <= p.ba_rounds; r++) {
+                const uint4 *in_lvl = r == 1 ? nullptr : b.ba_lvl[(r - 2) & 1];
+                uint4 *out_lvl = b.ba_lvl[(r - 1) & 1];
+                const uint32_t blocks = std::max<uint32_t>(1, p.ba_blocks[r - 1]);
+                if (r == 1)
+                    k_ba_pairs<C, true><<<blocks, BA_BT, 0, st>>>(lo, hi, r, b.sorted, b.points, in_lvl, b.ba_pre,
+                                                                  b.ba_co, b.ba_tot);
+                else
+                    k_ba_pairs<C, false><<<blocks, BA_BT, 0, st>>>(lo, hi, r, b.sorted, b.points, in_lvl, b.ba_pre,
+                                                                   b.ba_co, b.ba_tot);
+                HS_LAUNCH_CHECK(ctx);
+                k_ba_invert<C><<<(blocks + 63) / 64, 64, 0, st>>>(lo, hi, r, b.ba_tot, b.ba_inv);
+                HS_LAUNCH_CHECK(ctx);
+                if (r == 1)
+                    k_ba_finish<C, true><<<blocks, BA_BT, 0, st>>>(lo, hi, r, b.sorted, b.points, in_lvl, b.ba_pre,
+                                                                   b.ba_co, b.ba_inv, out_lvl);
+                else
+                    k_ba_finish<C, false><<<blocks, BA_BT, 0, st>>>(lo, hi, r, b.sorted, b.points, in_lvl,
+                                                                    b.ba_pre, b.ba_co, b.ba_inv, out_lvl);
+                HS_LAUNCH_CHECK(ctx);
+            }
+            const int threads = 128;
+            const uint64_t want = (p.max_segs + threads - 1) / threads;
+            const int blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)ctx.sm_count * 32));
+            if (j == 0)
+                k_accumulate_level<C, false><<<blocks, threads, 0, st>>>(b.segs, bound[0], bound[1], last, b.seg_sum);
             else
-                k_ba_pairs<C, false><<<blocks, BA_BT, 0, st>>>(b.offsets, p.NB, r, b.sorted, b.points, in_lvl,
-                                                               b.ba_pre, b.ba_co, b.ba_tot);
+                k_accumulate_level<C, true><<<blocks, threads, 0, st>>>(b.segs, bound[1], bound[2], last, b.seg_sum);
             HS_LAUNCH_CHECK(ctx);
-            k_ba_invert<C><<<(blocks + 63) / 64, 64, 0, st>>>(b.offsets, p.NB, r, b.ba_tot, b.ba_inv);
-            HS_LAUNCH_CHECK(ctx);
-            if (r == 1)
-                k_ba_finish<C, true><<<blocks, BA_BT, 0, st>>>(b.offsets, p.NB, r, b.sorted, b.points, in_lvl,
-                                                               b.ba_pre, b.ba_co, b.ba_inv, out_lvl);
-            else
-                k_ba_finish<C, false><<<blocks, BA_BT, 0, st>>>(b.offsets, p.NB, r, b.sorted, b.points, in_lvl,
-                                                                b.ba_pre, b.ba_co, b.ba_inv, out_lvl);
-            HS_LAUNCH_CHECK(ctx);
+            prof_end(ctx, ev0, j == 0 ? p.entries_pinned : 0);
         }
-        const int threads = 128;
-        const uint64_t want = (p.max_segs + threads - 1) / threads;
-        const int blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)ctx.sm_count * 32));
-        const size_t nh = (size_t)(p.L + 1) * p.hist_blocks;
-        k_accumulate_level<C><<<blocks, threads, 0, st>>>(b.segs, b.len_scan, b.len_scan + nh,
-                                                          b.ba_lvl[(p.ba_rounds - 1) & 1], b.seg_sum);
-        HS_LAUNCH_CHECK(ctx);
-        prof_end(ctx, ev0, p.entries_pinned);
     } else {
         const int threads = 128;
         const uint64_t want = (p.max_segs + threads - 1) / threads;

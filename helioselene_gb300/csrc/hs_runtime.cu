@@ -463,13 +463,19 @@ static uint32_t scan_blocks(uint32_t NB) { return (NB + SCAN_BLOCK - 1) / SCAN_B
 
 static size_t hist_len(const BatchPlan &p) { return (size_t)(p.L + 1) * p.hist_blocks * (p.part_slice ? 2 : 1); }
 
+// entry lists of a plan: one per bucket, or with batch-affine rounds and host
+// inputs in two parts, one per (part, bucket): list NB*part + bucket
+static uint32_t list_count(const BatchPlan &p) { return (p.ba_rounds && p.part_slice) ? 2 * p.NB : p.NB; }
+
 size_t batch_bytes(const BatchPlan &p)
 {
     size_t b = 0;
     const size_t nh = hist_len(p);
     b += align256((size_t)p.M * sizeof(MsmDesc));
-    b += 3 * align256((size_t)(p.NB + 1) * 4);                                             // counts, offsets, seg_off
-    b += align256((size_t)2 * scan_blocks((uint32_t)std::max<size_t>(p.NB, nh)) * 4 + 64);  // scan partials
+    const size_t nl = list_count(p);
+    b += align256((size_t)(p.NB + 1) * 4);                                                 // counts
+    b += 2 * align256((nl + 1) * 4);                                                       // offsets, seg_off
+    b += align256((size_t)2 * scan_blocks((uint32_t)std::max<size_t>(nl, nh)) * 4 + 64);   // scan partials
     b += 2 * align256((nh + 1) * 4);                                                       // length histogram + scan
     b += align256((size_t)p.max_entries * 4);                                              // sorted
     b += align256((size_t)p.max_segs * 16);                                                // segs
@@ -497,10 +503,11 @@ bool carve(DeviceArena &a, const BatchPlan &p, BatchBuffers &b)
 {
     const size_t nh = hist_len(p);
     b.desc = (MsmDesc *)a.take((size_t)p.M * sizeof(MsmDesc));
+    const size_t nl = list_count(p);
     b.counts = (uint32_t *)a.take((size_t)(p.NB + 1) * 4);
-    b.offsets = (uint32_t *)a.take((size_t)(p.NB + 1) * 4);
-    b.seg_off = (uint32_t *)a.take((size_t)(p.NB + 1) * 4);
-    b.scan_tmp = (uint32_t *)a.take((size_t)2 * scan_blocks((uint32_t)std::max<size_t>(p.NB, nh)) * 4 + 64);
+    b.offsets = (uint32_t *)a.take((nl + 1) * 4);
+    b.seg_off = (uint32_t *)a.take((nl + 1) * 4);
+    b.scan_tmp = (uint32_t *)a.take((size_t)2 * scan_blocks((uint32_t)std::max<size_t>(nl, nh)) * 4 + 64);
     b.len_hist = (uint32_t *)a.take((nh + 1) * 4);
     b.len_scan = (uint32_t *)a.take((nh + 1) * 4);
     b.sorted = (uint32_t *)a.take((size_t)p.max_entries * 4);
@@ -774,11 +781,12 @@ __global__ void __launch_bounds__(SORT_THREADS) k_sort_count(const uint32_t *__r
 }
 
 // one thread per bucket of the batch: total over its rows (mode 0), or turn the
-// rows into first slots from offsets (mode 1)
+// rows into first slots from offsets (mode 1; with offsets1, the rows from
+// qsplit on -- part 1 of host inputs -- start at offsets1[bucket], their own list)
 template <int MODE>
 __global__ void k_sort_rows(const MsmDesc *__restrict__ desc, uint32_t M, uint32_t NB, uint32_t *__restrict__ cnt,
                             uint32_t *__restrict__ counts, const uint32_t *__restrict__ offsets, uint32_t qsplit,
-                            uint32_t *__restrict__ counts0)
+                            uint32_t *__restrict__ counts0, const uint32_t *__restrict__ offsets1)
 {
     const uint32_t kb = blockIdx.x * blockDim.x + threadIdx.x;
     if (kb >= NB)
@@ -798,6 +806,8 @@ __global__ void k_sort_rows(const MsmDesc *__restrict__ desc, uint32_t M, uint32
             v[u] = q0 + u < Q ? col[(uint64_t)(q0 + u) * Bm] : 0u;
 #pragma unroll
         for (int u = 0; u < 8; u++) {
+            if (MODE == 1 && offsets1 && q0 + u == qsplit)
+                run = offsets1[kb];
             if (MODE == 1 && q0 + u < Q)
                 col[(uint64_t)(q0 + u) * Bm] = run;
             if (MODE == 0 && q0 + u == qsplit)
@@ -902,11 +912,15 @@ __device__ __forceinline__ uint32_t part_slots(uint32_t c, uint32_t c0, uint32_t
     return (c0 + L - 1) / L + (c1 + L - 1) / L - ((c0 && c1) ? 1u : 0u);
 }
 
-// pad: counts rounded up to a multiple of pad + 1 (a power of two) first
+// pad: counts rounded up to a multiple of pad + 1 (a power of two) first.
+// split_nb > 0 (batch-affine plans of host inputs in two parts): the n =
+// 2 split_nb lists are bucket k's part-0 entries (list k) and part-1 entries
+// (list split_nb + k), each padded, and bucket k's segment slots -- over the
+// last round's lists, 2^shift times shorter -- are counted at list k.
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_a(const uint32_t *__restrict__ counts, uint32_t NB, uint32_t L,
                                                         uint32_t *__restrict__ offsets, uint32_t *__restrict__ seg_off,
                                                         uint32_t *__restrict__ tmp, const uint32_t *__restrict__ counts0,
-                                                        uint32_t pad)
+                                                        uint32_t pad, uint32_t split_nb, uint32_t shift)
 {
     __shared__ uint2 tot;
     const uint32_t base = blockIdx.x * SCAN_BLOCK + threadIdx.x * SCAN_ITEMS;
@@ -915,8 +929,16 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_a(const uint32_t *__restr
 #pragma unroll
     for (int j = 0; j < SCAN_ITEMS; j++) {
         const uint32_t idx = base + j;
-        c[j] = idx < NB ? (counts[idx] + pad) & ~pad : 0u;
-        s[j] = counts0 ? (idx < NB ? part_slots(c[j], counts0[idx], L) : 0u) : (c[j] + L - 1) / L;
+        if (split_nb) {
+            const uint32_t k = idx < split_nb ? idx : idx - split_nb;
+            const uint32_t c0 = idx < NB ? (counts0[k] + pad) & ~pad : 0u;
+            const uint32_t c1 = idx < NB ? (counts[k] - counts0[k] + pad) & ~pad : 0u;
+            c[j] = idx < split_nb ? c0 : c1;
+            s[j] = idx < split_nb ? part_slots((c0 + c1) >> shift, c0 >> shift, L) : 0u;
+        } else {
+            c[j] = idx < NB ? (counts[idx] + pad) & ~pad : 0u;
+            s[j] = counts0 ? (idx < NB ? part_slots(c[j], counts0[idx], L) : 0u) : (c[j] + L - 1) / L;
+        }
         v.x += c[j];
         v.y += s[j];
     }
@@ -1001,21 +1023,49 @@ __global__ void k_scan_c(uint32_t *__restrict__ offsets, uint32_t *__restrict__ 
 // seg_off[bucket] + j, so a bucket's partial sums stay contiguous.
 // shift: the lists segmented are the entry lists shifted right by it (the last
 // batch-affine round's, 2^shift times shorter; offsets are multiples of 2^shift)
+// A bucket's list, or its two part lists: [start0, start0 + c0) and [start1,
+// start1 + c1).  One list (counts0 null): c1 = 0.  Host inputs in two parts:
+// the part-0 entries come first in the bucket's list (counts0), or with
+// offsets1 (batch-affine plans) each part has its own list, bucket kb's part-1
+// list starting at offsets1[kb].
+struct PartLists {
+    uint32_t start0, c0, start1, c1;
+};
+
+__device__ __forceinline__ PartLists part_lists(const uint32_t *__restrict__ offsets,
+                                                const uint32_t *__restrict__ offsets1,
+                                                const uint32_t *__restrict__ counts0, uint32_t kb, uint32_t shift)
+{
+    PartLists l;
+    l.start0 = offsets[kb] >> shift;
+    const uint32_t cnt = (offsets[kb + 1] >> shift) - l.start0;
+    if (offsets1) {
+        l.c0 = cnt;
+        l.start1 = offsets1[kb] >> shift;
+        l.c1 = (offsets1[kb + 1] >> shift) - l.start1;
+    } else {
+        l.c0 = counts0 ? counts0[kb] : cnt;
+        l.start1 = l.start0 + l.c0;
+        l.c1 = cnt - l.c0;
+    }
+    return l;
+}
+
 __global__ void __launch_bounds__(SEG_HIST_THREADS) k_seg_hist(const uint32_t *__restrict__ offsets, uint32_t NB,
                                                               uint32_t L, uint32_t nblk, uint32_t *__restrict__ hist,
-                                                              const uint32_t *__restrict__ counts0, uint32_t shift)
+                                                              const uint32_t *__restrict__ counts0, uint32_t shift,
+                                                              const uint32_t *__restrict__ offsets1)
 {
     extern __shared__ uint32_t h[];
-    const uint32_t parts = counts0 ? 2u : 1u;
+    const uint32_t parts = (counts0 || offsets1) ? 2u : 1u;
     for (uint32_t i = threadIdx.x; i < parts * (L + 1); i += blockDim.x)
         h[i] = 0;
     __syncthreads();
     const uint32_t kb = blockIdx.x * blockDim.x + threadIdx.x;
     if (kb < NB) {
-        const uint32_t cnt = (offsets[kb + 1] - offsets[kb]) >> shift;
-        const uint32_t c0 = counts0 ? counts0[kb] : cnt;
+        const PartLists pl = part_lists(offsets, offsets1, counts0, kb, shift);
         for (uint32_t part = 0; part < parts; part++) {
-            const uint32_t c = part ? cnt - c0 : c0;
+            const uint32_t c = part ? pl.c1 : pl.c0;
             const uint32_t nfull = c / L, rem = c % L;
             if (nfull)
                 atomicAdd(&h[part * (L + 1) + L], nfull);
@@ -1053,10 +1103,11 @@ __global__ void __launch_bounds__(SEG_HIST_THREADS) k_seg_scatter(const uint32_t
                                                                  uint32_t L, uint32_t nblk,
                                                                  const uint32_t *__restrict__ hist_scan,
                                                                  uint4 *__restrict__ segs,
-                                                                 const uint32_t *__restrict__ counts0, uint32_t shift)
+                                                                 const uint32_t *__restrict__ counts0, uint32_t shift,
+                                                                 const uint32_t *__restrict__ offsets1)
 {
     extern __shared__ uint32_t cur[];
-    const uint32_t parts = counts0 ? 2u : 1u;
+    const uint32_t parts = (counts0 || offsets1) ? 2u : 1u;
     for (uint32_t i = threadIdx.x; i < parts * (L + 1); i += blockDim.x) {
         const uint32_t part = i / (L + 1), len = i % (L + 1);
         cur[i] = hist_scan[(size_t)(part * (L + 1) + L - len) * nblk + blockIdx.x];
@@ -1065,25 +1116,25 @@ __global__ void __launch_bounds__(SEG_HIST_THREADS) k_seg_scatter(const uint32_t
     const uint32_t kb = blockIdx.x * blockDim.x + threadIdx.x;
     if (kb >= NB)
         return;
-    const uint32_t start = offsets[kb] >> shift, cnt = (offsets[kb + 1] >> shift) - start, dest = seg_off[kb];
-    if (!counts0) {
-        emit_segments(cur, L, start, cnt, dest, dest + 1, 0u, segs);
+    const PartLists pl = part_lists(offsets, offsets1, counts0, kb, shift);
+    const uint32_t dest = seg_off[kb];
+    emit_segments(cur, L, pl.start0, pl.c0, dest, dest + 1, 0u, segs);
+    if (parts == 1)
         return;
-    }
-    const uint32_t c0 = counts0[kb], s0 = (c0 + L - 1) / L;
-    emit_segments(cur, L, start, c0, dest, dest + 1, 0u, segs);
+    const uint32_t s0 = (pl.c0 + L - 1) / L;
     if (s0)
-        emit_segments(cur + (L + 1), L, start + c0, cnt - c0, dest, dest + s0, 1u, segs);
+        emit_segments(cur + (L + 1), L, pl.start1, pl.c1, dest, dest + s0, 1u, segs);
     else
-        emit_segments(cur + (L + 1), L, start + c0, cnt - c0, dest, dest + 1, 0u, segs);
+        emit_segments(cur + (L + 1), L, pl.start1, pl.c1, dest, dest + 1, 0u, segs);
 }
 
 static cudaError_t launch_scan(Context &ctx, const uint32_t *in, uint32_t n, uint32_t L, uint32_t *out,
-                               uint32_t *out2, uint32_t *tmp, const uint32_t *counts0 = nullptr, uint32_t pad = 0)
+                               uint32_t *out2, uint32_t *tmp, const uint32_t *counts0 = nullptr, uint32_t pad = 0,
+                               uint32_t split_nb = 0, uint32_t shift = 0)
 {
     cudaStream_t st = ctx.stream;
     const uint32_t nblk = std::max<uint32_t>(1, scan_blocks(n));
-    k_scan_a<<<nblk, SCAN_THREADS, 0, st>>>(in, n, L, out, out2, tmp, counts0, pad);
+    k_scan_a<<<nblk, SCAN_THREADS, 0, st>>>(in, n, L, out, out2, tmp, counts0, pad, split_nb, shift);
     HS_LAUNCH_CHECK(ctx);
     k_scan_b<<<1, SCAN_THREADS, 0, st>>>(tmp, nblk, out + n, out2 ? out2 + n : nullptr);
     HS_LAUNCH_CHECK(ctx);
@@ -1131,6 +1182,9 @@ cudaError_t launch_sort(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
     const uint32_t seg_L = p.L << p.ba_rounds;
     if (p.ba_rounds && (e = cudaMemsetAsync(b.sorted, 0xff, (size_t)p.max_entries * 4, st)) != cudaSuccess)
         return e;
+    // batch-affine rounds over host inputs in two parts: each part's entries of
+    // a bucket form their own padded list (list NB*part + bucket)
+    const bool split_lists = p.ba_rounds && p.part_slice;
     if (p.smem_sort()) {
         if ((e = sort_smem_attrs(ctx.device)) != cudaSuccess)
             return e;
@@ -1144,11 +1198,18 @@ cudaError_t launch_sort(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
         HS_LAUNCH_CHECK(ctx);
         const uint32_t *c0 = p.part_slice ? b.counts0 : nullptr;
         k_sort_rows<0><<<tb, 256, 0, st>>>(b.desc, p.M, p.NB, b.sort_cnt, b.counts, nullptr, p.part_slice,
-                                           p.part_slice ? b.counts0 : nullptr);
+                                           p.part_slice ? b.counts0 : nullptr, nullptr);
         HS_LAUNCH_CHECK(ctx);
-        if ((e = launch_scan(ctx, b.counts, p.NB, seg_L, b.offsets, b.seg_off, b.scan_tmp, c0, pad)) != cudaSuccess)
+        if (split_lists) {  // a list per (part, bucket), each padded; segment slots on the last round's lists
+            if ((e = launch_scan(ctx, b.counts, 2 * p.NB, p.L, b.offsets, b.seg_off, b.scan_tmp, c0, pad, p.NB,
+                                 p.ba_rounds)) != cudaSuccess)
+                return e;
+        } else if ((e = launch_scan(ctx, b.counts, p.NB, seg_L, b.offsets, b.seg_off, b.scan_tmp, c0, pad)) !=
+                   cudaSuccess) {
             return e;
-        k_sort_rows<1><<<tb, 256, 0, st>>>(b.desc, p.M, p.NB, b.sort_cnt, nullptr, b.offsets, 0u, nullptr);
+        }
+        k_sort_rows<1><<<tb, 256, 0, st>>>(b.desc, p.M, p.NB, b.sort_cnt, nullptr, b.offsets, p.part_slice, nullptr,
+                                           split_lists ? b.offsets + p.NB : nullptr);
         HS_LAUNCH_CHECK(ctx);
         k_sort_scatter<<<p.sort_blocks, SORT_THREADS, smem, st>>>(b.digits, b.desc, p.M, b.sort_cnt, b.sorted,
                                                                   b.pt_idx);
@@ -1173,15 +1234,16 @@ cudaError_t launch_sort(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
     }
     // segments, longest first
     const uint32_t nh = (uint32_t)hist_len(p);
-    const uint32_t *c0 = (p.part_slice && p.smem_sort()) ? b.counts0 : nullptr;
-    const size_t hsm = (size_t)(p.L + 1) * 4 * (c0 ? 2 : 1);
+    const uint32_t *c0 = (p.part_slice && p.smem_sort() && !split_lists) ? b.counts0 : nullptr;
+    const uint32_t *off1 = split_lists ? b.offsets + p.NB : nullptr;
+    const size_t hsm = (size_t)(p.L + 1) * 4 * ((c0 || off1) ? 2 : 1);
     k_seg_hist<<<p.hist_blocks, SEG_HIST_THREADS, hsm, st>>>(b.offsets, p.NB, p.L, p.hist_blocks, b.len_hist, c0,
-                                                             p.ba_rounds);
+                                                             p.ba_rounds, off1);
     HS_LAUNCH_CHECK(ctx);
     if ((e = launch_scan(ctx, b.len_hist, nh, 1u, b.len_scan, nullptr, b.scan_tmp)) != cudaSuccess)
         return e;
     k_seg_scatter<<<p.hist_blocks, SEG_HIST_THREADS, hsm, st>>>(b.offsets, b.seg_off, p.NB, p.L, p.hist_blocks,
-                                                                 b.len_scan, b.segs, c0, p.ba_rounds);
+                                                                 b.len_scan, b.segs, c0, p.ba_rounds, off1);
     HS_LAUNCH_CHECK(ctx);
     return cudaSuccess;
 }
@@ -1849,6 +1911,20 @@ int hs_msm_device(hs_context *h, int curve, const void *d_scalars, const void *d
 static void plan_parts(BatchPlan &p, uint32_t slice)
 {
     p.part_slice = slice;
+    if (p.ba_rounds) {
+        // each part's list of a bucket padded apart: up to NB (2^R - 1) more
+        // padding entries; the last round's 2 NB lists cut into segments of L
+        const uint64_t padded = (uint64_t)p.max_entries + (uint64_t)p.NB * ((1u << p.ba_rounds) - 1);
+        p.max_entries = (uint32_t)padded;
+        const uint64_t per_block = (uint64_t)BA_PLAN_K * BA_PLAN_BT;
+        for (uint32_t r = 1; r <= p.ba_rounds; r++) {
+            p.ba_items[r - 1] = (padded >> r) + 1;
+            p.ba_blocks[r - 1] = (uint32_t)((p.ba_items[r - 1] + per_block - 1) / per_block);
+        }
+        const uint64_t ent = p.ba_items[p.ba_rounds - 1];
+        p.max_segs = (uint32_t)std::min<uint64_t>(0xffffffffull, std::min<uint64_t>(ent, 2ull * p.NB) + ent / p.L + 1);
+        return;
+    }
     const uint64_t more = std::min<uint64_t>(p.entries_bound, p.NB);
     p.max_segs = (uint32_t)std::min<uint64_t>(0xffffffffull, (uint64_t)p.max_segs + more);
 }
@@ -1883,11 +1959,14 @@ static int msm_host(Context &ctx, int curve, const uint8_t *lead_scalar, const v
     // entries of a bucket are contiguous and get their own segments, and the
     // accumulation of part 0 runs while part 1 is still on the link.
     const MsmDesc &d0 = split ? s.lo.msms[0] : p.msms[0];
-    // (a batch-affine plan takes its bases in one part: its rounds pair entries
-    // of both parts)
+    // (a batch-affine plan gives each part's entries of a bucket their own list,
+    // so that each part's rounds pair only entries that have arrived)
+    const auto padded_fits = [](const BatchPlan &q) {
+        return !q.ba_rounds || (uint64_t)q.max_entries + (uint64_t)q.NB * ((1u << q.ba_rounds) - 1) < 0x80000000ull;
+    };
     const bool two = point_fmt != HS_FMT_COMPRESSED && d0.slices >= 2 &&
-                     (split ? (s.hi.smem_sort() && s.lo.smem_sort() && !s.hi.ba_rounds && !s.lo.ba_rounds)
-                            : (p.smem_sort() && !p.ba_rounds));
+                     (split ? (s.hi.smem_sort() && s.lo.smem_sort() && padded_fits(s.hi) && padded_fits(s.lo))
+                            : (p.smem_sort() && padded_fits(p)));
     size_t bound[3] = {0, total, total};
     if (two) {
         const uint32_t cut = d0.slices / 2;

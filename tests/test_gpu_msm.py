@@ -349,8 +349,9 @@ def test_host_inputs_every_format(ctx, curve):
     want_id = ctx.msm_batch([(curve, sc, pts_id)])[0]
     aff51 = np.concatenate([x51, y51], axis=1)
     try:
-        # XYZZ accumulation: bases in two parts; batch-affine rounds: one part
-        for rounds in (0, 2):
+        # bases in two parts, with XYZZ accumulation or batch-affine rounds (each
+        # part's entries of a bucket then in their own padded list)
+        for rounds in (0, 1, 2):
             ctx.set_batch_affine(rounds, 1 << 21)
             for split in (1 << 18, 0):
                 ctx.set_split(split)
@@ -394,8 +395,8 @@ def test_host_parts_edge_cases(ctx, curve):
     p3[: half // 2] = 0
     cases.append(("identity bases in part 0", w.scalars, p3))
     try:
-        for rounds in (0, 2):
-            ctx.set_batch_affine(rounds, 1 << 21)
+        for rounds in (0, 1, 3):
+            ctx.set_batch_affine(rounds, 1 << 20)
             for split in (1 << 18, 0):
                 ctx.set_split(split)
                 for name, s, p in cases:
