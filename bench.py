@@ -54,7 +54,8 @@ ACC_TRAFFIC = {
     1: {"bytes": (2923.5e6, 2941.9e6),
         "capture": "2026-12-04, commit d2e236f, k_ba_pairs + k_ba_invert + k_ba_finish + k_accumulate_level"},
 }
-DEFAULT_BA_ROUNDS = (1, 1)  # the library's default accumulation form (Helios, Selene)
+DEFAULT_BA_ROUNDS = (1, 1)  # the library's default accumulation form of device-resident MSMs (Helios, Selene)
+HOST_BA_ROUNDS = (0, 1)     # ... and of single MSMs from host buffers
 SPLIT_DEFAULT = 1 << 18  # the library's window-split threshold for single MSMs
 
 
@@ -924,14 +925,17 @@ def run_ours(args) -> None:
     ctx.set_split(head_split)
     ctx2.set_split(head_split)
     ctx2.set_priority(True)
-    # the accumulation form of each curve (batch-affine rounds), set explicitly
+    # the accumulation form of each curve (batch-affine rounds): the library's
+    # defaults, or set for every kind of plan by --ba-rounds
     rr = list(DEFAULT_BA_ROUNDS)
+    rr_host = list(HOST_BA_ROUNDS)
     if args.ba_rounds is not None:
         rr = [int(x) for x in str(args.ba_rounds).split(",")]
         rr = rr * 2 if len(rr) == 1 else rr
-    for c in (ctx, ctx2):
-        for curve in (hs.HELIOS, hs.SELENE):
-            c.set_batch_affine(rr[curve], 1 << 21, curve)
+        rr_host = list(rr)
+        for c in (ctx, ctx2):
+            for curve in (hs.HELIOS, hs.SELENE):
+                c.set_batch_affine(rr[curve], 1 << 21, curve)
     ctxs = {hs.HELIOS: ctx, hs.SELENE: ctx2}
     n = args.n
     data = make_inputs(hs, ctx, torch, n, device)
@@ -1145,6 +1149,7 @@ def run_ours(args) -> None:
                     "h2d_bytes_per_step": 2 * n * (32 + 120), "d2h_bytes_per_step": 2 * 120,
                     "api": "hs_msm(point_fmt=HS_FMT_JACOBIAN51, out_fmt=HS_FMT_JACOBIAN51), pinned host buffers",
                     "calls": "one per curve from a pool of two host threads, Selene first", "window_split_min": e2e_split,
+                    "ba_rounds": {"helios": rr_host[0], "selene": rr_host[1]},
                     "step_ms": {"median": statistics.median(e2e_step_ms), "min": min(e2e_step_ms),
                                 "max": max(e2e_step_ms), "all": [round(t, 3) for t in e2e_step_ms]},
                     "median_step_value": ws * 2 * n / (statistics.median(e2e_step_ms) * 1e-3),

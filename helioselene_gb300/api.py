@@ -102,14 +102,17 @@ class Context:
 
     def set_batch_affine(self, rounds: int, min_entries: int = 1 << 21, curve: int = None) -> None:
         """bucket accumulation by `rounds` rounds of batch-affine additions for plans of at
-        least min_entries entries (0: XYZZ mixed additions throughout), for one curve or both"""
+        least min_entries entries (0: XYZZ mixed additions throughout; -1: the library's
+        defaults), for one curve or both"""
         for c in ((L.HELIOS, L.SELENE) if curve is None else (curve,)):
             self._check(self._lib.hs_context_set_batch_affine(self._h, c, int(rounds), int(min_entries)),
                         "set_batch_affine")
 
     def default_batch_affine(self) -> None:
-        """the library's default accumulation form (one batch-affine round on both curves)"""
-        self.set_batch_affine(1, 1 << 21)
+        """the library's default accumulation forms: one batch-affine round on both curves,
+        except fixed-base commitments and single MSMs from host buffers, which take none on
+        Helios and one on Selene"""
+        self.set_batch_affine(-1)
 
     # -- instrumentation --
     def profile(self, on: bool = True) -> None:

@@ -47,6 +47,11 @@ struct GraphEntry {
     void *d_desc = nullptr;  // the batch descriptors, uploaded once at capture
 };
 
+// the library's batch-affine default for a curve's plans (below: the kinds of
+// plans that take their own until hs_context_set_batch_affine sets the curve)
+constexpr uint32_t BA_DEFAULT_ROUNDS = 1;
+constexpr uint64_t BA_DEFAULT_MIN_ENTRIES = uint64_t(1) << 21;
+
 struct Context {
     int device = 0;
     int sm_count = 0;
@@ -71,15 +76,20 @@ struct Context {
     // one round on both curves is fastest (5.15 ms per pair against 5.37 with
     // none): one curve's memory-bound round overlaps the other's
     // multiply-bound work.
-    uint32_t ba_rounds[2] = {1, 1};
-    uint64_t ba_min_entries[2] = {uint64_t(1) << 21, uint64_t(1) << 21};
-    // Fixed-base commitments run one curve at a time, where the round pays on
-    // Selene only (4096 commitments over 2^20 generators on GB300: Helios 617
-    // commitments/s without it, 568 with; Selene 397 without, 427 with), so
-    // until hs_context_set_batch_affine sets a curve, its fixed-base plans
-    // take these rounds.
+    uint32_t ba_rounds[2] = {BA_DEFAULT_ROUNDS, BA_DEFAULT_ROUNDS};
+    uint64_t ba_min_entries[2] = {BA_DEFAULT_MIN_ENTRIES, BA_DEFAULT_MIN_ENTRIES};
+    // Until hs_context_set_batch_affine sets a curve, two kinds of plans take
+    // their own rounds, because there a curve's MSMs run mostly alone, where
+    // the round pays on Selene only:
+    // - fixed-base commitments (4096 over 2^20 generators on GB300: Helios 617
+    //   commitments/s without a round, 568 with; Selene 397 without, 427 with);
+    // - single MSMs from host buffers, whose accumulation is pipelined with
+    //   the link (a Helios and a Selene call of 2^20 points from two host
+    //   threads: 6.06 ms per pair with one round on both, 5.91 ms without one
+    //   on Helios).
     bool ba_set[2] = {false, false};
     uint32_t fixed_ba_rounds[2] = {0, 1};
+    uint32_t host_ba_rounds[2] = {0, 1};
     std::vector<GraphEntry> graphs;
     DeviceArena arena;
     std::mutex mu;
@@ -241,7 +251,9 @@ __device__ __forceinline__ uint32_t find_msm(uint32_t M, uint32_t x, KeyFn key)
 }
 
 int choose_window(const Context &ctx, int curve, size_t n);
-BatchPlan make_batch_plan(const Context &ctx, int curve, const size_t *sizes, uint32_t M);
+// base_rounds >= 0: the batch-affine rounds in place of the curve's setting
+// (a window rule that names rounds still wins)
+BatchPlan make_batch_plan(const Context &ctx, int curve, const size_t *sizes, uint32_t M, int base_rounds = -1);
 // count fixed-base MSMs of n table generators each (window c), scalars back to back
 BatchPlan make_fixed_plan(int curve, size_t n, int c, uint32_t count);
 // M MSMs over rows of one window-multiple table (window c) named by index lists

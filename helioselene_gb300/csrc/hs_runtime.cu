@@ -216,7 +216,7 @@ static uint32_t seg_cap(uint64_t ent, uint64_t nb)
     return (uint32_t)std::min<uint64_t>(big, std::max<uint64_t>(least, ent / 65536));
 }
 
-BatchPlan make_batch_plan(const Context &ctx, int curve, const size_t *sizes, uint32_t M)
+BatchPlan make_batch_plan(const Context &ctx, int curve, const size_t *sizes, uint32_t M, int base_rounds)
 {
     BatchPlan p;
     p.curve = curve;
@@ -273,7 +273,7 @@ BatchPlan make_batch_plan(const Context &ctx, int curve, const size_t *sizes, ui
     // batch-affine rounds: those of the size class (window rule) holding most of
     // the plan's entries when that rule names some, else the curve's setting
     const auto &rules = ctx.rules[curve == HS_SELENE ? 1 : 0];
-    int rounds = (int)ctx.ba_rounds[curve == HS_SELENE];
+    int rounds = base_rounds >= 0 ? base_rounds : (int)ctx.ba_rounds[curve == HS_SELENE];
     if (!rules.empty()) {
         std::vector<uint64_t> by_rule(rules.size(), 0);
         for (uint32_t i = 0; i < M; i++) {
@@ -1558,14 +1558,16 @@ struct SplitPlan {
     BatchPlan hi, lo;
 };
 
-static SplitPlan make_split(const Context &ctx, int curve, size_t n)
+static SplitPlan make_split(const Context &ctx, int curve, size_t n, int base_rounds = -1)
 {
     const int c = choose_window(ctx, curve, n);
     const uint32_t W = (uint32_t)((257 + c - 1) / c);
     const uint32_t h = W / 2;
     SplitPlan sp{make_window_plan(curve, n, c, h, W - h), make_window_plan(curve, n, c, 0, h)};
-    plan_batch_affine(sp.hi, ctx.ba_rounds[curve == HS_SELENE], ctx.ba_min_entries[curve == HS_SELENE]);
-    plan_batch_affine(sp.lo, ctx.ba_rounds[curve == HS_SELENE], ctx.ba_min_entries[curve == HS_SELENE]);
+    const int k = curve == HS_SELENE;
+    const uint32_t rounds = base_rounds >= 0 ? (uint32_t)base_rounds : ctx.ba_rounds[k];
+    plan_batch_affine(sp.hi, rounds, ctx.ba_min_entries[k]);
+    plan_batch_affine(sp.lo, rounds, ctx.ba_min_entries[k]);
     return sp;
 }
 
@@ -1852,15 +1854,22 @@ int hs_context_set_split(hs_context *h, size_t min_points)
 
 int hs_context_set_batch_affine(hs_context *h, int curve, int rounds, size_t min_entries)
 {
-    if (!h || !valid_curve(curve) || rounds < 0 || rounds > (int)BA_MAX_ROUNDS)
+    if (!h || !valid_curve(curve) || rounds < -1 || rounds > (int)BA_MAX_ROUNDS)
         return HS_EINVAL;
     Context &ctx = h->c;
     std::lock_guard<std::mutex> lk(ctx.mu);
     DeviceGuard g(ctx.device);
     drop_graphs(ctx);
-    ctx.ba_rounds[curve == HS_SELENE] = (uint32_t)rounds;
-    ctx.ba_min_entries[curve == HS_SELENE] = min_entries;
-    ctx.ba_set[curve == HS_SELENE] = true;
+    const int k = curve == HS_SELENE;
+    if (rounds < 0) {  // the library's defaults
+        ctx.ba_rounds[k] = BA_DEFAULT_ROUNDS;
+        ctx.ba_min_entries[k] = BA_DEFAULT_MIN_ENTRIES;
+        ctx.ba_set[k] = false;
+        return HS_OK;
+    }
+    ctx.ba_rounds[k] = (uint32_t)rounds;
+    ctx.ba_min_entries[k] = min_entries;
+    ctx.ba_set[k] = true;
     return HS_OK;
 }
 
@@ -1946,13 +1955,15 @@ static int msm_host(Context &ctx, int curve, const uint8_t *lead_scalar, const v
     const size_t pb = fmt_bytes(point_fmt);
     const CurveOps &ops = curve_ops(curve);
     const bool split = ctx.split_min && total >= ctx.split_min;
+    const int k = curve == HS_SELENE;
+    const int base_rounds = ctx.ba_set[k] ? -1 : (int)ctx.host_ba_rounds[k];
     SplitPlan s;
     BatchPlan p;
     if (split)
-        s = make_split(ctx, curve, total);
+        s = make_split(ctx, curve, total, base_rounds);
     else {
         const size_t sizes[1] = {total};
-        p = make_batch_plan(ctx, curve, sizes, 1);
+        p = make_batch_plan(ctx, curve, sizes, 1, base_rounds);
     }
     // Bases spanning several counting-sort slices arrive in two parts, split at a
     // slice boundary: the entries of a bucket come in slice order, so each part's

@@ -151,3 +151,24 @@ def test_fixed_base_commitments_with_rounds(ba_ctx, curve):
             assert fb.commit(vals, blinds) == want, f"rounds={rounds}"
     finally:
         fb.close()
+
+
+@pytest.mark.parametrize("curve", [0, 1])
+def test_default_forms_restored(ba_ctx, curve):
+    """rounds = -1 restores the library's per-kind defaults (host-input MSMs and
+    fixed-base commitments: none on Helios, one on Selene; device MSMs: one),
+    and every kind of plan still matches the oracle"""
+    import helioselene_gb300 as hs
+    from helioselene_gb300._lib import HsError
+    n = 300000
+    sc, pts, _ = oracle_inputs(curve, n, seed=808 + curve, edge_fraction=0.01)
+    want = oracle.msm_mt(curve, sc, pts, 16)
+    ba_ctx.set_batch_affine(3, 0, curve)
+    assert ba_ctx.msm(curve, sc, pts) == want
+    ba_ctx.set_batch_affine(-1, 0, curve)
+    assert ba_ctx.msm(curve, sc, pts) == want
+    assert ba_ctx.msm_batch([(curve, sc, pts)])[0] == want
+    with pytest.raises(HsError):
+        ba_ctx.set_batch_affine(-2, 0, curve)
+    with pytest.raises(HsError):
+        ba_ctx.set_batch_affine(4, 0, curve)
