@@ -162,7 +162,7 @@ def test_default_forms_restored(ba_ctx, curve):
     from helioselene_gb300._lib import HsError
     n = 300000
     sc, pts, _ = oracle_inputs(curve, n, seed=808 + curve, edge_fraction=0.01)
-    want = oracle.msm_mt(curve, sc, pts, 16)
+    want = oracle.msm_mt(curve, sc, pts, oracle.default_threads())
     ba_ctx.set_batch_affine(3, 0, curve)
     assert ba_ctx.msm(curve, sc, pts) == want
     ba_ctx.set_batch_affine(-1, 0, curve)
