@@ -136,7 +136,8 @@ class Context:
         return {"mad_lo_hi": r[0], "mad_wide": r[1], "mad_lo": r[2], "mad_hi": r[3]}
 
     def field_op(self, field: int, op: int, a, b=None) -> np.ndarray:
-        """Element-wise device field arithmetic (0 mul, 1 sqr, 2 add, 3 sub, 4 canon, 5 inv, 6 neg)."""
+        """Element-wise device field arithmetic (0 mul, 1 sqr, 2 add, 3 sub, 4 canon, 5 inv, 6 neg;
+        the window combination's lane-sliced form: 7 mul, 8 (a - b)(a + b), 9 a^(2^32), 10 round trip)."""
         x = _u8(a)
         y = _u8(b) if b is not None else x
         n = x.size // 32

@@ -167,6 +167,7 @@ __device__ __forceinline__ void sqr_wide_8(uint32_t t[16], const uint32_t a[8])
 
 template <class P>
 struct Field {
+    using Params = P;
     static constexpr uint32_t M0 = P::M[0], M1 = P::M[1], M2 = P::M[2], M3 = P::M[3];
     static constexpr uint32_t M4 = P::M[4], M5 = P::M[5], M6 = P::M[6], M7 = P::M[7];
     static constexpr uint32_t C0 = P::C[0], C1 = P::C[1], C2 = P::C[2], C3 = P::C[3];

@@ -676,12 +676,6 @@ __global__ void __launch_bounds__(RED_CHUNK) k_window_sum(const uint4 *__restric
 // ---------------------------------------------------------------------------
 // 5. window combination (Horner) -> canonical Jacobian
 // ---------------------------------------------------------------------------
-// The 256 doublings of the Horner chain are inherently sequential, so each
-// doubling and addition is spread over the lanes of one warp: in every stage
-// the active lanes compute one independent product each (operands picked from
-// a shared-memory slot file by lane), with the linear steps in between done
-// by lane 0.  This turns the 9 (dbl) and 14 (add) sequential products into 3
-// and 4 product stages.
 template <class C>
 __device__ void store_jacobian_canon(uint32_t *out, const Xyzz &p)
 {
@@ -700,185 +694,379 @@ __device__ void store_jacobian_canon(uint32_t *out, const Xyzz &p)
     }
 }
 
-enum Slot : int {
-    sX, sY, sZZ, sZZZ,          // running total
-    sX2, sY2, sZZ2, sZZZ2,      // addend
-    sU, sV, sA, sB, sT, sW, sS, sM, sM2, sD, sYa, sYb, sXn, sZZn, sZZZn,
-    sU1, sU2, sS1, sS2, sZ12, sZZZ12, sP, sR, sPP, sRR, sPPP, sQ,
-    sZERO, sNSLOTS
+// Lane-sliced field elements for the Horner chain.  The chain's 256
+// doublings are sequential, so its time is the latency of one doubling.  In
+// eight 32-bit limbs a product is about 180 multiply instructions of serial
+// carry chains on one warp, bound by one scheduler's multiply pipe (about 525
+// cycles on F_p, 870 on F_q).  Here an element is spread over a warp: lane
+// l < 10 holds limb l of a radix-2^26 form (lanes 10..31 hold 0).  A product
+// is formed column-wise -- lane l sums a_i b_(l-i) in a 64-bit register --
+// then one carry step moves bits 26..51 of every column up one lane and bits
+// 52.. up two, and the columns at and above 2^260 are folded back: on F_p by
+// 2^260 == 608 (and 2^520 == 608^2); on F_q by a table of 2^(26(10+h)) mod q,
+// then the two limbs that carried past 2^260 by 2^260 mod q = 32 gamma.
+// Products come out with limbs below 2^27 (below 2^26 + 2^20 on F_p).
+// Additions are limb-wise; a subtraction adds Z or 2Z, multiples of m whose
+// limbs (Z: in [2^28, 1.25 * 2^28]) exceed every limb of the subtrahend.
+// A product's inputs must keep every column below 2^64: with limbs below
+// 2^30.1 and 2^29.8, ten products stay below 2^63.2.  Every function is
+// called by all 32 lanes of a warp.
+constexpr unsigned LF_ALL = 0xffffffffu;
+constexpr uint64_t LF_M26 = (1ull << 26) - 1;
+
+// Z = 129 p and 129 q in radix-2^26 limbs
+static __constant__ uint32_t LF_Z[2][10] = {
+    {0x13fff66du, 0x13fffffbu, 0x13fffffbu, 0x13fffffbu, 0x13fffffbu, 0x13fffffbu, 0x13fffffbu, 0x13fffffbu,
+     0x13fffffbu, 0x101ffffbu},
+    {0x110b971fu, 0x1002ebbfu, 0x1178fc9eu, 0x1221a868u, 0x137f3b8au, 0x13fffff3u, 0x13fffffbu, 0x13fffffbu,
+     0x13fffffbu, 0x101ffffbu}};
+// row h: 2^(26 (10 + h)) mod q in radix-2^26 limbs (row 0: 2^260 mod q = 32 gamma)
+static __constant__ uint32_t LF_RQ[11][10] = {
+            {0x3070c20u, 0x16c6c36u, 0x14f2292u, 0x1a44d4au, 0x01010fau, 0x0000002u, 0x0000000u, 0x0000000u, 0x0000000u, 0x0000000u},
+            {0x0000000u, 0x3070c20u, 0x16c6c36u, 0x14f2292u, 0x1a44d4au, 0x01010fau, 0x0000002u, 0x0000000u, 0x0000000u, 0x0000000u},
+            {0x0000000u, 0x0000000u, 0x3070c20u, 0x16c6c36u, 0x14f2292u, 0x1a44d4au, 0x01010fau, 0x0000002u, 0x0000000u, 0x0000000u},
+            {0x0000000u, 0x0000000u, 0x0000000u, 0x3070c20u, 0x16c6c36u, 0x14f2292u, 0x1a44d4au, 0x01010fau, 0x0000002u, 0x0000000u},
+            {0x0000000u, 0x0000000u, 0x0000000u, 0x0000000u, 0x3070c20u, 0x16c6c36u, 0x14f2292u, 0x1a44d4au, 0x01010fau, 0x0000002u},
+            {0x20e1840u, 0x2d8d86du, 0x29e4524u, 0x3489a94u, 0x02021f4u, 0x3070c24u, 0x16c6c36u, 0x14f2292u, 0x1a44d4au, 0x01010fau},
+            {0x09eb42du, 0x1f359fcu, 0x23798c8u, 0x17660e7u, 0x2f5edcbu, 0x0408471u, 0x3070c24u, 0x16c6c36u, 0x14f2292u, 0x0044d4au},
+            {0x3a1550au, 0x24f5d25u, 0x36b84ebu, 0x121f2c1u, 0x1a54480u, 0x2fe99a7u, 0x0408471u, 0x3070c24u, 0x16c6c36u, 0x00f2292u},
+            {0x2cb966bu, 0x248f1a0u, 0x0cf0f2fu, 0x10edbc3u, 0x1fe917eu, 0x1c3c66fu, 0x2fe99a7u, 0x0408471u, 0x3070c24u, 0x00c6c36u},
+            {0x25f57d8u, 0x2f3ea03u, 0x1679a21u, 0x0c9df95u, 0x1650e8du, 0x2179bd1u, 0x1c3c66fu, 0x2fe99a7u, 0x0408471u, 0x0070c24u},
+            {0x01fa542u, 0x0c733b9u, 0x04912c4u, 0x3c483d4u, 0x331e04fu, 0x1734323u, 0x2179bd1u, 0x1c3c66fu, 0x2fe99a7u, 0x0008471u},
 };
 
-struct SlotFile {
-    Fe f[sNSLOTS];
-    int flag;
+template <class F>
+struct LaneField {
+    static constexpr bool FQ = F::Params::NC != 1;
+
+    // this lane's constants, read once per thread
+    struct Regs {
+        uint32_t z, z2;   // limb `lane` of Z and 2Z (0 on lanes >= 10)
+        uint32_t r[11];   // F_q: limb `lane` of row h of the fold table
+        uint32_t k0, k1;  // F_q: limbs lane and lane - 1 of 2^260 mod q
+    };
+    __device__ __forceinline__ static Regs regs(int lane)
+    {
+        Regs g;
+        const bool in = lane < 10;
+        g.z = in ? LF_Z[FQ ? 1 : 0][in ? lane : 0] : 0u;
+        g.z2 = 2 * g.z;
+#pragma unroll
+        for (int h = 0; h < 11; h++)
+            g.r[h] = in ? LF_RQ[h][in ? lane : 0] : 0u;
+        g.k0 = lane < 6 ? LF_RQ[0][lane < 6 ? lane : 0] : 0u;
+        g.k1 = (lane >= 1 && lane <= 6) ? LF_RQ[0][(lane >= 1 && lane <= 6) ? lane - 1 : 0] : 0u;
+        return g;
+    }
+
+    // bits 26..51 of every lane's value up one lane, bits 52.. up two
+    __device__ __forceinline__ static uint64_t split_carry(uint64_t c, int lane)
+    {
+        const uint32_t u1 = __shfl_up_sync(LF_ALL, (uint32_t)(c >> 26) & (uint32_t)LF_M26, 1);
+        const uint32_t u2 = __shfl_up_sync(LF_ALL, (uint32_t)(c >> 52), 2);
+        return (c & LF_M26) + (lane >= 1 ? u1 : 0u) + (lane >= 2 ? u2 : 0u);
+    }
+
+    __device__ __forceinline__ static uint32_t mul(uint32_t a, uint32_t b, int lane, const Regs &g)
+    {
+        // columns: lane l gets sum_i a_i b_(l-i); b's index wraps to lanes >= 22
+        // when l < i, which hold 0, as do lanes >= 10
+        uint64_t c0 = 0, c1 = 0;
+#pragma unroll
+        for (int i = 0; i < 10; i += 2) {
+            const uint32_t a0 = __shfl_sync(LF_ALL, a, i), a1 = __shfl_sync(LF_ALL, a, i + 1);
+            const uint32_t b0 = __shfl_sync(LF_ALL, b, (lane - i) & 31);
+            const uint32_t b1 = __shfl_sync(LF_ALL, b, (lane - i - 1) & 31);
+            c0 += (uint64_t)a0 * b0;
+            c1 += (uint64_t)a1 * b1;
+        }
+        // 19 columns below 2^63.2 -> lanes 0..20 below 2^27.1 (lane 20 below 2^12)
+        const uint32_t cur = (uint32_t)split_carry(c0 + c1, lane);
+        if constexpr (!FQ) {
+            const uint32_t hi = __shfl_sync(LF_ALL, cur, (lane + 10) & 31);
+            const uint32_t top = __shfl_sync(LF_ALL, cur, 20);
+            // below 2^37
+            const uint64_t d =
+                lane < 10 ? (uint64_t)cur + 608ull * hi + (lane == 0 ? 369664ull * top : 0ull) : 0ull;
+            // one carry step, the excess of limb 9 folded into limb 0
+            const uint32_t e = (uint32_t)(d >> 26);
+            const uint32_t up = __shfl_up_sync(LF_ALL, e, 1);
+            const uint32_t e9 = __shfl_sync(LF_ALL, e, 9);
+            return lane < 10 ? (uint32_t)(d & LF_M26) + (lane ? up : 608u * e9) : 0u;
+        } else {
+            // columns 10..20 times their table rows (below 2^55)
+            uint64_t d = lane < 10 ? (uint64_t)cur : 0ull;
+#pragma unroll
+            for (int h = 0; h < 11; h++)
+                d += (uint64_t)__shfl_sync(LF_ALL, cur, 10 + h) * g.r[h];
+            // lanes 0..9 below 2^27, the carries past 2^260 at lanes 10 and 11
+            const uint32_t c = (uint32_t)split_carry(d, lane);
+            const uint32_t h10 = __shfl_sync(LF_ALL, c, 10), h11 = __shfl_sync(LF_ALL, c, 11);
+            const uint64_t e = lane < 10 ? (uint64_t)c + (uint64_t)h10 * g.k0 + (uint64_t)h11 * g.k1 : 0ull;
+            // one more carry step; limb 9 keeps its excess (below 2^27 + 2)
+            const uint32_t u1 = __shfl_up_sync(LF_ALL, (uint32_t)(e >> 26) & (uint32_t)LF_M26, 1);
+            const uint32_t u2 = __shfl_up_sync(LF_ALL, (uint32_t)(e >> 52), 2);
+            const uint32_t in = (lane >= 1 ? u1 : 0u) + (lane >= 2 ? u2 : 0u);
+            return lane < 9 ? (uint32_t)(e & LF_M26) + in : (lane == 9 ? (uint32_t)e + in : 0u);
+        }
+    }
+
+    // a - b + Z (zk = g.z) or + 2Z (zk = g.z2): b's limbs must not exceed zk's
+    __device__ __forceinline__ static uint32_t sub(uint32_t a, uint32_t b, uint32_t zk) { return a + zk - b; }
+
+    // eight 32-bit limbs (any value below 2^256) -> this lane's limb
+    __device__ __forceinline__ static uint32_t from_fe(const Fe &a, int lane)
+    {
+        uint32_t v = 0;
+#pragma unroll
+        for (int l = 0; l < 10; l++) {
+            const int bit = 26 * l, w = bit >> 5, off = bit & 31;
+            uint64_t x = a.w[w];
+            if (w + 1 < 8)
+                x |= (uint64_t)a.w[w + 1] << 32;
+            const uint32_t limb = (uint32_t)((x >> off) & LF_M26);
+            v = lane == l ? limb : v;
+        }
+        return v;
+    }
+
+    // -> eight 32-bit limbs, weakly reduced (below 2^256), the same on every lane
+    __device__ __forceinline__ static Fe to_fe(uint32_t v, int lane)
+    {
+        // exact carries: limbs 0..8 below 2^26, limb 9 keeps the excess
+        uint64_t d = lane < 10 ? v : 0u;
+#pragma unroll
+        for (int s = 0; s < 9; s++) {
+            const uint64_t up = __shfl_up_sync(LF_ALL, d >> 26, 1);
+            d = lane < 9 ? (d & LF_M26) + (lane ? up : 0ull) : (lane == 9 ? d + up : 0ull);
+        }
+        uint32_t L[10];
+#pragma unroll
+        for (int l = 0; l < 10; l++)
+            L[l] = (uint32_t)__shfl_sync(LF_ALL, d, l);
+        // pack bits 26 l .. of limb l (limb 9 may reach bit 266)
+        uint32_t t[16];
+#pragma unroll
+        for (int k = 0; k < 16; k++)
+            t[k] = 0;
+#pragma unroll
+        for (int l = 0; l < 10; l++) {
+            const int bit = 26 * l, w = bit >> 5, off = bit & 31;
+            const uint64_t x = (uint64_t)L[l] << off;
+            t[w] |= (uint32_t)x;
+            t[w + 1] |= (uint32_t)(x >> 32);
+        }
+        return F::reduce_wide(t);
+    }
 };
 
-// every lane < width computes f[dst[lane]] = f[a[lane]] * f[b[lane]]
-template <class C>
-__device__ __forceinline__ void lane_products(SlotFile &sf, int width, const int *a, const int *b, const int *dst)
-{
-    using F = typename C::F;
-    const int lane = threadIdx.x & 31;
-    __syncwarp();
-    if (lane < width) {
-        const Fe x = sf.f[a[lane]], y = sf.f[b[lane]];
-        const Fe r = F::mul(x, y);
-        sf.f[dst[lane]] = r;
-    }
-    __syncwarp();
-}
+// The Horner chain on one block of four warps (one per scheduler), the
+// operands in a shared slot file, one slot per field element (lane l reads
+// word l).  A stage of the doubling or addition formula puts its independent
+// products on different warps; the linear steps are done by the warp that
+// needs their result, in registers.  The running total is double-buffered:
+// set s holds X, Y = YA - YB, ZZ, ZZZ, and a doubling or addition writes set
+// s ^ 1.  Limb bounds: products are below 2^27; X, a difference, below
+// 2^29.6; the other product inputs below are sums of at most four products
+// plus Z or 2Z, each below 2^30.1 where the other operand is below 2^29.8.
+enum LaneSlot : int {
+    LX, LYA, LYB, LZZ, LZZZ,  // running total, set 0 (set 1: + LSET)
+    LSET = 5,
+    LV = 10, LM, LW, LS, LM2,                 // doubling
+    LX2, LY2, LZZ2, LZZZ2,                    // addend
+    LU1, LU2, LS1, LS2, LZ12, LZZZ12, LPP, LRR, LPPP, LQ,  // addition
+    LNSLOTS
+};
 
 template <class C>
-__device__ void coop_dbl(SlotFile &sf)
-{
+struct LaneHorner {
     using F = typename C::F;
-    const int lane = threadIdx.x & 31;
-    if (F::is_exact_zero(sf.f[sZZ]))
-        return;  // identity
-    if (lane == 0) {
-        sf.f[sU] = F::dbl(sf.f[sY]);
-        sf.f[sA] = F::sub(sf.f[sX], sf.f[sZZ]);
-        sf.f[sB] = F::add(sf.f[sX], sf.f[sZZ]);
-    }
+    using LF = LaneField<F>;
+    uint32_t (*sl)[32];
+    int lane, warp;
+    typename LF::Regs g;
+    uint32_t z, z2;  // this lane's limbs of Z and 2Z
+
+    __device__ __forceinline__ uint32_t ld(int slot) const { return sl[slot][lane]; }
+    __device__ __forceinline__ void st(int slot, uint32_t v) const { sl[slot][lane] = v; }
+
+    // set s -> set s ^ 1 (the total is not the identity)
+    __device__ void dbl(int s)
     {
-        const int a[2] = {sU, sA}, b[2] = {sU, sB}, d[2] = {sV, sT};
-        lane_products<C>(sf, 2, a, b, d);  // V = U^2, T = (X-ZZ)(X+ZZ)
-    }
-    if (lane == 0) {
-        const Fe t = sf.f[sT];
-        sf.f[sM] = F::add(F::dbl(t), t);  // M = 3(X^2 - ZZ^2), a = -3
-    }
-    {
-        const int a[4] = {sU, sX, sM, sV}, b[4] = {sV, sV, sM, sZZ}, d[4] = {sW, sS, sM2, sZZn};
-        lane_products<C>(sf, 4, a, b, d);  // W = U V, S = X V, M^2, ZZ' = V ZZ
-    }
-    if (lane == 0) {
-        const Fe xn = F::sub(sf.f[sM2], F::dbl(sf.f[sS]));
-        sf.f[sXn] = xn;
-        sf.f[sD] = F::sub(sf.f[sS], xn);
-    }
-    {
-        const int a[3] = {sM, sW, sW}, b[3] = {sD, sZZZ, sY}, d[3] = {sYa, sZZZn, sYb};
-        lane_products<C>(sf, 3, a, b, d);  // M (S - X'), W ZZZ, W Y
-    }
-    if (lane == 0) {
-        sf.f[sX] = sf.f[sXn];
-        sf.f[sY] = F::sub(sf.f[sYa], sf.f[sYb]);
-        sf.f[sZZ] = sf.f[sZZn];
-        sf.f[sZZZ] = sf.f[sZZZn];
-        if (F::is_zero(sf.f[sZZ])) {  // y == 0: no such point on a prime-order curve, kept complete
-            sf.f[sX] = sf.f[sY] = sf.f[sZZ] = sf.f[sZZZ] = F::zero();
+        const int o = s * LSET, n = (s ^ 1) * LSET;
+        if (warp == 0) {
+            const uint32_t y = LF::sub(ld(o + LYA), ld(o + LYB), z);
+            st(LV, LF::mul(y + y, y + y, lane, g));  // V = U^2, U = 2Y
+        } else if (warp == 1) {
+            const uint32_t x = ld(o + LX), zz = ld(o + LZZ);
+            const uint32_t t = LF::mul(LF::sub(x, zz, z), x + zz, lane, g);  // (X - ZZ)(X + ZZ)
+            st(LM, t + t + t);                                            // M = 3(X^2 - ZZ^2), a = -3
         }
+        __syncthreads();
+        if (warp == 0) {
+            const uint32_t y = LF::sub(ld(o + LYA), ld(o + LYB), z);
+            st(LW, LF::mul(y + y, ld(LV), lane, g));  // W = U V
+        } else if (warp == 1) {
+            st(LS, LF::mul(ld(o + LX), ld(LV), lane, g));  // S = X V
+        } else if (warp == 2) {
+            const uint32_t m = ld(LM);
+            st(LM2, LF::mul(m, m, lane, g));  // M^2
+        } else {
+            st(n + LZZ, LF::mul(ld(LV), ld(o + LZZ), lane, g));  // ZZ' = V ZZ
+        }
+        __syncthreads();
+        if (warp == 0) {
+            const uint32_t sv = ld(LS);
+            const uint32_t xn = LF::sub(ld(LM2), sv + sv, z);  // X' = M^2 - 2S
+            st(n + LX, xn);
+            st(n + LYA, LF::mul(ld(LM), LF::sub(sv, xn, z2), lane, g));  // M (S - X')
+        } else if (warp == 1) {
+            st(n + LZZZ, LF::mul(ld(LW), ld(o + LZZZ), lane, g));  // ZZZ' = W ZZZ
+        } else if (warp == 2) {
+            const uint32_t y = LF::sub(ld(o + LYA), ld(o + LYB), z);
+            st(n + LYB, LF::mul(ld(LW), y, lane, g));  // W Y; Y' = M (S - X') - W Y
+        }
+        __syncthreads();
     }
-    __syncwarp();
-}
 
-// total += addend (slots sX2..sZZZ2), complete
+    // set s += addend slots (neither is the identity): 0 -> the sum in set s ^ 1,
+    // 1 -> the operands are equal (the caller doubles), 2 -> they cancel
+    __device__ int add(int s)
+    {
+        const int o = s * LSET, n = (s ^ 1) * LSET;
+        if (warp == 0) {
+            st(LU1, LF::mul(ld(o + LX), ld(LZZ2), lane, g));
+            st(LZ12, LF::mul(ld(o + LZZ), ld(LZZ2), lane, g));
+        } else if (warp == 1) {
+            st(LU2, LF::mul(ld(LX2), ld(o + LZZ), lane, g));
+            st(LZZZ12, LF::mul(ld(o + LZZZ), ld(LZZZ2), lane, g));
+        } else if (warp == 2) {
+            const uint32_t y = LF::sub(ld(o + LYA), ld(o + LYB), z);
+            st(LS1, LF::mul(y, ld(LZZZ2), lane, g));
+        } else {
+            st(LS2, LF::mul(ld(LY2), ld(o + LZZZ), lane, g));
+        }
+        __syncthreads();
+        // P = U2 - U1, R = S2 - S1; every warp tests them (the same answer)
+        const uint32_t pv = LF::sub(ld(LU2), ld(LU1), z), rv = LF::sub(ld(LS2), ld(LS1), z);
+        if (F::is_zero(LF::to_fe(pv, lane)))
+            return F::is_zero(LF::to_fe(rv, lane)) ? 1 : 2;
+        if (warp == 0)
+            st(LPP, LF::mul(pv, pv, lane, g));
+        else if (warp == 1)
+            st(LRR, LF::mul(rv, rv, lane, g));
+        __syncthreads();
+        if (warp == 0)
+            st(LPPP, LF::mul(pv, ld(LPP), lane, g));
+        else if (warp == 1)
+            st(LQ, LF::mul(ld(LU1), ld(LPP), lane, g));
+        else if (warp == 2)
+            st(n + LZZ, LF::mul(ld(LZ12), ld(LPP), lane, g));
+        __syncthreads();
+        if (warp == 0) {
+            const uint32_t q = ld(LQ), ppp = ld(LPPP), rr = ld(LRR);
+            st(n + LX, LF::sub(rr, ppp + q + q, z2));                               // X' = R^2 - PPP - 2Q
+            st(n + LYA, LF::mul(rv, LF::sub(q + q + q + ppp, rr, z), lane, g));  // R (Q - X') = R (3Q + PPP - R^2)
+        } else if (warp == 1) {
+            st(n + LYB, LF::mul(ld(LS1), ld(LPPP), lane, g));  // S1 PPP
+        } else if (warp == 2) {
+            st(n + LZZZ, LF::mul(ld(LZZZ12), ld(LPPP), lane, g));  // ZZZ' = ZZZ12 PPP
+        }
+        __syncthreads();
+        return 0;
+    }
+};
+
+// one block of four warps per MSM of the batch
 template <class C>
-__device__ void coop_add(SlotFile &sf)
+__global__ void __launch_bounds__(128) k_combine(const uint4 *__restrict__ S, const MsmDesc *__restrict__ desc,
+                                                uint32_t *__restrict__ out)
 {
     using F = typename C::F;
-    const int lane = threadIdx.x & 31;
-    if (F::is_exact_zero(sf.f[sZZ2]))
-        return;
-    if (F::is_exact_zero(sf.f[sZZ])) {
-        __syncwarp();
-        if (lane == 0) {
-            sf.f[sX] = sf.f[sX2];
-            sf.f[sY] = sf.f[sY2];
-            sf.f[sZZ] = sf.f[sZZ2];
-            sf.f[sZZZ] = sf.f[sZZZ2];
-        }
-        __syncwarp();
-        return;
-    }
-    {
-        const int a[6] = {sX, sX2, sY, sY2, sZZ, sZZZ}, b[6] = {sZZ2, sZZ, sZZZ2, sZZZ, sZZ2, sZZZ2};
-        const int d[6] = {sU1, sU2, sS1, sS2, sZ12, sZZZ12};
-        lane_products<C>(sf, 6, a, b, d);
-    }
-    if (lane == 0) {
-        sf.f[sP] = F::sub(sf.f[sU2], sf.f[sU1]);
-        sf.f[sR] = F::sub(sf.f[sS2], sf.f[sS1]);
-        sf.flag = F::is_zero(sf.f[sP]) ? (F::is_zero(sf.f[sR]) ? 1 : 2) : 0;
-    }
-    __syncwarp();
-    const int flag = sf.flag;
-    if (flag == 1) {  // same point: double
-        coop_dbl<C>(sf);
-        return;
-    }
-    if (flag == 2) {  // opposite points
-        if (lane == 0)
-            sf.f[sX] = sf.f[sY] = sf.f[sZZ] = sf.f[sZZZ] = F::zero();
-        __syncwarp();
-        return;
-    }
-    {
-        const int a[2] = {sP, sR}, b[2] = {sP, sR}, d[2] = {sPP, sRR};
-        lane_products<C>(sf, 2, a, b, d);
-    }
-    {
-        const int a[3] = {sP, sU1, sZ12}, b[3] = {sPP, sPP, sPP}, d[3] = {sPPP, sQ, sZZn};
-        lane_products<C>(sf, 3, a, b, d);
-    }
-    if (lane == 0) {
-        const Fe xn = F::sub(F::sub(sf.f[sRR], sf.f[sPPP]), F::dbl(sf.f[sQ]));
-        sf.f[sXn] = xn;
-        sf.f[sD] = F::sub(sf.f[sQ], xn);
-    }
-    {
-        const int a[3] = {sR, sS1, sZZZ12}, b[3] = {sD, sPPP, sPPP}, d[3] = {sYa, sYb, sZZZn};
-        lane_products<C>(sf, 3, a, b, d);
-    }
-    if (lane == 0) {
-        sf.f[sX] = sf.f[sXn];
-        sf.f[sY] = F::sub(sf.f[sYa], sf.f[sYb]);
-        sf.f[sZZ] = sf.f[sZZn];
-        sf.f[sZZZ] = sf.f[sZZZn];
-    }
-    __syncwarp();
-}
-
-// one warp per MSM of the batch
-template <class C>
-__global__ void __launch_bounds__(32) k_combine(const uint4 *__restrict__ S, const MsmDesc *__restrict__ desc,
-                                               uint32_t *__restrict__ out)
-{
-    __shared__ SlotFile sf;
-    const int lane = threadIdx.x & 31;
+    using LF = LaneField<F>;
+    __shared__ uint32_t sl[LNSLOTS][32];
     const MsmDesc d = desc[blockIdx.x];
     const uint4 *Sm = S + 8 * (size_t)d.win_base;
-    if (lane == 0) {
-        const Xyzz top = load_xyzz(Sm + 8 * (size_t)(d.Wr - 1));
-        sf.f[sX] = top.X;
-        sf.f[sY] = top.Y;
-        sf.f[sZZ] = top.ZZ;
-        sf.f[sZZZ] = top.ZZZ;
+    if (d.Wr == 1 && d.shift == 0) {  // one window (fixed base): nothing to combine
+        if (threadIdx.x == 0)
+            store_jacobian_canon<C>(out + 24 * (size_t)blockIdx.x, load_xyzz(Sm));
+        return;
     }
-    __syncwarp();
-    for (int k = (int)d.Wr - 2; k >= 0; k--) {
-        for (uint32_t i = 0; i < d.c; i++)
-            coop_dbl<C>(sf);
-        if (lane == 0) {
-            const Xyzz a = load_xyzz(Sm + 8 * (size_t)k);
-            sf.f[sX2] = a.X;
-            sf.f[sY2] = a.Y;
-            sf.f[sZZ2] = a.ZZ;
-            sf.f[sZZZ2] = a.ZZZ;
+    LaneHorner<C> h;
+    h.sl = sl;
+    h.lane = threadIdx.x & 31;
+    h.warp = threadIdx.x >> 5;
+    h.g = LF::regs(h.lane);
+    h.z = h.g.z;
+    h.z2 = h.g.z2;
+    // words 10..31 of every slot stay 0
+    for (int i = threadIdx.x; i < LNSLOTS * 32; i += blockDim.x)
+        (&sl[0][0])[i] = 0;
+    __syncthreads();
+    // Load window sum k into the addend slots (warp w converts coordinate w);
+    // false when it is the identity.  Every thread reads its ZZ to decide.
+    auto load_addend = [&](int k) -> bool {
+        const uint4 *p = Sm + 8 * (size_t)k;
+        if (F::is_exact_zero(load_fe(p + 4)))
+            return false;
+        h.st(LX2 + h.warp, LF::from_fe(load_fe(p + 2 * h.warp), h.lane));  // LX2, LY2, LZZ2, LZZZ2
+        __syncthreads();
+        return true;
+    };
+    // copy the addend into set s as the total
+    auto take_addend = [&](int s) {
+        const int o = s * LSET;
+        if (h.warp == 0) {
+            h.st(o + LX, h.ld(LX2));
+            h.st(o + LYA, h.ld(LY2));
+            h.st(o + LYB, 0u);
+            h.st(o + LZZ, h.ld(LZZ2));
+            h.st(o + LZZZ, h.ld(LZZZ2));
         }
-        __syncwarp();
-        coop_add<C>(sf);
+        __syncthreads();
+    };
+    int s = 0;
+    bool ident = true;
+    for (int k = (int)d.Wr - 1; k >= 0; k--) {
+        if (!ident && k < (int)d.Wr - 1)
+            for (uint32_t i = 0; i < d.c; i++) {
+                h.dbl(s);
+                s ^= 1;
+            }
+        if (!load_addend(k))
+            continue;
+        if (ident) {
+            take_addend(s);
+            ident = false;
+            continue;
+        }
+        const int r = h.add(s);
+        if (r == 0) {
+            s ^= 1;
+        } else if (r == 1) {  // equal operands: double
+            h.dbl(s);
+            s ^= 1;
+        } else {  // they cancel
+            ident = true;
+        }
+        __syncthreads();  // the addend slots are reused by the next window
     }
-    for (uint32_t i = 0; i < d.shift; i++)  // upper window-split half: times 2^(c w_lo)
-        coop_dbl<C>(sf);
-    if (lane == 0) {
-        Xyzz t;
-        t.X = sf.f[sX];
-        t.Y = sf.f[sY];
-        t.ZZ = sf.f[sZZ];
-        t.ZZZ = sf.f[sZZZ];
-        store_jacobian_canon<C>(out + 24 * (size_t)blockIdx.x, t);
+    if (!ident)
+        for (uint32_t i = 0; i < d.shift; i++) {  // upper window-split half: times 2^(c w_lo)
+            h.dbl(s);
+            s ^= 1;
+        }
+    if (h.warp == 0) {
+        Xyzz t = Group<C>::inf();
+        if (!ident) {
+            const int o = s * LSET;
+            t.X = LF::to_fe(h.ld(o + LX), h.lane);
+            t.Y = LF::to_fe(LF::sub(h.ld(o + LYA), h.ld(o + LYB), h.z), h.lane);
+            t.ZZ = LF::to_fe(h.ld(o + LZZ), h.lane);
+            t.ZZZ = LF::to_fe(h.ld(o + LZZZ), h.lane);
+        }
+        if (h.lane == 0)
+            store_jacobian_canon<C>(out + 24 * (size_t)blockIdx.x, t);
     }
 }
 
@@ -1008,8 +1196,8 @@ cudaError_t msm_tail(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
             HS_LAUNCH_CHECK(ctx);
         }
     }
-    // 5. Horner over windows, one warp per MSM
-    k_combine<C><<<p.M, 32, 0, st>>>(b.redS, b.desc, b.out_jac);
+    // 5. Horner over windows, one block of four warps per MSM
+    k_combine<C><<<p.M, 128, 0, st>>>(b.redS, b.desc, b.out_jac);
     HS_LAUNCH_CHECK(ctx);
     return cudaSuccess;
 }
@@ -1483,12 +1671,50 @@ __global__ void k_field_op(int op, const uint4 *__restrict__ a, const uint4 *__r
     store_fe(out + 2 * i, F::canon(r));
 }
 
+// The lane-sliced field of the Horner chain, one warp per element: op 7
+// a*b, 8 (a - b)(a + b) (a subtraction's bound), 9 a^(2^32) by 32 squarings
+// (repeated products of products), 10 the conversion in and out.
+template <class C>
+__global__ void k_field_lane_op(int op, const uint4 *__restrict__ a, const uint4 *__restrict__ b, size_t n,
+                                uint4 *__restrict__ out)
+{
+    using F = typename C::F;
+    using LF = LaneField<F>;
+    const size_t i = blockIdx.x * (size_t)(blockDim.x / 32) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (i >= n)  // whole warps leave together
+        return;
+    const typename LF::Regs g = LF::regs(lane);
+    const uint32_t x = LF::from_fe(load_fe(a + 2 * i), lane);
+    const uint32_t y = op == 7 || op == 8 ? LF::from_fe(load_fe(b + 2 * i), lane) : 0u;
+    uint32_t r;
+    switch (op) {
+    case 7: r = LF::mul(x, y, lane, g); break;
+    case 8: r = LF::mul(LF::sub(x, y, g.z), x + y, lane, g); break;
+    case 9:
+        r = x;
+        for (int k = 0; k < 32; k++)
+            r = LF::mul(r, r, lane, g);
+        break;
+    default: r = x; break;
+    }
+    const Fe f = LF::to_fe(r, lane);
+    if (lane == 0)
+        store_fe(out + 2 * i, F::canon(f));
+}
+
 template <class C>
 cudaError_t field_op(Context &ctx, int op, const void *d_a, const void *d_b, size_t n, void *d_out)
 {
     if (n == 0)
         return cudaSuccess;
     const int threads = 128;
+    if (op >= 7) {
+        k_field_lane_op<C><<<(unsigned)((n + 3) / 4), threads, 0, ctx.stream>>>(op, (const uint4 *)d_a,
+                                                                               (const uint4 *)d_b, n, (uint4 *)d_out);
+        HS_LAUNCH_CHECK(ctx);
+        return cudaSuccess;
+    }
     k_field_op<C><<<(unsigned)((n + threads - 1) / threads), threads, 0, ctx.stream>>>(
         op, (const uint4 *)d_a, (const uint4 *)d_b, n, (uint4 *)d_out);
     HS_LAUNCH_CHECK(ctx);

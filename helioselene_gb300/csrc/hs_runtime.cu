@@ -2424,8 +2424,8 @@ int hs_scalar_mul(hs_context *h, int curve, const uint8_t *scalars, const void *
 
 int hs_field_op(hs_context *h, int field, int op, const uint8_t *a, const uint8_t *b, size_t n, uint8_t *out)
 {
-    const bool binary = op == 0 || op == 2 || op == 3;
-    if (!h || !valid_curve(field) || op < 0 || op > 6 || (n && (!a || !out || (binary && !b))))
+    const bool binary = op == 0 || op == 2 || op == 3 || op == 7 || op == 8;
+    if (!h || !valid_curve(field) || op < 0 || op > 10 || (n && (!a || !out || (binary && !b))))
         return HS_EINVAL;
     if (n == 0)
         return HS_OK;

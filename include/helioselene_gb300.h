@@ -361,7 +361,9 @@ int hs_measure_imad_rates(hs_context *ctx, double rates[4]);
 
 /* Field arithmetic on the device, for validation of the field layer:
  * field HS_HELIOS selects F_p (2^255-19), HS_SELENE selects F_q (2^255-gamma).
- * op: 0 mul, 1 square, 2 add, 3 sub, 4 canonical reduce, 5 invert (0 -> 0), 6 negate.
+ * op: 0 mul, 1 square, 2 add, 3 sub, 4 canonical reduce, 5 invert (0 -> 0), 6 negate;
+ * the lane-sliced form of the window combination: 7 mul, 8 (a - b)(a + b),
+ * 9 a^(2^32) by repeated squaring, 10 conversion in and out (canonical reduce).
  * a, b, out: n little-endian 32-byte values in host memory (b unused for unary ops);
  * inputs may be any 256-bit value, outputs are canonical. */
 int hs_field_op(hs_context *ctx, int field, int op, const uint8_t *a, const uint8_t *b, size_t n, uint8_t *out);

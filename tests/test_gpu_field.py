@@ -75,3 +75,31 @@ def test_chained_products_stay_reduced(ctx, field):
         X = ctx.field_op(field, 0, S, X)
         xs = [(v * v % m) * v % m for v in xs]
     assert from_bytes(X) == xs
+
+
+@pytest.mark.parametrize("field", [0, 1])
+def test_lane_sliced_field_matches_integers(ctx, field):
+    """the window combination's field form (radix-2^26 limbs across a warp's
+    lanes, column products, carry steps and folds by 2^260 mod m) against
+    Python integers, on the weak-reduction edges and random values"""
+    m = MODULI[field]
+    rng = random.Random(field + 71)
+    edges = edge_values(m)
+    a = edges + [rng.getrandbits(256) for _ in range(4000)] + [2**256 - 1 - rng.getrandbits(20) for _ in range(500)]
+    b = list(reversed(edges)) + [rng.getrandbits(256) for _ in range(4000)] + [2**256 - 1 - rng.getrandbits(20)
+                                                                             for _ in range(500)]
+    for x in edges:
+        for y in edges:
+            a.append(x)
+            b.append(y)
+    A, B = to_bytes(a), to_bytes(b)
+    checks = {
+        7: [(x * y) % m for x, y in zip(a, b)],
+        8: [((x - y) * (x + y)) % m for x, y in zip(a, b)],
+        9: [pow(x, 2**32, m) for x in a],
+        10: [x % m for x in a],
+    }
+    for op, want in checks.items():
+        got = from_bytes(ctx.field_op(field, op, A, B))
+        bad = [i for i, (g, w) in enumerate(zip(got, want)) if g != w]
+        assert not bad, f"field {field} op {op}: {len(bad)} mismatches, first a={a[bad[0]]:#x} b={b[bad[0]]:#x}"
