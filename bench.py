@@ -924,7 +924,10 @@ def run_ours(args) -> None:
     head_split = 0 if args.split is None else args.split
     ctx.set_split(head_split)
     ctx2.set_split(head_split)
-    ctx2.set_priority(True)
+    if args.priority == "selene":
+        ctx2.set_priority(True)
+    elif args.priority == "helios":
+        ctx.set_priority(True)
     # the accumulation form of each curve (batch-affine rounds): the library's
     # defaults, or set for every kind of plan by --ba-rounds
     rr = list(DEFAULT_BA_ROUNDS)
@@ -1136,7 +1139,8 @@ def run_ours(args) -> None:
             "vs_baseline": None, "dtype": "u32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "n": n, "curves": ["helios", "selene"], "parallelism": f"replicas{ws}",
                        "window_split_min_points": head_split,
-                       "streams": "Helios and Selene MSMs on two context streams, Selene's of high priority",
+                       "streams": "Helios and Selene MSMs on two context streams" + (
+                           f", {args.priority.capitalize()}'s of high priority" if args.priority != "none" else ""),
                        "l2": "inputs of one step (2 x 96 MiB scalars + bases, plus the bucket workspaces) exceed "
                              "L2 (129 MB); steps are issued back to back and the events bracket all K of them",
                        "isolated_ms_per_step": isolated_ms,
@@ -1319,6 +1323,8 @@ def main() -> None:
     ap.add_argument("--no-tree", action="store_true", help="skip the FCMP++ tree-hash layer section")
     ap.add_argument("--no-verify", action="store_true", help="skip the FCMP++ verification-batch section")
     ap.add_argument("--no-scalar-mul", action="store_true", help="skip the independent scalar-multiplication section")
+    ap.add_argument("--priority", default="selene", choices=["selene", "helios", "none"],
+                    help="the curve whose context stream gets the high priority in the throughput step")
     ap.add_argument("--ba-rounds", default=None,
                     help="batch-affine accumulation rounds for plans of >= 2^21 entries, one value for both curves "
                          "or 'helios,selene' (0: XYZZ; default: the library's)")
