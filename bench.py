@@ -54,7 +54,7 @@ ACC_TRAFFIC = {
     1: {"bytes": (2923.5e6, 2941.9e6),
         "capture": "2026-12-04, commit d2e236f, k_ba_pairs + k_ba_invert + k_ba_finish + k_accumulate_level"},
 }
-DEFAULT_BA_ROUNDS = (1, 1)  # the library's default accumulation form of device-resident MSMs (Helios, Selene)
+DEFAULT_BA_ROUNDS = (1, 2)  # the library's default accumulation form of device-resident MSMs (Helios, Selene)
 HOST_BA_ROUNDS = (0, 1)     # ... and of single MSMs from host buffers
 SPLIT_DEFAULT = 1 << 18  # the library's window-split threshold for single MSMs
 
@@ -847,18 +847,22 @@ def executed_per_entry(rounds: int, curve: int) -> float:
     return sum(pair / 2**r for r in range(1, rounds + 1)) + madd / 2**rounds
 
 
+def _traffic(rounds: int, c: int):
+    t = ACC_TRAFFIC.get(rounds)
+    return (t["bytes"][c], t["capture"]) if t and t["bytes"][c] is not None else (None, None)
+
+
 def traffic_of(rr) -> float:
     """the captured accumulation-phase DRAM bytes per MSM, mean of the curves (None if not captured)"""
-    vals = [ACC_TRAFFIC[rr[c]]["bytes"][c] for c in (0, 1) if rr[c] in ACC_TRAFFIC]
-    return sum(vals) / len(vals) if len(vals) == 2 else None
+    vals = [_traffic(rr[c], c)[0] for c in (0, 1)]
+    return sum(vals) / 2 if None not in vals else None
 
 
 def traffic_source(rr) -> str:
     parts = []
     for c, name in ((0, "Helios"), (1, "Selene")):
-        t = ACC_TRAFFIC.get(rr[c])
-        parts.append(f"{name}: " + (f"{t['bytes'][c] / 1e6:.1f} MB, ncu capture {t['capture']}" if t else
-                                    "no capture of this form"))
+        b, cap = _traffic(rr[c], c)
+        parts.append(f"{name}: " + (f"{b / 1e6:.1f} MB, ncu capture {cap}" if b else "no capture of this form"))
     return "; ".join(parts)
 
 

@@ -109,9 +109,9 @@ class Context:
                         "set_batch_affine")
 
     def default_batch_affine(self) -> None:
-        """the library's default accumulation forms: one batch-affine round on both curves,
-        except fixed-base commitments and single MSMs from host buffers, which take none on
-        Helios and one on Selene"""
+        """the library's default accumulation forms: one batch-affine round on Helios and two
+        on Selene, except fixed-base commitments and single MSMs from host buffers, which
+        take none on Helios and one on Selene"""
         self.set_batch_affine(-1)
 
     # -- instrumentation --

@@ -47,9 +47,10 @@ struct GraphEntry {
     void *d_desc = nullptr;  // the batch descriptors, uploaded once at capture
 };
 
-// the library's batch-affine default for a curve's plans (below: the kinds of
-// plans that take their own until hs_context_set_batch_affine sets the curve)
-constexpr uint32_t BA_DEFAULT_ROUNDS = 1;
+// the library's batch-affine default for a curve's plans: one round on
+// Helios, two on Selene (Context: the kinds of plans that take their own
+// until hs_context_set_batch_affine sets the curve)
+constexpr uint32_t BA_DEFAULT_ROUNDS[2] = {1, 2};
 constexpr uint64_t BA_DEFAULT_MIN_ENTRIES = uint64_t(1) << 21;
 
 struct Context {
@@ -69,14 +70,15 @@ struct Context {
     // input events (recorded outside the capture) become external event waits
     bool capturing_host = false;
     size_t split_min = size_t(1) << 18;  // single MSMs this large run as two window halves (0: never)
-    // Batch-affine accumulation per curve: rounds (0: off) for plans of at least
-    // ba_min_entries entries.  Measured at n = 2^20 on GB300 (accumulation per
-    // MSM, ms): Selene 2.54 -> 2.39 with one round, Helios 1.54 -> 1.61; for a
-    // Helios and a Selene MSM side by side on two streams (the throughput form)
-    // one round on both curves is fastest (5.15 ms per pair against 5.37 with
-    // none): one curve's memory-bound round overlaps the other's
-    // multiply-bound work.
-    uint32_t ba_rounds[2] = {BA_DEFAULT_ROUNDS, BA_DEFAULT_ROUNDS};
+    // Batch-affine accumulation per curve: rounds (0: off) for plans of at
+    // least ba_min_entries entries.  Measured at n = 2^20 on GB300
+    // (accumulation per MSM, ms): Selene 2.54 -> 2.29 with one round, 2.27
+    // with two; Helios 1.55 -> 1.56 with one.  For a Helios and a Selene MSM
+    // side by side on two streams, back to back (the throughput form): 4.78
+    // ms per pair with one round on Helios and two on Selene, 5.07 with one on
+    // both, 5.06 with none on Helios: one curve's memory-bound rounds overlap
+    // the other's multiply-bound work.
+    uint32_t ba_rounds[2] = {BA_DEFAULT_ROUNDS[0], BA_DEFAULT_ROUNDS[1]};
     uint64_t ba_min_entries[2] = {BA_DEFAULT_MIN_ENTRIES, BA_DEFAULT_MIN_ENTRIES};
     // Until hs_context_set_batch_affine sets a curve, two kinds of plans take
     // their own rounds, because there a curve's MSMs run mostly alone, where

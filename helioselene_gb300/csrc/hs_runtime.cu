@@ -1862,7 +1862,7 @@ int hs_context_set_batch_affine(hs_context *h, int curve, int rounds, size_t min
     drop_graphs(ctx);
     const int k = curve == HS_SELENE;
     if (rounds < 0) {  // the library's defaults
-        ctx.ba_rounds[k] = BA_DEFAULT_ROUNDS;
+        ctx.ba_rounds[k] = BA_DEFAULT_ROUNDS[k];
         ctx.ba_min_entries[k] = BA_DEFAULT_MIN_ENTRIES;
         ctx.ba_set[k] = false;
         return HS_OK;

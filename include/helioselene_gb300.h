@@ -92,10 +92,10 @@ void *hs_context_stream(hs_context *ctx);
  * bucket additions), then an XYZZ fold of what is left; 0 keeps the XYZZ mixed
  * additions of every entry (helios/src/x64/helios_msm_vartime.cpp:296-325 is
  * the bucket loop both replace).  Results are identical either way.  Default:
- * one round on both curves, from 2^21 entries, except in two kinds of plans
- * where a curve's MSMs mostly run alone: fixed-base commitments and single
- * MSMs from host buffers take no round on Helios and one on Selene, until this
- * call sets the curve.  rounds = -1 restores the defaults.  Host-input calls
+ * one round on Helios and two on Selene, from 2^21 entries, except in two
+ * kinds of plans where a curve's MSMs mostly run alone: fixed-base commitments
+ * and single MSMs from host buffers take no round on Helios and one on
+ * Selene, until this call sets the curve.  rounds = -1 restores the defaults.  Host-input calls
  * send their bases in two parts either way: with rounds, each part's entries
  * of a bucket form their own list, whose rounds run once that part is in. */
 int hs_context_set_batch_affine(hs_context *ctx, int curve, int rounds, size_t min_entries);
