@@ -50,9 +50,13 @@ IMAD_PER_MODMUL = {0: 144, 1: 232}  # F_p, F_q: 2 IMAD per 32x32->64 product
 # workload, by accumulation form (batch-affine rounds): 0 is k_accumulate, 1 is
 # k_ba_pairs + k_ba_invert + k_ba_finish + k_accumulate_level
 ACC_TRAFFIC = {
-    0: {"bytes": (477.2e6, 497.5e6), "capture": "2026-12-04, commit 14d24da, k_accumulate"},
-    1: {"bytes": (2923.5e6, 2941.9e6),
-        "capture": "2026-12-04, commit d2e236f, k_ba_pairs + k_ba_invert + k_ba_finish + k_accumulate_level"},
+    0: {"bytes": (477.2e6, 497.5e6), "capture": ("2026-12-04, commit 14d24da, k_accumulate",) * 2},
+    1: {"bytes": (2916.1e6, 2941.9e6),
+        "capture": ("2026-12-04, commit f0491f5, k_ba_pairs + k_ba_invert + k_ba_finish + k_accumulate_level",
+                    "2026-12-04, commit d2e236f, k_ba_pairs + k_ba_invert + k_ba_finish + k_accumulate_level")},
+    2: {"bytes": (None, 4316.5e6),
+        "capture": (None, "2026-12-04, commit f0491f5, two rounds of k_ba_pairs + k_ba_invert + k_ba_finish, "
+                          "then k_accumulate_level")},
 }
 DEFAULT_BA_ROUNDS = (1, 2)  # the library's default accumulation form of device-resident MSMs (Helios, Selene)
 HOST_BA_ROUNDS = (0, 1)     # ... and of single MSMs from host buffers
@@ -849,7 +853,7 @@ def executed_per_entry(rounds: int, curve: int) -> float:
 
 def _traffic(rounds: int, c: int):
     t = ACC_TRAFFIC.get(rounds)
-    return (t["bytes"][c], t["capture"]) if t and t["bytes"][c] is not None else (None, None)
+    return (t["bytes"][c], t["capture"][c]) if t and t["bytes"][c] is not None else (None, None)
 
 
 def traffic_of(rr) -> float:
