@@ -1070,6 +1070,238 @@ __global__ void __launch_bounds__(128) k_combine(const uint4 *__restrict__ S, co
     }
 }
 
+// Point operations on groups of eight lanes (four groups per warp): the
+// independent products of a formula stage run on different lanes of the group,
+// each in eight 32-bit limbs, so an addition is 4 product stages and a
+// doubling 3, against 14 and 9 products in sequence on one thread; the linear
+// steps are done by the group's lane 0.  Each group keeps its points and
+// temporaries in its own shared slot file and synchronises only its own lanes,
+// so groups may take different branches.  The formulas are Group's (add-2008-s,
+// dbl-2008-s-1 with a = -3), complete.
+enum GroupSlot : int {
+    GRUN = 0, GACC = 4, GTMP = 8,  // points: X, Y, ZZ, ZZZ at base + 0..3
+    GU = 12, GV, GW, GS, GM, GM2, GT, GA, GB, GD, GYA, GYB, GXN, GZZN, GZZZN,
+    GU1, GU2, GS1, GS2, GZ12, GZZZ12, GP, GR, GPP, GRR, GPPP, GQ,
+    GNSLOTS
+};
+
+struct GroupSlots {
+    Fe f[GNSLOTS];
+    int flag;
+};
+
+template <class C>
+struct Group8 {
+    using F = typename C::F;
+    GroupSlots *sf;
+    int gl;          // lane within the group
+    unsigned gmask;  // the group's lanes in the warp
+
+    __device__ __forceinline__ void sync() const { __syncwarp(gmask); }
+
+    // slot lists packed six bits per lane: lane k's slot is bits 6k..6k+5
+    __device__ __forceinline__ static constexpr uint64_t pk(int s0, int s1 = 0, int s2 = 0, int s3 = 0, int s4 = 0,
+                                                           int s5 = 0)
+    {
+        return (uint64_t)s0 | (uint64_t)s1 << 6 | (uint64_t)s2 << 12 | (uint64_t)s3 << 18 | (uint64_t)s4 << 24 |
+               (uint64_t)s5 << 30;
+    }
+
+    // lanes gl < width: f[d[gl]] = f[a[gl]] * f[b[gl]]
+    __device__ __forceinline__ void products(int width, uint64_t a, uint64_t b, uint64_t d) const
+    {
+        sync();
+        if (gl < width) {
+            const int sh = 6 * gl;
+            const Fe x = sf->f[(a >> sh) & 63], y = sf->f[(b >> sh) & 63];
+            sf->f[(d >> sh) & 63] = F::mul(x, y);
+        }
+        sync();
+    }
+
+    __device__ __forceinline__ bool is_inf(int base) const { return F::is_exact_zero(sf->f[base + 2]); }
+
+    __device__ __forceinline__ void set_inf(int base) const
+    {
+        sync();
+        if (gl < 4)
+            sf->f[base + gl] = F::zero();
+        sync();
+    }
+
+    __device__ __forceinline__ void copy(int dst, int src) const
+    {
+        sync();
+        if (gl < 4)
+            sf->f[dst + gl] = sf->f[src + gl];
+        sync();
+    }
+
+    // p = 2p (p at base)
+    __device__ void dbl(int base) const
+    {
+        sync();
+        if (is_inf(base))
+            return;
+        const int X = base, Y = base + 1, ZZ = base + 2, ZZZ = base + 3;
+        if (gl == 0) {
+            sf->f[GU] = F::dbl(sf->f[Y]);
+            sf->f[GA] = F::sub(sf->f[X], sf->f[ZZ]);
+            sf->f[GB] = F::add(sf->f[X], sf->f[ZZ]);
+        }
+        products(2, pk(GU, GA), pk(GU, GB), pk(GV, GT));  // V = U^2, T = (X - ZZ)(X + ZZ)
+        if (gl == 0) {
+            const Fe t = sf->f[GT];
+            sf->f[GM] = F::add(F::dbl(t), t);  // M = 3(X^2 - ZZ^2), a = -3
+        }
+        // W = U V, S = X V, M^2, ZZ' = V ZZ
+        products(4, pk(GU, X, GM, GV), pk(GV, GV, GM, ZZ), pk(GW, GS, GM2, GZZN));
+        if (gl == 0) {
+            const Fe xn = F::sub(sf->f[GM2], F::dbl(sf->f[GS]));
+            sf->f[GXN] = xn;
+            sf->f[GD] = F::sub(sf->f[GS], xn);
+        }
+        products(3, pk(GM, GW, GW), pk(GD, ZZZ, Y), pk(GYA, GZZZN, GYB));  // M (S - X'), W ZZZ, W Y
+        if (gl == 0) {
+            sf->f[X] = sf->f[GXN];
+            sf->f[Y] = F::sub(sf->f[GYA], sf->f[GYB]);
+            sf->f[ZZ] = sf->f[GZZN];
+            sf->f[ZZZ] = sf->f[GZZZN];
+            if (F::is_zero(sf->f[ZZ]))  // y = 0: no such point on a prime-order curve, kept complete
+                sf->f[X] = sf->f[Y] = sf->f[ZZ] = sf->f[ZZZ] = F::zero();
+        }
+        sync();
+    }
+
+    // p += q (p at dst, q at src)
+    __device__ void add(int dst, int src) const
+    {
+        sync();
+        if (is_inf(src))
+            return;
+        if (is_inf(dst)) {
+            copy(dst, src);
+            return;
+        }
+        const int X1 = dst, Y1 = dst + 1, ZZ1 = dst + 2, ZZZ1 = dst + 3;
+        const int X2 = src, Y2 = src + 1, ZZ2 = src + 2, ZZZ2 = src + 3;
+        products(6, pk(X1, X2, Y1, Y2, ZZ1, ZZZ1), pk(ZZ2, ZZ1, ZZZ2, ZZZ1, ZZ2, ZZZ2),
+                 pk(GU1, GU2, GS1, GS2, GZ12, GZZZ12));
+        if (gl == 0) {
+            sf->f[GP] = F::sub(sf->f[GU2], sf->f[GU1]);
+            sf->f[GR] = F::sub(sf->f[GS2], sf->f[GS1]);
+            sf->flag = F::is_zero(sf->f[GP]) ? (F::is_zero(sf->f[GR]) ? 1 : 2) : 0;
+        }
+        sync();
+        const int flag = sf->flag;
+        if (flag == 1) {  // equal points: double
+            dbl(dst);
+            return;
+        }
+        if (flag == 2) {  // opposite points
+            set_inf(dst);
+            return;
+        }
+        products(2, pk(GP, GR), pk(GP, GR), pk(GPP, GRR));
+        products(3, pk(GP, GU1, GZ12), pk(GPP, GPP, GPP), pk(GPPP, GQ, GZZN));
+        if (gl == 0) {
+            const Fe xn = F::sub(F::sub(sf->f[GRR], sf->f[GPPP]), F::dbl(sf->f[GQ]));
+            sf->f[GXN] = xn;
+            sf->f[GD] = F::sub(sf->f[GQ], xn);
+        }
+        products(3, pk(GR, GS1, GZZZ12), pk(GD, GPPP, GPPP), pk(GYA, GYB, GZZZN));
+        if (gl == 0) {
+            sf->f[X1] = sf->f[GXN];
+            sf->f[Y1] = F::sub(sf->f[GYA], sf->f[GYB]);
+            sf->f[ZZ1] = sf->f[GZZN];
+            sf->f[ZZZ1] = sf->f[GZZZN];
+        }
+        sync();
+    }
+};
+
+// Window sums of a plan of few windows of at most WG_MAX_B buckets, where the
+// two-level reduction's chains of one-thread additions set the time: one block
+// of WG_GROUPS eight-lane groups per window, group g taking the q = B / groups
+// buckets [g q, (g + 1) q):
+//     run_g = sum_j B_j,   acc_g = sum_j (j - g q + 1) B_j   (top-down running sum),
+// then S = sum_g acc_g + q sum_{g >= 1} R_g with R_g = sum_{h >= g} run_h (a
+// suffix scan over the groups), q R_g by doublings, and a tree sum.
+constexpr int WG_GROUPS = 32;
+constexpr uint32_t WG_MAX_B = 256;
+
+template <class C>
+__global__ void __launch_bounds__(WG_GROUPS * 8) k_window_groups(const uint32_t *__restrict__ seg_off,
+                                                                const uint4 *__restrict__ seg_sum,
+                                                                const MsmDesc *__restrict__ desc, uint32_t M,
+                                                                uint4 *__restrict__ S)
+{
+    __shared__ GroupSlots sl[WG_GROUPS];
+    const uint32_t s = blockIdx.x;
+    const uint32_t mi = find_msm(M, s, [&](uint32_t k) { return desc[k].win_base; });
+    const MsmDesc d = desc[mi];
+    const uint32_t k = s - d.win_base;
+    const uint32_t g = threadIdx.x >> 3;
+    Group8<C> op;
+    op.sf = &sl[g];
+    op.gl = (int)(threadIdx.x & 7);
+    op.gmask = 0xffu << (8 * (g & 3));
+    const uint32_t nga = d.B < (uint32_t)WG_GROUPS ? d.B : (uint32_t)WG_GROUPS;  // B is a power of two
+    const uint32_t q = d.B / nga;
+    const bool active = g < nga;
+    op.set_inf(GRUN);
+    op.set_inf(GACC);
+    if (active) {
+        for (int j = (int)((g + 1) * q) - 1; j >= (int)(g * q); j--) {
+            const uint32_t kb = d.bucket_base + k * d.B + (uint32_t)j;
+            const uint32_t s0 = seg_off[kb];
+            if (seg_off[kb + 1] != s0) {
+                op.sync();
+                if (op.gl < 4)
+                    op.sf->f[GTMP + op.gl] = load_fe(seg_sum + 8 * (size_t)s0 + 2 * op.gl);
+                op.add(GRUN, GTMP);
+            }
+            op.add(GACC, GRUN);
+        }
+    }
+    __syncthreads();
+    for (uint32_t dl = 1; dl < nga; dl <<= 1) {  // R_g
+        const bool take = active && g + dl < nga;
+        if (take && op.gl < 4)
+            op.sf->f[GTMP + op.gl] = sl[g + dl].f[GRUN + op.gl];
+        __syncthreads();
+        if (take)
+            op.add(GRUN, GTMP);
+        __syncthreads();
+    }
+    if (active) {  // v_g = q R_g [g >= 1] + acc_g, in GRUN
+        if (g >= 1) {
+            for (uint32_t m = q; m > 1; m >>= 1)
+                op.dbl(GRUN);
+        } else {
+            op.set_inf(GRUN);
+        }
+        op.add(GRUN, GACC);
+    }
+    __syncthreads();
+    for (uint32_t st = nga / 2; st > 0; st >>= 1) {
+        if (g < st) {
+            if (op.gl < 4)
+                op.sf->f[GTMP + op.gl] = sl[g + st].f[GRUN + op.gl];
+            op.add(GRUN, GTMP);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        Xyzz t;
+        t.X = sl[0].f[GRUN];
+        t.Y = sl[0].f[GRUN + 1];
+        t.ZZ = sl[0].f[GRUN + 2];
+        t.ZZZ = sl[0].f[GRUN + 3];
+        store_xyzz(S + 8 * (size_t)s, t);
+    }
+}
+
 template <class C>
 cudaError_t msm_tail(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
 {
@@ -1169,8 +1401,13 @@ cudaError_t msm_tail(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
         k_merge_heavy<C><<<ctx.sm_count, HEAVY_THREADS, 0, st>>>(b.seg_off, b.heavy, b.heavy_n, b.seg_sum);
         HS_LAUNCH_CHECK(ctx);
     }
-    // 4. bucket reduction: group running sums, then one block per window
-    {
+    // 4. bucket reduction: group running sums, then one block per window; a
+    //    plan of few windows of at most WG_MAX_B buckets reduces each window on
+    //    one block of eight-lane groups
+    if (p.max_B <= WG_MAX_B && p.WS <= 4u * (uint32_t)ctx.sm_count) {
+        k_window_groups<C><<<p.WS, WG_GROUPS * 8, 0, st>>>(b.seg_off, b.seg_sum, b.desc, p.M, b.redS);
+        HS_LAUNCH_CHECK(ctx);
+    } else {
         const int threads = 128;
         k_reduce_groups<C><<<(p.G + threads - 1) / threads, threads, 0, st>>>(b.seg_off, b.seg_sum, b.desc, p.M,
                                                                             p.G, b.redA);
