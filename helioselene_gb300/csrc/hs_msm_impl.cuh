@@ -833,17 +833,17 @@ struct LaneField {
     // -> eight 32-bit limbs, weakly reduced (below 2^256), the same on every lane
     __device__ __forceinline__ static Fe to_fe(uint32_t v, int lane)
     {
-        // exact carries: limbs 0..8 below 2^26, limb 9 keeps the excess
-        uint64_t d = lane < 10 ? v : 0u;
-#pragma unroll
-        for (int s = 0; s < 9; s++) {
-            const uint64_t up = __shfl_up_sync(LF_ALL, d >> 26, 1);
-            d = lane < 9 ? (d & LF_M26) + (lane ? up : 0ull) : (lane == 9 ? d + up : 0ull);
-        }
+        // every lane gathers the limbs (below 2^32), then carries exactly in
+        // registers: limbs 0..8 below 2^26, limb 9 keeps the excess
         uint32_t L[10];
 #pragma unroll
         for (int l = 0; l < 10; l++)
-            L[l] = (uint32_t)__shfl_sync(LF_ALL, d, l);
+            L[l] = __shfl_sync(LF_ALL, v, l);
+#pragma unroll
+        for (int l = 0; l < 9; l++) {
+            L[l + 1] += L[l] >> 26;
+            L[l] &= (uint32_t)LF_M26;
+        }
         // pack bits 26 l .. of limb l (limb 9 may reach bit 266)
         uint32_t t[16];
 #pragma unroll
@@ -931,15 +931,13 @@ struct LaneHorner {
 
     // set s += addend slots (neither is the identity): 0 -> the sum in set s ^ 1,
     // 1 -> the operands are equal (the caller doubles), 2 -> they cancel
-    __device__ int add(int s)
+    __device__ int add(int s, int *flag)
     {
         const int o = s * LSET, n = (s ^ 1) * LSET;
         if (warp == 0) {
             st(LU1, LF::mul(ld(o + LX), ld(LZZ2), lane, g));
-            st(LZ12, LF::mul(ld(o + LZZ), ld(LZZ2), lane, g));
         } else if (warp == 1) {
             st(LU2, LF::mul(ld(LX2), ld(o + LZZ), lane, g));
-            st(LZZZ12, LF::mul(ld(o + LZZZ), ld(LZZZ2), lane, g));
         } else if (warp == 2) {
             const uint32_t y = LF::sub(ld(o + LYA), ld(o + LYB), z);
             st(LS1, LF::mul(y, ld(LZZZ2), lane, g));
@@ -947,15 +945,25 @@ struct LaneHorner {
             st(LS2, LF::mul(ld(LY2), ld(o + LZZZ), lane, g));
         }
         __syncthreads();
-        // P = U2 - U1, R = S2 - S1; every warp tests them (the same answer)
+        // P = U2 - U1, R = S2 - S1: their squares and ZZ1 ZZ2, ZZZ1 ZZZ2 while
+        // warp 3 also tests P and R for zero (rare: then the products go unused)
         const uint32_t pv = LF::sub(ld(LU2), ld(LU1), z), rv = LF::sub(ld(LS2), ld(LS1), z);
-        if (F::is_zero(LF::to_fe(pv, lane)))
-            return F::is_zero(LF::to_fe(rv, lane)) ? 1 : 2;
-        if (warp == 0)
+        if (warp == 0) {
             st(LPP, LF::mul(pv, pv, lane, g));
-        else if (warp == 1)
+        } else if (warp == 1) {
             st(LRR, LF::mul(rv, rv, lane, g));
+        } else if (warp == 2) {
+            st(LZ12, LF::mul(ld(o + LZZ), ld(LZZ2), lane, g));
+        } else {
+            st(LZZZ12, LF::mul(ld(o + LZZZ), ld(LZZZ2), lane, g));
+            const int f = F::is_zero(LF::to_fe(pv, lane)) ? (F::is_zero(LF::to_fe(rv, lane)) ? 1 : 2) : 0;
+            if (lane == 0)
+                *flag = f;
+        }
         __syncthreads();
+        const int f = *flag;
+        if (f)
+            return f;
         if (warp == 0)
             st(LPPP, LF::mul(pv, ld(LPP), lane, g));
         else if (warp == 1)
@@ -985,6 +993,7 @@ __global__ void __launch_bounds__(128) k_combine(const uint4 *__restrict__ S, co
     using F = typename C::F;
     using LF = LaneField<F>;
     __shared__ uint32_t sl[LNSLOTS][32];
+    __shared__ int add_flag;
     const MsmDesc d = desc[blockIdx.x];
     const uint4 *Sm = S + 8 * (size_t)d.win_base;
     if (d.Wr == 1 && d.shift == 0) {  // one window (fixed base): nothing to combine
@@ -1040,7 +1049,7 @@ __global__ void __launch_bounds__(128) k_combine(const uint4 *__restrict__ S, co
             ident = false;
             continue;
         }
-        const int r = h.add(s);
+        const int r = h.add(s, &add_flag);
         if (r == 0) {
             s ^= 1;
         } else if (r == 1) {  // equal operands: double
