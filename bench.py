@@ -26,6 +26,8 @@ workload, rank 0 only.
 from __future__ import annotations
 
 import argparse
+import contextlib
+import gc
 import json
 import os
 import statistics
@@ -61,6 +63,22 @@ ACC_TRAFFIC = {
 DEFAULT_BA_ROUNDS = (1, 2)  # the library's default accumulation form of device-resident MSMs (Helios, Selene)
 HOST_BA_ROUNDS = (0, 1)     # ... and of single MSMs from host buffers
 SPLIT_DEFAULT = 1 << 18  # the library's window-split threshold for single MSMs
+
+
+@contextlib.contextmanager
+def no_python_gc():
+    """Python's cyclic garbage collector paused around a host-timed loop: a full
+    collection in a process holding torch's objects takes 10-20 ms and landed in
+    about one run in six as a single slow step.  The library's calls are native
+    code; the pause is the harness's, not theirs."""
+    gc.collect()
+    gc.freeze()
+    gc.disable()
+    try:
+        yield
+    finally:
+        gc.enable()
+        gc.unfreeze()
 
 
 def modmul_count(n: int) -> tuple:
@@ -372,16 +390,17 @@ def run_serving(hs, torch, device: str, local: int, requests_per_rate: int = 100
         if arrivals is None:
             arrivals = np.cumsum(rng.exponential(1.0 / rate, len(reqs))) if rate else np.zeros(len(reqs))
         tickets = []
-        t0 = time.perf_counter()
-        for r, at in zip(reqs, arrivals):
-            delay = at - (time.perf_counter() - t0)
-            if delay > 0:
-                time.sleep(delay)
-            curve, sc, idx, fr = views(r)
-            tickets.append(srv.submit(curve, sc, idx, fr))
-        done = [srv.wait(t, 600000) for t in tickets]
+        with no_python_gc():
+            t0 = time.perf_counter()
+            for r, at in zip(reqs, arrivals):
+                delay = at - (time.perf_counter() - t0)
+                if delay > 0:
+                    time.sleep(delay)
+                curve, sc, idx, fr = views(r)
+                tickets.append(srv.submit(curve, sc, idx, fr))
+            done = [srv.wait(t, 600000) for t in tickets]
+            wall = time.perf_counter() - t0
         lat = [d[1] for d in done]
-        wall = time.perf_counter() - t0
         if results is not None:
             results.extend(d[0] for d in done)
         return {"rate_offered": rate or "all-at-once", "requests": len(reqs), "msms_per_s": len(reqs) / wall,
@@ -1086,22 +1105,24 @@ def run_ours(args) -> None:
             for f in [pool.submit(ctxs[c].msm, *args_of[c]) for c in (hs.SELENE, hs.HELIOS)]:
                 f.result()
         e2e_step_ms = []
-        t0 = time.perf_counter()
-        for _ in range(e2e_steps):
-            ts = time.perf_counter()
-            for f in [pool.submit(ctxs[c].msm, *args_of[c]) for c in (hs.SELENE, hs.HELIOS)]:
-                f.result()
-            e2e_step_ms.append((time.perf_counter() - ts) * 1e3)
-        e2e_s = (time.perf_counter() - t0) / e2e_steps
+        with no_python_gc():
+            t0 = time.perf_counter()
+            for _ in range(e2e_steps):
+                ts = time.perf_counter()
+                for f in [pool.submit(ctxs[c].msm, *args_of[c]) for c in (hs.SELENE, hs.HELIOS)]:
+                    f.result()
+                e2e_step_ms.append((time.perf_counter() - ts) * 1e3)
+            e2e_s = (time.perf_counter() - t0) / e2e_steps
     for c in ctxs.values():
         c.set_split(head_split)
     # the same pair as one hs_msm_batch call (both curves, one context)
     pair = [(c, data[c]["h_sc"].numpy(), data[c]["h_jac"].numpy()) for c in (hs.SELENE, hs.HELIOS)]
     ctx.msm_batch(pair, hs.FMT_JACOBIAN51, hs.FMT_JACOBIAN51)
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        ctx.msm_batch(pair, hs.FMT_JACOBIAN51, hs.FMT_JACOBIAN51)
-    e2e_batch_s = (time.perf_counter() - t0) / e2e_steps
+    with no_python_gc():
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            ctx.msm_batch(pair, hs.FMT_JACOBIAN51, hs.FMT_JACOBIAN51)
+        e2e_batch_s = (time.perf_counter() - t0) / e2e_steps
     if dist:
         t = torch.tensor([e2e_s], dtype=torch.float64, device=device)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -1162,6 +1183,7 @@ def run_ours(args) -> None:
                     "api": "hs_msm(point_fmt=HS_FMT_JACOBIAN51, out_fmt=HS_FMT_JACOBIAN51), pinned host buffers",
                     "calls": "one per curve from a pool of two host threads, Selene first", "window_split_min": e2e_split,
                     "ba_rounds": {"helios": rr_host[0], "selene": rr_host[1]},
+                    "python_gc": "paused during the timed steps (collected and frozen first)",
                     "step_ms": {"median": statistics.median(e2e_step_ms), "min": min(e2e_step_ms),
                                 "max": max(e2e_step_ms), "all": [round(t, 3) for t in e2e_step_ms]},
                     "median_step_value": ws * 2 * n / (statistics.median(e2e_step_ms) * 1e-3),
