@@ -1227,6 +1227,82 @@ struct Group8 {
         }
         sync();
     }
+
+    // p = 2 (x, y) for the affine point at src (x, y at src, src + 1), into dst
+    // (mdbl-2008-s-1, M = 3 x^2 - 3)
+    __device__ void dbl_affine(int dst, int src) const
+    {
+        sync();
+        if (gl == 0)
+            sf->f[GU] = F::dbl(sf->f[src + 1]);
+        products(2, pk(GU, src), pk(GU, src), pk(GV, GT));  // V = U^2, x^2
+        if (gl == 0) {
+            const Fe t = F::sub(sf->f[GT], F::one());
+            sf->f[GM] = F::add(F::dbl(t), t);
+        }
+        products(3, pk(GU, src, GM), pk(GV, GV, GM), pk(GW, GS, GM2));  // W = U V, S = x V, M^2
+        if (gl == 0) {
+            const Fe xn = F::sub(sf->f[GM2], F::dbl(sf->f[GS]));
+            sf->f[GXN] = xn;
+            sf->f[GD] = F::sub(sf->f[GS], xn);
+        }
+        products(2, pk(GM, GW), pk(GD, src + 1), pk(GYA, GYB));  // M (S - X'), W y
+        if (gl == 0) {
+            if (F::is_zero(sf->f[GV])) {  // y = 0: no such point on a prime-order curve, kept complete
+                sf->f[dst] = sf->f[dst + 1] = sf->f[dst + 2] = sf->f[dst + 3] = F::zero();
+            } else {
+                sf->f[dst] = sf->f[GXN];
+                sf->f[dst + 1] = F::sub(sf->f[GYA], sf->f[GYB]);
+                sf->f[dst + 2] = sf->f[GV];
+                sf->f[dst + 3] = sf->f[GW];
+            }
+        }
+        sync();
+    }
+
+    // p += (x, y), the affine point at src (never the identity): madd-2008-s
+    __device__ void madd(int dst, int src) const
+    {
+        sync();
+        if (is_inf(dst)) {
+            if (gl < 4)
+                sf->f[dst + gl] = gl < 2 ? sf->f[src + gl] : F::one();
+            sync();
+            return;
+        }
+        const int X1 = dst, Y1 = dst + 1, ZZ1 = dst + 2, ZZZ1 = dst + 3;
+        products(2, pk(src, src + 1), pk(ZZ1, ZZZ1), pk(GU2, GS2));  // U2 = x ZZ1, S2 = y ZZZ1
+        if (gl == 0) {
+            sf->f[GP] = F::sub(sf->f[GU2], sf->f[X1]);
+            sf->f[GR] = F::sub(sf->f[GS2], sf->f[Y1]);
+            sf->flag = F::is_zero(sf->f[GP]) ? (F::is_zero(sf->f[GR]) ? 1 : 2) : 0;
+        }
+        sync();
+        const int flag = sf->flag;
+        if (flag == 1) {  // same point: double
+            dbl_affine(dst, src);
+            return;
+        }
+        if (flag == 2) {  // opposite points
+            set_inf(dst);
+            return;
+        }
+        products(2, pk(GP, GR), pk(GP, GR), pk(GPP, GRR));
+        products(3, pk(GP, X1, ZZ1), pk(GPP, GPP, GPP), pk(GPPP, GQ, GZZN));  // PPP, Q = X1 PP, ZZ1 PP
+        if (gl == 0) {
+            const Fe xn = F::sub(F::sub(sf->f[GRR], sf->f[GPPP]), F::dbl(sf->f[GQ]));
+            sf->f[GXN] = xn;
+            sf->f[GD] = F::sub(sf->f[GQ], xn);
+        }
+        products(3, pk(GR, Y1, ZZZ1), pk(GD, GPPP, GPPP), pk(GYA, GYB, GZZZN));  // R (Q - X'), Y1 PPP, ZZZ1 PPP
+        if (gl == 0) {
+            sf->f[X1] = sf->f[GXN];
+            sf->f[Y1] = F::sub(sf->f[GYA], sf->f[GYB]);
+            sf->f[ZZ1] = sf->f[GZZN];
+            sf->f[ZZZ1] = sf->f[GZZZN];
+        }
+        sync();
+    }
 };
 
 // Window sums of a plan of few windows of at most WG_MAX_B buckets, where the
@@ -1311,10 +1387,92 @@ __global__ void __launch_bounds__(WG_GROUPS * 8) k_window_groups(const uint32_t 
     }
 }
 
+// Bucket accumulation and merges of small plans on eight-lane groups (a mixed
+// addition is 4 product stages against 10 products on one thread): one group
+// per segment, then one group per bucket of 2..8 segments (more go to the
+// heavy-bucket list as in k_merge_light).  About 3.7 times the instructions
+// per entry of the one-thread form, so only for plans of at most
+// ACC_GROUPS_MAX_ENTRIES entries.
+constexpr uint64_t ACC_GROUPS_MAX_ENTRIES = 98304;
+
+template <class C>
+__global__ void __launch_bounds__(256) k_accumulate_groups(const uint4 *__restrict__ segs,
+                                                          const uint32_t *__restrict__ seg_lo,
+                                                          const uint32_t *__restrict__ seg_hi,
+                                                          const uint32_t *__restrict__ sorted,
+                                                          const uint4 *__restrict__ pts, uint4 *__restrict__ seg_sum)
+{
+    using F = typename C::F;
+    __shared__ GroupSlots sl[32];
+    const uint32_t g = threadIdx.x >> 3;
+    Group8<C> op;
+    op.sf = &sl[g];
+    op.gl = (int)(threadIdx.x & 7);
+    op.gmask = 0xffu << (8 * (g & 3));
+    const uint32_t S0 = *seg_lo, S = *seg_hi;
+    for (uint32_t s = S0 + blockIdx.x * 32 + g; s < S; s += gridDim.x * 32) {
+        const uint4 d = segs[s];  // start, length, destination slot
+        op.set_inf(GRUN);
+        for (uint32_t i = 0; i < d.y; i++) {
+            const uint32_t e = __ldg(sorted + d.x + i);
+            Fe x, y;
+            load_affine(pts, e & 0x7fffffffu, x, y);
+            if (F::is_exact_zero(x) && F::is_exact_zero(y))
+                continue;  // identity base
+            op.sync();
+            if (op.gl == 0)
+                op.sf->f[GTMP] = x;
+            else if (op.gl == 1)
+                op.sf->f[GTMP + 1] = (e >> 31) ? F::neg(y) : y;
+            op.madd(GRUN, GTMP);
+        }
+        op.sync();
+        if (op.gl < 4)
+            store_fe(seg_sum + 8 * (size_t)d.z + 2 * op.gl, op.sf->f[GRUN + op.gl]);
+    }
+}
+
+template <class C>
+__global__ void __launch_bounds__(256) k_merge_groups(const uint32_t *__restrict__ seg_off, uint32_t NB,
+                                                     uint4 *__restrict__ seg_sum, uint32_t *__restrict__ heavy,
+                                                     uint32_t *__restrict__ heavy_n, uint32_t heavy_min)
+{
+    __shared__ GroupSlots sl[32];
+    const uint32_t g = threadIdx.x >> 3;
+    Group8<C> op;
+    op.sf = &sl[g];
+    op.gl = (int)(threadIdx.x & 7);
+    op.gmask = 0xffu << (8 * (g & 3));
+    for (uint32_t kb = blockIdx.x * 32 + g; kb < NB; kb += gridDim.x * 32) {
+        const uint32_t s0 = seg_off[kb], ns = seg_off[kb + 1] - s0;
+        if (ns < 2)
+            continue;
+        if (ns > heavy_min) {
+            if (op.gl == 0)
+                heavy[atomicAdd(heavy_n, 1u)] = kb;
+            continue;
+        }
+        op.sync();
+        if (op.gl < 4)
+            op.sf->f[GRUN + op.gl] = load_fe(seg_sum + 8 * (size_t)s0 + 2 * op.gl);
+        for (uint32_t j = 1; j < ns; j++) {
+            op.sync();
+            if (op.gl < 4)
+                op.sf->f[GTMP + op.gl] = load_fe(seg_sum + 8 * (size_t)(s0 + j) + 2 * op.gl);
+            op.add(GRUN, GTMP);
+        }
+        op.sync();
+        if (op.gl < 4)
+            store_fe(seg_sum + 8 * (size_t)s0 + 2 * op.gl, op.sf->f[GRUN + op.gl]);
+    }
+}
+
 template <class C>
 cudaError_t msm_tail(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
 {
     cudaStream_t st = ctx.stream;
+    // a small plan: accumulation and merges on eight-lane groups
+    const bool small = !p.ba_rounds && !p.part_slice && p.entries_bound <= ACC_GROUPS_MAX_ENTRIES;
     // 2. accumulate: a grid of short blocks (up to 32 per SM, several waves), each
     //    thread taking segments at a stride of the grid.  Segments come longest
     //    first, so every block gets a like mix of long and short ones; blocks end
@@ -1371,6 +1529,16 @@ cudaError_t msm_tail(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
             HS_LAUNCH_CHECK(ctx);
             prof_end(ctx, ev0, j == 0 ? p.entries_pinned : 0);
         }
+    } else if (small) {
+        const uint64_t want = (p.max_segs + 31) / 32;
+        const int blocks = (int)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)ctx.sm_count * 8));
+        const size_t nh = (size_t)(p.L + 1) * p.hist_blocks;
+        cudaEvent_t ev0 = nullptr;
+        prof_begin(ctx, &ev0);
+        k_accumulate_groups<C><<<blocks, 256, 0, st>>>(b.segs, b.len_scan, b.len_scan + nh, b.sorted, b.points,
+                                                       b.seg_sum);
+        HS_LAUNCH_CHECK(ctx);
+        prof_end(ctx, ev0, p.entries_pinned);
     } else {
         const int threads = 128;
         const uint64_t want = (p.max_segs + threads - 1) / threads;
@@ -1404,8 +1572,14 @@ cudaError_t msm_tail(Context &ctx, const BatchPlan &p, const BatchBuffers &b)
         if (e != cudaSuccess)
             return e;
         const int threads = 256;
-        k_merge_light<C><<<(p.NB + threads - 1) / threads, threads, 0, st>>>(b.seg_off, p.NB, b.seg_sum, b.heavy,
-                                                                           b.heavy_n, 8);
+        if (small) {
+            const unsigned mb = (unsigned)std::max<uint32_t>(1, std::min<uint32_t>((p.NB + 31) / 32,
+                                                                                   (uint32_t)ctx.sm_count * 8));
+            k_merge_groups<C><<<mb, 256, 0, st>>>(b.seg_off, p.NB, b.seg_sum, b.heavy, b.heavy_n, 8);
+        } else {
+            k_merge_light<C><<<(p.NB + threads - 1) / threads, threads, 0, st>>>(b.seg_off, p.NB, b.seg_sum,
+                                                                               b.heavy, b.heavy_n, 8);
+        }
         HS_LAUNCH_CHECK(ctx);
         k_merge_heavy<C><<<ctx.sm_count, HEAVY_THREADS, 0, st>>>(b.seg_off, b.heavy, b.heavy_n, b.seg_sum);
         HS_LAUNCH_CHECK(ctx);
