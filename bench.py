@@ -1076,7 +1076,9 @@ def run_ours(args) -> None:
     e2e_split = SPLIT_DEFAULT if args.split is None else args.split
     for c in ctxs.values():
         c.set_split(e2e_split)
-    e2e_steps = max(10, min(args.steps, 30))
+    # at least 60 steps (about 0.35 s): a single stalled step, seen in about one
+    # run in six, then weighs a few percent rather than a third
+    e2e_steps = max(60, args.steps)
     for _ in range(2):
         for curve in (hs.HELIOS, hs.SELENE):
             ctxs[curve].msm(curve, data[curve]["h_sc"].numpy(), data[curve]["h_jac"].numpy(), hs.FMT_JACOBIAN51,
@@ -1104,15 +1106,27 @@ def run_ours(args) -> None:
         for _ in range(3):
             for f in [pool.submit(ctxs[c].msm, *args_of[c]) for c in (hs.SELENE, hs.HELIOS)]:
                 f.result()
-        e2e_step_ms = []
+        e2e_step_ms, e2e_calls = [], []
+
+        def timed_call(c):
+            t = time.perf_counter()
+            ctxs[c].msm(*args_of[c])
+            return t, time.perf_counter()
+
         with no_python_gc():
             t0 = time.perf_counter()
             for _ in range(e2e_steps):
                 ts = time.perf_counter()
-                for f in [pool.submit(ctxs[c].msm, *args_of[c]) for c in (hs.SELENE, hs.HELIOS)]:
-                    f.result()
-                e2e_step_ms.append((time.perf_counter() - ts) * 1e3)
+                fut = {c: pool.submit(timed_call, c) for c in (hs.SELENE, hs.HELIOS)}
+                span = {c: f.result() for c, f in fut.items()}
+                te = time.perf_counter()
+                e2e_step_ms.append((te - ts) * 1e3)
+                e2e_calls.append({("selene" if c == hs.SELENE else "helios"):
+                                  [round((a - ts) * 1e3, 3), round((b - ts) * 1e3, 3)] for c, (a, b) in span.items()})
             e2e_s = (time.perf_counter() - t0) / e2e_steps
+        e2e_med = statistics.median(e2e_step_ms)
+        e2e_slow = [{"step": i, "ms": round(t, 3), "calls_start_end_ms": e2e_calls[i]}
+                    for i, t in enumerate(e2e_step_ms) if t > 1.5 * e2e_med]
     for c in ctxs.values():
         c.set_split(head_split)
     # the same pair as one hs_msm_batch call (both curves, one context)
@@ -1186,6 +1200,7 @@ def run_ours(args) -> None:
                     "python_gc": "paused during the timed steps (collected and frozen first)",
                     "step_ms": {"median": statistics.median(e2e_step_ms), "min": min(e2e_step_ms),
                                 "max": max(e2e_step_ms), "all": [round(t, 3) for t in e2e_step_ms]},
+                    "slow_steps": e2e_slow,
                     "median_step_value": ws * 2 * n / (statistics.median(e2e_step_ms) * 1e-3),
                     "h2d_GBps_before": round(statistics.median(h2d_gbps), 1),
                     "one_batch_call": {"value": ws * 2 * n / e2e_batch_s, "unit": "points/s",
