@@ -405,3 +405,26 @@ def test_host_parts_edge_cases(ctx, curve):
     finally:
         ctx.set_split(1 << 18)
         ctx.default_batch_affine()
+
+
+@pytest.mark.parametrize("curve", [0, 1])
+@pytest.mark.parametrize("n", [300, 2000])
+def test_small_plan_heavy_buckets(ctx, curve, n):
+    """small plans run the eight-lane group kernels (accumulation, merges, window
+    reduction): one base repeated with one scalar fills one bucket per window
+    with hundreds of entries (many segments: group merges and the heavy-bucket
+    path), P and -P with equal scalars cancel inside buckets, and equal points
+    with equal scalars double in the mixed addition"""
+    sc, pts, _ = oracle_inputs(curve, n, seed=400 + n + curve)
+    F = pyref.CURVES["helios" if curve == 0 else "selene"].F
+    rep = n // 3
+    pts[1:rep] = pts[0]
+    sc[1:rep] = sc[0]
+    for i in range(rep, rep + 40, 2):  # P, -P pairs with one scalar
+        y = int.from_bytes(pts[i, 32:].tobytes(), "little")
+        pts[i + 1, :32] = pts[i, :32]
+        pts[i + 1, 32:] = np.frombuffer(((F - y) % F).to_bytes(32, "little"), np.uint8)
+        sc[i + 1] = sc[i]
+    assert ctx.msm(curve, sc, pts) == oracle.msm(curve, sc, pts)
+    assert ctx.msm_batch([(curve, sc, pts), (curve, sc[: n // 2], pts[: n // 2])]) == [
+        oracle.msm(curve, sc, pts), oracle.msm(curve, sc[: n // 2], pts[: n // 2])]
