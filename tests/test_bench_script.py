@@ -1,4 +1,5 @@
-"""bench.py and __graft_entry__.py compile and parse their flags without a GPU."""
+"""bench.py, __graft_entry__.py and the batched-form runner compile, and bench.py parses
+its flags, without a GPU."""
 
 import pathlib
 import py_compile
@@ -9,8 +10,8 @@ ROOT = pathlib.Path(__file__).resolve().parents[1]
 
 
 def test_scripts_compile(tmp_path):
-    for name in ("bench.py", "__graft_entry__.py"):
-        py_compile.compile(str(ROOT / name), cfile=str(tmp_path / (name + "c")), doraise=True)
+    for name in ("bench.py", "__graft_entry__.py", "helioselene_gb300/batchrun.py"):
+        py_compile.compile(str(ROOT / name), cfile=str(tmp_path / (name.replace("/", "_") + "c")), doraise=True)
 
 
 def test_bench_help():
