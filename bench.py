@@ -81,6 +81,61 @@ def no_python_gc():
         gc.unfreeze()
 
 
+def host_cpu_state() -> dict:
+    """The process's CPU time and its cgroup's CPU quota and throttling counters
+    (cgroup v2 or v1), for reading host-timed loops: a cgroup that exhausts its
+    quota in a scheduling period has every thread descheduled until the period
+    ends (up to 100 ms by default)."""
+    out = {"process_cpu_s": time.process_time(), "wall_s": time.perf_counter()}
+    try:  # time the hypervisor ran something else on this machine's CPUs (all CPUs, USER_HZ ticks)
+        with open("/proc/stat") as f:
+            fields = f.readline().split()
+        if fields[0] == "cpu" and len(fields) > 8:
+            out["steal_ms"] = int(fields[8]) * 1e3 / os.sysconf("SC_CLK_TCK")
+    except (OSError, ValueError):
+        pass
+    for stat, quota in (("/sys/fs/cgroup/cpu.stat", "/sys/fs/cgroup/cpu.max"),
+                        ("/sys/fs/cgroup/cpu,cpuacct/cpu.stat", None), ("/sys/fs/cgroup/cpu/cpu.stat", None)):
+        try:
+            with open(stat) as f:
+                kv = dict(line.split() for line in f if len(line.split()) == 2)
+        except OSError:
+            continue
+        out["nr_throttled"] = int(kv.get("nr_throttled", 0))
+        if "throttled_usec" in kv:
+            out["throttled_ms"] = int(kv["throttled_usec"]) / 1e3
+        elif "throttled_time" in kv:  # v1: nanoseconds
+            out["throttled_ms"] = int(kv["throttled_time"]) / 1e6
+        try:
+            if quota:
+                with open(quota) as f:
+                    out["quota"] = f.read().strip()
+            else:
+                base = os.path.dirname(stat)
+                with open(os.path.join(base, "cpu.cfs_quota_us")) as f, \
+                        open(os.path.join(base, "cpu.cfs_period_us")) as g:
+                    out["quota"] = f"{f.read().strip()} {g.read().strip()}"
+        except OSError:
+            pass
+        break
+    return out
+
+
+def host_cpu_delta(a: dict, b: dict, steps: int) -> dict:
+    """what a host-timed loop of `steps` steps cost on the host, from two host_cpu_state() reads"""
+    out = {"process_cpu_ms_per_step": round((b["process_cpu_s"] - a["process_cpu_s"]) * 1e3 / steps, 3),
+           "cpus_busy": round((b["process_cpu_s"] - a["process_cpu_s"]) / max(1e-9, b["wall_s"] - a["wall_s"]), 2),
+           "cpus_usable": len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()}
+    if "steal_ms" in a and "steal_ms" in b:
+        out["steal_ms_all_cpus"] = round(b["steal_ms"] - a["steal_ms"], 1)
+    if "nr_throttled" in a and "nr_throttled" in b:
+        out["cgroup_quota"] = b.get("quota")
+        out["cgroup_throttled_periods"] = b["nr_throttled"] - a["nr_throttled"]
+        if "throttled_ms" in a:
+            out["cgroup_throttled_ms"] = round(b["throttled_ms"] - a["throttled_ms"], 3)
+    return out
+
+
 def modmul_count(n: int) -> tuple:
     """Pinned algorithmic work: M(n) = min_c ceil(256/c) (6n + 16 2^c) + 2048 + 16 ceil(256/c)."""
     best = None
@@ -1109,11 +1164,15 @@ def run_ours(args) -> None:
         e2e_step_ms, e2e_calls = [], []
 
         def timed_call(c):
-            t = time.perf_counter()
+            # the calling thread's CPU time beside its wall time: a thread that was
+            # descheduled shows less CPU than wall time, one that waited on the
+            # device (the runtime spins in its synchronise) about as much
+            t, u = time.perf_counter(), time.thread_time()
             ctxs[c].msm(*args_of[c])
-            return t, time.perf_counter()
+            return t, time.perf_counter(), time.thread_time() - u
 
         with no_python_gc():
+            cpu0 = host_cpu_state()
             t0 = time.perf_counter()
             for _ in range(e2e_steps):
                 ts = time.perf_counter()
@@ -1122,10 +1181,12 @@ def run_ours(args) -> None:
                 te = time.perf_counter()
                 e2e_step_ms.append((te - ts) * 1e3)
                 e2e_calls.append({("selene" if c == hs.SELENE else "helios"):
-                                  [round((a - ts) * 1e3, 3), round((b - ts) * 1e3, 3)] for c, (a, b) in span.items()})
+                                  [round((a - ts) * 1e3, 3), round((b - ts) * 1e3, 3), round(u * 1e3, 3)]
+                                  for c, (a, b, u) in span.items()})
             e2e_s = (time.perf_counter() - t0) / e2e_steps
+            e2e_host = host_cpu_delta(cpu0, host_cpu_state(), e2e_steps)
         e2e_med = statistics.median(e2e_step_ms)
-        e2e_slow = [{"step": i, "ms": round(t, 3), "calls_start_end_ms": e2e_calls[i]}
+        e2e_slow = [{"step": i, "ms": round(t, 3), "calls_start_end_cpu_ms": e2e_calls[i]}
                     for i, t in enumerate(e2e_step_ms) if t > 1.5 * e2e_med]
     for c in ctxs.values():
         c.set_split(head_split)
@@ -1201,6 +1262,7 @@ def run_ours(args) -> None:
                     "step_ms": {"median": statistics.median(e2e_step_ms), "min": min(e2e_step_ms),
                                 "max": max(e2e_step_ms), "all": [round(t, 3) for t in e2e_step_ms]},
                     "slow_steps": e2e_slow,
+                    "host": e2e_host,
                     "median_step_value": ws * 2 * n / (statistics.median(e2e_step_ms) * 1e-3),
                     "h2d_GBps_before": round(statistics.median(h2d_gbps), 1),
                     "one_batch_call": {"value": ws * 2 * n / e2e_batch_s, "unit": "points/s",
