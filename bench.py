@@ -1188,6 +1188,24 @@ def run_ours(args) -> None:
         e2e_med = statistics.median(e2e_step_ms)
         e2e_slow = [{"step": i, "ms": round(t, 3), "calls_start_end_cpu_ms": e2e_calls[i]}
                     for i, t in enumerate(e2e_step_ms) if t > 1.5 * e2e_med]
+        # the same calls from pageable copies of the inputs (ordinary arrays, as
+        # a caller of the drop-ins holds them)
+        args_pg = {c: (c, np.array(data[c]["h_sc"].numpy()), np.array(data[c]["h_jac"].numpy()), hs.FMT_JACOBIAN51,
+                       hs.FMT_JACOBIAN51) for c in (hs.SELENE, hs.HELIOS)}
+        for _ in range(3):
+            for f in [pool.submit(ctxs[c].msm, *args_pg[c]) for c in (hs.SELENE, hs.HELIOS)]:
+                f.result()
+        pg_step_ms = []
+        with no_python_gc():
+            for _ in range(e2e_steps):
+                ts = time.perf_counter()
+                for f in [pool.submit(ctxs[c].msm, *args_pg[c]) for c in (hs.SELENE, hs.HELIOS)]:
+                    f.result()
+                pg_step_ms.append((time.perf_counter() - ts) * 1e3)
+        del args_pg
+    e2e_pageable = {"value": ws * 2 * n / (statistics.mean(pg_step_ms) * 1e-3), "unit": "points/s",
+                    "median_step_value": ws * 2 * n / (statistics.median(pg_step_ms) * 1e-3),
+                    "steps": e2e_steps, "api": "the same calls with the inputs in pageable host memory (numpy arrays)"}
     for c in ctxs.values():
         c.set_split(head_split)
     # the same pair as one hs_msm_batch call (both curves, one context)
@@ -1263,6 +1281,7 @@ def run_ours(args) -> None:
                                 "max": max(e2e_step_ms), "all": [round(t, 3) for t in e2e_step_ms]},
                     "slow_steps": e2e_slow,
                     "host": e2e_host,
+                    "pageable": e2e_pageable,
                     "median_step_value": ws * 2 * n / (statistics.median(e2e_step_ms) * 1e-3),
                     "h2d_GBps_before": round(statistics.median(h2d_gbps), 1),
                     "one_batch_call": {"value": ws * 2 * n / e2e_batch_s, "unit": "points/s",

@@ -66,6 +66,9 @@ struct Context {
     cudaEvent_t ev_rec[2] = {};    // input records on the device (per part)
     cudaEvent_t ev_pts[2] = {};    // affine bases ready (per part)
     bool use_graphs = true;
+    // the device reads pageable host memory directly (cudaDevAttrPageableMemoryAccess):
+    // host inputs in pageable memory are then pulled by a copy kernel (h2d_async)
+    bool pageable_access = false;
     // set while a launch sequence of host inputs is being captured: waits on the
     // input events (recorded outside the capture) become external event waits
     bool capturing_host = false;

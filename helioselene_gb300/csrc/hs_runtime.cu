@@ -1543,7 +1543,11 @@ static cudaError_t link_stream(int device, LinkStream **out)
         LinkStream *ls = new (std::nothrow) LinkStream();
         if (!ls)
             return cudaErrorMemoryAllocation;
-        const cudaError_t e = cudaStreamCreateWithFlags(&ls->s, cudaStreamNonBlocking);
+        // the greatest priority: the copy kernels of pageable inputs (h2d_async)
+        // then take SM slots ahead of the compute kernels waiting for them
+        int least = 0, greatest = 0;
+        cudaDeviceGetStreamPriorityRange(&least, &greatest);
+        const cudaError_t e = cudaStreamCreateWithPriority(&ls->s, cudaStreamNonBlocking, greatest);
         if (e != cudaSuccess) {
             delete ls;
             return e;
@@ -1552,6 +1556,103 @@ static cudaError_t link_stream(int device, LinkStream **out)
     }
     *out = reg[device];
     return cudaSuccess;
+}
+
+// Host-to-device copies from pageable host memory.  A copy-engine copy from
+// pageable memory returns only once its data has been staged: it holds the
+// calling thread for the whole transfer (after draining the stream), so the
+// launches queued behind it -- and other threads' copies on the shared link
+// stream -- start late.  On a device that reads pageable host memory directly
+// (cudaDevAttrPageableMemoryAccess: Grace-class hosts, where the GPU reaches
+// system memory through the host's page tables) a copy kernel reading the
+// caller's pages is stream-ordered and returns at once, like a copy from pinned
+// memory, and runs at the same link rate (about 209 GB/s on GB300 for both, and
+// for copy-engine copies from pinned memory).  Pinned, registered, managed and
+// device memory keep the copy engine.
+constexpr int PULL_DEPTH = 8;
+constexpr int PULL_BLOCK_DIV = 4;
+
+template <class Word>
+__global__ void __launch_bounds__(256) k_pull(const Word *__restrict__ src, Word *__restrict__ dst, size_t words,
+                                              const uint8_t *__restrict__ src_tail, uint8_t *__restrict__ dst_tail,
+                                              uint32_t tail)
+{
+    const size_t T = (size_t)gridDim.x * blockDim.x;
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    // PULL_DEPTH loads in flight per thread: the link's latency is microseconds
+    for (; i + (PULL_DEPTH - 1) * T < words; i += PULL_DEPTH * T) {
+        Word v[PULL_DEPTH];
+#pragma unroll
+        for (int k = 0; k < PULL_DEPTH; k++)
+            v[k] = src[i + k * T];
+#pragma unroll
+        for (int k = 0; k < PULL_DEPTH; k++)
+            dst[i + k * T] = v[k];
+    }
+    for (; i < words; i += T)
+        dst[i] = src[i];
+    if (blockIdx.x == 0 && threadIdx.x < tail)
+        dst_tail[threadIdx.x] = src_tail[threadIdx.x];
+}
+
+template <class Word>
+static void launch_pull(Context &ctx, void *dst, const void *src, size_t bytes, cudaStream_t s)
+{
+    const size_t words = bytes / sizeof(Word);
+    const uint32_t tail = (uint32_t)(bytes % sizeof(Word));
+    // A quarter as many blocks as SMs keep about 1.2 MB of 16-byte loads in
+    // flight and leave the other SM slots to the compute kernels running beside
+    // the copy.  On GB300, a Helios and a Selene call of 2^20 points from two
+    // threads took per pair: 6.99 ms with 152 blocks of four loads, 6.30 with
+    // 76, 6.08 with 38; 6.06 with 38 blocks of eight loads, 6.25 with 19 and
+    // 6.72 with 9 (fewer SMs do not fill the link); 5.90 from pinned buffers by
+    // the copy engine, and 6.70 from pageable ones by the copy engine.
+    const size_t per_block = 256 * PULL_DEPTH;
+    const unsigned blocks = (unsigned)std::max<size_t>(
+        1, std::min<size_t>((size_t)std::max(1, ctx.sm_count / PULL_BLOCK_DIV), (words + per_block - 1) / per_block));
+    k_pull<Word><<<blocks, 256, 0, s>>>(static_cast<const Word *>(src), static_cast<Word *>(dst), words,
+                                        static_cast<const uint8_t *>(src) + words * sizeof(Word),
+                                        static_cast<uint8_t *>(dst) + words * sizeof(Word), tail);
+    ctx.launches++;
+}
+
+// true when p is ordinary pageable host memory (not pinned, registered, managed or device)
+static bool is_pageable(const void *p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return true;
+    }
+    return a.type == cudaMemoryTypeUnregistered;
+}
+
+// drains a stream on scope exit unless cleared
+struct LinkDrain {
+    cudaStream_t s;
+    ~LinkDrain()
+    {
+        if (s)
+            cudaStreamSynchronize(s);
+    }
+};
+
+static cudaError_t h2d_async(Context &ctx, void *dst, const void *src, size_t bytes, cudaStream_t s)
+{
+    if (!bytes)
+        return cudaSuccess;
+    if (!ctx.pageable_access || !is_pageable(src))
+        return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
+    const uintptr_t al = reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src);
+    if (al % 16 == 0)
+        launch_pull<uint4>(ctx, dst, src, bytes, s);
+    else if (al % 8 == 0)
+        launch_pull<uint2>(ctx, dst, src, bytes, s);
+    else if (al % 4 == 0)
+        launch_pull<uint32_t>(ctx, dst, src, bytes, s);
+    else
+        launch_pull<uint8_t>(ctx, dst, src, bytes, s);
+    return cudaGetLastError();
 }
 
 struct SplitPlan {
@@ -1743,6 +1844,11 @@ int hs_context_create(hs_context **out, int device)
     e = cudaStreamCreateWithFlags(&ctx.stream, cudaStreamNonBlocking);
     if (e == cudaSuccess)
         e = cudaDeviceGetAttribute(&ctx.sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) {
+        int pma = 0;
+        e = cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, device);
+        ctx.pageable_access = pma == 1;
+    }
     if (e == cudaSuccess)
         e = sort_smem_attrs(device);
     if (e != cudaSuccess) {
@@ -2009,26 +2115,29 @@ static int msm_host(Context &ctx, int curve, const uint8_t *lead_scalar, const v
     LinkStream *link = nullptr;
     HS_CU(link_stream(ctx.device, &link), "stream creation");
     cudaStream_t st = ctx.stream, s2 = ctx.stream2, s3 = ctx.stream3;
+    // a copy kernel may still be reading the caller's pages when the call fails
+    // part way: the link stream drains before such a return
+    LinkDrain drain{link->s};
     HS_CU(cudaEventRecord(ctx.ev_fork, st), "event");  // earlier work on the buffers comes first
     {
         std::lock_guard<std::mutex> lk(link->mu);
         cudaStream_t cs = link->s;
         HS_CU(cudaStreamWaitEvent(cs, ctx.ev_fork, 0), "stream wait");
         if (lead)
-            HS_CU(cudaMemcpyAsync(d_sc, lead_scalar, 32, cudaMemcpyHostToDevice, cs), "H2D scalars");
+            HS_CU(h2d_async(ctx, d_sc, lead_scalar, 32, cs), "H2D scalars");
         if (n)
-            HS_CU(cudaMemcpyAsync(d_sc + 32 * lead, scalars, n * 32, cudaMemcpyHostToDevice, cs), "H2D scalars");
+            HS_CU(h2d_async(ctx, d_sc + 32 * lead, scalars, n * 32, cs), "H2D scalars");
         HS_CU(cudaEventRecord(ctx.ev_sc, cs), "event");
         for (int j = 0; j < nparts; j++) {
             // point g of the MSM: the lead term at 0, then points[g - lead]
             size_t g = bound[j];
             if (lead && g == 0 && bound[j + 1] > 0) {
-                HS_CU(cudaMemcpyAsync(d_raw, lead_point, pb, cudaMemcpyHostToDevice, cs), "H2D points");
+                HS_CU(h2d_async(ctx, d_raw, lead_point, pb, cs), "H2D points");
                 g = 1;
             }
             if (bound[j + 1] > g)
-                HS_CU(cudaMemcpyAsync(d_raw + pb * g, static_cast<const uint8_t *>(points) + pb * (g - lead),
-                                      pb * (bound[j + 1] - g), cudaMemcpyHostToDevice, cs),
+                HS_CU(h2d_async(ctx, d_raw + pb * g, static_cast<const uint8_t *>(points) + pb * (g - lead),
+                                pb * (bound[j + 1] - g), cs),
                       "H2D points");
             HS_CU(cudaEventRecord(ctx.ev_rec[j], cs), "event");
         }
@@ -2171,6 +2280,7 @@ static int msm_host(Context &ctx, int curve, const uint8_t *lead_scalar, const v
     }
     HS_CU(cudaMemcpyAsync(out, d_out, fmt_bytes(out_fmt), cudaMemcpyDeviceToHost, st), "D2H result");
     HS_CU(cudaStreamSynchronize(st), "MSM");
+    drain.s = nullptr;  // the launch sequence waited for every input copy
     if (point_fmt == HS_FMT_COMPRESSED)
         return check_decoded(ctx, d_scratch);
     return HS_OK;
@@ -2528,6 +2638,10 @@ int hs_msm_batch(hs_context *h, const hs_msm_desc *descs, size_t count, int poin
     LinkStream *link = nullptr;
     HS_CU(link_stream(ctx.device, &link), "stream creation");
     cudaStream_t s1 = ctx.stream, s3 = ctx.stream3;
+    LinkDrain drain{link->s};  // drained before an early return (copy kernels may read the caller's pages)
+    // copy kernels for pageable inputs (h2d_async) only while the launches stay
+    // few: many small MSMs keep the copy engine
+    const bool few = idx[0].size() + idx[1].size() <= 16;
     // per curve group: inputs on the device, bases converted; and the join
     cudaEvent_t ev_rec[2] = {}, ev_pts[2] = {}, ev_done = nullptr;
     struct EvGuard {
@@ -2572,7 +2686,10 @@ int hs_msm_batch(hs_context *h, const hs_msm_desc *descs, size_t count, int poin
             size_t off = 0;
             for (size_t j = 0; j < idx[k].size(); j++) {
                 const hs_msm_desc &d = descs[idx[k][j]];
-                if (d.n) {
+                if (d.n && few) {
+                    HS_CU(h2d_async(ctx, (uint8_t *)bufs[k].scalars + 32 * off, d.scalars, d.n * 32, cs), "H2D");
+                    HS_CU(h2d_async(ctx, d_raw_k[k] + pb * off, d.points, d.n * pb, cs), "H2D");
+                } else if (d.n) {
                     HS_CU(cudaMemcpyAsync((uint8_t *)bufs[k].scalars + 32 * off, d.scalars, d.n * 32,
                                           cudaMemcpyHostToDevice, cs),
                           "H2D");
@@ -2621,6 +2738,7 @@ int hs_msm_batch(hs_context *h, const hs_msm_desc *descs, size_t count, int poin
         HS_CU(cudaMemcpyAsync(host_out[k].data(), d_out[k], host_out[k].size(), cudaMemcpyDeviceToHost, s1), "D2H");
     }
     HS_CU(cudaStreamSynchronize(s1), "MSM batch");
+    drain.s = nullptr;  // both groups waited for their input copies
     if (point_fmt == HS_FMT_COMPRESSED)
         for (int k = 0; k < 2; k++)
             if (!idx[k].empty() && totals[k] && (rc = check_decoded(ctx, d_scr_k[k])) != HS_OK)

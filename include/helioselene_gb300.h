@@ -132,9 +132,13 @@ int hs_context_set_priority(hs_context *ctx, int high);
  * at c = 16; beyond that it returns HS_ERANGE and the caller sums the results
  * of slices (they add as points).
  * The host-to-device copies of every context on a device go through one copy
- * stream in call order (pinned host memory keeps them asynchronous); the
- * scalars go first, and bases of more than 2^17 points go in two parts whose
- * first is accumulated while the second is in transit. */
+ * stream in call order; the scalars go first, and bases of more than 2^17
+ * points go in two parts whose first is accumulated while the second is in
+ * transit.  Pinned host memory is copied by the copy engine.  Pageable memory
+ * (an ordinary array) is read by a copy kernel where the device reads pageable
+ * host memory (Grace-class hosts), which keeps the copies asynchronous too;
+ * elsewhere the copy engine stages it, which holds the calling thread for each
+ * copy.  hs_msm_batch does the same for batches of at most 16 MSMs. */
 int hs_msm(hs_context *ctx, int curve, const uint8_t *scalars, const void *points, int point_fmt, size_t n,
            void *out, int out_fmt);
 

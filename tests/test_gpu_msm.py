@@ -428,3 +428,58 @@ def test_small_plan_heavy_buckets(ctx, curve, n):
     assert ctx.msm(curve, sc, pts) == oracle.msm(curve, sc, pts)
     assert ctx.msm_batch([(curve, sc, pts), (curve, sc[: n // 2], pts[: n // 2])]) == [
         oracle.msm(curve, sc, pts), oracle.msm(curve, sc[: n // 2], pts[: n // 2])]
+
+
+def _placed(data: np.ndarray, offset: int, pinned: bool = False) -> np.ndarray:
+    """a copy of the bytes of `data` starting `offset` bytes past a 16-byte
+    boundary, in pageable (numpy) or pinned (torch) host memory"""
+    raw = np.ascontiguousarray(data).view(np.uint8).reshape(-1)
+    if pinned:
+        import torch
+        buf = torch.empty(raw.size + 32, dtype=torch.uint8, pin_memory=True).numpy()
+    else:
+        buf = np.empty(raw.size + 32, np.uint8)
+    base = (-buf.ctypes.data) % 16
+    view = buf[base + offset:base + offset + raw.size]
+    view[:] = raw
+    return view
+
+
+@pytest.mark.parametrize("curve", [0, 1])
+def test_host_buffers_pinned_pageable_unaligned(ctx, curve):
+    """Host inputs in pageable memory -- pulled by a copy kernel that reads the
+    caller's pages where the device reads pageable memory, by the copy engine
+    elsewhere -- at byte offsets 0, 1, 4 and 8 from a 16-byte boundary (the
+    kernel's 16-, 8-, 4- and 1-byte word forms, with ragged tails), and in
+    pinned memory (copy engine): single MSMs with the bases in two parts,
+    Pedersen with its lead term, and small host batches, against the oracle."""
+    n = (1 << 18) + 3
+    from helioselene_gb300.workload import make_workload
+    w = make_workload(curve, n, seed=5150 + curve, edge_fraction=0.01)
+    pts = ctx.map_to_curve(curve, w.u, HS_AFF).reshape(n, 64)
+    sc = w.scalars.reshape(n, 32)
+    want = oracle.msm_mt(curve, sc, pts, oracle.default_threads())
+    jac = np.zeros((n, 15), np.uint64)
+    jac[:, 0:5], jac[:, 5:10], jac[:, 10] = _to_fe51_rows(pts[:, :32]), _to_fe51_rows(pts[:, 32:]), 1
+    sizes = (1000, 77, 2001)
+    cuts = np.cumsum((0,) + sizes)
+    want_small = [oracle.msm(curve, sc[a:b], pts[a:b]) for a, b in zip(cuts[:-1], cuts[1:])]
+    counts = {}
+    for pinned, offsets in ((False, (0, 1, 4, 8)), (True, (0, 1))):
+        for off in offsets:
+            tag = f"{'pinned' if pinned else 'pageable'} offset {off}"
+            s_v = _placed(sc, off, pinned)
+            j_v = _placed(jac, off, pinned)
+            p_v = _placed(pts, off, pinned)
+            before = ctx.launches
+            assert ctx.msm(curve, s_v, j_v, HS_JAC51) == want, tag
+            counts[(pinned, off)] = ctx.launches - before
+            assert ctx.msm(curve, s_v, p_v, HS_AFF) == want, tag
+            assert ctx.pedersen(curve, s_v[:32], p_v[:64], s_v[32:], p_v[64:]) == want, f"pedersen, {tag}"
+            items = [(curve, s_v[32 * a:32 * b], p_v[64 * a:64 * b]) for a, b in zip(cuts[:-1], cuts[1:])]
+            assert ctx.msm_batch(items) == want_small, f"batch, {tag}"
+    # a pageable call launches the same sequence as a pinned one, plus one copy
+    # kernel per input copy (scalars and two parts of bases) where the device
+    # reads pageable memory
+    extra = {counts[(False, off)] - counts[(True, 0)] for off in (0, 1, 4, 8)}
+    assert extra in ({0}, {3}), counts
