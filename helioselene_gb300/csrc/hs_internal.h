@@ -309,6 +309,28 @@ const CurveOps &curve_ops(int curve);
 size_t fmt_bytes(int fmt);
 size_t align256(size_t b);
 
+// One piece of a gathered host-to-device copy (pull_list): a device that reads
+// pageable host memory (Context::pageable_access) copies the pieces with one
+// kernel, reading the list and the sources where they lie in host memory.
+struct PullChunk {
+    const uint8_t *src;
+    uint8_t *dst;
+    uint64_t bytes;
+};
+constexpr size_t PULL_CHUNK_BYTES = size_t(256) << 10;  // a block copies one piece at a time
+
+// append a copy of `bytes` from src to dst, cut into pieces of at most PULL_CHUNK_BYTES
+inline void pull_add(std::vector<PullChunk> &list, void *dst, const void *src, size_t bytes)
+{
+    for (size_t o = 0; o < bytes; o += PULL_CHUNK_BYTES)
+        list.push_back({static_cast<const uint8_t *>(src) + o, static_cast<uint8_t *>(dst) + o,
+                        std::min(PULL_CHUNK_BYTES, bytes - o)});
+}
+
+// one kernel copying every piece of `list` (host memory the device reads, left
+// untouched until the stream has passed the kernel) on stream s
+cudaError_t pull_list(Context &ctx, const PullChunk *list, size_t count, cudaStream_t s);
+
 // make `dev` current for a scope
 struct DeviceGuard {
     int prev = -1;

@@ -1627,6 +1627,62 @@ static bool is_pageable(const void *p)
     return a.type == cudaMemoryTypeUnregistered;
 }
 
+// A block copies one piece of a gathered copy in `Word`s, then the ragged tail
+template <class Word>
+__device__ __forceinline__ void pull_piece(const uint8_t *__restrict__ src, uint8_t *__restrict__ dst, size_t bytes)
+{
+    const size_t words = bytes / sizeof(Word);
+    const Word *s = reinterpret_cast<const Word *>(src);
+    Word *d = reinterpret_cast<Word *>(dst);
+    const size_t T = blockDim.x;
+    size_t i = threadIdx.x;
+    for (; i + (PULL_DEPTH - 1) * T < words; i += PULL_DEPTH * T) {
+        Word v[PULL_DEPTH];
+#pragma unroll
+        for (int k = 0; k < PULL_DEPTH; k++)
+            v[k] = s[i + k * T];
+#pragma unroll
+        for (int k = 0; k < PULL_DEPTH; k++)
+            d[i + k * T] = v[k];
+    }
+    for (; i < words; i += T)
+        d[i] = s[i];
+    const size_t done = words * sizeof(Word);
+    if (threadIdx.x < bytes - done)
+        dst[done + threadIdx.x] = src[done + threadIdx.x];
+}
+
+// the pieces of a gathered copy, one block per piece at a time; the list and
+// the sources are read where they lie in host memory
+__global__ void __launch_bounds__(256) k_pull_list(const PullChunk *__restrict__ list, uint32_t count)
+{
+    for (uint32_t c = blockIdx.x; c < count; c += gridDim.x) {
+        const PullChunk ch = list[c];
+        const uintptr_t al = reinterpret_cast<uintptr_t>(ch.src) | reinterpret_cast<uintptr_t>(ch.dst);
+        if (al % 16 == 0)
+            pull_piece<uint4>(ch.src, ch.dst, ch.bytes);
+        else if (al % 8 == 0)
+            pull_piece<uint2>(ch.src, ch.dst, ch.bytes);
+        else if (al % 4 == 0)
+            pull_piece<uint32_t>(ch.src, ch.dst, ch.bytes);
+        else
+            pull_piece<uint8_t>(ch.src, ch.dst, ch.bytes);
+    }
+}
+
+cudaError_t pull_list(Context &ctx, const PullChunk *list, size_t count, cudaStream_t s)
+{
+    if (!count)
+        return cudaSuccess;
+    if (count >= 0xffffffffull)
+        return cudaErrorInvalidValue;
+    const unsigned blocks =
+        (unsigned)std::max<size_t>(1, std::min<size_t>((size_t)std::max(1, ctx.sm_count / PULL_BLOCK_DIV), count));
+    k_pull_list<<<blocks, 256, 0, s>>>(list, (uint32_t)count);
+    ctx.launches++;
+    return cudaGetLastError();
+}
+
 // drains a stream on scope exit unless cleared
 struct LinkDrain {
     cudaStream_t s;

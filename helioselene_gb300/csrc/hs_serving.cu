@@ -77,6 +77,9 @@ struct Slot {
     uint8_t *pinned_out = nullptr;
     size_t pinned_cap = 0;
     std::vector<uint4> h_seg;  // per request: (first point, first pool index, pool count); kept until retire
+    // the batch's input copies as one gathered copy (pull_list, devices that read
+    // pageable host memory); read by the device, so kept until retire
+    std::vector<PullChunk> h_pull;
 };
 
 struct Pool {
@@ -159,6 +162,16 @@ static bool fail_requests(Server &S, Slot &s, const std::vector<uint64_t> &batch
     return true;
 }
 
+// a batch that fails after its copies were issued: the slot's stream drains
+// first (a copy kernel may still be reading the requests' buffers, which their
+// callers may free once told of the failure)
+static bool fail_staged(Server &S, Slot &s, const std::vector<uint64_t> &batch, int code)
+{
+    cudaStreamSynchronize(s.ctx.stream);
+    cudaGetLastError();
+    return fail_requests(S, s, batch, code);
+}
+
 static bool ensure_pinned_out(Slot &s, size_t bytes)
 {
     if (s.pinned_cap >= bytes)
@@ -213,29 +226,37 @@ static bool launch_table(Server &S, Slot &s, std::vector<uint64_t> &batch, int c
     cudaStream_t st = ctx.stream;
     cudaError_t e = cudaSuccess;
     size_t off = 0;
+    s.h_pull.clear();
     for (uint64_t t : batch) {
         const hs_request &q = S.reqs[t].req;
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(d_sc + 32 * off, q.scalars, 32 * q.n_pool, cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess)
-            e = cudaMemcpyAsync(d_idx + off, q.pool_idx, 4 * q.n_pool, cudaMemcpyHostToDevice, st);
+        if (ctx.pageable_access) {
+            pull_add(s.h_pull, d_sc + 32 * off, q.scalars, 32 * q.n_pool);
+            pull_add(s.h_pull, d_idx + off, q.pool_idx, 4 * q.n_pool);
+        } else {
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(d_sc + 32 * off, q.scalars, 32 * q.n_pool, cudaMemcpyHostToDevice, st);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(d_idx + off, q.pool_idx, 4 * q.n_pool, cudaMemcpyHostToDevice, st);
+        }
         off += q.n_pool;
     }
+    if (e == cudaSuccess)
+        e = pull_list(ctx, s.h_pull.data(), s.h_pull.size(), st);
     if (e != cudaSuccess) {
         ctx.last_error = std::string("staging: ") + cudaGetErrorString(e);
-        return fail_requests(S, s, batch, HS_ECUDA);
+        return fail_staged(S, s, batch, HS_ECUDA);
     }
     b.scalars = (const uint32_t *)d_sc;
     b.points = pool.table;
     b.pt_idx = d_idx;
     if (execute_batch(ctx, p, b, d_out, S.cfg.out_fmt) != HS_OK)
-        return fail_requests(S, s, batch, HS_ECUDA);
+        return fail_staged(S, s, batch, HS_ECUDA);
     e = cudaMemcpyAsync(s.pinned_out, d_out, (size_t)M * ob, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess)
         e = cudaEventRecord(s.done, st);
     if (e != cudaSuccess) {
         ctx.last_error = std::string("result copy: ") + cudaGetErrorString(e);
-        return fail_requests(S, s, batch, HS_ECUDA);
+        return fail_staged(S, s, batch, HS_ECUDA);
     }
     finish_launch(S, s, batch, curve, bytes);
     return true;
@@ -287,25 +308,40 @@ static bool launch(Server &S, Slot &s, std::vector<uint64_t> &batch, int curve)
     // per request: its scalars, fresh bases and pool indices copied straight from
     // the caller's buffers, plus one table row; the pooled bases are gathered on
     // the device
+    // (on a device that reads pageable host memory, all of them as one gathered
+    // copy: the scheduler then issues one launch instead of staging each copy
+    // through the driver, which holds it -- and the server lock -- per copy)
     s.h_seg.clear();
+    s.h_pull.clear();
     size_t off = 0, poff = 0;
     cudaError_t e = cudaSuccess;
     for (uint64_t t : batch) {
         const hs_request &q = S.reqs[t].req;
         const size_t n = q.n_pool + q.n_fresh;
-        if (n && e == cudaSuccess)
-            e = cudaMemcpyAsync(d_sc + 32 * off, q.scalars, 32 * n, cudaMemcpyHostToDevice, st);
-        if (q.n_fresh && e == cudaSuccess)
-            e = cudaMemcpyAsync(d_pts + 64 * (off + q.n_pool), q.fresh_points, 64 * q.n_fresh,
-                                cudaMemcpyHostToDevice, st);
-        if (q.n_pool && e == cudaSuccess)
-            e = cudaMemcpyAsync(d_src + poff, q.pool_idx, 4 * q.n_pool, cudaMemcpyHostToDevice, st);
+        if (ctx.pageable_access) {
+            pull_add(s.h_pull, d_sc + 32 * off, q.scalars, 32 * n);
+            pull_add(s.h_pull, d_pts + 64 * (off + q.n_pool), q.fresh_points, 64 * q.n_fresh);
+            pull_add(s.h_pull, d_src + poff, q.pool_idx, 4 * q.n_pool);
+        } else {
+            if (n && e == cudaSuccess)
+                e = cudaMemcpyAsync(d_sc + 32 * off, q.scalars, 32 * n, cudaMemcpyHostToDevice, st);
+            if (q.n_fresh && e == cudaSuccess)
+                e = cudaMemcpyAsync(d_pts + 64 * (off + q.n_pool), q.fresh_points, 64 * q.n_fresh,
+                                    cudaMemcpyHostToDevice, st);
+            if (q.n_pool && e == cudaSuccess)
+                e = cudaMemcpyAsync(d_src + poff, q.pool_idx, 4 * q.n_pool, cudaMemcpyHostToDevice, st);
+        }
         s.h_seg.push_back(make_uint4((uint32_t)off, (uint32_t)poff, (uint32_t)q.n_pool, 0u));
         off += n;
         poff += q.n_pool;
     }
+    if (total_pool && ctx.pageable_access)
+        pull_add(s.h_pull, d_seg, s.h_seg.data(), 16 * s.h_seg.size());
+    if (e == cudaSuccess)
+        e = pull_list(ctx, s.h_pull.data(), s.h_pull.size(), st);
     if (total_pool && e == cudaSuccess) {
-        e = cudaMemcpyAsync(d_seg, s.h_seg.data(), 16 * s.h_seg.size(), cudaMemcpyHostToDevice, st);
+        if (!ctx.pageable_access)
+            e = cudaMemcpyAsync(d_seg, s.h_seg.data(), 16 * s.h_seg.size(), cudaMemcpyHostToDevice, st);
         if (e == cudaSuccess) {
             k_gather_pool<<<(unsigned)((total_pool + 255) / 256), 256, 0, st>>>(
                 S.pools[curve].d, d_src, d_seg, (uint32_t)s.h_seg.size(), (uint32_t)total_pool, (uint4 *)d_pts);
@@ -315,18 +351,18 @@ static bool launch(Server &S, Slot &s, std::vector<uint64_t> &batch, int curve)
     }
     if (e != cudaSuccess) {
         ctx.last_error = std::string("staging: ") + cudaGetErrorString(e);
-        return fail_batch(HS_ECUDA);
+        return fail_staged(S, s, batch, HS_ECUDA);
     }
     b.scalars = (const uint32_t *)d_sc;
     b.points = (const uint4 *)d_pts;
     if (execute_batch(ctx, p, b, d_out, S.cfg.out_fmt) != HS_OK)
-        return fail_batch(HS_ECUDA);
+        return fail_staged(S, s, batch, HS_ECUDA);
     e = cudaMemcpyAsync(s.pinned_out, d_out, batch.size() * ob, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess)
         e = cudaEventRecord(s.done, st);
     if (e != cudaSuccess) {
         ctx.last_error = std::string("result copy: ") + cudaGetErrorString(e);
-        return fail_batch(HS_ECUDA);
+        return fail_staged(S, s, batch, HS_ECUDA);
     }
     finish_launch(S, s, batch, curve, bytes);
     return true;
@@ -490,12 +526,14 @@ int hs_server_create(hs_server **out, const hs_server_config *cfg)
         cudaGetLastError();
         return HS_ECUDA;
     }
-    int pools = 0;
+    int pools = 0, pageable = 0;
     cudaDeviceGetAttribute(&pools, cudaDevAttrMemoryPoolsSupported, S.cfg.device);
+    cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, S.cfg.device);
     for (int i = 0; i < S.cfg.slots; i++) {
         auto sl = std::make_unique<Slot>();
         sl->ctx.device = S.cfg.device;
         sl->ctx.sm_count = sms;
+        sl->ctx.pageable_access = pageable == 1;
         sl->ctx.use_graphs = false;  // request shapes rarely repeat
         if (cudaStreamCreateWithFlags(&sl->ctx.stream, cudaStreamNonBlocking) != cudaSuccess ||
             cudaEventCreateWithFlags(&sl->done, cudaEventDisableTiming) != cudaSuccess) {
