@@ -259,7 +259,9 @@ void hs_fixed_base_destroy(hs_fixed_base *fb);
  * batches overlap on the device.  Completion is detected with CUDA events and
  * bounded host waits only.  A request's buffers (scalars, indices, fresh
  * points, out) must stay valid until hs_server_wait has returned for it;
- * page-locked buffers let the copies run asynchronously.  Results are the
+ * a batch's copies from them run asynchronously (on a device that reads
+ * pageable host memory, as one gathered copy kernel; elsewhere page-locked
+ * buffers keep the copy engine's copies asynchronous).  Results are the
  * same whichever requests share a batch: with HS_FMT_COMPRESSED or
  * HS_FMT_AFFINE the bytes are identical alone and in the mix (a Jacobian
  * result is the same point, its Z depends on the summation order). */
