@@ -1158,7 +1158,8 @@ def run_ours(args) -> None:
     args_of = {c: (c, data[c]["h_sc"].numpy(), data[c]["h_jac"].numpy(), hs.FMT_JACOBIAN51, hs.FMT_JACOBIAN51)
                for c in (hs.SELENE, hs.HELIOS)}
     with ThreadPoolExecutor(max_workers=2) as pool:
-        for _ in range(3):
+        # ten warm-up pairs: the device has idled through the host-side work before
+        for _ in range(10):
             for f in [pool.submit(ctxs[c].msm, *args_of[c]) for c in (hs.SELENE, hs.HELIOS)]:
                 f.result()
         e2e_step_ms, e2e_calls = [], []
