@@ -138,7 +138,9 @@ int hs_context_set_priority(hs_context *ctx, int high);
  * (an ordinary array) is read by a copy kernel where the device reads pageable
  * host memory (Grace-class hosts), which keeps the copies asynchronous too;
  * elsewhere the copy engine stages it, which holds the calling thread for each
- * copy.  hs_msm_batch does the same for batches of at most 16 MSMs. */
+ * copy.  hs_msm_batch gathers a curve group's copies into one copy kernel
+ * there when they come from pageable memory or the group has more than 16
+ * MSMs. */
 int hs_msm(hs_context *ctx, int curve, const uint8_t *scalars, const void *points, int point_fmt, size_t n,
            void *out, int out_fmt);
 
