@@ -452,7 +452,8 @@ def test_host_buffers_pinned_pageable_unaligned(ctx, curve):
     elsewhere -- at byte offsets 0, 1, 4 and 8 from a 16-byte boundary (the
     kernel's 16-, 8-, 4- and 1-byte word forms, with ragged tails), and in
     pinned memory (copy engine): single MSMs with the bases in two parts,
-    Pedersen with its lead term, and small host batches, against the oracle."""
+    Pedersen with its lead term, and host batches of 3 and of 20 MSMs (the
+    latter a gathered copy kernel from either memory), against the oracle."""
     n = (1 << 18) + 3
     from helioselene_gb300.workload import make_workload
     w = make_workload(curve, n, seed=5150 + curve, edge_fraction=0.01)
@@ -464,6 +465,9 @@ def test_host_buffers_pinned_pageable_unaligned(ctx, curve):
     sizes = (1000, 77, 2001)
     cuts = np.cumsum((0,) + sizes)
     want_small = [oracle.msm(curve, sc[a:b], pts[a:b]) for a, b in zip(cuts[:-1], cuts[1:])]
+    # more than 16 MSMs in a group: one gathered copy kernel whatever the memory
+    many = np.cumsum([0] + [37 + 11 * i for i in range(20)])
+    want_many = [oracle.msm(curve, sc[a:b], pts[a:b]) for a, b in zip(many[:-1], many[1:])]
     counts = {}
     for pinned, offsets in ((False, (0, 1, 4, 8)), (True, (0, 1))):
         for off in offsets:
@@ -478,6 +482,8 @@ def test_host_buffers_pinned_pageable_unaligned(ctx, curve):
             assert ctx.pedersen(curve, s_v[:32], p_v[:64], s_v[32:], p_v[64:]) == want, f"pedersen, {tag}"
             items = [(curve, s_v[32 * a:32 * b], p_v[64 * a:64 * b]) for a, b in zip(cuts[:-1], cuts[1:])]
             assert ctx.msm_batch(items) == want_small, f"batch, {tag}"
+            items = [(curve, s_v[32 * a:32 * b], p_v[64 * a:64 * b]) for a, b in zip(many[:-1], many[1:])]
+            assert ctx.msm_batch(items) == want_many, f"batch of 20, {tag}"
     # a pageable call launches the same sequence as a pinned one, plus one copy
     # kernel per input copy (scalars and two parts of bases) where the device
     # reads pageable memory
