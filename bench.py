@@ -1131,9 +1131,10 @@ def run_ours(args) -> None:
     e2e_split = SPLIT_DEFAULT if args.split is None else args.split
     for c in ctxs.values():
         c.set_split(e2e_split)
-    # at least 60 steps (about 0.35 s): a single stalled step, seen in about one
-    # run in six, then weighs a few percent rather than a third
-    e2e_steps = max(60, args.steps)
+    # at least 150 steps (about 0.9 s): stalled steps, seen in about one run in
+    # six, cost the mean about the same fraction on average whatever the loop's
+    # length, but a longer loop spreads that cost evenly over the runs
+    e2e_steps = max(150, args.steps)
     for _ in range(2):
         for curve in (hs.HELIOS, hs.SELENE):
             ctxs[curve].msm(curve, data[curve]["h_sc"].numpy(), data[curve]["h_jac"].numpy(), hs.FMT_JACOBIAN51,
