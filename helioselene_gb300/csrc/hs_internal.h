@@ -319,9 +319,23 @@ struct PullChunk {
 };
 constexpr size_t PULL_CHUNK_BYTES = size_t(256) << 10;  // a block copies one piece at a time
 
+// A caller's buffer is read on the CPU at its first and last byte before a copy
+// kernel reads it: a bad pointer, or a buffer shorter than its count where the
+// memory past it is unmapped, then fails on the host -- as a copy-engine copy
+// from pageable memory, which the CPU stages, would -- and not on the device.
+inline void touch_host_range(const void *p, size_t bytes)
+{
+    if (!bytes)
+        return;
+    const volatile uint8_t *b = static_cast<const volatile uint8_t *>(p);
+    (void)b[0];
+    (void)b[bytes - 1];
+}
+
 // append a copy of `bytes` from src to dst, cut into pieces of at most PULL_CHUNK_BYTES
 inline void pull_add(std::vector<PullChunk> &list, void *dst, const void *src, size_t bytes)
 {
+    touch_host_range(src, bytes);
     for (size_t o = 0; o < bytes; o += PULL_CHUNK_BYTES)
         list.push_back({static_cast<const uint8_t *>(src) + o, static_cast<uint8_t *>(dst) + o,
                         std::min(PULL_CHUNK_BYTES, bytes - o)});

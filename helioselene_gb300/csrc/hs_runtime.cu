@@ -1616,13 +1616,14 @@ static void launch_pull(Context &ctx, void *dst, const void *src, size_t bytes, 
     ctx.launches++;
 }
 
-// true when p is ordinary pageable host memory (not pinned, registered, managed or device)
+// true when p is ordinary pageable host memory (not pinned, registered, managed
+// or device); a pointer the runtime cannot classify keeps the copy engine
 static bool is_pageable(const void *p)
 {
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         cudaGetLastError();
-        return true;
+        return false;
     }
     return a.type == cudaMemoryTypeUnregistered;
 }
@@ -1699,6 +1700,7 @@ static cudaError_t h2d_async(Context &ctx, void *dst, const void *src, size_t by
         return cudaSuccess;
     if (!ctx.pageable_access || !is_pageable(src))
         return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s);
+    touch_host_range(src, bytes);
     const uintptr_t al = reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src);
     if (al % 16 == 0)
         launch_pull<uint4>(ctx, dst, src, bytes, s);
